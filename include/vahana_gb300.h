@@ -1,0 +1,324 @@
+/*
+ * vahana_gb300.h -- C ABI of the GB300-native Vahana.jl transition step.
+ *
+ * One shared library (libvahana_gb300.so) owns every device buffer of a
+ * simulation: agent state as struct-of-arrays read/write double buffers,
+ * and each edge type as a CSR keyed by target agent, kept in the
+ * reference's edge-insertion order.  Transition functions are bound by
+ * name to hand-written sm_103a kernels.  The signatures below are what a
+ * Julia `ccall` (or Python ctypes) binding of Vahana's public API calls;
+ * each entry cites the reference function it replaces (paths are relative
+ * to the Vahana.jl v1.4.7 source tree).
+ *
+ * Conventions
+ *   - Every function returns an int status: VG_OK (0) or a VG_ERR_* code.
+ *     VG_ERR_ASSERT marks the cases where the reference raises an
+ *     AssertionError; a binding rethrows it as AssertionError.
+ *     vg_last_error() returns the message of the last failure of the
+ *     calling thread.
+ *   - Agent IDs keep the reference's bit layout (src/Agent.jl:30-115):
+ *     type_nr << 56 | process << 36 | agent_nr, with process = 0 (one GPU,
+ *     no MPI ranks) and agent_nr 1-based.
+ *   - A "type reference" (used in call/read/write/add_existing lists) is
+ *     an agent type number (1..255) or VG_EDGE(edge_type_index).
+ *   - Host pointers are plain host memory; nothing here takes a torch type.
+ *   - All device work of a simulation runs on one CUDA stream (given at
+ *     vg_sim_create, or the library's own); calls on one handle are not
+ *     re-entrant (the reference is single threaded, src/MPIinit.jl:22).
+ */
+#ifndef VAHANA_GB300_H
+#define VAHANA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define VG_OK 0
+#define VG_ERR_ASSERT 1   /* reference raises AssertionError                */
+#define VG_ERR_ARG 2      /* malformed argument (unknown name, bad pointer) */
+#define VG_ERR_CUDA 3     /* CUDA runtime error                             */
+#define VG_ERR_NOMEM 4    /* device allocation failed / over a stated limit */
+#define VG_ERR_DEVICE 5   /* a kernel reported an error through its status  */
+#define VG_ERR_STATE 6    /* call not allowed in the current phase          */
+
+/* ---- field data types (SoA columns of agent and edge state) ----------- */
+#define VG_BOOL 1
+#define VG_U8 2
+#define VG_I8 3
+#define VG_U16 4
+#define VG_I16 5
+#define VG_U32 6
+#define VG_I32 7
+#define VG_U64 8
+#define VG_I64 9
+#define VG_F32 10
+#define VG_F64 11
+
+/* ---- hints (src/ModelTypes.jl:81-230) ---------------------------------- */
+#define VG_HINT_IMMORTAL 0x01u          /* agent  :Immortal                 */
+#define VG_HINT_INDEPENDENT 0x02u       /* agent  :Independent              */
+#define VG_HINT_STATELESS 0x10u         /* edge   :Stateless                */
+#define VG_HINT_IGNOREFROM 0x20u        /* edge   :IgnoreFrom               */
+#define VG_HINT_SINGLETYPE 0x40u        /* edge   :SingleType (target=...)  */
+#define VG_HINT_SINGLEEDGE 0x80u        /* edge   :SingleEdge               */
+#define VG_HINT_IGNORESOURCESTATE 0x100u /* edge  :IgnoreSourceState        */
+#define VG_HINT_NUMEDGESONLY 0x200u     /* edge   :NumEdgesOnly             */
+#define VG_HINT_HASEDGEONLY 0x400u      /* edge   :HasEdgeOnly              */
+
+/* ---- type references in call/read/write lists -------------------------- */
+#define VG_EDGE(e) (0x10000 | (e))
+
+/* ---- reduction operators of mapreduce (src/Helpers.jl:44-81) ----------- */
+#define VG_OP_ADD 1
+#define VG_OP_MUL 2
+#define VG_OP_MAX 3
+#define VG_OP_MIN 4
+#define VG_OP_AND 5
+#define VG_OP_OR 6
+
+/* map function applied to each element before the reduction (mapreduce's
+ * `f`): the field itself, or the field compared with a constant. */
+#define VG_MAP_FIELD 0
+#define VG_MAP_EQ 1
+#define VG_MAP_NE 2
+#define VG_MAP_LT 3
+#define VG_MAP_GT 4
+
+/* raster metrics (src/Raster.jl:82-96) */
+#define VG_METRIC_CHEBYSHEV 0
+#define VG_METRIC_EUCLIDEAN 1
+#define VG_METRIC_MANHATTEN 2
+
+typedef struct vg_model vg_model;
+typedef struct vg_sim vg_sim;
+
+/* ---- library ----------------------------------------------------------- */
+const char *vg_last_error(void);
+int vg_version(void);
+/* Number of CUDA devices visible (0 here means: no GPU; every compute call
+ * will fail with VG_ERR_CUDA, there is no CPU fallback). */
+int vg_device_count(int *out);
+
+/* ---- model registry ---------------------------------------------------- */
+/* ModelTypes() -- src/ModelTypes.jl:32-41 */
+int vg_model_create(vg_model **out);
+void vg_model_destroy(vg_model *m);
+/* register_agenttype!(types, T, hints...) -- src/ModelTypes.jl:81-106.
+ * Fields are the struct's fields in declaration order. *type_nr_out is the
+ * 1-based type number used in AgentIDs. */
+int vg_model_register_agenttype(vg_model *m, const char *name, int nfields,
+                                const char *const *field_names,
+                                const int *field_dtypes, unsigned hints,
+                                int *type_nr_out);
+/* register_edgetype!(types, T, hints...; target, size) --
+ * src/ModelTypes.jl:158-230.  target_type_nr is 0 unless :SingleType;
+ * size is the optional `size` keyword (0 = not given). */
+int vg_model_register_edgetype(vg_model *m, const char *name, int nfields,
+                               const char *const *field_names,
+                               const int *field_dtypes, unsigned hints,
+                               int target_type_nr, int64_t size,
+                               int *edge_type_out);
+/* register_param! / register_global! -- scalar f64 values by name. */
+int vg_model_register_param(vg_model *m, const char *name, double dflt);
+int vg_model_register_global(vg_model *m, const char *name, double dflt);
+/* create_model(types, name) -- src/Simulation.jl:115-207 */
+int vg_model_finalize(vg_model *m, const char *name);
+/* has_hint(sim, T, hint) -- src/ModelTypes.jl:235-242; returns the effective
+ * (normalised) hint bits of an edge type. */
+int vg_model_edge_hints(const vg_model *m, int edge_type, unsigned *out);
+int vg_model_type_by_name(const vg_model *m, const char *name, int *out);
+
+/* ---- simulation lifecycle ---------------------------------------------- */
+/* create_simulation(model, params, globals; name) -- src/Simulation.jl:261-339.
+ * stream is a cudaStream_t (NULL = the library creates its own). */
+int vg_sim_create(vg_model *m, const char *name, void *stream, vg_sim **out);
+/* finish_simulation! -- src/Simulation.jl:551-573 */
+int vg_sim_destroy(vg_sim *s);
+/* copy_simulation(sim) -- src/Simulation.jl:500-510 */
+int vg_sim_copy(vg_sim *s, vg_sim **out);
+/* finish_init!(sim) -- src/Simulation.jl:403-476 (one process: no
+ * partitioning, ids stay as issued). Uploads the staged graph and builds the
+ * device CSR of every edge type in insertion order. */
+int vg_finish_init(vg_sim *s);
+int vg_sim_num_transitions(vg_sim *s, int64_t *out);
+int vg_sim_set_stream(vg_sim *s, void *stream);
+int vg_sim_synchronize(vg_sim *s);
+/* Bytes of device memory the simulation holds (admission by footprint). */
+int vg_sim_device_bytes(vg_sim *s, uint64_t *out);
+/* disable_transition_checks(sim, disable) -- src/Helpers.jl:259-262 */
+int vg_disable_transition_checks(vg_sim *s, int disable);
+
+/* ---- params and globals (src/Simulation.jl:587-630, src/Global.jl) ----- */
+int vg_set_param(vg_sim *s, const char *name, double v);
+int vg_param(vg_sim *s, const char *name, double *out);
+int vg_set_global(vg_sim *s, const char *name, double v);
+int vg_get_global(vg_sim *s, const char *name, double *out);
+int vg_push_global(vg_sim *s, const char *name, double v);
+int vg_global_series(vg_sim *s, const char *name, double *out, uint64_t cap,
+                     uint64_t *n_out);
+
+/* ---- agents ------------------------------------------------------------ */
+/* add_agents!(sim, agents) / add_agent! -- src/Agent.jl:174-180,
+ * src/AgentMethods.jl:65-89.  fields[i] points to n values of field i
+ * (SoA, the field's dtype).  Before finish_init! only, or through
+ * vg_add_agent_per_process after it (src/Agent.jl:367-388). */
+int vg_add_agents(vg_sim *s, int type_nr, uint64_t n,
+                  const void *const *fields, uint64_t *ids_out);
+int vg_add_agent_per_process(vg_sim *s, int type_nr,
+                             const void *const *fields, uint64_t *id_out);
+/* agentstate(sim, id, T) -- src/AgentMethods.jl:91-154 (host read back) */
+int vg_agentstate(vg_sim *s, uint64_t id, int type_nr, void *const *fields_out);
+/* num_agents(sim, T) -- src/Agent.jl:324-343 */
+int vg_num_agents(vg_sim *s, int type_nr, uint64_t *out);
+/* Slot count (nextid - 1): the length of the state vectors. */
+int vg_agent_slots(vg_sim *s, int type_nr, uint64_t *out);
+/* all_agents / all_agentids -- src/Agent.jl:234-313.  Writes the living
+ * agents in index order; call with cap = 0 to get the count. */
+int vg_all_agents(vg_sim *s, int type_nr, void *const *fields_out,
+                  uint64_t *ids_out, uint64_t cap, uint64_t *n_out);
+/* Bulk read of all slots (living and died) of the read buffers; died_out
+ * may be NULL.  Used for parity checks of whole states. */
+int vg_read_agents(vg_sim *s, int type_nr, void *const *fields_out,
+                   uint8_t *died_out, uint64_t cap, uint64_t *n_out);
+/* Device pointer of a field's read buffer (for zero-copy consumers). */
+int vg_agent_field_device_ptr(vg_sim *s, int type_nr, int field, void **out);
+
+/* ---- edges ------------------------------------------------------------- */
+/* add_edge!(sim, from, to, state) / add_edges! -- src/EdgeMethods.jl:388-523,
+ * src/Edge.jl:81-96.  Before finish_init!, or between transitions when
+ * transition checks are disabled (as the reference's tests do).
+ * payload[i] points to n values of edge field i (may be NULL for stateless
+ * types).  Edges are appended in array order. */
+int vg_add_edges(vg_sim *s, int edge_type, uint64_t n, const uint64_t *from,
+                 const uint64_t *to, const void *const *payload);
+/* remove_edges!(sim, to, T) and remove_edges!(sim, from, to, T) --
+ * src/EdgeMethods.jl:527-599.  from may be NULL (remove all edges to `to`). */
+int vg_remove_edges(vg_sim *s, int edge_type, uint64_t n, const uint64_t *from,
+                    const uint64_t *to);
+/* Per-target accessors, read back to the host --
+ * edges / neighborids / edgestates: src/EdgeMethods.jl:705-848;
+ * num_edges / has_edge: :850-892.  *count_out = -1 means the reference
+ * returns `nothing` (no container for this agent).  from_out / payload_out
+ * may be NULL; at most cap entries are written. */
+int vg_edges(vg_sim *s, uint64_t to, int edge_type, uint64_t *from_out,
+             void *const *payload_out, uint64_t cap, int64_t *count_out);
+int vg_neighborids(vg_sim *s, uint64_t to, int edge_type, uint64_t *from_out,
+                   uint64_t cap, int64_t *count_out);
+int vg_edgestates(vg_sim *s, uint64_t to, int edge_type,
+                  void *const *payload_out, uint64_t cap, int64_t *count_out);
+int vg_num_edges(vg_sim *s, uint64_t to, int edge_type, int64_t *out);
+int vg_has_edge(vg_sim *s, uint64_t to, int edge_type, int *out);
+/* num_edges(sim, T; write) -- src/Edge.jl:373-389 */
+int vg_num_edges_total(vg_sim *s, int edge_type, int write, uint64_t *out);
+/* Bulk read of one edge type's CSR for one target type: row_ptr (nrows+1,
+ * u64), from ids (AgentIDs), payload columns.  Pass NULL to query sizes. */
+int vg_read_edges(vg_sim *s, int edge_type, int target_type_nr,
+                  uint64_t *row_ptr_out, uint64_t *from_out,
+                  void *const *payload_out, uint64_t *nrows_out,
+                  uint64_t *nedges_out);
+
+/* ---- transitions ------------------------------------------------------- */
+/* apply!(sim, f, call, read, write; add_existing, with_edge) --
+ * src/Simulation.jl:720-821.  `transition` names a kernel registered in the
+ * library (vg_transition_names).  Lists hold type references.  with_edge is
+ * an edge type index or -1.  params/nparams are the transition's own
+ * arguments (documented per transition). */
+int vg_apply(vg_sim *s, const char *transition, const int *call, int ncall,
+             const int *read, int nread, const int *write, int nwrite,
+             const int *add_existing, int nadd, int with_edge,
+             const double *params, int nparams);
+/* Comma-separated list of the registered transition names. */
+const char *vg_transition_names(void);
+
+/* ---- mapreduce -- src/AgentMethods.jl:533-565 (agents),
+ *      src/EdgeMethods.jl:972-1001 (edges); identities from val4empty,
+ *      src/Helpers.jl:44-81.  The result is written as out_dtype
+ *      (VG_I64, VG_F64 or VG_BOOL).  has_init/init give the `init`
+ *      keyword. */
+int vg_mapreduce_agents(vg_sim *s, int type_nr, int field, int map_kind,
+                        double map_arg, int op, int out_dtype, int has_init,
+                        double init, void *out);
+int vg_mapreduce_edges(vg_sim *s, int edge_type, int field, int map_kind,
+                       double map_arg, int op, int out_dtype, int has_init,
+                       double init, void *out);
+
+/* ---- rasters -- src/Raster.jl ------------------------------------------- */
+/* add_raster!(sim, name, dims, constructor) -- :32-54.  The cells' state is
+ * given as SoA columns in column-major CartesianIndices order (first index
+ * fastest); ids_out (may be NULL) receives the cell ids in that order. */
+int vg_add_raster(vg_sim *s, const char *name, int ndims, const int64_t *dims,
+                  int type_nr, const void *const *fields, uint64_t *ids_out);
+/* connect_raster_neighbors!(sim, name, ctor; distance, metric, periodic) --
+ * :139-167.  The edge constructor is a constant payload.  implicit != 0
+ * keeps the edges implicit (stencil indexing, no CSR); the accessors and
+ * the stencil kernels still see them in the reference's order. */
+int vg_connect_raster_neighbors(vg_sim *s, const char *name, int edge_type,
+                                const void *const *payload, double distance,
+                                int metric, int periodic, int implicit);
+/* move_to!(sim, name, id, pos, edge_from_raster, edge_to_raster; distance,
+ * metric, periodic, only_surrounding) -- :437-477, in the init phase.
+ * edge types may be -1 for `nothing`. */
+int vg_move_to(vg_sim *s, const char *name, uint64_t id, const int64_t *pos,
+               int edge_from_raster, const void *const *payload_from,
+               int edge_to_raster, const void *const *payload_to,
+               double distance, int metric, int periodic,
+               int only_surrounding);
+/* cellid(sim, name, pos) -- :403-405 (pos is 1-based) */
+int vg_cellid(vg_sim *s, const char *name, const int64_t *pos, uint64_t *out);
+int vg_raster_dims(vg_sim *s, const char *name, int64_t *dims_out,
+                   int *ndims_out);
+/* rastervalues(sim, name, field) / calc_rasterstate(sim, name, c -> c.field)
+ * -- :282-387.  Writes prod(dims) values of the field's dtype, column-major. */
+int vg_rastervalues(vg_sim *s, const char *name, int field, void *out);
+
+/* ---- seeded graph generators of the test models ---------------------------
+ * Each plays the part of the model script's add_edge! loop before
+ * finish_init! and appends its records, in the loop's call order, to the
+ * edge type's staging (no reference counterpart: the reference builds graphs
+ * with host loops of add_edge!, src/EdgeMethods.jl:478-522). */
+/* agent i (1-based) of type_nr adds k edges i -> t, t uniform in [1, N],
+ * t != i; Philox counter (i, j, TAG_EDGE), order (i, j). */
+int vg_gen_uniform_out_edges(vg_sim *s, int edge_type, int type_nr, uint32_t k,
+                             uint64_t seed);
+/* directed Chung-Lu over the agents of type_nr: expected degrees
+ * w_i = min(c * i^(-1/(gamma-1)), wmax) with mean `mean`; edge e draws its
+ * source and target proportional to w and a weight in (0, 1] into the
+ * Float64 field weight_field (-1: none). */
+int vg_gen_chung_lu_edges(vg_sim *s, int edge_type, int type_nr, uint64_t nedges,
+                          double mean, double gamma, double wmax, uint64_t seed,
+                          int weight_field);
+/* Staged edge records of an edge type before finish_init!, in call order. */
+int vg_read_staged_edges(vg_sim *s, int edge_type, uint64_t *from_out,
+                         uint64_t *to_out, void *const *payload_out, uint64_t cap,
+                         uint64_t *n_out);
+
+/* ---- batched ensemble (many independent SIR instances in one arena) ----- */
+typedef struct vg_batch vg_batch;
+/* Instances i = 0..n-1 with agent counts N[i], out-degree deg[i], infection
+ * probability beta[i], recovery steps rec[i], seed seeds[i].  Graphs and
+ * initial states are generated on the device from the seeds. */
+int vg_batch_create_sir(int n, const int64_t *N, const int32_t *deg,
+                        const double *beta, const int32_t *rec,
+                        const uint64_t *seeds, int64_t n_init_infected_per_1000,
+                        void *stream, vg_batch **out);
+/* Advance every instance by `steps` transitions.  mode 0: one persistent
+ * kernel per step over all instances; mode 1: the same, with the step
+ * loop captured once in a CUDA graph and replayed. */
+int vg_batch_step(vg_batch *b, int steps, int mode);
+/* Plain path for comparison: step instance i alone with the plain kernels. */
+int vg_batch_step_one(vg_batch *b, int i, int steps);
+int vg_batch_read_states(vg_batch *b, int i, uint8_t *state_out,
+                         int32_t *days_out, uint64_t cap, uint64_t *n_out);
+int vg_batch_read_graph(vg_batch *b, int i, uint32_t *row_ptr_out,
+                        uint32_t *src_out, uint64_t *nrows_out,
+                        uint64_t *nedges_out);
+int vg_batch_destroy(vg_batch *b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VAHANA_GB300_H */

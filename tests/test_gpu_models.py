@@ -1,0 +1,77 @@
+"""Parity of the three test models' transition steps (GPU, through the C ABI)
+against the oracle's C restatement, on the same seeded inputs.
+
+Integer, Bool and UInt8 state must be bit-exact; Float64 state of the
+bounded-confidence model is bit-exact too (the kernels fold in container
+order with separately rounded operations), so the tolerance is 0.
+"""
+import numpy as np
+import pytest
+
+from oracle import models as om
+
+pytestmark = pytest.mark.gpu
+
+
+def test_sir_bit_exact(vh):
+    from vahana_gb300 import models
+    run = models.build_sir(n=3000, degree=10, beta=0.05, recovery=7, seed=7, n_infected=30)
+    sim = run.sim
+    frm, to, _ = models.staged_edges(sim, "Contact")
+    st0, d0 = vh.read_agents(sim, "Person")[0].values()
+    vh.finish_init(sim)
+    steps = 40
+    for _ in range(steps):
+        run.step()
+    cols, died = vh.read_agents(sim, "Person")
+    s_ref, d_ref = om.run_sir(run.n, frm, to, st0, d0, 0.05, 7, 7, steps, first_step=1)
+    assert not died.any()
+    np.testing.assert_array_equal(cols["state"], s_ref)
+    np.testing.assert_array_equal(cols["days"], d_ref)
+    assert (s_ref == 2).sum() > 0  # the epidemic ran
+    run.close()
+
+
+@pytest.mark.parametrize("hub", [256, 16])
+def test_opinion_bit_exact(vh, hub):
+    from vahana_gb300 import models
+    run = models.build_opinion(n=20000, mean_degree=20, gamma=2.5, wmax=2000, eps=0.3, seed=11,
+                               hub_threshold=hub)
+    sim = run.sim
+    frm, to, pl = models.staged_edges(sim, "Weight")
+    x0 = vh.read_agents(sim, "Opinion")[0]["x"].copy()
+    vh.finish_init(sim)
+    steps = 12
+    for _ in range(steps):
+        run.step()
+    x = vh.read_agents(sim, "Opinion")[0]["x"]
+    x_ref = om.run_opinion(run.n, frm, to, pl["w"], x0, 0.3, steps)
+    # tolerance 0: bit-exact on the ordered path (hub warps fold in order too)
+    np.testing.assert_array_equal(x.view(np.uint64), x_ref.view(np.uint64))
+    assert not np.array_equal(x, x0)
+    run.close()
+
+
+def test_life_walkers_bit_exact(vh):
+    from vahana_gb300 import models
+    W, H, nw, seed = 96, 80, 700, 5
+    run = models.build_life(W, H, nw, 0.3, seed)
+    sim = run.sim
+    a0 = vh.read_agents(sim, "Cell")[0]["alive"].copy()
+    wc = vh.read_agents(sim, "Walker")[0]
+    x0, y0 = wc["x"].copy(), wc["y"].copy()
+    vh.finish_init(sim)
+    steps = 15
+    for _ in range(steps):
+        run.step()
+    a = vh.read_agents(sim, "Cell")[0]["alive"]
+    w = vh.read_agents(sim, "Walker")[0]
+    a_ref, x_ref, y_ref, rp_ref, src_ref = om.run_life_walkers(a0, x0, y0, W, H, seed, steps)
+    np.testing.assert_array_equal(a.astype(np.uint8), a_ref)
+    np.testing.assert_array_equal(w["x"], x_ref)
+    np.testing.assert_array_equal(w["y"], y_ref)
+    # walker -> cell edges rebuilt every step, in call (walker) order per cell
+    rp, frm, _ = vh.read_edges(sim, "OnCell", "Cell")
+    np.testing.assert_array_equal(rp, rp_ref)
+    np.testing.assert_array_equal(frm & np.uint64((1 << 36) - 1), src_ref)
+    run.close()

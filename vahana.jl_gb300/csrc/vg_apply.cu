@@ -1,0 +1,647 @@
+// apply! (src/Simulation.jl:720-821) and mapreduce
+// (src/AgentMethods.jl:533-565, src/EdgeMethods.jl:972-1001).
+//
+// apply! runs, in the reference's order: the argument checks, prepare_read!
+// (readable flags), prepare_write! (reset of written agent types that are
+// neither called nor in add_existing; new or kept edge containers), the
+// sweep of every called type by the named kernel, then finish_write! of the
+// agent types (swap of the double buffers, collection of the agents that
+// died into the reuse stack, removal of their edges) and of the edge types
+// (the new CSR replaces the read container).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+
+#include "vg_internal.h"
+
+namespace vg {
+
+bool ApplyCtx::in_read(int ref) const {
+  return std::find(read.begin(), read.end(), ref) != read.end();
+}
+bool ApplyCtx::in_write(int ref) const {
+  return std::find(write.begin(), write.end(), ref) != write.end();
+}
+bool ApplyCtx::writes_call() const { return in_write(call_type); }
+
+EdgeAppend *ApplyCtx::append_for(int e, uint64_t capacity, bool ordered) {
+  for (auto &a : appends)
+    if (a->edge_type == e) {
+      if (a->ordered != ordered || ordered)
+        fail(VG_ERR_ARG, "one transition call appends to an edge type once");
+      return a.get();
+    }
+  Sim &s = *sim;
+  const EdgeTypeDesc &ed = s.model->et(e);
+  auto a = std::make_unique<EdgeAppend>();
+  a->edge_type = e;
+  a->cap = std::max<uint64_t>(capacity, 1);
+  a->ordered = ordered;
+  a->to.alloc(a->cap * 8, &s.footprint);
+  a->from.alloc(a->cap * 8, &s.footprint);
+  if (!ordered) a->key.alloc(a->cap * 8, &s.footprint);
+  int nf = ed.stores_payload() ? (int)ed.fields.size() : 0;
+  a->payload.resize(nf);
+  for (int f = 0; f < nf; f++) a->payload[f].alloc(a->cap * ed.fields[f].size, &s.footprint);
+  a->counter.alloc(8, &s.footprint);
+  VG_CUDA(cudaMemsetAsync(a->counter.p, 0, 8, s.stream));
+  appends.push_back(std::move(a));
+  return appends.back().get();
+}
+
+namespace {
+
+constexpr int TPB = 256;
+inline unsigned nblk(uint64_t n, int tpb = TPB) {
+  uint64_t b = (n + tpb - 1) / tpb;
+  return (unsigned)std::max<uint64_t>(b, 1);
+}
+
+__global__ void k_new_deaths(const uint8_t *died_new, const uint8_t *died_old,
+                             uint64_t n, uint32_t *flag) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) flag[i] = (died_new[i] && !died_old[i]) ? 1u : 0u;
+}
+
+__global__ void k_push_reuse(const uint32_t *flag, const uint32_t *pos, uint64_t n,
+                             uint64_t *stack, uint64_t base) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && flag[i]) stack[base + pos[i]] = i + 1;  // agent numbers, in index order
+}
+
+bool is_edge_ref(int r) { return (r & 0x10000) != 0; }
+int edge_of(int r) { return r & 0xFFFF; }
+
+std::string ref_name(Sim &s, int r) {
+  return is_edge_ref(r) ? s.model->et(edge_of(r)).name : s.model->at(r).name;
+}
+
+void validate_refs(Sim &s, const int *v, int n) {
+  for (int i = 0; i < n; i++) {
+    if (is_edge_ref(v[i])) s.model->et(edge_of(v[i]));
+    else s.model->at(v[i]);
+  }
+}
+
+// ------------------------------------------------------------- mapreduce
+// val4empty (src/Helpers.jl:44-81): identity of op for datatype MT; MT is
+// Bool for & and | and Int64 otherwise unless `datatype` says else.
+struct RedAcc {
+  int64_t i;
+  double f;
+};
+
+__device__ __forceinline__ int64_t red_i(int op, int64_t a, int64_t b) {
+  switch (op) {
+    case VG_OP_ADD: return (int64_t)((uint64_t)a + (uint64_t)b);
+    case VG_OP_MUL: return (int64_t)((uint64_t)a * (uint64_t)b);
+    case VG_OP_MAX: return a > b ? a : b;
+    case VG_OP_MIN: return a < b ? a : b;
+    case VG_OP_AND: return a & b;
+    case VG_OP_OR: return a | b;
+  }
+  return 0;
+}
+__device__ __forceinline__ double red_f(int op, double a, double b) {
+  switch (op) {
+    case VG_OP_ADD: return __dadd_rn(a, b);
+    case VG_OP_MUL: return __dmul_rn(a, b);
+    case VG_OP_MAX: return fmax(a, b);
+    case VG_OP_MIN: return fmin(a, b);
+  }
+  return 0;
+}
+
+__device__ __forceinline__ double load_val(const void *p, int dt, uint64_t i, bool *isf,
+                                           int64_t *iv) {
+  switch (dt) {
+    case VG_BOOL: case VG_U8: *iv = ((const uint8_t *)p)[i]; break;
+    case VG_I8: *iv = ((const int8_t *)p)[i]; break;
+    case VG_U16: *iv = ((const uint16_t *)p)[i]; break;
+    case VG_I16: *iv = ((const int16_t *)p)[i]; break;
+    case VG_U32: *iv = ((const uint32_t *)p)[i]; break;
+    case VG_I32: *iv = ((const int32_t *)p)[i]; break;
+    case VG_U64: case VG_I64: *iv = ((const int64_t *)p)[i]; break;
+    case VG_F32: *isf = true; return ((const float *)p)[i];
+    case VG_F64: *isf = true; return ((const double *)p)[i];
+  }
+  *isf = false;
+  return (double)*iv;
+}
+
+// map f: field, or field compared with a constant (result Bool)
+__device__ __forceinline__ void map_val(int kind, double arg, const void *p, int dt, uint64_t i,
+                                        bool float_acc, int64_t *vi, double *vf) {
+  bool isf = false;
+  int64_t iv = 0;
+  double fv = load_val(p, dt, i, &isf, &iv);
+  if (kind != VG_MAP_FIELD) {
+    bool r = false;
+    double x = isf ? fv : (double)iv;
+    switch (kind) {
+      case VG_MAP_EQ: r = x == arg; break;
+      case VG_MAP_NE: r = x != arg; break;
+      case VG_MAP_LT: r = x < arg; break;
+      case VG_MAP_GT: r = x > arg; break;
+    }
+    *vi = r;
+    *vf = r;
+    return;
+  }
+  *vi = isf ? (int64_t)fv : iv;
+  *vf = isf ? fv : (double)iv;
+  (void)float_acc;
+}
+
+struct RedArgs {
+  const void *p;
+  int dt;
+  uint64_t n;
+  const uint8_t *died;  // agents: skip died; null for edges
+  int kind;
+  double arg;
+  int op;
+  int float_acc;
+  int64_t init_i;   // the reduction's init (val4empty or the `init` keyword)
+  double init_f;
+  int64_t neut_i;   // neutral element of op for the partial reductions
+  double neut_f;
+};
+
+// pass 1: per-block partial (deterministic block order)
+__global__ void k_reduce_partial(RedArgs a, int64_t *pi, double *pf) {
+  __shared__ int64_t si[TPB];
+  __shared__ double sf[TPB];
+  int64_t acc_i = a.neut_i;
+  double acc_f = a.neut_f;
+  bool have = false;
+  uint64_t chunk = (a.n + gridDim.x - 1) / gridDim.x;
+  uint64_t b = (uint64_t)blockIdx.x * chunk, e = min(a.n, b + chunk);
+  for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+    if (a.died && a.died[i]) continue;
+    int64_t vi;
+    double vf;
+    map_val(a.kind, a.arg, a.p, a.dt, i, a.float_acc, &vi, &vf);
+    if (!have) {
+      acc_i = vi;
+      acc_f = vf;
+      have = true;
+    } else {
+      acc_i = red_i(a.op, vi, acc_i);
+      acc_f = red_f(a.op, vf, acc_f);
+    }
+  }
+  // empty threads contribute the neutral element
+  if (!have) {
+    acc_i = a.neut_i;
+    acc_f = a.neut_f;
+  }
+  si[threadIdx.x] = acc_i;
+  sf[threadIdx.x] = acc_f;
+  __syncthreads();
+  for (int s = TPB / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      si[threadIdx.x] = red_i(a.op, si[threadIdx.x + s], si[threadIdx.x]);
+      sf[threadIdx.x] = red_f(a.op, sf[threadIdx.x + s], sf[threadIdx.x]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    pi[blockIdx.x] = si[0];
+    pf[blockIdx.x] = sf[0];
+  }
+}
+
+__global__ void k_reduce_final(const int64_t *pi, const double *pf, int nb, int op,
+                               int64_t init_i, double init_f, int64_t *oi, double *of) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int64_t ai = init_i;
+  double af = init_f;
+  for (int b = 0; b < nb; b++) {
+    ai = red_i(op, pi[b], ai);
+    af = red_f(op, pf[b], af);
+  }
+  *oi = ai;
+  *of = af;
+}
+
+// sequential left fold in index order: reduced = op(f(x), reduced)
+__global__ void k_reduce_ordered(RedArgs a, int64_t *oi, double *of) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int64_t ai = a.init_i;
+  double af = a.init_f;
+  for (uint64_t i = 0; i < a.n; i++) {
+    if (a.died && a.died[i]) continue;
+    int64_t vi;
+    double vf;
+    map_val(a.kind, a.arg, a.p, a.dt, i, a.float_acc, &vi, &vf);
+    ai = red_i(a.op, vi, ai);
+    af = red_f(a.op, vf, af);
+  }
+  *oi = ai;
+  *of = af;
+}
+
+void identity_for(int op, int out_dtype, int has_init, double init, int64_t *ii,
+                  double *fi) {
+  if (has_init) {
+    *ii = (int64_t)init;
+    *fi = init;
+    return;
+  }
+  bool boolean = out_dtype == VG_BOOL;
+  switch (op) {
+    case VG_OP_ADD: *ii = 0; *fi = 0; break;
+    case VG_OP_MUL: *ii = 1; *fi = 1; break;
+    case VG_OP_MAX:
+      *ii = boolean ? -1 : -std::numeric_limits<int64_t>::max();
+      *fi = (double)*ii;
+      break;
+    case VG_OP_MIN:
+      *ii = boolean ? 1 : std::numeric_limits<int64_t>::max();
+      *fi = (double)*ii;
+      break;
+    case VG_OP_AND:
+      *ii = boolean ? 1 : std::numeric_limits<int64_t>::max();
+      *fi = (double)*ii;
+      break;
+    case VG_OP_OR: *ii = 0; *fi = 0; break;
+    default: fail(VG_ERR_ASSERT, "Can not derive the init value for the operator. You must "
+                                 "add this information via the `init` keyword.");
+  }
+}
+
+void neutral_for(int op, int64_t *ni, double *nf) {
+  switch (op) {
+    case VG_OP_ADD: *ni = 0; *nf = 0.0; break;
+    case VG_OP_MUL: *ni = 1; *nf = 1.0; break;
+    case VG_OP_MAX: *ni = std::numeric_limits<int64_t>::min(); *nf = -INFINITY; break;
+    case VG_OP_MIN: *ni = std::numeric_limits<int64_t>::max(); *nf = INFINITY; break;
+    case VG_OP_AND: *ni = -1; *nf = 0.0; break;
+    default: *ni = 0; *nf = 0.0;
+  }
+}
+
+void run_reduce(Sim &s, RedArgs a, int out_dtype, bool ordered, void *out) {
+  neutral_for(a.op, &a.neut_i, &a.neut_f);
+  int64_t ri = a.init_i;
+  double rf = a.init_f;
+  if (a.n > 0) {
+    int64_t *d = nullptr;
+    VG_CUDA(cudaMallocAsync((void **)&d, 16 + 2 * 8 * 1024, s.stream));
+    int64_t *oi = d;
+    double *of = (double *)(d + 1);
+    if (ordered) {
+      k_reduce_ordered<<<1, 32, 0, s.stream>>>(a, oi, of);
+    } else {
+      int nb = (int)std::min<uint64_t>(1024, (a.n + TPB - 1) / TPB);
+      int64_t *pi = d + 2;
+      double *pf = (double *)(d + 2 + 1024);
+      k_reduce_partial<<<nb, TPB, 0, s.stream>>>(a, pi, pf);
+      k_reduce_final<<<1, 32, 0, s.stream>>>(pi, pf, nb, a.op, a.init_i, a.init_f, oi, of);
+    }
+    VG_CUDA(cudaGetLastError());
+    VG_CUDA(cudaMemcpyAsync(&ri, oi, 8, cudaMemcpyDeviceToHost, s.stream));
+    VG_CUDA(cudaMemcpyAsync(&rf, of, 8, cudaMemcpyDeviceToHost, s.stream));
+    VG_CUDA(cudaFreeAsync(d, s.stream));
+    VG_CUDA(cudaStreamSynchronize(s.stream));
+  }
+  if (out_dtype == VG_F64) *(double *)out = a.float_acc ? rf : (double)ri;
+  else if (out_dtype == VG_BOOL) *(uint8_t *)out = (a.float_acc ? rf : (double)ri) != 0;
+  else *(int64_t *)out = a.float_acc ? (int64_t)rf : ri;
+}
+
+}  // namespace
+}  // namespace vg
+
+using namespace vg;
+
+#define API_BEGIN try {
+#define API_END                       \
+  return VG_OK;                       \
+  }                                   \
+  catch (const Error &e) {            \
+    set_last_error(e.msg);            \
+    return e.code;                    \
+  }                                   \
+  catch (const std::exception &e) {   \
+    set_last_error(e.what());         \
+    return VG_ERR_ARG;                \
+  }
+
+namespace vg {
+void set_last_error(const std::string &m);
+}
+
+static Sim &S(vg_sim *s) {
+  if (!s || !s->s) fail(VG_ERR_ARG, "null simulation handle");
+  return *s->s;
+}
+
+extern "C" {
+
+const char *vg_transition_names(void) {
+  static std::string names;
+  if (names.empty())
+    for (auto &t : transitions()) {
+      if (!names.empty()) names += ",";
+      names += t.name;
+    }
+  return names.c_str();
+}
+
+int vg_apply(vg_sim *h, const char *tname, const int *call, int ncall, const int *read,
+             int nread, const int *write, int nwrite, const int *ae, int nae, int with_edge,
+             const double *params, int nparams) {
+  API_BEGIN
+  Sim &s = S(h);
+  if (!s.initialized) fail(VG_ERR_ASSERT, "You must call finish_init! before apply!");
+  const TransitionDef *def = nullptr;
+  for (auto &t : transitions())
+    if (std::strcmp(t.name, tname) == 0) def = &t;
+  if (!def) fail(VG_ERR_ARG, std::string("unknown transition ") + tname);
+  validate_refs(s, call, ncall);
+  validate_refs(s, read, nread);
+  validate_refs(s, write, nwrite);
+  validate_refs(s, ae, nae);
+  if (with_edge >= 0 && s.model->et(with_edge).singletype())
+    fail(VG_ERR_ASSERT, "The `with_edge` keyword can only be used for edgetypes without the "
+                        ":SingleType hint.");
+  ApplyCtx ctx;
+  ctx.sim = &s;
+  ctx.read.assign(read, read + nread);
+  ctx.write.assign(write, write + nwrite);
+  ctx.add_existing.assign(ae, ae + nae);
+  ctx.with_edge = with_edge;
+  ctx.params = params;
+  ctx.nparams = nparams;
+  ctx.step = s.num_transitions;
+  auto in = [](const std::vector<int> &v, int r) {
+    return std::find(v.begin(), v.end(), r) != v.end();
+  };
+  std::vector<int> C(call, call + ncall);
+  for (int c : C) {
+    if (is_edge_ref(c)) fail(VG_ERR_ARG, "call holds agent types only");
+    if (in(ctx.add_existing, c))
+      fail(VG_ERR_ASSERT, ref_name(s, c) + " can not be element of `add_existing`");
+  }
+  for (int a : ctx.add_existing)
+    if (!in(ctx.write, a))
+      fail(VG_ERR_ASSERT, ref_name(s, a) + " is in `add_existing` but not in `write`");
+
+  struct Flags {
+    Sim &s;
+    ~Flags() {
+      s.intransition = false;
+      for (auto &a : s.agents) a.readable = a.writeable = false;
+      for (auto &e : s.edges) e.readable = e.writeable = e.add_existing = false;
+    }
+  } flags{s};
+  s.intransition = true;
+  for (int r : ctx.read) {
+    if (is_edge_ref(r)) s.edges[edge_of(r)].readable = true;
+    else s.agents[r - 1].readable = true;
+  }
+  // prepare_write! (src/AgentMethods.jl:271-298, src/EdgeMethods.jl:639-663)
+  for (int w : ctx.write) {
+    if (is_edge_ref(w)) {
+      EdgeStore &es = s.edges[edge_of(w)];
+      if (es.implicit) fail(VG_ERR_ARG, "implicit raster edges are not written by transitions");
+      es.writeable = true;
+      es.add_existing = in(ctx.add_existing, w);
+      continue;
+    }
+    const AgentTypeDesc &ad = s.model->at(w);
+    bool aex = in(C, w) || in(ctx.add_existing, w);
+    if (ad.immortal() && !aex)
+      fail(VG_ERR_ASSERT, "You can add " + ad.name + " to the `write` argument only when " +
+                              ad.name + " is also included in the `add_existing` argument, as " +
+                              ad.name + " has the hint :Immortal.");
+    AgentStore &a = s.agents[w - 1];
+    if (!aex) {
+      a.n = 0;
+      a.nreuse = 0;
+      a.nliving = 0;
+    }
+    a.writeable = true;
+  }
+  // the sweep
+  for (int pos = 0; pos < (int)C.size(); pos++) {
+    ctx.call_type = C[pos];
+    ctx.call_pos = pos;
+    def->launch(ctx);
+  }
+  check_device_status(s, tname);
+
+  // finish_write! of the agent types (src/AgentMethods.jl:300-439)
+  std::vector<int> died_types;
+  for (int T : C) {
+    if (!in(ctx.write, T)) continue;
+    AgentStore &a = s.agents[T - 1];
+    const AgentTypeDesc &ad = s.model->at(T);
+    std::swap(a.rd, a.wr);
+    if (ad.immortal() || a.n == 0) continue;
+    std::swap(a.died_rd, a.died_wr);
+    // agents that died in this transition, in index order (writereuseable)
+    uint32_t *flag = nullptr, *pos = nullptr;
+    VG_CUDA(cudaMallocAsync((void **)&flag, (a.n + 1) * 4, s.stream));
+    VG_CUDA(cudaMallocAsync((void **)&pos, (a.n + 1) * 4, s.stream));
+    k_new_deaths<<<nblk(a.n), TPB, 0, s.stream>>>(a.died_rd.as<uint8_t>(),
+                                                   a.died_wr.as<uint8_t>(), a.n, flag);
+    VG_CUDA(cudaMemsetAsync(flag + a.n, 0, 4, s.stream));
+    exclusive_scan_u32(flag, pos, a.n + 1, s.stream, s);
+    uint32_t k = 0;
+    VG_CUDA(cudaMemcpyAsync(&k, pos + a.n, 4, cudaMemcpyDeviceToHost, s.stream));
+    VG_CUDA(cudaStreamSynchronize(s.stream));
+    if (k) {
+      if (a.nreuse + k > a.reuse_cap) {
+        uint64_t nc = std::max<uint64_t>(a.nreuse + k, 2 * a.reuse_cap);
+        DevBuf nb;
+        nb.alloc(nc * 8, &s.footprint);
+        if (a.nreuse)
+          VG_CUDA(cudaMemcpyAsync(nb.p, a.reuse.p, a.nreuse * 8, cudaMemcpyDeviceToDevice, s.stream));
+        a.reuse = std::move(nb);
+        a.reuse_cap = nc;
+      }
+      // readreuseable = [readreuseable; writereuseable]
+      k_push_reuse<<<nblk(a.n), TPB, 0, s.stream>>>(flag, pos, a.n, a.reuse.as<uint64_t>(), a.nreuse);
+      a.nreuse += k;
+      a.nliving -= std::min<uint64_t>(a.nliving, k);
+      died_types.push_back(T);
+    }
+    VG_CUDA(cudaFreeAsync(flag, s.stream));
+    VG_CUDA(cudaFreeAsync(pos, s.stream));
+  }
+  // edges of the written edge types: new container from the appended
+  // records (and the old edges with add_existing)
+  for (int w : ctx.write) {
+    if (!is_edge_ref(w)) continue;
+    int e = edge_of(w);
+    EdgeAppend *ap = nullptr;
+    for (auto &x : ctx.appends)
+      if (x->edge_type == e) ap = x.get();
+    uint64_t n = 0;
+    if (ap) {
+      if (ap->ordered) {
+        n = ap->fixed_count;
+      } else {
+        VG_CUDA(cudaMemcpyAsync(&n, ap->counter.p, 8, cudaMemcpyDeviceToHost, s.stream));
+        VG_CUDA(cudaStreamSynchronize(s.stream));
+      }
+      if (n > ap->cap) fail(VG_ERR_DEVICE, "edge append buffer overflow");
+    }
+    std::vector<const void *> pl;
+    if (ap)
+      for (auto &b : ap->payload) pl.push_back(b.p);
+    bool merge = s.edges[e].add_existing;
+    build_csr_from_records(s, e, ap ? ap->from.as<uint64_t>() : nullptr,
+                           ap ? ap->to.as<uint64_t>() : nullptr, pl, n,
+                           ap ? ap->ordered : true, ap ? ap->key.as<uint64_t>() : nullptr,
+                           merge);
+  }
+  // remove the edges of agents that died (src/AgentMethods.jl:314-345)
+  for (int T : died_types) {
+    AgentStore &a = s.agents[T - 1];
+    remove_died_edges(s, T, a.died_rd.as<uint8_t>(), a.n);
+  }
+  ctx.appends.clear();
+  s.num_transitions++;
+  API_END
+}
+
+int vg_mapreduce_agents(vg_sim *h, int nr, int field, int map_kind, double map_arg, int op,
+                        int out_dtype, int has_init, double init, void *out) {
+  API_BEGIN
+  Sim &s = S(h);
+  const AgentTypeDesc &ad = s.model->at(nr);
+  if (s.intransition && s.check_readable)
+    fail(VG_ERR_ASSERT, "You can not call mapreduce inside of a transition function.");
+  if (field < 0 || field >= (int)ad.fields.size()) fail(VG_ERR_ARG, "bad field");
+  bool ordered = (op & 0x100) != 0;
+  op &= 0xff;
+  if ((op == VG_OP_AND || op == VG_OP_OR) && (ad.fields[field].dtype == VG_F32 ||
+                                              ad.fields[field].dtype == VG_F64) &&
+      map_kind == VG_MAP_FIELD)
+    fail(VG_ERR_ASSERT, "The & operator is only supported for integer and boolean types");
+  AgentStore &a = s.agents[nr - 1];
+  RedArgs r{};
+  identity_for(op, out_dtype, has_init, init, &r.init_i, &r.init_f);
+  int dt = ad.fields[field].dtype;
+  r.float_acc = (map_kind == VG_MAP_FIELD && (dt == VG_F32 || dt == VG_F64)) || out_dtype == VG_F64;
+  if (!s.initialized) {
+    // staged agents on the host
+    uint64_t n = a.h_n;
+    int64_t ai = r.init_i;
+    double af = r.init_f;
+    size_t sz = ad.fields[field].size;
+    for (uint64_t i = 0; i < n; i++) {
+      double v;
+      int64_t iv;
+      const uint8_t *p = a.h_fields[field].data() + i * sz;
+      switch (dt) {
+        case VG_F64: v = *(const double *)p; iv = (int64_t)v; break;
+        case VG_F32: v = *(const float *)p; iv = (int64_t)v; break;
+        case VG_BOOL: case VG_U8: iv = *p; v = iv; break;
+        case VG_I32: iv = *(const int32_t *)p; v = iv; break;
+        case VG_U32: iv = *(const uint32_t *)p; v = iv; break;
+        case VG_I16: iv = *(const int16_t *)p; v = iv; break;
+        case VG_U16: iv = *(const uint16_t *)p; v = iv; break;
+        case VG_I8: iv = *(const int8_t *)p; v = iv; break;
+        default: iv = *(const int64_t *)p; v = (double)iv;
+      }
+      if (map_kind != VG_MAP_FIELD) {
+        bool b = false;
+        switch (map_kind) {
+          case VG_MAP_EQ: b = v == map_arg; break;
+          case VG_MAP_NE: b = v != map_arg; break;
+          case VG_MAP_LT: b = v < map_arg; break;
+          case VG_MAP_GT: b = v > map_arg; break;
+        }
+        iv = b;
+        v = b;
+      }
+      switch (op) {
+        case VG_OP_ADD: ai = (int64_t)((uint64_t)iv + (uint64_t)ai); af = v + af; break;
+        case VG_OP_MUL: ai = (int64_t)((uint64_t)iv * (uint64_t)ai); af = v * af; break;
+        case VG_OP_MAX: ai = std::max(iv, ai); af = std::fmax(v, af); break;
+        case VG_OP_MIN: ai = std::min(iv, ai); af = std::fmin(v, af); break;
+        case VG_OP_AND: ai = iv & ai; break;
+        case VG_OP_OR: ai = iv | ai; break;
+      }
+    }
+    if (out_dtype == VG_F64) *(double *)out = r.float_acc ? af : (double)ai;
+    else if (out_dtype == VG_BOOL) *(uint8_t *)out = (r.float_acc ? af : (double)ai) != 0;
+    else *(int64_t *)out = r.float_acc ? (int64_t)af : ai;
+    return VG_OK;
+  }
+  r.p = a.rd[field].p;
+  r.dt = dt;
+  r.n = a.n;
+  r.died = ad.immortal() ? nullptr : a.died_rd.as<uint8_t>();
+  r.kind = map_kind;
+  r.arg = map_arg;
+  r.op = op;
+  run_reduce(s, r, out_dtype, ordered, out);
+  API_END
+}
+
+int vg_mapreduce_edges(vg_sim *h, int e, int field, int map_kind, double map_arg, int op,
+                       int out_dtype, int has_init, double init, void *out) {
+  API_BEGIN
+  Sim &s = S(h);
+  const EdgeTypeDesc &ed = s.model->et(e);
+  if (ed.stateless())
+    fail(VG_ERR_ASSERT, "mapreduce is not defined for the hint combination of " + ed.name);
+  if (field < 0 || field >= (int)ed.fields.size()) fail(VG_ERR_ARG, "bad field");
+  bool ordered = (op & 0x100) != 0;
+  op &= 0xff;
+  RedArgs r{};
+  identity_for(op, out_dtype, has_init, init, &r.init_i, &r.init_f);
+  int dt = ed.fields[field].dtype;
+  r.float_acc = (map_kind == VG_MAP_FIELD && (dt == VG_F32 || dt == VG_F64)) || out_dtype == VG_F64;
+  if (!s.initialized) {
+    // Before finish_init! the reference reduces over the (empty) read
+    // container: the identity.
+    if (out_dtype == VG_F64) *(double *)out = r.float_acc ? r.init_f : (double)r.init_i;
+    else if (out_dtype == VG_BOOL) *(uint8_t *)out = r.init_i != 0;
+    else *(int64_t *)out = r.init_i;
+    return VG_OK;
+  }
+  EdgeStore &es = s.edges[e];
+  // fold over the CSR of every target type in (type, row, insertion) order
+  int64_t ai = r.init_i;
+  double af = r.init_f;
+  bool any = false;
+  for (int T = 1; T < (int)es.csr.size(); T++) {
+    CSR &c = es.csr[T];
+    if (!c.nedges) continue;
+    RedArgs q = r;
+    q.p = c.payload[field].p;
+    q.dt = dt;
+    q.n = c.nedges;
+    q.died = nullptr;
+    q.kind = map_kind;
+    q.arg = map_arg;
+    q.op = op;
+    q.init_i = ai;
+    q.init_f = af;
+    if (r.float_acc) {
+      double v;
+      run_reduce(s, q, VG_F64, ordered, &v);
+      af = v;
+    } else {
+      int64_t v;
+      run_reduce(s, q, VG_I64, ordered, &v);
+      ai = v;
+    }
+    any = true;
+  }
+  (void)any;
+  if (out_dtype == VG_F64) *(double *)out = r.float_acc ? af : (double)ai;
+  else if (out_dtype == VG_BOOL) *(uint8_t *)out = (r.float_acc ? af : (double)ai) != 0;
+  else *(int64_t *)out = r.float_acc ? (int64_t)af : ai;
+  API_END
+}
+
+}  // extern "C"

@@ -1,0 +1,501 @@
+// CSR construction and maintenance.
+//
+// build_csr_from_records rebuilds an edge type's containers from a batch of
+// edge records that are in Vahana's call order (or carry an order key):
+// the per-target order that results is the one `push!` produces in
+// add_edge! (src/EdgeMethods.jl:478-522).  With merge_existing the old
+// edges of a row come first, as with add_existing (src/EdgeMethods.jl:
+// 639-663, where the write container starts as a copy of the read one).
+//
+// remove_died_edges removes the edges of agents that died in a transition:
+// rows of died targets (_remove_edges_agent_target!, src/EdgeMethods.jl:
+// 897-920) and, for edge types that store the source, edges whose source
+// died (_remove_edges_agent_source!, :606-631).
+#include <algorithm>
+
+#include "vg_internal.h"
+
+namespace vg {
+
+namespace {
+
+constexpr int TPB = 256;
+inline unsigned nblk(uint64_t n, int tpb = TPB) {
+  uint64_t b = (n + tpb - 1) / tpb;
+  return (unsigned)std::max<uint64_t>(b, 1);
+}
+
+__global__ void k_type_hist(const uint64_t *to, const uint64_t *from, uint64_t n,
+                            unsigned long long *counts, unsigned *srcmask) {
+  __shared__ unsigned long long sc[MAX_AGENT_TYPES];
+  __shared__ unsigned sm;
+  if (threadIdx.x < MAX_AGENT_TYPES) sc[threadIdx.x] = 0;
+  if (threadIdx.x == 0) sm = 0;
+  __syncthreads();
+  unsigned mymask = 0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    unsigned t = (unsigned)(to[i] >> SHIFT_TYPE);
+    if (t < MAX_AGENT_TYPES) atomicAdd(&sc[t], 1ull);
+    if (from) {
+      unsigned f = (unsigned)(from[i] >> SHIFT_TYPE);
+      if (f < 32) mymask |= 1u << f;
+    }
+  }
+  if (mymask) atomicOr(&sm, mymask);
+  __syncthreads();
+  if (threadIdx.x < MAX_AGENT_TYPES && sc[threadIdx.x])
+    atomicAdd(&counts[threadIdx.x], sc[threadIdx.x]);
+  if (threadIdx.x == 0 && sm) atomicOr(srcmask, sm);
+}
+
+__global__ void k_iota(uint32_t *v, uint64_t n) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) v[i] = (uint32_t)i;
+}
+
+__global__ void k_copy_u64(const uint64_t *a, uint64_t *b, uint64_t n) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = a[i];
+}
+
+__global__ void k_flag_type(const uint64_t *to, const uint32_t *ord, uint64_t n,
+                            unsigned T, uint32_t *flags) {
+  uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n) flags[j] = ((unsigned)(to[ord[j]] >> SHIFT_TYPE) == T) ? 1u : 0u;
+}
+
+__global__ void k_compact_sel(const uint32_t *ord, const uint32_t *flags,
+                              const uint32_t *pos, uint64_t n, uint32_t *out) {
+  uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n && flags[j]) out[pos[j]] = ord[j];
+}
+
+__global__ void k_row_keys(const uint64_t *to, const uint32_t *sel, uint64_t m,
+                           uint64_t nrows, uint32_t *keys, uint32_t *vals,
+                           int *status) {
+  uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= m) return;
+  uint32_t r = sel[j];
+  uint64_t nr = to[r] & NR_MASK;
+  if (nr == 0 || nr > nrows) {
+    atomicExch(status, 101);  // edge to an agent number that does not exist
+    nr = 1;
+  }
+  keys[j] = (uint32_t)(nr - 1);
+  vals[j] = r;
+}
+
+__global__ void k_hist_rows(const uint32_t *keys, uint64_t m, uint32_t *cnt) {
+  uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < m) atomicAdd(&cnt[keys[j]], 1u);
+}
+
+__global__ void k_add_old_counts(const uint32_t *old_rp, uint64_t old_nrows,
+                                 const uint32_t *newcnt, uint32_t *tot,
+                                 uint32_t *oldcnt, uint64_t nrows) {
+  uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  uint32_t o = 0;
+  if (old_rp && r < old_nrows) o = old_rp[r + 1] - old_rp[r];
+  oldcnt[r] = o;
+  tot[r] = o + newcnt[r];
+}
+
+__global__ void k_clamp1(uint32_t *cnt, uint64_t nrows) {
+  uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < nrows && cnt[r] > 1) cnt[r] = 1;
+}
+
+__global__ void k_max_u32(const uint32_t *v, uint64_t n, unsigned *out) {
+  unsigned m = 0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    m = max(m, v[i]);
+  for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+// destination of old edge k: same offset inside its row of the new CSR
+__global__ void k_old_dest(const uint32_t *old_rp, uint64_t old_nrows,
+                           uint64_t old_ne, const uint32_t *new_rp,
+                           uint32_t *dest) {
+  uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= old_ne) return;
+  // binary search: last r with old_rp[r] <= k
+  uint64_t lo = 0, hi = old_nrows;  // old_rp[lo] <= k < old_rp[hi]
+  while (hi - lo > 1) {
+    uint64_t mid = (lo + hi) >> 1;
+    if (old_rp[mid] <= k) lo = mid; else hi = mid;
+  }
+  dest[k] = new_rp[lo] + (uint32_t)(k - old_rp[lo]);
+}
+
+__global__ void k_new_dest(const uint32_t *keys, uint64_t m,
+                           const uint32_t *new_rp, const uint32_t *oldcnt,
+                           const uint32_t *seg, uint32_t *dest, int dedupe) {
+  uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= m) return;
+  uint32_t r = keys[j];
+  uint32_t within = (uint32_t)j - seg[r];
+  if (dedupe && (within + oldcnt[r]) > 0) {
+    dest[j] = 0xffffffffu;  // HasEdgeOnly keeps a single `true`
+    return;
+  }
+  dest[j] = new_rp[r] + oldcnt[r] + within;
+}
+
+__global__ void k_place_src(const uint64_t *from, const uint32_t *rec,
+                            const uint32_t *dest, uint64_t m, uint32_t *src,
+                            uint8_t *src_type) {
+  uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= m || dest[j] == 0xffffffffu) return;
+  uint64_t f = from[rec[j]];
+  src[dest[j]] = (uint32_t)((f & NR_MASK) - 1);
+  if (src_type) src_type[dest[j]] = (uint8_t)(f >> SHIFT_TYPE);
+}
+
+template <class E>
+__global__ void k_scatter_col(const E *in, const uint32_t *rec,
+                              const uint32_t *dest, uint64_t m, E *out) {
+  uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= m || dest[j] == 0xffffffffu) return;
+  out[dest[j]] = rec ? in[rec[j]] : in[j];
+}
+
+__global__ void k_fill_u8(uint8_t *p, uint8_t v, const uint32_t *dest,
+                          uint64_t m) {
+  uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < m) p[dest ? dest[j] : j] = v;
+}
+
+void scatter_column(int esz, const void *in, const uint32_t *rec,
+                    const uint32_t *dest, uint64_t m, void *out,
+                    cudaStream_t st) {
+  if (m == 0) return;
+  switch (esz) {
+    case 1: k_scatter_col<uint8_t><<<nblk(m), TPB, 0, st>>>((const uint8_t *)in, rec, dest, m, (uint8_t *)out); break;
+    case 2: k_scatter_col<uint16_t><<<nblk(m), TPB, 0, st>>>((const uint16_t *)in, rec, dest, m, (uint16_t *)out); break;
+    case 4: k_scatter_col<uint32_t><<<nblk(m), TPB, 0, st>>>((const uint32_t *)in, rec, dest, m, (uint32_t *)out); break;
+    case 8: k_scatter_col<uint64_t><<<nblk(m), TPB, 0, st>>>((const uint64_t *)in, rec, dest, m, (uint64_t *)out); break;
+    default: fail(VG_ERR_ARG, "unsupported field size");
+  }
+  VG_CUDA(cudaGetLastError());
+}
+
+template <class T> struct Tmp {
+  T *p = nullptr;
+  cudaStream_t st;
+  Tmp(uint64_t n, cudaStream_t s) : st(s) {
+    VG_CUDA(cudaMallocAsync((void **)&p, std::max<uint64_t>(n, 1) * sizeof(T), st));
+  }
+  ~Tmp() { if (p) cudaFreeAsync(p, st); }
+};
+
+// ------------------------------------------------------ died-edge removal
+__global__ void k_keep_flags(const uint32_t *rp, uint64_t nrows,
+                             const uint32_t *src, const uint8_t *src_type,
+                             int src_type_const, const uint8_t *died,
+                             uint64_t died_n, int died_type, int target_is_died,
+                             int check_src, uint32_t *keep) {
+  uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  uint32_t b = rp[r], e = rp[r + 1];
+  bool tdead = target_is_died && r < died_n && died[r];
+  for (uint32_t k = b; k < e; k++) {
+    bool kp = !tdead;
+    if (kp && check_src) {
+      int t = src_type ? src_type[k] : src_type_const;
+      uint32_t sidx = src[k];
+      if (t == died_type && sidx < died_n && died[sidx]) kp = false;
+    }
+    keep[k] = kp ? 1u : 0u;
+  }
+}
+
+__global__ void k_new_rowptr(const uint32_t *rp, uint64_t nrows,
+                             const uint32_t *keep_scan, uint32_t *out) {
+  uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r <= nrows) out[r] = keep_scan[rp[r]];
+}
+
+__global__ void k_compact_dest(const uint32_t *keep, const uint32_t *scan,
+                               uint64_t n, uint32_t *dest) {
+  uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) dest[k] = keep[k] ? scan[k] : 0xffffffffu;
+}
+
+__global__ void k_hub_rows(const uint32_t *rp, uint64_t nrows, uint32_t thr,
+                           uint32_t *out, unsigned long long *cnt) {
+  uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  if (rp[r + 1] - rp[r] > thr) {
+    unsigned long long i = atomicAdd(cnt, 1ull);
+    out[i] = (uint32_t)r;
+  }
+}
+
+}  // namespace
+
+uint64_t csr_edges_total(const EdgeStore &es) {
+  uint64_t t = 0;
+  for (auto &c : es.csr) t += c.nedges;
+  return t;
+}
+
+void build_csr_from_records(Sim &s, int e, const uint64_t *d_from,
+                            const uint64_t *d_to,
+                            const std::vector<const void *> &d_payload,
+                            uint64_t n, bool records_sorted_by_key,
+                            const uint64_t *d_key, bool merge_existing) {
+  const EdgeTypeDesc &ed = s.model->et(e);
+  EdgeStore &es = s.edges[e];
+  cudaStream_t st = s.stream;
+  if (n >= (1ull << 31)) fail(VG_ERR_NOMEM, "more than 2^31 edge records in one build");
+
+  // 1. target types and source types of the records
+  unsigned long long h_counts[MAX_AGENT_TYPES] = {0};
+  unsigned h_srcmask = 0;
+  if (n > 0) {
+    Tmp<unsigned long long> counts(MAX_AGENT_TYPES + 1, st);
+    VG_CUDA(cudaMemsetAsync(counts.p, 0, (MAX_AGENT_TYPES + 1) * 8, st));
+    unsigned *d_mask = (unsigned *)(counts.p + MAX_AGENT_TYPES);
+    k_type_hist<<<std::min<unsigned>(nblk(n), 1024), TPB, 0, st>>>(
+        d_to, ed.stores_src() ? d_from : nullptr, n, counts.p, d_mask);
+    VG_CUDA(cudaGetLastError());
+    VG_CUDA(cudaMemcpyAsync(h_counts, counts.p, MAX_AGENT_TYPES * 8, cudaMemcpyDeviceToHost, st));
+    VG_CUDA(cudaMemcpyAsync(&h_srcmask, d_mask, 4, cudaMemcpyDeviceToHost, st));
+    VG_CUDA(cudaStreamSynchronize(st));
+  }
+  if (es.csr.size() < (size_t)MAX_AGENT_TYPES) es.csr.resize(MAX_AGENT_TYPES);
+  int ntypes_present = 0;
+  for (int T = 1; T < MAX_AGENT_TYPES; T++) ntypes_present += h_counts[T] > 0;
+  if (h_counts[0] > 0) fail(VG_ERR_ASSERT, "edge target is not a valid agent id");
+  for (int T = 1; T < MAX_AGENT_TYPES; T++) {
+    if (h_counts[T] == 0) continue;
+    if (T > (int)s.model->atypes.size())
+      fail(VG_ERR_ASSERT, "edge target has an unknown agent type");
+    if (ed.singletype() && T != ed.target)
+      fail(VG_ERR_ASSERT, "The :SingleType hint is set for " + ed.name +
+                              ", and the agent type is specified as " +
+                              s.model->at(ed.target).name +
+                              ". But the type for the given agent is " +
+                              s.model->at(T).name + ".");
+  }
+
+  // 2. order permutation of the records
+  Tmp<uint32_t> ord(n, st);
+  if (n > 0) {
+    k_iota<<<nblk(n), TPB, 0, st>>>(ord.p, n);
+    if (d_key && !records_sorted_by_key) {
+      Tmp<uint64_t> kk(n, st);
+      k_copy_u64<<<nblk(n), TPB, 0, st>>>(d_key, kk.p, n);
+      radix_sort_pairs_u64(kk.p, ord.p, n, 64, st, s);
+    }
+  }
+
+  // 3. per target type
+  for (int T = 1; T < MAX_AGENT_TYPES; T++) {
+    CSR &old = es.csr[T];
+    bool has_old = merge_existing && old.nedges + old.nrows > 0 && old.row_ptr.p;
+    if (h_counts[T] == 0 && !has_old) {
+      if (!merge_existing) es.csr[T] = CSR();
+      continue;
+    }
+    if (T > (int)s.model->atypes.size()) continue;
+    uint64_t nrows = s.agents[T - 1].n;
+    uint64_t m = h_counts[T];
+    // select the records of this target type in order
+    Tmp<uint32_t> sel(m, st);
+    const uint32_t *selp = ord.p;
+    if (m > 0 && ntypes_present > 1) {
+      Tmp<uint32_t> flags(n + 1, st), pos(n + 1, st);
+      k_flag_type<<<nblk(n), TPB, 0, st>>>(d_to, ord.p, n, (unsigned)T, flags.p);
+      exclusive_scan_u32(flags.p, pos.p, n, st, s);
+      k_compact_sel<<<nblk(n), TPB, 0, st>>>(ord.p, flags.p, pos.p, n, sel.p);
+      selp = sel.p;
+    }
+    Tmp<uint32_t> keys(m, st), rec(m, st);
+    Tmp<int> status(1, st);
+    VG_CUDA(cudaMemsetAsync(status.p, 0, 4, st));
+    if (m > 0) {
+      k_row_keys<<<nblk(m), TPB, 0, st>>>(d_to, selp, m, nrows, keys.p, rec.p, status.p);
+      radix_sort_pairs_u32(keys.p, rec.p, m, bits_for(nrows ? nrows - 1 : 0), st, s);
+    }
+    int h_status = 0;
+    VG_CUDA(cudaMemcpyAsync(&h_status, status.p, 4, cudaMemcpyDeviceToHost, st));
+    // counts
+    Tmp<uint32_t> newcnt(nrows + 1, st), oldcnt(nrows + 1, st),
+        tot(nrows + 1, st), seg(nrows + 1, st);
+    VG_CUDA(cudaMemsetAsync(newcnt.p, 0, (nrows + 1) * 4, st));
+    if (m > 0) k_hist_rows<<<nblk(m), TPB, 0, st>>>(keys.p, m, newcnt.p);
+    exclusive_scan_u32(newcnt.p, seg.p, nrows + 1, st, s);
+    k_add_old_counts<<<nblk(nrows + 1), TPB, 0, st>>>(
+        has_old ? old.row_ptr.as<uint32_t>() : nullptr, has_old ? old.nrows : 0,
+        newcnt.p, tot.p, oldcnt.p, nrows);
+    VG_CUDA(cudaMemsetAsync(tot.p + nrows, 0, 4, st));
+    VG_CUDA(cudaMemsetAsync(oldcnt.p + nrows, 0, 4, st));
+    bool dedupe = ed.bool_only();
+    if (dedupe) k_clamp1<<<nblk(nrows + 1), TPB, 0, st>>>(tot.p, nrows);
+    CSR c;
+    c.nrows = nrows;
+    c.row_ptr.alloc((nrows + 1) * 4, &s.footprint);
+    exclusive_scan_u32(tot.p, c.row_ptr.as<uint32_t>(), nrows + 1, st, s);
+    uint32_t h_total = 0;
+    VG_CUDA(cudaMemcpyAsync(&h_total, c.row_ptr.as<uint32_t>() + nrows, 4, cudaMemcpyDeviceToHost, st));
+    {
+      Tmp<unsigned> mx(1, st);
+      VG_CUDA(cudaMemsetAsync(mx.p, 0, 4, st));
+      k_max_u32<<<std::min<unsigned>(nblk(nrows), 1024), TPB, 0, st>>>(tot.p, nrows, mx.p);
+      VG_CUDA(cudaMemcpyAsync(&c.max_degree, mx.p, 4, cudaMemcpyDeviceToHost, st));
+    }
+    VG_CUDA(cudaStreamSynchronize(st));
+    if (h_status) fail(VG_ERR_ASSERT, "an edge targets an agent that does not exist");
+    if (ed.singleedge() && !dedupe && c.max_degree > 1)
+      fail(VG_ERR_ASSERT, "An edge has already been added to an agent of edge type " +
+                              ed.name + " (which has the :SingleEdge hint).");
+    c.nedges = h_total;
+    // source types
+    unsigned mask = 0;
+    if (ed.stores_src()) {
+      mask = m > 0 ? h_srcmask : 0;  // conservative: mask of all records
+      if (has_old) {
+        if (old.src_type_const > 0) mask |= 1u << old.src_type_const;
+        if (old.src_type_const < 0) mask |= 0xfffeu;  // mixed: keep mixed
+      }
+    }
+    int npop = __builtin_popcount(mask);
+    c.src_type_const = npop == 0 ? 0 : (npop == 1 ? __builtin_ctz(mask) : -1);
+    uint64_t ne = c.nedges;
+    if (ed.stores_src()) {
+      c.src.alloc(std::max<uint64_t>(ne, 1) * 4, &s.footprint);
+      if (c.src_type_const < 0) c.src_type.alloc(std::max<uint64_t>(ne, 1), &s.footprint);
+    }
+    int nf = ed.stores_payload() ? (int)ed.fields.size() : 0;
+    c.payload.resize(nf);
+    for (int f = 0; f < nf; f++)
+      c.payload[f].alloc(std::max<uint64_t>(ne, 1) * ed.fields[f].size, &s.footprint);
+    // old edges
+    if (has_old && old.nedges > 0) {
+      Tmp<uint32_t> dest(old.nedges, st);
+      k_old_dest<<<nblk(old.nedges), TPB, 0, st>>>(old.row_ptr.as<uint32_t>(), old.nrows,
+                                                   old.nedges, c.row_ptr.as<uint32_t>(), dest.p);
+      if (dedupe) {
+        // rows keep one entry; old rows already hold at most one
+      }
+      if (ed.stores_src()) {
+        scatter_column(4, old.src.p, nullptr, dest.p, old.nedges, c.src.p, st);
+        if (c.src_type_const < 0) {
+          if (old.src_type.p)
+            scatter_column(1, old.src_type.p, nullptr, dest.p, old.nedges, c.src_type.p, st);
+          else
+            k_fill_u8<<<nblk(old.nedges), TPB, 0, st>>>(c.src_type.as<uint8_t>(),
+                                                        (uint8_t)old.src_type_const, dest.p, old.nedges);
+        }
+      }
+      for (int f = 0; f < nf; f++)
+        scatter_column(ed.fields[f].size, old.payload[f].p, nullptr, dest.p, old.nedges,
+                       c.payload[f].p, st);
+    }
+    // new records
+    if (m > 0) {
+      Tmp<uint32_t> dest(m, st);
+      k_new_dest<<<nblk(m), TPB, 0, st>>>(keys.p, m, c.row_ptr.as<uint32_t>(), oldcnt.p,
+                                          seg.p, dest.p, dedupe ? 1 : 0);
+      if (ed.stores_src())
+        k_place_src<<<nblk(m), TPB, 0, st>>>(d_from, rec.p, dest.p, m, c.src.as<uint32_t>(),
+                                             c.src_type_const < 0 ? c.src_type.as<uint8_t>() : nullptr);
+      for (int f = 0; f < nf; f++)
+        scatter_column(ed.fields[f].size, d_payload[f], rec.p, dest.p, m, c.payload[f].p, st);
+    }
+    VG_CUDA(cudaGetLastError());
+    es.csr[T] = std::move(c);
+  }
+  VG_CUDA(cudaStreamSynchronize(st));
+}
+
+void remove_died_edges(Sim &s, int died_type, const uint8_t *died,
+                       uint64_t died_n) {
+  cudaStream_t st = s.stream;
+  for (size_t e = 0; e < s.edges.size(); e++) {
+    EdgeStore &es = s.edges[e];
+    const EdgeTypeDesc &ed = s.model->et((int)e);
+    if (es.implicit) continue;
+    for (int T = 1; T < (int)es.csr.size(); T++) {
+      CSR &c = es.csr[T];
+      if (c.nedges == 0) continue;
+      bool tgt = (T == died_type);
+      bool srcchk = ed.stores_src() &&
+                    (c.src_type_const == died_type || c.src_type_const < 0);
+      if (!tgt && !srcchk) continue;
+      uint64_t ne = c.nedges;
+      Tmp<uint32_t> keep(ne + 1, st), scan(ne + 1, st);
+      VG_CUDA(cudaMemsetAsync(keep.p + ne, 0, 4, st));
+      k_keep_flags<<<nblk(c.nrows), TPB, 0, st>>>(
+          c.row_ptr.as<uint32_t>(), c.nrows, c.src.as<uint32_t>(),
+          c.src_type.as<uint8_t>(), c.src_type_const, died, died_n, died_type,
+          tgt ? 1 : 0, srcchk ? 1 : 0, keep.p);
+      exclusive_scan_u32(keep.p, scan.p, ne + 1, st, s);
+      uint32_t newtotal = 0;
+      VG_CUDA(cudaMemcpyAsync(&newtotal, scan.p + ne, 4, cudaMemcpyDeviceToHost, st));
+      VG_CUDA(cudaStreamSynchronize(st));
+      if (newtotal == ne) continue;
+      CSR n2;
+      n2.nrows = c.nrows;
+      n2.nedges = newtotal;
+      n2.src_type_const = c.src_type_const;
+      n2.row_ptr.alloc((c.nrows + 1) * 4, &s.footprint);
+      k_new_rowptr<<<nblk(c.nrows + 1), TPB, 0, st>>>(c.row_ptr.as<uint32_t>(), c.nrows,
+                                                      scan.p, n2.row_ptr.as<uint32_t>());
+      Tmp<uint32_t> dest(ne, st);
+      k_compact_dest<<<nblk(ne), TPB, 0, st>>>(keep.p, scan.p, ne, dest.p);
+      uint64_t alloc_n = std::max<uint64_t>(newtotal, 1);
+      if (c.src.p) {
+        n2.src.alloc(alloc_n * 4, &s.footprint);
+        scatter_column(4, c.src.p, nullptr, dest.p, ne, n2.src.p, st);
+      }
+      if (c.src_type.p) {
+        n2.src_type.alloc(alloc_n, &s.footprint);
+        scatter_column(1, c.src_type.p, nullptr, dest.p, ne, n2.src_type.p, st);
+      }
+      n2.payload.resize(c.payload.size());
+      for (size_t f = 0; f < c.payload.size(); f++) {
+        n2.payload[f].alloc(alloc_n * ed.fields[f].size, &s.footprint);
+        scatter_column(ed.fields[f].size, c.payload[f].p, nullptr, dest.p, ne,
+                       n2.payload[f].p, st);
+      }
+      n2.max_degree = c.max_degree;
+      VG_CUDA(cudaStreamSynchronize(st));
+      c = std::move(n2);
+    }
+  }
+}
+
+void ensure_schedule(Sim &s, CSR &c, uint32_t thr) {
+  if (c.schedule_valid && c.hub_threshold == thr) return;
+  cudaStream_t st = s.stream;
+  c.hub_rows.release();
+  c.nhub = 0;
+  if (c.nrows > 0) {
+    Tmp<unsigned long long> cnt(1, st);
+    VG_CUDA(cudaMemsetAsync(cnt.p, 0, 8, st));
+    Tmp<uint32_t> tmp(c.nrows, st);
+    k_hub_rows<<<nblk(c.nrows), TPB, 0, st>>>(c.row_ptr.as<uint32_t>(), c.nrows, thr,
+                                              tmp.p, cnt.p);
+    unsigned long long h = 0;
+    VG_CUDA(cudaMemcpyAsync(&h, cnt.p, 8, cudaMemcpyDeviceToHost, st));
+    VG_CUDA(cudaStreamSynchronize(st));
+    c.nhub = h;
+    if (h) {
+      c.hub_rows.alloc(h * 4, &s.footprint);
+      VG_CUDA(cudaMemcpyAsync(c.hub_rows.p, tmp.p, h * 4, cudaMemcpyDeviceToDevice, st));
+      // process the largest hubs first: sort rows by descending degree is
+      // not needed for the result; keep discovery order
+    }
+    VG_CUDA(cudaStreamSynchronize(st));
+  }
+  c.hub_threshold = thr;
+  c.schedule_valid = true;
+}
+
+}  // namespace vg

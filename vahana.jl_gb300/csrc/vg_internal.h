@@ -1,0 +1,317 @@
+// Internal runtime structures of libvahana_gb300.
+//
+// Layout in HBM (one simulation):
+//   agent type T  : n slots (nextid-1); per field a read and a write column
+//                   (SoA, dtype-sized); died_rd/died_wr byte columns for
+//                   mortal types; a device stack of reusable agent numbers.
+//   edge type E   : per target agent type one CSR: row_ptr u32[n_T+1] over
+//                   target slots, src u32[E] (agent_nr-1 of the source),
+//                   src_type u8[E] only when sources have several types,
+//                   one column per payload field.  Edges of a row are in the
+//                   reference's insertion order.
+//   implicit raster edges keep no CSR: a stencil descriptor answers rows.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/vahana_gb300.h"
+
+namespace vg {
+
+constexpr int MAX_FIELDS = 8;
+constexpr int MAX_AGENT_TYPES = 16;  // type numbers 1..15
+constexpr int MAX_EDGE_TYPES = 64;
+constexpr int MAX_DIMS = 4;
+constexpr int SHIFT_TYPE = 56;   // src/Agent.jl:64 (BITS_PROCESS + BITS_AGENTNR)
+constexpr int SHIFT_RANK = 36;   // src/Agent.jl:65
+constexpr uint64_t NR_MASK = (1ull << 36) - 1;
+
+inline uint64_t make_id(int type_nr, uint64_t nr) {
+  return ((uint64_t)type_nr << SHIFT_TYPE) | nr;  // process bits stay 0
+}
+inline int id_type(uint64_t id) { return (int)(id >> SHIFT_TYPE); }
+inline uint64_t id_nr(uint64_t id) { return id & NR_MASK; }
+inline int id_process(uint64_t id) { return (int)((id >> SHIFT_RANK) & 0xFFFFF); }
+
+int dtype_size(int dt);
+
+struct Error {
+  int code;
+  std::string msg;
+};
+[[noreturn]] void fail(int code, const std::string &msg);
+void cuda_check(cudaError_t e, const char *what);
+#define VG_CUDA(x) ::vg::cuda_check((x), #x)
+#define VG_REQUIRE(cond, msg) \
+  do {                        \
+    if (!(cond)) ::vg::fail(VG_ERR_ASSERT, (msg)); \
+  } while (0)
+
+// ---------------------------------------------------------------- buffers
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  uint64_t *footprint = nullptr;  // owning simulation's byte counter
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  DevBuf(DevBuf &&o) noexcept { *this = std::move(o); }
+  DevBuf &operator=(DevBuf &&o) noexcept;
+  ~DevBuf() { release(); }
+  void alloc(size_t b, uint64_t *fp);
+  void release();
+  template <class T> T *as() const { return (T *)p; }
+};
+
+// ---------------------------------------------------------------- model
+struct FieldDesc {
+  std::string name;
+  int dtype;
+  int size;
+};
+
+struct AgentTypeDesc {
+  std::string name;
+  std::vector<FieldDesc> fields;
+  unsigned hints = 0;
+  int nr = 0;
+  bool immortal() const { return hints & VG_HINT_IMMORTAL; }
+  bool independent() const { return hints & VG_HINT_INDEPENDENT; }
+  int field_index(const std::string &n) const;
+};
+
+struct EdgeTypeDesc {
+  std::string name;
+  std::vector<FieldDesc> fields;
+  unsigned hints = 0;  // normalised (NumEdgesOnly / HasEdgeOnly expanded)
+  int target = 0;      // :SingleType target type number
+  int64_t size = 0;
+  int idx = 0;
+  bool stateless() const { return hints & VG_HINT_STATELESS; }
+  bool ignorefrom() const { return hints & VG_HINT_IGNOREFROM; }
+  bool singletype() const { return hints & VG_HINT_SINGLETYPE; }
+  bool singleedge() const { return hints & VG_HINT_SINGLEEDGE; }
+  bool stores_src() const { return !ignorefrom(); }
+  bool stores_payload() const { return !stateless() && !fields.empty(); }
+  bool count_only() const { return stateless() && ignorefrom() && !singleedge(); }
+  bool bool_only() const { return stateless() && ignorefrom() && singleedge(); }
+  int field_index(const std::string &n) const;
+};
+
+struct Model {
+  std::string name;
+  std::vector<AgentTypeDesc> atypes;  // index = nr - 1
+  std::vector<EdgeTypeDesc> etypes;   // index = edge type index
+  std::vector<std::pair<std::string, double>> params, globals;
+  bool finalized = false;
+  bool all_immortal() const {
+    for (auto &a : atypes)
+      if (!a.immortal()) return false;
+    return true;
+  }
+  const AgentTypeDesc &at(int nr) const;
+  const EdgeTypeDesc &et(int e) const;
+};
+
+// ---------------------------------------------------------------- state
+struct AgentStore {
+  uint64_t n = 0;    // slots in use = nextid - 1 (src/AgentMethods.jl:37-63)
+  uint64_t cap = 0;  // allocated slots
+  std::vector<DevBuf> rd, wr;
+  DevBuf died_rd, died_wr;  // mortal types only
+  DevBuf reuse;             // u64 agent numbers, LIFO (readreuseable)
+  uint64_t nreuse = 0, reuse_cap = 0;
+  uint64_t nliving = 0;     // cached count of living agents
+  // staging before finish_init!
+  std::vector<std::vector<uint8_t>> h_fields;
+  uint64_t h_n = 0;
+  bool readable = false, writeable = false;
+};
+
+struct CSR {
+  uint64_t nrows = 0, nedges = 0;
+  DevBuf row_ptr;  // u32[nrows + 1]
+  DevBuf src;      // u32[nedges] source agent_nr - 1
+  DevBuf src_type; // u8[nedges] when src_type_const < 0
+  int src_type_const = 0;  // >0 all sources of that type, 0 none, -1 mixed
+  std::vector<DevBuf> payload;
+  uint32_t max_degree = 0;
+  // derived schedule of the degree-bucketed gather kernels (hub rows)
+  DevBuf hub_rows;  // u32 rows with degree above the hub threshold
+  uint64_t nhub = 0;
+  uint32_t hub_threshold = 0;
+  bool schedule_valid = false;
+};
+
+struct StencilDesc {
+  int raster = -1;         // index into Sim::rasters
+  int ndims = 0;
+  int64_t dims[MAX_DIMS] = {0, 0, 0, 0};
+  int noff = 0;
+  std::vector<int> offsets;  // noff * ndims, in the reference's order
+  int periodic = 1;
+  int target_type = 0;
+  std::vector<uint8_t> payload;  // constant payload of every stencil edge
+};
+
+// A contiguous run of staged edges (before finish_init!, or added between
+// transitions with the checks disabled).  Either host or device resident.
+struct EdgeSegment {
+  bool device = false;
+  uint64_t n = 0;
+  std::vector<uint64_t> h_from, h_to;
+  std::vector<std::vector<uint8_t>> h_payload;
+  DevBuf d_from, d_to;
+  std::vector<DevBuf> d_payload;
+};
+
+struct EdgeStore {
+  std::vector<CSR> csr;  // index = target type number (0 unused)
+  bool implicit = false;
+  StencilDesc st;
+  std::vector<EdgeSegment> staged;  // pending adds in call order
+  uint64_t nstaged = 0;
+  // single-edge bookkeeping of staged host adds (target -> slot)
+  std::map<uint64_t, uint64_t> single_seen;
+  bool readable = false, writeable = false, add_existing = false;
+};
+
+struct Raster {
+  std::string name;
+  int ndims = 0;
+  int64_t dims[MAX_DIMS] = {0, 0, 0, 0};
+  int type_nr = 0;
+  uint64_t first_nr = 0;  // agent_nr of the cell at linear index 0
+  uint64_t ncells = 0;
+};
+
+struct Sim {
+  std::shared_ptr<Model> model;
+  std::string name;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  bool initialized = false;
+  bool intransition = false;
+  bool check_readable = true;
+  int64_t num_transitions = 0;
+  uint64_t footprint = 0;
+  std::vector<AgentStore> agents;  // index = nr - 1
+  std::vector<EdgeStore> edges;    // index = edge type index
+  std::vector<Raster> rasters;
+  std::map<std::string, double> params, globals;
+  std::map<std::string, std::vector<double>> global_series;
+  // scratch
+  DevBuf d_status;  // int32 device error word
+  DevBuf d_scratch;
+  size_t scratch_bytes = 0;
+  void *scratch(size_t bytes);
+  int raster_index(const std::string &n) const;
+  // stream and status word are created on first device use, so that the
+  // init phase (registry, staging) runs without a GPU
+  bool device_ready = false;
+  void ensure_device();
+};
+
+// ---------------------------------------------------------------- kernels
+// Views passed to kernels by value.
+struct DevAgentView {
+  uint64_t n;
+  void *rd[MAX_FIELDS];
+  void *wr[MAX_FIELDS];
+  uint8_t *died_rd;
+  uint8_t *died_wr;
+};
+struct DevCSRView {
+  uint64_t nrows, nedges;
+  const uint32_t *row_ptr;
+  const uint32_t *src;
+  const uint8_t *src_type;
+  int src_type_const;
+  const void *payload[MAX_FIELDS];
+};
+
+DevAgentView agent_view(Sim &s, int type_nr);
+DevCSRView csr_view(Sim &s, int edge_type, int target_type_nr);
+
+struct EdgeAppend {
+  int edge_type = -1;
+  uint64_t cap = 0;
+  DevBuf to, from, key;  // u64 target id, u64 source id, u64 order key
+  std::vector<DevBuf> payload;
+  DevBuf counter;  // u64 device counter
+  bool ordered = false;  // records already in order-key order
+  uint64_t fixed_count = 0;  // when the count is known on the host
+};
+
+// Apply context handed to a transition launcher.
+struct ApplyCtx {
+  Sim *sim;
+  int call_type;  // agent type number being swept
+  int call_pos;   // position in `call`
+  std::vector<int> read, write, add_existing;
+  int with_edge;
+  const double *params;
+  int nparams;
+  int64_t step;  // num_transitions at the start of apply!
+  bool in_read(int ref) const;
+  bool in_write(int ref) const;
+  bool writes_call() const;
+  double param(int i, double dflt) const {
+    return i < nparams ? params[i] : dflt;
+  }
+  // edge records appended by the launchers, per written edge type
+  std::vector<std::unique_ptr<EdgeAppend>> appends;
+  EdgeAppend *append_for(int edge_type, uint64_t capacity, bool ordered);
+};
+
+
+typedef void (*TransitionLauncher)(ApplyCtx &ctx);
+struct TransitionDef {
+  const char *name;
+  TransitionLauncher launch;
+};
+const std::vector<TransitionDef> &transitions();
+
+// primitives (vg_sort.cu)
+void exclusive_scan_u32(const uint32_t *in, uint32_t *out, uint64_t n,
+                        cudaStream_t st, Sim &s);
+void exclusive_scan_u64(const uint64_t *in, uint64_t *out, uint64_t n,
+                        cudaStream_t st, Sim &s);
+// stable LSD radix sort of (key, value) pairs over key bits [0, bits)
+void radix_sort_pairs_u32(uint32_t *keys, uint32_t *vals, uint64_t n,
+                          int bits, cudaStream_t st, Sim &s);
+void radix_sort_pairs_u64(uint64_t *keys, uint32_t *vals, uint64_t n,
+                          int bits, cudaStream_t st, Sim &s);
+int bits_for(uint64_t maxval);
+
+// graph building (vg_graph.cu)
+void build_csr_from_records(Sim &s, int edge_type, const uint64_t *d_from,
+                            const uint64_t *d_to,
+                            const std::vector<const void *> &d_payload,
+                            uint64_t n, bool records_sorted_by_key,
+                            const uint64_t *d_key, bool merge_existing);
+void remove_died_edges(Sim &s, int died_type, const uint8_t *died_now,
+                       uint64_t n_died);
+void ensure_schedule(Sim &s, CSR &c, uint32_t hub_threshold);
+uint64_t csr_edges_total(const EdgeStore &es);
+
+// agents (vg_api.cu)
+void agent_reserve(Sim &s, int type_nr, uint64_t slots);
+void apply_finish_agents(Sim &s, int type_nr, bool swapped);
+
+// misc
+void check_device_status(Sim &s, const char *what);
+
+}  // namespace vg
+
+struct vg_model {
+  std::shared_ptr<vg::Model> m;
+};
+struct vg_sim {
+  std::unique_ptr<vg::Sim> s;
+};

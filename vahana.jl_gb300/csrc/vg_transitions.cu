@@ -1,0 +1,905 @@
+// Transition kernels bound by name (the `f` of apply!, src/Simulation.jl:
+// 720-821).  Every kernel sweeps the agents of the called type in index
+// order semantics (transition_with_read!, src/AgentMethods.jl:193-207):
+// died agents are skipped, a returned state is written to the write buffer
+// (transition_with_write!, :159-181) and `nothing` marks the agent died.
+//
+// Floating-point arithmetic on the ordered paths uses explicitly rounded
+// intrinsics (__dadd_rn, __dmul_rn, __ddiv_rn) in the reference's
+// left-to-right order, so results are bit-identical to the sequential CPU
+// fold (the library is also compiled with -fmad=false).
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "vg_internal.h"
+#include "vg_philox.cuh"
+
+namespace vg {
+
+namespace {
+
+constexpr int TPB = 256;
+inline unsigned nblk(uint64_t n, int tpb = TPB) {
+  uint64_t b = (n + tpb - 1) / tpb;
+  return (unsigned)std::max<uint64_t>(b, 1);
+}
+
+__device__ __forceinline__ void set_status(int *st, int code) {
+  atomicCAS(st, 0, code);
+}
+
+// ----------------------------------------------------------- field access
+__device__ __forceinline__ int64_t ld_i64(const void *p, int dt, uint64_t i) {
+  switch (dt) {
+    case VG_BOOL: case VG_U8: return ((const uint8_t *)p)[i];
+    case VG_I8: return ((const int8_t *)p)[i];
+    case VG_U16: return ((const uint16_t *)p)[i];
+    case VG_I16: return ((const int16_t *)p)[i];
+    case VG_U32: return ((const uint32_t *)p)[i];
+    case VG_I32: return ((const int32_t *)p)[i];
+    case VG_U64: case VG_I64: return ((const int64_t *)p)[i];
+    case VG_F32: return (int64_t)((const float *)p)[i];
+    case VG_F64: return (int64_t)((const double *)p)[i];
+  }
+  return 0;
+}
+__device__ __forceinline__ double ld_f64(const void *p, int dt, uint64_t i) {
+  switch (dt) {
+    case VG_F32: return (double)((const float *)p)[i];
+    case VG_F64: return ((const double *)p)[i];
+    case VG_U64: return (double)((const uint64_t *)p)[i];
+  }
+  return (double)ld_i64(p, dt, i);
+}
+__device__ __forceinline__ void st_i64(void *p, int dt, uint64_t i, int64_t v) {
+  switch (dt) {
+    case VG_BOOL: ((uint8_t *)p)[i] = v != 0; break;
+    case VG_U8: case VG_I8: ((uint8_t *)p)[i] = (uint8_t)v; break;
+    case VG_U16: case VG_I16: ((uint16_t *)p)[i] = (uint16_t)v; break;
+    case VG_U32: case VG_I32: ((uint32_t *)p)[i] = (uint32_t)v; break;
+    case VG_U64: case VG_I64: ((int64_t *)p)[i] = v; break;
+    case VG_F32: ((float *)p)[i] = (float)v; break;
+    case VG_F64: ((double *)p)[i] = (double)v; break;
+  }
+}
+__device__ __forceinline__ void st_f64(void *p, int dt, uint64_t i, double v) {
+  switch (dt) {
+    case VG_F32: ((float *)p)[i] = (float)v; break;
+    case VG_F64: ((double *)p)[i] = v; break;
+    default: st_i64(p, dt, i, (int64_t)v);
+  }
+}
+__device__ __forceinline__ bool is_float(int dt) { return dt == VG_F32 || dt == VG_F64; }
+
+// ------------------------------------------------------------ sweep frame
+struct Sweep {
+  DevAgentView a;
+  int nfields;
+  int fsize[MAX_FIELDS];
+  int fdt[MAX_FIELDS];
+  int mortal;
+  int writes;              // the called type is in `write`
+  const uint32_t *with_rp; // with_edge: row_ptr of that edge type, or null
+  uint64_t with_nrows;
+  int type_nr;
+  int *status;
+};
+
+__device__ void sw_copy(const Sweep &s, uint64_t i) {
+  for (int f = 0; f < s.nfields; f++) {
+    switch (s.fsize[f]) {
+      case 1: ((uint8_t *)s.a.wr[f])[i] = ((const uint8_t *)s.a.rd[f])[i]; break;
+      case 2: ((uint16_t *)s.a.wr[f])[i] = ((const uint16_t *)s.a.rd[f])[i]; break;
+      case 4: ((uint32_t *)s.a.wr[f])[i] = ((const uint32_t *)s.a.rd[f])[i]; break;
+      case 8: ((uint64_t *)s.a.wr[f])[i] = ((const uint64_t *)s.a.rd[f])[i]; break;
+    }
+  }
+  if (s.mortal) s.a.died_wr[i] = 0;
+}
+
+// Returns true when agent i is swept.  Died agents stay died; with_edge
+// restricts the sweep to targets of that edge type (src/AgentMethods.jl:
+// 209-229), the others keep their state.
+__device__ __forceinline__ bool sw_begin(const Sweep &s, uint64_t i) {
+  if (s.mortal && s.a.died_rd[i]) {
+    if (s.writes) s.a.died_wr[i] = 1;
+    return false;
+  }
+  if (s.with_rp) {
+    bool has = i < s.with_nrows && s.with_rp[i + 1] > s.with_rp[i];
+    if (!has) {
+      if (s.writes) sw_copy(s, i);
+      return false;
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void sw_die(const Sweep &s, uint64_t i) {
+  if (!s.mortal) {
+    set_status(s.status, 201);  // `nothing` returned for an immortal agent
+    sw_copy(s, i);
+    return;
+  }
+  s.a.died_wr[i] = 1;
+}
+
+// source field of every agent type (flexible neighbour states)
+struct SrcTable {
+  const void *ptr[MAX_AGENT_TYPES];
+  int dt[MAX_AGENT_TYPES];
+  const uint8_t *died[MAX_AGENT_TYPES];
+};
+
+__device__ __forceinline__ int edge_src_type(const DevCSRView &c, uint64_t k) {
+  return c.src_type ? (int)c.src_type[k] : c.src_type_const;
+}
+
+// --------------------------------------------------- generic neighbour ops
+// mode 0: dst = sum of the neighbours' field (neighbor_sum)
+// mode 1: dst = own dst || any neighbour field != 0 (neighbor_or)
+// mode 2: dst = number of edges (count_edges)
+__global__ void k_neighbor_op(Sweep s, DevCSRView c, SrcTable t, int dst,
+                              int mode) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s.a.n || !sw_begin(s, i)) return;
+  int ddt = s.fdt[dst];
+  int64_t si = 0;
+  double sf = 0.0;
+  bool anyv = false;
+  uint32_t b = 0, e = 0;
+  if (i < c.nrows) {
+    b = c.row_ptr[i];
+    e = c.row_ptr[i + 1];
+  }
+  for (uint32_t k = b; k < e && mode != 2; k++) {
+    int ty = edge_src_type(c, k);
+    uint32_t j = c.src[k];
+    if (ty <= 0 || ty >= MAX_AGENT_TYPES || !t.ptr[ty]) {
+      set_status(s.status, 202);  // source type not readable
+      continue;
+    }
+    if (t.died[ty] && t.died[ty][j]) set_status(s.status, 203);
+    if (mode == 0) {
+      if (is_float(ddt)) sf = __dadd_rn(sf, ld_f64(t.ptr[ty], t.dt[ty], j));
+      else si = (int64_t)((uint64_t)si + (uint64_t)ld_i64(t.ptr[ty], t.dt[ty], j));
+    } else {
+      anyv |= ld_i64(t.ptr[ty], t.dt[ty], j) != 0;
+    }
+  }
+  if (!s.writes) return;
+  sw_copy(s, i);
+  if (mode == 0) {
+    if (is_float(ddt)) st_f64(s.a.wr[dst], ddt, i, sf);
+    else st_i64(s.a.wr[dst], ddt, i, si);
+  } else if (mode == 1) {
+    bool own = ld_i64(s.a.rd[dst], ddt, i) != 0;
+    st_i64(s.a.wr[dst], ddt, i, (own || anyv) ? 1 : 0);
+  } else {
+    st_i64(s.a.wr[dst], ddt, i, (int64_t)(e - b));
+  }
+}
+
+// die_if: kind 0 always; 1 field >= arg; 2 field % arg != 0; 3 the agent has
+// no edge of the given edge type (num_edges == 0)
+__global__ void k_die_if(Sweep s, int kind, int field, double arg,
+                         const uint32_t *rp2, uint64_t nrows2) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s.a.n || !sw_begin(s, i)) return;
+  bool die = false;
+  if (kind == 0) die = true;
+  else if (kind == 1) die = ld_f64(s.a.rd[field], s.fdt[field], i) >= arg;
+  else if (kind == 2) die = (ld_i64(s.a.rd[field], s.fdt[field], i) % (int64_t)arg) != 0;
+  else if (kind == 3) die = !(rp2 && i < nrows2 && rp2[i + 1] > rp2[i]);
+  if (!s.writes) return;
+  if (die) sw_die(s, i);
+  else sw_copy(s, i);
+}
+
+// set_field: kind 0 constant; 1 (agent id mod 2 == 1)
+__global__ void k_set_field(Sweep s, int field, int kind, double value) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s.a.n || !sw_begin(s, i)) return;
+  if (!s.writes) return;
+  sw_copy(s, i);
+  int dt = s.fdt[field];
+  if (kind == 0) {
+    if (is_float(dt)) st_f64(s.a.wr[field], dt, i, value);
+    else st_i64(s.a.wr[field], dt, i, (int64_t)value);
+  } else {
+    uint64_t id = ((uint64_t)s.type_nr << SHIFT_TYPE) | (i + 1);
+    st_i64(s.a.wr[field], dt, i, (id % 2) == 1 ? 1 : 0);
+  }
+}
+
+__global__ void k_keep(Sweep s) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s.a.n || !sw_begin(s, i)) return;
+  if (s.writes) sw_copy(s, i);
+}
+
+// edge appends with an order key (call position, caller index, sequence):
+// the order in which the reference's sequential sweep calls add_edge!.
+struct Append {
+  uint64_t *to, *from, *key;
+  void *payload[MAX_FIELDS];
+  int psize[MAX_FIELDS];
+  int npayload;
+  unsigned long long *counter;
+  uint64_t cap;
+};
+
+__device__ __forceinline__ uint64_t order_key(int call_pos, uint64_t i,
+                                              uint32_t seq) {
+  return ((uint64_t)call_pos << 60) | ((i & ((1ull << 40) - 1)) << 20) | seq;
+}
+
+__device__ __forceinline__ int64_t append_slot(const Append &ap, int *status) {
+  unsigned long long k = atomicAdd(ap.counter, 1ull);
+  if (k >= ap.cap) {
+    set_status(status, 301);  // append buffer overflow
+    return -1;
+  }
+  return (int64_t)k;
+}
+
+// add_edge!(sim, id, id, state) for every swept agent
+__global__ void k_self_edge(Sweep s, Append ap, int call_pos, const uint8_t *pl) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s.a.n || !sw_begin(s, i)) return;
+  if (s.writes) sw_copy(s, i);
+  int64_t k = append_slot(ap, s.status);
+  if (k < 0) return;
+  uint64_t id = ((uint64_t)s.type_nr << SHIFT_TYPE) | (i + 1);
+  ap.to[k] = id;
+  ap.from[k] = id;
+  ap.key[k] = order_key(call_pos, i, 0);
+  int off = 0;
+  for (int f = 0; f < ap.npayload; f++) {
+    for (int b = 0; b < ap.psize[f]; b++)
+      ((uint8_t *)ap.payload[f])[k * ap.psize[f] + b] = pl[off + b];
+    off += ap.psize[f];
+  }
+}
+
+// add_edges!(sim, id, edges(sim, id, ET)): re-add every in-edge of the agent
+__global__ void k_readd_edges(Sweep s, DevCSRView c, Append ap, int call_pos) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s.a.n || !sw_begin(s, i)) return;
+  if (s.writes) sw_copy(s, i);
+  if (i >= c.nrows) return;
+  uint64_t id = ((uint64_t)s.type_nr << SHIFT_TYPE) | (i + 1);
+  for (uint32_t e = c.row_ptr[i], q = 0; e < c.row_ptr[i + 1]; e++, q++) {
+    int64_t k = append_slot(ap, s.status);
+    if (k < 0) return;
+    ap.to[k] = id;
+    ap.from[k] = ((uint64_t)edge_src_type(c, e) << SHIFT_TYPE) | ((uint64_t)c.src[e] + 1);
+    ap.key[k] = order_key(call_pos, i, q);
+    for (int f = 0; f < ap.npayload; f++) {
+      int sz = ap.psize[f];
+      for (int b = 0; b < sz; b++)
+        ((uint8_t *)ap.payload[f])[k * sz + b] = ((const uint8_t *)c.payload[f])[(uint64_t)e * sz + b];
+    }
+  }
+}
+
+// ---------------------------------------------------------- SIR (cfg 0)
+// Person{state::UInt8 (0 S, 1 I, 2 R), days::Int32}.  A susceptible agent
+// with k infected in-neighbours is infected with p_k = 1 - (1 - beta)^k
+// (p_k from the host table, built by the same repeated multiplication);
+// an infected agent recovers when days reaches `recovery`.
+__global__ void k_sir(const uint32_t *__restrict__ rp, const uint32_t *__restrict__ src,
+                      const uint8_t *__restrict__ st_rd, const int32_t *__restrict__ d_rd,
+                      uint8_t *__restrict__ st_wr, int32_t *__restrict__ d_wr, uint64_t n,
+                      uint64_t nrows, const double *__restrict__ ptab, uint32_t ptab_n,
+                      uint64_t seed, uint32_t step, int32_t recovery, int *status) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint8_t s = st_rd[i];
+  int32_t d = d_rd[i];
+  if (s == 0) {
+    uint32_t k = 0;
+    if (i < nrows) {
+      uint32_t e = rp[i + 1];
+      for (uint32_t q = rp[i]; q < e; q++) k += (__ldg(st_rd + src[q]) == 1);
+    }
+    if (k > 0) {
+      if (k >= ptab_n) {
+        set_status(status, 401);
+      } else {
+        double u = u64_to_unit(philox_u64(philox_draw(seed, i + 1, step, TAG_INFECT)));
+        if (u < ptab[k]) {
+          s = 1;
+          d = 0;
+        }
+      }
+    }
+  } else if (s == 1) {
+    d = d + 1;
+    if (d >= recovery) s = 2;
+  }
+  st_wr[i] = s;
+  d_wr[i] = d;
+}
+
+// ------------------------------------------- bounded confidence (cfg 1)
+// Opinion x (f64), in-edges with weight w (f64).  Sequential over the
+// in-edges in insertion order: neighbours with |x_j - x| < eps contribute
+// w_j to sw and w_j * x_j to swx; x' = a x + b (swx / sw), or x when none
+// qualify.  Degree-bucketed: rows above the hub threshold are processed by
+// one warp each (lanes load and multiply in parallel, lane 0 folds in
+// order), the first blocks of the grid take the hubs so they start first;
+// the other rows are processed by one thread each.
+struct OpinionArgs {
+  const uint32_t *__restrict__ rp;
+  const uint32_t *__restrict__ src;
+  const double *__restrict__ w;
+  const double *__restrict__ x;
+  double *__restrict__ xo;
+  uint64_t n, nrows;
+  const uint32_t *__restrict__ hub_rows;
+  uint64_t nhub;
+  uint32_t hub_thr;
+  unsigned hub_blocks;
+  double eps, a, b;
+};
+
+__device__ __forceinline__ double opinion_finish(const OpinionArgs &p, double xi,
+                                                 double sw, double swx, uint32_t cnt) {
+  return cnt ? __dadd_rn(__dmul_rn(p.a, xi), __dmul_rn(p.b, __ddiv_rn(swx, sw))) : xi;
+}
+
+__global__ void __launch_bounds__(TPB) k_opinion(OpinionArgs p) {
+  if (blockIdx.x < p.hub_blocks) {
+    const int lane = threadIdx.x & 31;
+    uint64_t h = (uint64_t)blockIdx.x * (TPB / 32) + (threadIdx.x >> 5);
+    if (h >= p.nhub) return;
+    uint32_t r = p.hub_rows[h];
+    double xi = p.x[r];
+    double sw = 0.0, swx = 0.0;
+    uint32_t cnt = 0;
+    uint32_t b = p.rp[r], e = p.rp[r + 1];
+    for (uint32_t base = b; base < e; base += 32) {
+      uint32_t k = base + lane;
+      bool q = false;
+      double wk = 0.0, pk = 0.0;
+      if (k < e) {
+        double xj = __ldg(p.x + p.src[k]);
+        q = fabs(__dsub_rn(xj, xi)) < p.eps;
+        wk = p.w[k];
+        pk = __dmul_rn(wk, xj);
+      }
+      unsigned qm = __ballot_sync(0xffffffffu, q);
+      int m = (int)min(32u, e - base);
+      for (int l = 0; l < m; l++) {
+        double wl = __shfl_sync(0xffffffffu, wk, l);
+        double pl = __shfl_sync(0xffffffffu, pk, l);
+        if ((qm >> l) & 1u) {
+          sw = __dadd_rn(sw, wl);
+          swx = __dadd_rn(swx, pl);
+          cnt++;
+        }
+      }
+    }
+    if (lane == 0) p.xo[r] = opinion_finish(p, xi, sw, swx, cnt);
+    return;
+  }
+  uint64_t i = (uint64_t)(blockIdx.x - p.hub_blocks) * TPB + threadIdx.x;
+  if (i >= p.n) return;
+  double xi = p.x[i];
+  if (i >= p.nrows) {
+    p.xo[i] = xi;
+    return;
+  }
+  uint32_t b = p.rp[i], e = p.rp[i + 1];
+  if (e - b > p.hub_thr) return;  // handled by a hub warp
+  double sw = 0.0, swx = 0.0;
+  uint32_t cnt = 0;
+  for (uint32_t k = b; k < e; k++) {
+    double xj = __ldg(p.x + __ldg(p.src + k));
+    if (fabs(__dsub_rn(xj, xi)) < p.eps) {
+      double wk = __ldg(p.w + k);
+      sw = __dadd_rn(sw, wk);
+      swx = __dadd_rn(swx, __dmul_rn(wk, xj));
+      cnt++;
+    }
+  }
+  p.xo[i] = opinion_finish(p, xi, sw, swx, cnt);
+}
+
+// ------------------------------------------------ Life B3/S23 (cfg 2)
+// Cells of a 2-D raster, implicit Moore stencil (chebyshev, distance 1).
+// The count of alive neighbours does not depend on edge order.
+__global__ void k_life2d(const uint8_t *__restrict__ a, uint8_t *__restrict__ o,
+                         int64_t W, int64_t H, int periodic) {
+  int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t y = (int64_t)blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= W || y >= H) return;
+  int cnt = 0;
+#pragma unroll
+  for (int dy = -1; dy <= 1; dy++) {
+    int64_t yy = y + dy;
+    if (yy < 0 || yy >= H) {
+      if (!periodic) continue;
+      yy = (yy + H) % H;
+    }
+#pragma unroll
+    for (int dx = -1; dx <= 1; dx++) {
+      if (!dx && !dy) continue;
+      int64_t xx = x + dx;
+      if (xx < 0 || xx >= W) {
+        if (!periodic) continue;
+        xx = (xx + W) % W;
+      }
+      cnt += __ldg(a + yy * W + xx);
+    }
+  }
+  uint8_t alive = a[y * W + x];
+  o[y * W + x] = (cnt == 3 || (alive && cnt == 2)) ? 1 : 0;
+}
+
+// general implicit stencil (any dims, offsets): count of alive sources
+struct StencilArgs {
+  int ndims;
+  int64_t dims[MAX_DIMS];
+  int noff;
+  int8_t off[128 * MAX_DIMS];
+  int periodic;
+};
+
+__global__ void k_life_stencil(const uint8_t *__restrict__ a, uint8_t *__restrict__ o,
+                               uint64_t ncells, StencilArgs st, int birth_mask,
+                               int survive_mask) {
+  uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  int64_t pos[MAX_DIMS];
+  uint64_t t = c;
+  for (int i = 0; i < st.ndims; i++) {
+    pos[i] = (int64_t)(t % st.dims[i]);
+    t /= st.dims[i];
+  }
+  int cnt = 0;
+  for (int k = 0; k < st.noff; k++) {
+    uint64_t lin = 0, m = 1;
+    bool ok = true;
+    for (int i = 0; i < st.ndims; i++) {
+      int64_t q = pos[i] - st.off[k * st.ndims + i];
+      if (q < 0 || q >= st.dims[i]) {
+        if (!st.periodic) { ok = false; break; }
+        q = ((q % st.dims[i]) + st.dims[i]) % st.dims[i];
+      }
+      lin += (uint64_t)q * m;
+      m *= st.dims[i];
+    }
+    if (ok) cnt += a[lin];
+  }
+  uint8_t alive = a[c];
+  int bit = cnt < 31 ? (1 << cnt) : 0;
+  o[c] = alive ? ((survive_mask & bit) ? 1 : 0) : ((birth_mask & bit) ? 1 : 0);
+}
+
+// ------------------------------------------------- random walk (cfg 2)
+// Walker{x::Int32, y::Int32} (1-based cell position).  Each step a walker
+// moves by one of the 8 Moore offsets, drawn by Philox, wraps (mod1) and
+// calls move_to!(sim, raster, id, (x', y'), nothing, OnCell()): one edge
+// walker -> cell.  Record i belongs to walker i, so records come out in the
+// reference's sweep order without atomics.
+__global__ void k_random_walk(const int32_t *__restrict__ x, const int32_t *__restrict__ y,
+                              int32_t *__restrict__ xo, int32_t *__restrict__ yo, uint64_t n,
+                              int64_t W, int64_t H, uint64_t seed, uint32_t step,
+                              uint64_t *__restrict__ to, uint64_t *__restrict__ from,
+                              int walker_type, int cell_type, uint64_t cell_first_nr) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  Philox4 r = philox_draw(seed, i + 1, step, TAG_MOVE);
+  uint32_t k = bounded32(r.v[0], 8);
+  // Moore offsets in stencil order (first dimension fastest, centre removed)
+  uint32_t m = k < 4 ? k : k + 1;
+  int64_t nx = (int64_t)x[i] + (int)(m % 3) - 1;
+  int64_t ny = (int64_t)y[i] + (int)(m / 3) - 1;
+  nx = ((nx - 1) % W + W) % W + 1;
+  ny = ((ny - 1) % H + H) % H + 1;
+  xo[i] = (int32_t)nx;
+  yo[i] = (int32_t)ny;
+  from[i] = ((uint64_t)walker_type << SHIFT_TYPE) | (i + 1);
+  to[i] = ((uint64_t)cell_type << SHIFT_TYPE) |
+          (cell_first_nr + (uint64_t)(nx - 1) + (uint64_t)(ny - 1) * (uint64_t)W);
+}
+
+// ------------------------------------------------------------- launchers
+Sweep make_sweep(ApplyCtx &c) {
+  Sim &s = *c.sim;
+  const AgentTypeDesc &ad = s.model->at(c.call_type);
+  Sweep w{};
+  w.a = agent_view(s, c.call_type);
+  w.nfields = (int)ad.fields.size();
+  for (int f = 0; f < w.nfields; f++) {
+    w.fsize[f] = ad.fields[f].size;
+    w.fdt[f] = ad.fields[f].dtype;
+  }
+  w.mortal = !ad.immortal();
+  w.writes = c.writes_call() ? 1 : 0;
+  w.type_nr = c.call_type;
+  w.status = s.d_status.as<int>();
+  if (c.with_edge >= 0) {
+    EdgeStore &es = s.edges[c.with_edge];
+    if (c.call_type < (int)es.csr.size() && es.csr[c.call_type].row_ptr.p) {
+      w.with_rp = es.csr[c.call_type].row_ptr.as<uint32_t>();
+      w.with_nrows = es.csr[c.call_type].nrows;
+    } else {
+      // no agent of this type is the target of such an edge: with_nrows = 0
+      // makes every row empty (the pointer is never dereferenced)
+      w.with_rp = (const uint32_t *)s.d_status.p;
+      w.with_nrows = 0;
+    }
+  }
+  return w;
+}
+
+int need_edge_param(ApplyCtx &c, int idx) {
+  Sim &s = *c.sim;
+  if (idx >= c.nparams) fail(VG_ERR_ARG, "transition parameter missing: edge type");
+  int e = (int)c.params[idx];
+  s.model->et(e);
+  return e;
+}
+
+void require_read(ApplyCtx &c, int ref, const std::string &what) {
+  if (!c.in_read(ref) && c.sim->check_readable) fail(VG_ERR_ASSERT, what);
+}
+
+void require_edge_read(ApplyCtx &c, int e) {
+  require_read(c, VG_EDGE(e),
+               "You try to access an edge of type " + c.sim->model->et(e).name +
+                   " but the type is not in the `read` argument of the apply! function.");
+}
+
+void require_agent_read(ApplyCtx &c, int T) {
+  require_read(c, T, c.sim->model->at(T).name +
+                         " must be in the `read` argument of the transition function.");
+}
+
+// the source types present in a CSR must be readable
+void require_sources_read(ApplyCtx &c, int e, int T) {
+  Sim &s = *c.sim;
+  EdgeStore &es = s.edges[e];
+  if (T >= (int)es.csr.size()) return;
+  CSR &cs = es.csr[T];
+  if (cs.nedges == 0) return;
+  std::vector<int> types;
+  if (cs.src_type_const > 0) {
+    types.push_back(cs.src_type_const);
+  } else if (cs.src_type_const < 0) {
+    std::vector<uint8_t> st(cs.nedges);
+    VG_CUDA(cudaMemcpyAsync(st.data(), cs.src_type.p, cs.nedges, cudaMemcpyDeviceToHost, s.stream));
+    VG_CUDA(cudaStreamSynchronize(s.stream));
+    bool seen[256] = {false};
+    for (auto t : st) seen[t] = true;
+    for (int t = 1; t < 256; t++)
+      if (seen[t]) types.push_back(t);
+  }
+  for (int t : types) require_agent_read(c, t);
+}
+
+SrcTable make_src_table(ApplyCtx &c, int field_index) {
+  Sim &s = *c.sim;
+  SrcTable t{};
+  for (int T = 1; T <= (int)s.model->atypes.size() && T < MAX_AGENT_TYPES; T++) {
+    const AgentTypeDesc &ad = s.model->at(T);
+    if (field_index < (int)ad.fields.size() && !s.agents[T - 1].rd.empty()) {
+      t.ptr[T] = s.agents[T - 1].rd[field_index].p;
+      t.dt[T] = ad.fields[field_index].dtype;
+    }
+    t.died[T] = ad.immortal() ? nullptr : s.agents[T - 1].died_rd.as<uint8_t>();
+  }
+  return t;
+}
+
+void launch_neighbor_op(ApplyCtx &c, int mode) {
+  Sim &s = *c.sim;
+  int e = need_edge_param(c, 0);
+  int sf = (int)c.param(1, 0), df = (int)c.param(2, 0);
+  const AgentTypeDesc &ad = s.model->at(c.call_type);
+  if (df < 0 || df >= (int)ad.fields.size()) fail(VG_ERR_ARG, "destination field out of range");
+  require_edge_read(c, e);
+  if (mode != 2) require_sources_read(c, e, c.call_type);
+  Sweep w = make_sweep(c);
+  DevCSRView v = csr_view(s, e, c.call_type);
+  SrcTable t = make_src_table(c, sf);
+  if (w.a.n == 0) return;
+  k_neighbor_op<<<nblk(w.a.n), TPB, 0, s.stream>>>(w, v, t, df, mode);
+  VG_CUDA(cudaGetLastError());
+}
+
+void tr_neighbor_sum(ApplyCtx &c) { launch_neighbor_op(c, 0); }
+void tr_neighbor_or(ApplyCtx &c) { launch_neighbor_op(c, 1); }
+void tr_count_edges(ApplyCtx &c) { launch_neighbor_op(c, 2); }
+
+void tr_die_if(ApplyCtx &c) {
+  Sim &s = *c.sim;
+  int kind = (int)c.param(0, 0);
+  int field = (int)c.param(1, 0);
+  double arg = c.param(2, 0);
+  const uint32_t *rp2 = nullptr;
+  uint64_t n2 = 0;
+  if (kind == 3) {
+    int e = field;
+    s.model->et(e);
+    require_edge_read(c, e);
+    DevCSRView v = csr_view(s, e, c.call_type);
+    rp2 = v.row_ptr;
+    n2 = v.nrows;
+    field = 0;
+  } else if (kind == 1 || kind == 2) {
+    if (field < 0 || field >= (int)s.model->at(c.call_type).fields.size())
+      fail(VG_ERR_ARG, "field out of range");
+    require_agent_read(c, c.call_type);
+  }
+  Sweep w = make_sweep(c);
+  if (w.a.n == 0) return;
+  k_die_if<<<nblk(w.a.n), TPB, 0, s.stream>>>(w, kind, field, arg, rp2, n2);
+  VG_CUDA(cudaGetLastError());
+}
+
+void tr_set_field(ApplyCtx &c) {
+  Sim &s = *c.sim;
+  int field = (int)c.param(0, 0);
+  if (field < 0 || field >= (int)s.model->at(c.call_type).fields.size())
+    fail(VG_ERR_ARG, "field out of range");
+  Sweep w = make_sweep(c);
+  if (w.a.n == 0) return;
+  k_set_field<<<nblk(w.a.n), TPB, 0, s.stream>>>(w, field, (int)c.param(1, 0), c.param(2, 0));
+  VG_CUDA(cudaGetLastError());
+}
+
+void tr_keep(ApplyCtx &c) {
+  Sim &s = *c.sim;
+  Sweep w = make_sweep(c);
+  if (w.a.n == 0) return;
+  k_keep<<<nblk(w.a.n), TPB, 0, s.stream>>>(w);
+  VG_CUDA(cudaGetLastError());
+}
+
+Append make_append(ApplyCtx &c, int e, uint64_t cap) {
+  Sim &s = *c.sim;
+  const EdgeTypeDesc &ed = s.model->et(e);
+  if (!c.in_write(VG_EDGE(e)) && s.check_readable)
+    fail(VG_ERR_ASSERT, ed.name + " must be in the `write` argument of the transition function.");
+  EdgeAppend *a = c.append_for(e, cap, false);
+  Append ap{};
+  ap.to = a->to.as<uint64_t>();
+  ap.from = a->from.as<uint64_t>();
+  ap.key = a->key.as<uint64_t>();
+  ap.npayload = (int)a->payload.size();
+  for (int f = 0; f < ap.npayload; f++) {
+    ap.payload[f] = a->payload[f].p;
+    ap.psize[f] = ed.fields[f].size;
+  }
+  ap.counter = a->counter.as<unsigned long long>();
+  ap.cap = a->cap;
+  return ap;
+}
+
+void tr_self_edge(ApplyCtx &c) {
+  Sim &s = *c.sim;
+  int e = need_edge_param(c, 0);
+  const EdgeTypeDesc &ed = s.model->et(e);
+  Sweep w = make_sweep(c);
+  if (w.a.n == 0) return;
+  Append ap = make_append(c, e, w.a.n);
+  // constant payload from params[1..]: one value per field
+  std::vector<uint8_t> pl;
+  if (ed.stores_payload())
+    for (size_t f = 0; f < ed.fields.size(); f++) {
+      double v = c.param(1 + (int)f, 0);
+      uint8_t buf[8] = {0};
+      int dt = ed.fields[f].dtype;
+      if (dt == VG_F64) std::memcpy(buf, &v, 8);
+      else if (dt == VG_F32) { float x = (float)v; std::memcpy(buf, &x, 4); }
+      else { int64_t x = (int64_t)v; std::memcpy(buf, &x, 8); }
+      pl.insert(pl.end(), buf, buf + ed.fields[f].size);
+    }
+  uint8_t *d_pl = (uint8_t *)s.scratch(std::max<size_t>(pl.size(), 8));
+  if (!pl.empty())
+    VG_CUDA(cudaMemcpyAsync(d_pl, pl.data(), pl.size(), cudaMemcpyHostToDevice, s.stream));
+  k_self_edge<<<nblk(w.a.n), TPB, 0, s.stream>>>(w, ap, c.call_pos, d_pl);
+  VG_CUDA(cudaGetLastError());
+  VG_CUDA(cudaStreamSynchronize(s.stream));
+}
+
+void tr_readd_edges(ApplyCtx &c) {
+  Sim &s = *c.sim;
+  int e = need_edge_param(c, 0);
+  const EdgeTypeDesc &ed = s.model->et(e);
+  if (ed.stateless() || ed.ignorefrom())
+    fail(VG_ERR_ASSERT, "edges is not defined for the hint combination of " + ed.name);
+  require_edge_read(c, e);
+  Sweep w = make_sweep(c);
+  DevCSRView v = csr_view(s, e, c.call_type);
+  if (w.a.n == 0) return;
+  Append ap = make_append(c, e, std::max<uint64_t>(v.nedges, 1));
+  k_readd_edges<<<nblk(w.a.n), TPB, 0, s.stream>>>(w, v, ap, c.call_pos);
+  VG_CUDA(cudaGetLastError());
+}
+
+void tr_sir(ApplyCtx &c) {
+  Sim &s = *c.sim;
+  const AgentTypeDesc &ad = s.model->at(c.call_type);
+  if (ad.fields.size() < 2 || ad.fields[0].dtype != VG_U8 || ad.fields[1].dtype != VG_I32)
+    fail(VG_ERR_ARG, "sir: agent type needs fields (state::UInt8, days::Int32)");
+  if (!ad.immortal()) fail(VG_ERR_ARG, "sir: Person is :Immortal");
+  int e = need_edge_param(c, 0);
+  double beta = c.param(1, 0.05);
+  int32_t rec = (int32_t)c.param(2, 7);
+  uint64_t seed = (uint64_t)c.param(3, 0);
+  require_edge_read(c, e);
+  require_agent_read(c, c.call_type);
+  if (!c.writes_call()) fail(VG_ERR_ARG, "sir: the called type must be in `write`");
+  EdgeStore &es = s.edges[e];
+  DevCSRView v = csr_view(s, e, c.call_type);
+  if (v.nedges && v.src_type_const != c.call_type)
+    fail(VG_ERR_ARG, "sir: contact sources must be of the called type");
+  uint32_t maxdeg = c.call_type < (int)es.csr.size() ? es.csr[c.call_type].max_degree : 0;
+  // p_k = 1 - q^k by repeated multiplication, k = 0..maxdeg
+  std::vector<double> ptab(maxdeg + 1);
+  double q = 1.0, om = 1.0 - beta;
+  ptab[0] = 0.0;
+  for (uint32_t k = 1; k <= maxdeg; k++) {
+    q = q * om;
+    ptab[k] = 1.0 - q;
+  }
+  double *d_ptab = (double *)s.scratch(ptab.size() * 8);
+  VG_CUDA(cudaMemcpyAsync(d_ptab, ptab.data(), ptab.size() * 8, cudaMemcpyHostToDevice, s.stream));
+  DevAgentView a = agent_view(s, c.call_type);
+  if (a.n == 0) return;
+  k_sir<<<nblk(a.n), TPB, 0, s.stream>>>(v.row_ptr, v.src, (const uint8_t *)a.rd[0],
+                                         (const int32_t *)a.rd[1], (uint8_t *)a.wr[0],
+                                         (int32_t *)a.wr[1], a.n, v.nrows, d_ptab,
+                                         (uint32_t)ptab.size(), seed, (uint32_t)c.step, rec,
+                                         s.d_status.as<int>());
+  VG_CUDA(cudaGetLastError());
+}
+
+void tr_bounded_confidence(ApplyCtx &c) {
+  Sim &s = *c.sim;
+  const AgentTypeDesc &ad = s.model->at(c.call_type);
+  if (ad.fields.empty() || ad.fields[0].dtype != VG_F64)
+    fail(VG_ERR_ARG, "bounded_confidence: agent field 0 must be Float64");
+  if (!ad.immortal()) fail(VG_ERR_ARG, "bounded_confidence: the opinion type is :Immortal");
+  int e = need_edge_param(c, 0);
+  const EdgeTypeDesc &ed = s.model->et(e);
+  if (!ed.stores_payload() || ed.fields[0].dtype != VG_F64 || !ed.stores_src())
+    fail(VG_ERR_ARG, "bounded_confidence: edges need a source and a Float64 weight");
+  require_edge_read(c, e);
+  require_agent_read(c, c.call_type);
+  if (!c.writes_call()) fail(VG_ERR_ARG, "bounded_confidence: the called type must be in `write`");
+  double eps = c.param(1, 0.3);
+  double a = c.param(2, 0.5);
+  double b = c.nparams > 3 ? c.params[3] : 1.0 - a;
+  uint32_t thr = (uint32_t)c.param(4, 256);
+  EdgeStore &es = s.edges[e];
+  DevCSRView v = csr_view(s, e, c.call_type);
+  if (v.nedges && v.src_type_const != c.call_type)
+    fail(VG_ERR_ARG, "bounded_confidence: sources must be of the called type");
+  DevAgentView av = agent_view(s, c.call_type);
+  if (av.n == 0) return;
+  OpinionArgs p{};
+  p.rp = v.row_ptr;
+  p.src = v.src;
+  p.w = (const double *)v.payload[0];
+  p.x = (const double *)av.rd[0];
+  p.xo = (double *)av.wr[0];
+  p.n = av.n;
+  p.nrows = v.nrows;
+  p.eps = eps;
+  p.a = a;
+  p.b = b;
+  p.hub_thr = 0xffffffffu;
+  if (v.nedges && c.call_type < (int)es.csr.size()) {
+    CSR &cs = es.csr[c.call_type];
+    ensure_schedule(s, cs, thr);
+    p.hub_rows = cs.hub_rows.as<uint32_t>();
+    p.nhub = cs.nhub;
+    p.hub_thr = thr;
+    p.hub_blocks = (unsigned)((cs.nhub + (TPB / 32) - 1) / (TPB / 32));
+  }
+  unsigned grid = p.hub_blocks + nblk(av.n);
+  k_opinion<<<grid, TPB, 0, s.stream>>>(p);
+  VG_CUDA(cudaGetLastError());
+}
+
+void tr_life(ApplyCtx &c) {
+  Sim &s = *c.sim;
+  const AgentTypeDesc &ad = s.model->at(c.call_type);
+  if (ad.fields.empty() || (ad.fields[0].dtype != VG_BOOL && ad.fields[0].dtype != VG_U8))
+    fail(VG_ERR_ARG, "life: cell field 0 must be Bool");
+  int e = need_edge_param(c, 0);
+  EdgeStore &es = s.edges[e];
+  if (!es.implicit) fail(VG_ERR_ARG, "life: the neighbour edges must be implicit raster edges");
+  require_edge_read(c, e);
+  require_agent_read(c, c.call_type);
+  if (!c.writes_call()) fail(VG_ERR_ARG, "life: the called type must be in `write`");
+  const StencilDesc &st = es.st;
+  const Raster &R = s.rasters[st.raster];
+  if (R.type_nr != c.call_type) fail(VG_ERR_ARG, "life: raster cells must be the called type");
+  AgentStore &A = s.agents[c.call_type - 1];
+  if (R.first_nr != 1 || R.ncells != A.n)
+    fail(VG_ERR_ARG, "life: the raster must hold all agents of its type");
+  const uint8_t *in = A.rd[0].as<uint8_t>();
+  uint8_t *out = A.wr[0].as<uint8_t>();
+  int birth = (int)c.param(1, 8), survive = (int)c.param(2, 12);  // B3 = 1<<3, S23 = 1<<2|1<<3
+  bool moore2d = st.ndims == 2 && st.noff == 8 && birth == 8 && survive == 12;
+  if (moore2d) {
+    for (int k = 0; k < 8; k++) {
+      int ox = st.offsets[2 * k], oy = st.offsets[2 * k + 1];
+      if (std::abs(ox) > 1 || std::abs(oy) > 1) moore2d = false;
+    }
+  }
+  if (moore2d) {
+    dim3 blk(32, 8);
+    dim3 grd((unsigned)((st.dims[0] + 31) / 32), (unsigned)((st.dims[1] + 7) / 8));
+    k_life2d<<<grd, blk, 0, s.stream>>>(in, out, st.dims[0], st.dims[1], st.periodic);
+  } else {
+    if (st.noff > 128) fail(VG_ERR_ARG, "life: at most 128 stencil offsets");
+    StencilArgs sa{};
+    sa.ndims = st.ndims;
+    for (int i = 0; i < st.ndims; i++) sa.dims[i] = st.dims[i];
+    sa.noff = st.noff;
+    for (int k = 0; k < st.noff * st.ndims; k++) sa.off[k] = (int8_t)st.offsets[k];
+    sa.periodic = st.periodic;
+    k_life_stencil<<<nblk(R.ncells), TPB, 0, s.stream>>>(in, out, R.ncells, sa, birth, survive);
+  }
+  VG_CUDA(cudaGetLastError());
+}
+
+void tr_random_walk(ApplyCtx &c) {
+  Sim &s = *c.sim;
+  const AgentTypeDesc &ad = s.model->at(c.call_type);
+  if (ad.fields.size() < 2 || ad.fields[0].dtype != VG_I32 || ad.fields[1].dtype != VG_I32)
+    fail(VG_ERR_ARG, "random_walk: walker fields (x::Int32, y::Int32)");
+  if (!ad.immortal()) fail(VG_ERR_ARG, "random_walk: walkers are :Immortal");
+  int e = need_edge_param(c, 0);
+  int ri = (int)c.param(1, 0);
+  uint64_t seed = (uint64_t)c.param(2, 0);
+  if (ri < 0 || ri >= (int)s.rasters.size()) fail(VG_ERR_ARG, "random_walk: raster index");
+  const Raster &R = s.rasters[ri];
+  if (R.ndims != 2) fail(VG_ERR_ARG, "random_walk: 2-D raster");
+  const EdgeTypeDesc &ed = s.model->et(e);
+  if (ed.stores_payload()) fail(VG_ERR_ARG, "random_walk: OnCell edges are stateless");
+  if (!c.writes_call()) fail(VG_ERR_ARG, "random_walk: the called type must be in `write`");
+  if (!c.in_write(VG_EDGE(e)))
+    fail(VG_ERR_ASSERT, ed.name + " must be in the `write` argument of the transition function.");
+  require_agent_read(c, c.call_type);
+  DevAgentView a = agent_view(s, c.call_type);
+  if (a.n == 0) return;
+  EdgeAppend *ap = c.append_for(e, a.n, true);
+  ap->fixed_count = a.n;
+  k_random_walk<<<nblk(a.n), TPB, 0, s.stream>>>(
+      (const int32_t *)a.rd[0], (const int32_t *)a.rd[1], (int32_t *)a.wr[0],
+      (int32_t *)a.wr[1], a.n, R.dims[0], R.dims[1], seed, (uint32_t)c.step,
+      ap->to.as<uint64_t>(), ap->from.as<uint64_t>(), c.call_type, R.type_nr, R.first_nr);
+  VG_CUDA(cudaGetLastError());
+}
+
+}  // namespace
+
+const std::vector<TransitionDef> &transitions() {
+  static const std::vector<TransitionDef> defs = {
+      {"bounded_confidence", tr_bounded_confidence},
+      {"sir", tr_sir},
+      {"life", tr_life},
+      {"random_walk", tr_random_walk},
+      {"neighbor_sum", tr_neighbor_sum},
+      {"neighbor_or", tr_neighbor_or},
+      {"count_edges", tr_count_edges},
+      {"die_if", tr_die_if},
+      {"set_field", tr_set_field},
+      {"keep", tr_keep},
+      {"self_edge", tr_self_edge},
+      {"readd_edges", tr_readd_edges},
+  };
+  return defs;
+}
+
+}  // namespace vg

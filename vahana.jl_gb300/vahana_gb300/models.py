@@ -1,0 +1,164 @@
+"""The three test models of the transition step, written against the API.
+
+Each builder returns a `Run` with the simulation, its types and a `step()`
+that performs one model step (one or more apply! calls).  Initial states are
+drawn with Philox4x32-10 on the host; graphs come from the device
+generators (the add_edge! loops of the model scripts).
+
+  sir:      Person{state::UInt8, days::Int32} (:Immortal), Contact
+            (:Stateless, :SingleType target=Person); k uniform out-edges per
+            agent; transition "sir".
+  opinion:  Opinion{x::Float64} (:Immortal), Weight{w::Float64}
+            (:SingleType target=Opinion); directed Chung-Lu graph;
+            transition "bounded_confidence".
+  life:     Cell{alive::Bool} raster with implicit Moore edges (Neighbor),
+            Walker{x::Int32, y::Int32} moving by Philox Moore offsets and
+            rebuilding walker -> cell edges (OnCell, :Stateless, :SingleType
+            target=Cell) every step; transitions "life" and "random_walk".
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import api, philox
+from ._lib import check, lib
+
+
+class Run:
+    def __init__(self, sim, **kw):
+        self.sim = sim
+        self.__dict__.update(kw)
+
+    def close(self):
+        self.sim.close()
+
+
+# ------------------------------------------------------------------- SIR
+def sir_model(name="SIR"):
+    return (api.ModelTypes()
+            .register_agenttype("Person", [("state", "u8"), ("days", "i32")], ":Immortal")
+            .register_edgetype("Contact", [], ":Stateless", target="Person")
+            .create_model(name))
+
+
+def sir_initial_state(n, seed, n_infected=None):
+    """0.1 % of the agents (the n_infected with the smallest init draw, ties
+    by index) start infected with days = 0."""
+    if n_infected is None:
+        n_infected = max(1, int(round(n / 1000)))
+    d = philox.to_u64(philox.draw(seed, np.arange(1, n + 1, dtype=np.uint64), 0, philox.TAG_INIT))
+    order = np.lexsort((np.arange(n), d))
+    state = np.zeros(n, dtype=np.uint8)
+    state[order[:n_infected]] = 1
+    return state, np.zeros(n, dtype=np.int32)
+
+
+def build_sir(n=100_000, degree=10, beta=0.05, recovery=7, seed=1, stream=None,
+              n_infected=None):
+    model = sir_model()
+    sim = api.create_simulation(model, stream=stream)
+    state, days = sir_initial_state(n, seed, n_infected)
+    ids = api.add_agents(sim, "Person", n, state=state, days=days)
+    check(lib().vg_gen_uniform_out_edges(sim._h, model["Contact"].index, model["Person"].index,
+                                         int(degree), int(seed)))
+    run = Run(sim, model=model, ids=ids, beta=beta, recovery=recovery, seed=seed, n=n,
+              degree=degree)
+
+    def step():
+        api.apply_(sim, "sir", ["Person"], ["Person", "Contact"], ["Person"],
+                   params=[model["Contact"].index, beta, recovery, seed])
+    run.step = step
+    run.edges_per_step = lambda: n * degree
+    return run
+
+
+# ---------------------------------------------------------------- opinion
+def opinion_model(name="Opinion"):
+    return (api.ModelTypes()
+            .register_agenttype("Opinion", [("x", "f64")], ":Immortal")
+            .register_edgetype("Weight", [("w", "f64")], target="Opinion")
+            .create_model(name))
+
+
+def opinion_initial_state(n, seed):
+    return philox.unit(philox.to_u64(philox.draw(seed, np.arange(1, n + 1, dtype=np.uint64), 0,
+                                                 philox.TAG_INIT)))
+
+
+def build_opinion(n=10_000_000, mean_degree=20, gamma=2.5, wmax=1e4, eps=0.3, seed=1,
+                  stream=None, hub_threshold=256):
+    model = opinion_model()
+    sim = api.create_simulation(model, stream=stream)
+    x = opinion_initial_state(n, seed)
+    ids = api.add_agents(sim, "Opinion", n, x=x)
+    nedges = int(round(mean_degree * n))
+    check(lib().vg_gen_chung_lu_edges(sim._h, model["Weight"].index, model["Opinion"].index,
+                                      nedges, float(mean_degree), float(gamma), float(wmax),
+                                      int(seed), 0))
+    run = Run(sim, model=model, ids=ids, eps=eps, seed=seed, n=n, nedges=nedges)
+
+    def step():
+        api.apply_(sim, "bounded_confidence", ["Opinion"], ["Opinion", "Weight"], ["Opinion"],
+                   params=[model["Weight"].index, eps, 0.5, 0.5, hub_threshold])
+    run.step = step
+    run.edges_per_step = lambda: nedges
+    return run
+
+
+def staged_edges(sim, E):
+    """Edge records staged before finish_init!, in call order: (from, to, payload)."""
+    t = sim.T(E)
+    n = C.c_uint64()
+    check(lib().vg_read_staged_edges(sim._h, t.index, None, None, None, 0, C.byref(n)))
+    frm = np.zeros(n.value, dtype=np.uint64)
+    to = np.zeros(n.value, dtype=np.uint64)
+    cols = [np.zeros(n.value, dtype=t.dtype(f)) for f in range(len(t.fields))]
+    ptrs = (C.c_void_p * max(len(cols), 1))(*[c.ctypes.data for c in cols])
+    check(lib().vg_read_staged_edges(sim._h, t.index, frm.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                     to.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                     ptrs if cols else None, n.value, C.byref(n)))
+    return frm, to, {f[0]: c for f, c in zip(t.fields, cols)}
+
+
+# ------------------------------------------------------- Life + walkers
+def life_model(name="Life"):
+    return (api.ModelTypes()
+            .register_agenttype("Cell", [("alive", "bool")], ":Immortal")
+            .register_agenttype("Walker", [("x", "i32"), ("y", "i32")], ":Immortal")
+            .register_edgetype("Neighbor", [], ":Stateless", target="Cell")
+            .register_edgetype("OnCell", [], ":Stateless", target="Cell")
+            .create_model(name))
+
+
+def life_initial_state(width, height, n_walkers, density, seed):
+    c = width * height
+    alive = philox.unit(philox.to_u64(philox.draw(seed, np.arange(1, c + 1, dtype=np.uint64), 0,
+                                                  philox.TAG_INIT))) < density
+    w = philox.draw(seed, np.arange(1, n_walkers + 1, dtype=np.uint64), 1, philox.TAG_INIT)
+    x = (philox.bounded32(w[0], width) + 1).astype(np.int32)
+    y = (philox.bounded32(w[1], height) + 1).astype(np.int32)
+    return alive, x, y
+
+
+def build_life(width=4096, height=4096, n_walkers=1_000_000, density=0.3, seed=1, stream=None):
+    model = life_model()
+    sim = api.create_simulation(model, stream=stream)
+    alive, x, y = life_initial_state(width, height, n_walkers, density, seed)
+    api.add_raster(sim, "raster", (width, height), "Cell", alive=alive)
+    api.connect_raster_neighbors(sim, "raster", "Neighbor", implicit=True)
+    wids = api.add_agents(sim, "Walker", n_walkers, x=x, y=y)
+    # initial walker -> cell edges (move_to! in the init phase)
+    cells = (np.uint64(model["Cell"].index) << np.uint64(56)) | (
+        (x.astype(np.uint64) - 1) + (y.astype(np.uint64) - 1) * np.uint64(width) + np.uint64(1))
+    if n_walkers:
+        api.add_edges(sim, "OnCell", wids, cells)
+    run = Run(sim, model=model, width=width, height=height, n_walkers=n_walkers, seed=seed)
+
+    def step():
+        api.apply_(sim, "life", ["Cell"], ["Cell", "Neighbor"], ["Cell"],
+                   params=[model["Neighbor"].index])
+        api.apply_(sim, "random_walk", ["Walker"], ["Walker"], ["Walker", "OnCell"],
+                   params=[model["OnCell"].index, 0, seed])
+    run.step = step
+    run.edges_per_step = lambda: 8 * width * height + n_walkers
+    return run
