@@ -1,0 +1,350 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 transition step (apply! of Vahana.jl).
+
+Workload: bounded-confidence opinion dynamics, Opinion{x::Float64} with
+N = 10^7 agents on a directed Chung-Lu graph (exponent 2.5, mean in-degree
+20, expected degree capped at 10^4, E = 2*10^8 edges with Float64 weights),
+all inputs synthetic and seeded (Philox4x32-10).  One bench step is one
+apply!(sim, bounded_confidence, Opinion, [Opinion, Weight], Opinion).
+
+  value  edge-updates/s with the state resident in HBM (CUDA events on the
+         simulation's stream around K steps; inputs are larger than L2).
+  e2e    the same metric through the C ABI with host buffers: each step
+         uploads the opinions from pinned host memory (vg_write_agents),
+         runs apply! and reads the new opinions back (vg_read_agents).
+  roofline  algorithmic bytes of one launch of the gather kernel,
+         12 E + 20 N + 4 (4 B source index + 8 B weight per edge, row
+         pointers, opinion read and write), over its CUDA-event duration,
+         against the measured HBM copy bandwidth.
+  cpu_baseline  the oracle's C restatement of the same step (OpenMP over
+         all host cores) on the same graph.
+
+--impl reference times that CPU restatement alone on this workload (the
+reference itself is Julia and cannot run here).
+Multi-GPU: replicas only (one independent simulation per rank).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for p in (ROOT, os.path.join(ROOT, "vahana.jl_gb300")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+METRIC = "edge-updates/s"
+WORKLOAD = "bounded_confidence_opinion_chung_lu"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=10_000_000)
+    ap.add_argument("--mean-degree", type=float, default=20.0)
+    ap.add_argument("--wmax", type=float, default=1e4)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--hub-threshold", type=int, default=256)
+    ap.add_argument("--e2e-steps", type=int, default=50)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def config(args):
+    return {"workload": WORKLOAD, "agents": args.n, "edges": int(round(args.mean_degree * args.n)),
+            "mean_in_degree": args.mean_degree, "degree_exponent": 2.5,
+            "max_expected_degree": args.wmax, "eps": 0.3, "mix": 0.5,
+            "model_steps_reference": 50, "l2": "inputs larger than L2 (2.6 GB per step)",
+            "parallelism": "replicas"}
+
+
+# ---------------------------------------------------------------- helpers
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(nm)
+        sm.sort()
+        med = sm[len(sm) // 2] if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_launch():
+    """DRAM bytes per launch of the gather kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "k_opinion_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("bytes_per_launch_full_size")
+    return None
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# ------------------------------------------------------------- CPU legs
+def cpu_graph_from_device(vh, run):
+    """CSR of the built graph (row_ptr, src, w) read back for the CPU step."""
+    rp, frm, pl = vh.read_edges(run.sim, "Weight", "Opinion")
+    src = ((frm & ((1 << 36) - 1)) - 1).astype("uint32")
+    return rp.astype("uint64"), src, pl["w"].astype("float64")
+
+
+def cpu_graph_host(args):
+    """The same graph built on the host by the oracle's generator."""
+    from oracle import models as om
+    n = args.n
+    e = int(round(args.mean_degree * n))
+    frm, to, w = om.gen_chung_lu(n, e, args.mean_degree, 2.5, args.wmax, args.seed)
+    g = om.build_inedges(n, frm, to)
+    del frm, to
+    import numpy as np
+    w_in = np.ascontiguousarray(w[g[2]])
+    return g[0], g[1], w_in
+
+
+def time_cpu(g, x0, max_seconds):
+    """Run the oracle's step until max_seconds have passed (at least one)."""
+    from oracle import models as om
+    rp, src, w = g
+    threads = om.threads()
+    x = x0.copy()
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        x = om.opinion_step((rp, src, None), w, x, 0.3, 0.5, 0.5, nthreads=threads)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= max_seconds or steps >= 50:
+            break
+    return steps, el, threads
+
+
+# ----------------------------------------------------------------- arms
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from vahana_gb300 import models
+    from oracle import models as om
+    g = cpu_graph_host(args)
+    x0 = models.opinion_initial_state(args.n, args.seed)
+    e = int(g[0][-1])
+    # one warm-up step, then timed full steps (each one bounded sample of the
+    # workload) until --cpu-seconds have passed or --steps are done
+    time_cpu(g, x0, 0.0)
+    threads = om.threads()
+    times, x, t_all = [], x0, time.perf_counter()
+    while len(times) < max(1, args.steps):
+        t0 = time.perf_counter()
+        x = om.opinion_step((g[0], g[1], None), g[2], x, 0.3, 0.5, 0.5, nthreads=threads)
+        times.append(time.perf_counter() - t0)
+        if time.perf_counter() - t_all > args.cpu_seconds:
+            break
+    ms = 1e3 * sum(times) / len(times)
+    v = e / (ms * 1e-3)
+    out = {"metric": METRIC, "value": v, "unit": "edge-updates/s", "n_gpus": args.gpus,
+           "steps": len(times), "warmup": 1, "ms_per_step": ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "impl": "reference", "config": config(args),
+           "cpu_baseline": {"value": v, "unit": "edge-updates/s", "cores": threads,
+                            "kind": "port",
+                            "sample": "%d full steps of the oracle's C restatement (OpenMP) "
+                                      "on the same graph" % len(times)},
+           "e2e": {"value": v, "unit": "edge-updates/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    import vahana_gb300 as vh
+    from vahana_gb300 import models
+    vh.build()
+    stream = torch.cuda.Stream()
+    run = models.build_opinion(n=args.n, mean_degree=args.mean_degree, wmax=args.wmax,
+                               seed=args.seed, stream=stream.cuda_stream,
+                               hub_threshold=args.hub_threshold)
+    vh.finish_init(run.sim)
+    vh.set_async(run.sim, True)
+    E, N = run.nedges, run.n
+    for _ in range(args.warmup):
+        run.step()
+    vh.synchronize(run.sim)
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+
+    # ---- device-resident timed region
+    K = args.steps
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(K)]
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clk = Clocks(local)
+    barrier()
+    torch.cuda.synchronize()
+    clk.start()
+    time.sleep(0.3)
+    start.record(stream)
+    for k in range(K):
+        ev[k][0].record(stream)
+        run.step()
+        ev[k][1].record(stream)
+    end.record(stream)
+    vh.synchronize(run.sim)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    barrier()
+    total_ms = start.elapsed_time(end)
+    kernel_ms = sorted(a.elapsed_time(b) for a, b in ev)
+    mean_kernel_ms = sum(kernel_ms) / len(kernel_ms)
+    if ws > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = ws * E * K / (total_ms * 1e-3)
+
+    # ---- end to end through the C ABI with pinned host buffers
+    Ke = args.e2e_steps
+    xh = torch.empty(N, dtype=torch.float64, pin_memory=True)
+    xo = torch.empty(N, dtype=torch.float64, pin_memory=True)
+    xh.numpy()[:] = vh.read_agents(run.sim, "Opinion")[0]["x"]
+    import ctypes as C
+    from vahana_gb300._lib import lib, check
+    tn = run.model["Opinion"].index
+    inp = (C.c_void_p * 1)(xh.data_ptr())
+    outp = (C.c_void_p * 1)(xo.data_ptr())
+    nout = C.c_uint64()
+
+    def e2e_step():
+        check(lib().vg_write_agents(run.sim._h, tn, inp, N))
+        run.step()
+        check(lib().vg_read_agents(run.sim._h, tn, outp, None, N, C.byref(nout)))
+    e2e_step()
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(Ke):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if ws > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": ws * E * Ke / e2e_s, "unit": "edge-updates/s",
+           "h2d_bytes_per_step": 8 * N, "d2h_bytes_per_step": 8 * N}
+
+    # ---- roofline of the gather kernel
+    alg_bytes = 12 * E + 20 * N + 4
+    peak, kind = peaks()
+    achieved = alg_bytes / (mean_kernel_ms * 1e-3) / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_kind": kind, "traffic": traffic_per_launch(),
+            "algorithmic_bytes_per_launch": alg_bytes, "kernel": "k_opinion",
+            "kernel_ms_mean": mean_kernel_ms, "kernel_ms_median": kernel_ms[len(kernel_ms) // 2]}
+
+    out = {"metric": METRIC, "value": value, "unit": "edge-updates/s", "n_gpus": ws,
+           "steps": K, "warmup": args.warmup, "ms_per_step": total_ms / K,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic", "config": config(args), "e2e": e2e, "roofline": roof,
+           "clocks": clocks, "gpu_launches": K}
+
+    # ---- CPU baseline (rank 0, N = 1 only)
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        g = cpu_graph_from_device(vh, run)
+        x0 = vh.read_agents(run.sim, "Opinion")[0]["x"].copy()
+        steps, el, threads = time_cpu(g, x0, args.cpu_seconds)
+        cv = E * steps / el
+        out["cpu_baseline"] = {"value": cv, "unit": "edge-updates/s", "cores": threads,
+                               "kind": "port",
+                               "sample": "%d full steps (%.1f s) of the oracle's C restatement "
+                                         "on the same graph" % (steps, el)}
+    run.close()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -146,7 +146,19 @@ int vg_sim_copy(vg_sim *s, vg_sim **out);
 int vg_finish_init(vg_sim *s);
 int vg_sim_num_transitions(vg_sim *s, int64_t *out);
 int vg_sim_set_stream(vg_sim *s, void *stream);
+/* Waits for the simulation's stream and reports a kernel status word set
+ * by an asynchronous apply! (as the AssertionError apply! would raise). */
 int vg_sim_synchronize(vg_sim *s);
+/* async != 0: apply! returns without waiting for the device; errors that
+ * kernels report surface at the next synchronizing call (vg_sim_synchronize,
+ * a read back, or switching async off).  Default off: every apply! checks. */
+int vg_sim_set_async(vg_sim *s, int async);
+/* Overwrite the first n agents' state of a type from host SoA columns
+ * between transitions (fields[i] may be NULL to keep a column).  No direct
+ * reference counterpart: it is how a host binding pushes a state array it
+ * changed back into a device-resident simulation. */
+int vg_write_agents(vg_sim *s, int type_nr, const void *const *fields,
+                    uint64_t n);
 /* Bytes of device memory the simulation holds (admission by footprint). */
 int vg_sim_device_bytes(vg_sim *s, uint64_t *out);
 /* disable_transition_checks(sim, disable) -- src/Helpers.jl:259-262 */

@@ -200,3 +200,85 @@ void or_walk_step(int64_t n, int64_t W, int64_t H, const int32_t *x, const int32
     cell_out[i] = (nx - 1) + (ny - 1) * W;
   }
 }
+
+/* ---- directed Chung-Lu generator (input construction, host) -----------
+ * The same generator as the library's device generator, restated: expected
+ * degrees w_i = min(c i^(-1/(gamma-1)), wmax) with c found by bisection on
+ * the capped sum (mean degree `mean`), cumulative sums in index order; edge
+ * e draws source and target by the smallest index whose cumulative sum
+ * exceeds unit(Philox(seed, e, 0, tag)) * total and a weight (top53+1)/2^53. */
+static uint64_t sample_cdf(const double *cdf, uint64_t n, double u) {
+  uint64_t lo = 0, hi = n - 1;
+  while (lo < hi) {
+    uint64_t mid = (lo + hi) >> 1;
+    if (cdf[mid] > u) hi = mid; else lo = mid + 1;
+  }
+  return lo;
+}
+
+int or_gen_chung_lu(uint64_t N, uint64_t E, double mean, double gamma, double wmax,
+                    uint64_t seed, int type_nr, uint64_t *from, uint64_t *to, double *w,
+                    int nthreads) {
+  double *r = (double *)malloc(N * sizeof(double));
+  double *suffix = (double *)malloc((N + 1) * sizeof(double));
+  double *cdf = (double *)malloc(N * sizeof(double));
+  if (!r || !suffix || !cdf) return 1;
+  double ex = -1.0 / (gamma - 1.0);
+  for (uint64_t i = 0; i < N; i++) r[i] = pow((double)(i + 1), ex);
+  suffix[N] = 0.0;
+  for (uint64_t i = N; i-- > 0;) suffix[i] = suffix[i + 1] + r[i];
+  double target = mean * (double)N, lo = 0.0, hi = wmax / r[N - 1];
+  for (int it = 0; it < 200; it++) {
+    double mid = 0.5 * (lo + hi);
+    uint64_t a = 0, b = N;
+    while (a < b) {
+      uint64_t m = (a + b) / 2;
+      if (mid * r[m] >= wmax) a = m + 1; else b = m;
+    }
+    double sum = wmax * (double)a + mid * suffix[a];
+    if (sum < target) lo = mid; else hi = mid;
+  }
+  double c = 0.5 * (lo + hi), acc = 0.0;
+  for (uint64_t i = 0; i < N; i++) {
+    double wi = c * r[i];
+    if (wi > wmax) wi = wmax;
+    acc += wi;
+    cdf[i] = acc;
+  }
+  uint64_t tb = (uint64_t)type_nr << SHIFT_TYPE;
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+  for (int64_t e = 0; e < (int64_t)E; e++) {
+    uint32_t o[4];
+    draw(seed, (uint64_t)e, 0, 5, o);
+    uint64_t s = sample_cdf(cdf, N, unit(o) * acc);
+    draw(seed, (uint64_t)e, 0, 6, o);
+    uint64_t d = sample_cdf(cdf, N, unit(o) * acc);
+    from[e] = tb | (s + 1);
+    to[e] = tb | (d + 1);
+    if (w) {
+      draw(seed, (uint64_t)e, 0, 7, o);
+      uint64_t u = ((uint64_t)o[1] << 32) | o[0];
+      w[e] = (double)((u >> 11) + 1) * (1.0 / 9007199254740992.0);
+    }
+  }
+  free(r);
+  free(suffix);
+  free(cdf);
+  return 0;
+}
+
+/* uniform out-edges: agent i adds k edges to t uniform in [1, N], t != i */
+void or_gen_uniform_out(uint64_t N, uint32_t k, uint64_t seed, int type_nr, uint64_t *from,
+                        uint64_t *to) {
+  uint64_t tb = (uint64_t)type_nr << SHIFT_TYPE;
+  for (uint64_t i = 1; i <= N; i++)
+    for (uint32_t j = 1; j <= k; j++) {
+      uint32_t o[4];
+      draw(seed, i, j, TAG_EDGE, o);
+      uint64_t t = (((uint64_t)o[0] * (uint64_t)(N - 1)) >> 32) + 1;
+      if (t >= i) t += 1;
+      uint64_t r = (i - 1) * k + (j - 1);
+      from[r] = tb | i;
+      to[r] = tb | t;
+    }
+}

@@ -28,6 +28,11 @@ def lib():
                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32,
                                     C.c_int]
         _L.or_philox.argtypes = [C.c_uint32] * 4 + [C.c_uint64, C.c_void_p]
+        _L.or_gen_chung_lu.argtypes = [C.c_uint64, C.c_uint64, C.c_double, C.c_double,
+                                       C.c_double, C.c_uint64, C.c_int, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_int]
+        _L.or_gen_uniform_out.argtypes = [C.c_uint64, C.c_uint32, C.c_uint64, C.c_int,
+                                          C.c_void_p, C.c_void_p]
     return _L
 
 
@@ -43,6 +48,24 @@ def philox(c0, c1, c2, c3, seed):
     out = np.zeros(4, dtype=np.uint32)
     lib().or_philox(c0, c1, c2, c3, seed, _p(out))
     return out
+
+
+def gen_chung_lu(n, nedges, mean, gamma, wmax, seed, type_nr=1):
+    """Host restatement of the device Chung-Lu generator: (from, to, w)."""
+    frm = np.zeros(nedges, dtype=np.uint64)
+    to = np.zeros(nedges, dtype=np.uint64)
+    w = np.zeros(nedges, dtype=np.float64)
+    if lib().or_gen_chung_lu(n, nedges, mean, gamma, wmax, seed, type_nr, _p(frm), _p(to),
+                             _p(w), threads()):
+        raise MemoryError("oracle generator")
+    return frm, to, w
+
+
+def gen_uniform_out(n, k, seed, type_nr=1):
+    frm = np.zeros(n * k, dtype=np.uint64)
+    to = np.zeros(n * k, dtype=np.uint64)
+    lib().or_gen_uniform_out(n, k, seed, type_nr, _p(frm), _p(to))
+    return frm, to
 
 
 def build_inedges(n, frm, to):

@@ -52,6 +52,25 @@ def test_opinion_bit_exact(vh, hub):
     run.close()
 
 
+def test_generators_match_host_restatement(vh):
+    """The device graph generators emit the same records, in the same call
+    order, as the oracle's host restatement."""
+    from vahana_gb300 import models
+    run = models.build_opinion(n=50000, mean_degree=20, gamma=2.5, wmax=1e4, seed=9)
+    frm, to, pl = models.staged_edges(run.sim, "Weight")
+    f2, t2, w2 = om.gen_chung_lu(50000, 1_000_000, 20, 2.5, 1e4, 9)
+    np.testing.assert_array_equal(frm, f2)
+    np.testing.assert_array_equal(to, t2)
+    np.testing.assert_array_equal(pl["w"].view(np.uint64), w2.view(np.uint64))
+    run.close()
+    run = models.build_sir(n=4000, degree=10, seed=4)
+    frm, to, _ = models.staged_edges(run.sim, "Contact")
+    f2, t2 = om.gen_uniform_out(4000, 10, 4)
+    np.testing.assert_array_equal(frm, f2)
+    np.testing.assert_array_equal(to, t2)
+    run.close()
+
+
 def test_life_walkers_bit_exact(vh):
     from vahana_gb300 import models
     W, H, nw, seed = 96, 80, 700, 5

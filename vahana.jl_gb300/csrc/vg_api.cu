@@ -382,6 +382,32 @@ int vg_sim_synchronize(vg_sim *h) {
   API_BEGIN
   S(h).ensure_device();
   VG_CUDA(cudaStreamSynchronize(S(h).stream));
+  check_device_status(S(h), "asynchronous transition");
+  API_END
+}
+
+int vg_sim_set_async(vg_sim *h, int async) {
+  API_BEGIN
+  Sim &s = S(h);
+  if (s.async && !async && s.device_ready) check_device_status(s, "asynchronous transition");
+  s.async = async != 0;
+  API_END
+}
+
+int vg_write_agents(vg_sim *h, int nr, const void *const *fields, uint64_t n) {
+  API_BEGIN
+  Sim &s = S(h);
+  const AgentTypeDesc &ad = s.model->at(nr);
+  if (!s.initialized) fail(VG_ERR_STATE, "vg_write_agents runs after finish_init!");
+  if (s.intransition) fail(VG_ERR_ASSERT, "agent states cannot be set inside a transition");
+  AgentStore &a = s.agents[nr - 1];
+  if (n > a.n) fail(VG_ERR_ARG, "more values than agent slots");
+  for (size_t f = 0; f < ad.fields.size(); f++) {
+    if (!fields || !fields[f]) continue;
+    VG_CUDA(cudaMemcpyAsync(a.rd[f].p, fields[f], n * ad.fields[f].size, cudaMemcpyHostToDevice,
+                            s.stream));
+  }
+  if (!s.async) VG_CUDA(cudaStreamSynchronize(s.stream));
   API_END
 }
 
@@ -673,6 +699,7 @@ int vg_read_agents(vg_sim *h, int nr, void *const *fields_out, uint8_t *died_out
   *n_out = n;
   uint64_t m = std::min(n, cap);
   if (!m) return VG_OK;
+  if (s.initialized && s.async) check_device_status(s, "asynchronous transition");
   for (size_t f = 0; f < ad.fields.size(); f++) {
     if (!fields_out || !fields_out[f]) continue;
     size_t sz = ad.fields[f].size;

@@ -432,7 +432,7 @@ int vg_apply(vg_sim *h, const char *tname, const int *call, int ncall, const int
     ctx.call_pos = pos;
     def->launch(ctx);
   }
-  check_device_status(s, tname);
+  if (!s.async) check_device_status(s, tname);
 
   // finish_write! of the agent types (src/AgentMethods.jl:300-439)
   std::vector<int> died_types;

@@ -215,6 +215,9 @@ struct Sim {
   // init phase (registry, staging) runs without a GPU
   bool device_ready = false;
   void ensure_device();
+  // asynchronous mode: apply! does not wait for the device; the kernels'
+  // status word is checked at the next synchronizing call
+  bool async = false;
 };
 
 // ---------------------------------------------------------------- kernels

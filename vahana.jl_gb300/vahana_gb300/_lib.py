@@ -89,6 +89,8 @@ SIGNATURES = {
     "vg_sim_num_transitions": (I, [P, PI64]),
     "vg_sim_set_stream": (I, [P, P]),
     "vg_sim_synchronize": (I, [P]),
+    "vg_sim_set_async": (I, [P, I]),
+    "vg_write_agents": (I, [P, I, PP, U64]),
     "vg_sim_device_bytes": (I, [P, PU64]),
     "vg_disable_transition_checks": (I, [P, I]),
     "vg_set_param": (I, [P, CP, D]),

@@ -227,6 +227,24 @@ def device_bytes(sim):
     return v.value
 
 
+def set_async(sim, flag):
+    check(lib().vg_sim_set_async(sim._h, int(bool(flag))))
+
+
+def write_agents(sim, T, **fields):
+    """Overwrite the first n agents' fields (between transitions) from host arrays."""
+    t = sim.T(T)
+    n = max([np.size(v) for v in fields.values()] or [0])
+    cols = []
+    ptrs = (C.c_void_p * max(len(t.fields), 1))()
+    for i, (fname, dt) in enumerate(t.fields):
+        if fname in fields:
+            a = np.ascontiguousarray(np.asarray(fields[fname], dtype=NP_DTYPES[dt]))
+            cols.append(a)
+            ptrs[i] = a.ctypes.data
+    check(lib().vg_write_agents(sim._h, t.index, ptrs, n))
+
+
 def set_stream(sim, stream):
     check(lib().vg_sim_set_stream(sim._h, C.c_void_p(stream)))
 
