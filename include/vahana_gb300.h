@@ -308,6 +308,13 @@ int vg_read_staged_edges(vg_sim *s, int edge_type, uint64_t *from_out,
                          uint64_t *to_out, void *const *payload_out, uint64_t cap,
                          uint64_t *n_out);
 
+/* ---- self test ----------------------------------------------------------
+ * Compares the integer-pipe binary64 add/mul/div used by the gather kernels
+ * with the hardware instructions on n generated operand pairs (no reference
+ * counterpart).  counts_out[6]: mismatches of add, mul, div, then the
+ * number of out-of-range fallbacks of each. */
+int vg_selftest_fp64(uint64_t n, uint64_t seed, uint64_t *counts_out);
+
 /* ---- batched ensemble (many independent SIR instances in one arena) ----- */
 typedef struct vg_batch vg_batch;
 /* Instances i = 0..n-1 with agent counts N[i], out-degree deg[i], infection

@@ -32,11 +32,14 @@ def test_sir_bit_exact(vh):
     run.close()
 
 
-@pytest.mark.parametrize("hub", [256, 16])
-def test_opinion_bit_exact(vh, hub):
+NO_SPLIT = 4294967295  # hub threshold that keeps every row on the ordered path
+
+
+def test_opinion_bit_exact(vh):
+    """Ordered path (no hub split): tolerance 0, bit-identical binary64."""
     from vahana_gb300 import models
     run = models.build_opinion(n=20000, mean_degree=20, gamma=2.5, wmax=2000, eps=0.3, seed=11,
-                               hub_threshold=hub)
+                               hub_threshold=NO_SPLIT)
     sim = run.sim
     frm, to, pl = models.staged_edges(sim, "Weight")
     x0 = vh.read_agents(sim, "Opinion")[0]["x"].copy()
@@ -46,10 +49,50 @@ def test_opinion_bit_exact(vh, hub):
         run.step()
     x = vh.read_agents(sim, "Opinion")[0]["x"]
     x_ref = om.run_opinion(run.n, frm, to, pl["w"], x0, 0.3, steps)
-    # tolerance 0: bit-exact on the ordered path (hub warps fold in order too)
     np.testing.assert_array_equal(x.view(np.uint64), x_ref.view(np.uint64))
     assert not np.array_equal(x, x0)
     run.close()
+
+
+@pytest.mark.parametrize("hub", [256, 16])
+def test_opinion_hub_split(vh, hub):
+    """Hub rows (in-degree > hub) are summed in split chunks: within 1e-12
+    relative of the sequential fold; every other row stays bit-exact after
+    one step, and all rows stay within 1e-12 over several steps."""
+    from vahana_gb300 import models
+    run = models.build_opinion(n=20000, mean_degree=20, gamma=2.5, wmax=2000, eps=0.3, seed=11,
+                               hub_threshold=hub)
+    sim = run.sim
+    frm, to, pl = models.staged_edges(sim, "Weight")
+    x0 = vh.read_agents(sim, "Opinion")[0]["x"].copy()
+    vh.finish_init(sim)
+    run.step()
+    x1 = vh.read_agents(sim, "Opinion")[0]["x"].copy()
+    ref1 = om.run_opinion(run.n, frm, to, pl["w"], x0, 0.3, 1)
+    deg = np.bincount((to & np.uint64((1 << 36) - 1)).astype(np.int64) - 1, minlength=run.n)
+    hubs = deg > hub
+    assert hubs.any()
+    np.testing.assert_array_equal(x1[~hubs].view(np.uint64), ref1[~hubs].view(np.uint64))
+    np.testing.assert_allclose(x1[hubs], ref1[hubs], rtol=1e-12, atol=0)
+    for _ in range(5):
+        run.step()
+    x = vh.read_agents(sim, "Opinion")[0]["x"]
+    ref = om.run_opinion(run.n, frm, to, pl["w"], x0, 0.3, 6)
+    np.testing.assert_allclose(x, ref, rtol=1e-12, atol=0)
+    run.close()
+
+
+def test_fp64_integer_arithmetic_matches_hardware(vh):
+    """The integer-pipe binary64 add/mul/div used by the gather kernels
+    equal the hardware instructions on 4M operand pairs (random, ties,
+    carries, exponent gaps); out-of-range cases fall back."""
+    import ctypes as C
+    from vahana_gb300._lib import check, lib
+    counts = (C.c_uint64 * 6)()
+    check(lib().vg_selftest_fp64(4 << 20, 12345, counts))
+    add_bad, mul_bad, div_bad, add_fb, mul_fb, div_fb = list(counts)
+    assert (add_bad, mul_bad, div_bad) == (0, 0, 0)
+    assert add_fb < (4 << 20) // 4 and mul_fb < (4 << 20) // 4
 
 
 def test_generators_match_host_restatement(vh):

@@ -1,0 +1,132 @@
+// Exact IEEE-754 binary64 round-to-nearest-even arithmetic on the integer
+// pipe, for the hot gather kernels.
+//
+// GB300 executes FP64 at about 2 operations per clock per SM, 64x below
+// its integer/FP32 issue rate.  The ordered neighbour folds need results
+// bit-identical to sequential binary64 arithmetic, so this file implements
+// the operations themselves with integer instructions, following the
+// textbook algorithms (significand alignment with guard/round/sticky bits
+// and normalisation for addition, the double-width significand product for
+// multiplication, restoring quotient digits with a remainder test for
+// division; e.g. J.-M. Muller et al., Handbook of Floating-Point Arithmetic,
+// 2nd ed., Birkhauser 2018, ch. 7-8; D. Goldberg, What every computer
+// scientist should know about floating-point arithmetic, 1991).
+//
+// Scope: non-negative, finite, normal operands and results (zero operands
+// are handled).  Anything else sets ok = false and the caller uses the
+// hardware instruction instead, so every result is the correctly rounded
+// binary64 value.  A device self-test compares these functions with the
+// hardware instructions on random and constructed operands.
+#pragma once
+#include <stdint.h>
+
+namespace vg {
+
+constexpr uint64_t EMU_M52 = (1ull << 52) - 1;
+constexpr uint64_t EMU_H53 = 1ull << 52;
+
+// a + b for non-negative doubles given as bit patterns.
+__device__ __forceinline__ uint64_t emu_add_pos(uint64_t a, uint64_t b, bool &ok) {
+  uint64_t hi = a > b ? a : b, lo = a > b ? b : a;  // bit order == value order
+  if (lo == 0) return hi;
+  unsigned eh = (unsigned)(hi >> 52), el = (unsigned)(lo >> 52);
+  if (el == 0 || eh >= 2046) {  // subnormal operand or possible overflow
+    ok = false;
+    return 0;
+  }
+  uint64_t A = ((hi & EMU_M52) | EMU_H53) << 10;  // [2^62, 2^63), 10 low zero bits
+  uint64_t B = ((lo & EMU_M52) | EMU_H53) << 10;
+  unsigned d = eh - el;
+  uint64_t Bs;
+  if (d >= 64) Bs = 1;  // only the sticky bit remains
+  else if (d) Bs = (B >> d) | (uint64_t)((B << (64 - d)) != 0);
+  else Bs = B;
+  uint64_t S = A + Bs;  // < 2^64
+  unsigned e = eh;
+  if (S >> 63) {
+    S = (S >> 1) | (S & 1);
+    e++;
+  }
+  uint64_t q = S >> 10;  // 53-bit significand
+  unsigned r = (unsigned)S & 0x3FFu;  // guard bit 9, round/sticky below
+  q += (r > 0x200u) || (r == 0x200u && (q & 1));
+  if (q >> 53) {  // rounding carried out: q == 2^53
+    q >>= 1;
+    e++;
+  }
+  if (e >= 2047) {
+    ok = false;
+    return 0;
+  }
+  return ((uint64_t)e << 52) | (q & EMU_M52);
+}
+
+// a * b for non-negative doubles given as bit patterns.
+__device__ __forceinline__ uint64_t emu_mul_pos(uint64_t a, uint64_t b, bool &ok) {
+  if (a == 0 || b == 0) return 0;
+  int ea = (int)(a >> 52), eb = (int)(b >> 52);
+  if (ea == 0 || eb == 0 || ea == 2047 || eb == 2047) {
+    ok = false;
+    return 0;
+  }
+  uint64_t ma = (a & EMU_M52) | EMU_H53, mb = (b & EMU_M52) | EMU_H53;
+  uint64_t lo = ma * mb, hi = __umul64hi(ma, mb);  // P in [2^104, 2^106)
+  int e = ea + eb - 1023;
+  int s = 52;
+  if (hi >> 41) {  // P >= 2^105
+    s = 53;
+    e++;
+  }
+  uint64_t q = (hi << (64 - s)) | (lo >> s);  // top 53 bits
+  uint64_t half = 1ull << (s - 1);
+  uint64_t rem = lo & ((1ull << s) - 1);
+  q += (rem > half) || (rem == half && (q & 1));
+  if (q >> 53) {
+    q >>= 1;
+    e++;
+  }
+  if (e <= 0 || e >= 2047) {
+    ok = false;
+    return 0;
+  }
+  return ((uint64_t)e << 52) | (q & EMU_M52);
+}
+
+// a / b for positive normal doubles (b > 0), restoring division of the
+// significands: 53 quotient bits, then the remainder decides the rounding.
+__device__ __forceinline__ uint64_t emu_div_pos(uint64_t a, uint64_t b, bool &ok) {
+  if (a == 0) return 0;
+  int ea = (int)(a >> 52), eb = (int)(b >> 52);
+  if (ea == 0 || eb == 0 || ea == 2047 || eb == 2047 || b == 0) {
+    ok = false;
+    return 0;
+  }
+  uint64_t ma = (a & EMU_M52) | EMU_H53, mb = (b & EMU_M52) | EMU_H53;
+  int e = ea - eb + 1023;
+  if (ma < mb) {  // bring the quotient into [1, 2)
+    ma <<= 1;
+    e--;
+  }
+  // quotient bits of ma / mb, most significant first; invariant R < 2 mb
+  uint64_t R = ma, q = 0;
+#pragma unroll 4
+  for (int i = 0; i < 53; i++) {
+    uint64_t t = R - mb;
+    bool ge = R >= mb;
+    q = (q << 1) | (uint64_t)ge;
+    R = (ge ? t : R) << 1;
+  }
+  // R = 2 * remainder; compare with mb for the half-way point
+  q += (R > mb) || (R == mb && (q & 1));
+  if (q >> 53) {
+    q >>= 1;
+    e++;
+  }
+  if (e <= 0 || e >= 2047) {
+    ok = false;
+    return 0;
+  }
+  return ((uint64_t)e << 52) | (q & EMU_M52);
+}
+
+}  // namespace vg

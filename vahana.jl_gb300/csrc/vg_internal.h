@@ -279,6 +279,8 @@ struct TransitionDef {
   TransitionLauncher launch;
 };
 const std::vector<TransitionDef> &transitions();
+// launchers that live in their own translation units
+void tr_bounded_confidence(ApplyCtx &ctx);  // vg_opinion.cu
 
 // primitives (vg_sort.cu)
 void exclusive_scan_u32(const uint32_t *in, uint32_t *out, uint64_t n,

@@ -1,0 +1,105 @@
+// Device self-tests of the integer-pipe binary64 arithmetic (vg_fp64emu.cuh)
+// against the hardware instructions, reachable through the C ABI so that the
+// test suite checks the exact code the kernels use.
+#include "vg_fp64emu.cuh"
+#include "vg_internal.h"
+#include "vg_philox.cuh"
+
+namespace vg {
+namespace {
+
+__device__ __forceinline__ uint64_t dbits(double x) { return (uint64_t)__double_as_longlong(x); }
+__device__ __forceinline__ double bdbl(uint64_t x) { return __longlong_as_double((long long)x); }
+
+// operand pairs of several shapes: random exponents, equal exponents, wide
+// exponent gaps, all-ones significands (carries), exact half-way cases,
+// numbers near the subnormal range, zeros, and values in [0, 1)
+__device__ void make_pair(uint64_t i, uint64_t seed, uint64_t &a, uint64_t &b) {
+  Philox4 r = philox_draw(seed, i, 0, 11);
+  Philox4 s = philox_draw(seed, i, 1, 11);
+  uint64_t ma = ((uint64_t)r.v[1] << 32 | r.v[0]) & EMU_M52;
+  uint64_t mb = ((uint64_t)s.v[1] << 32 | s.v[0]) & EMU_M52;
+  unsigned kind = r.v[2] % 9;
+  int ea = 900 + (int)(r.v[3] % 200), eb = 900 + (int)(s.v[3] % 200);
+  switch (kind) {
+    case 1: eb = ea; break;
+    case 2: eb = ea - (int)(s.v[2] % 70); break;
+    case 3: ma = EMU_M52 - (r.v[3] & 7); mb = EMU_M52 - (s.v[3] & 7); eb = ea - (int)(s.v[2] % 4); break;
+    case 4: {  // b is exactly half an ulp of a (or of a's neighbour) -> ties
+      eb = ea - 53 + (int)(s.v[2] % 3);
+      mb = (s.v[2] & 8) ? 0 : (1ull << 51);
+      break;
+    }
+    case 5: ea = 1 + (int)(r.v[3] % 60); eb = 1 + (int)(s.v[3] % 60); break;
+    case 6: ea = 0; ma = 0; break;
+    case 7: ea = 1012 + (int)(r.v[3] % 11); eb = 1012 + (int)(s.v[3] % 11); break;
+    case 8: eb = ea - 52 - (int)(s.v[2] % 4); break;
+    default: break;
+  }
+  if (eb < 0) eb = 0;
+  if (ea < 0) ea = 0;
+  a = ((uint64_t)ea << 52) | ma;
+  b = ((uint64_t)eb << 52) | mb;
+  if (eb == 0) b = mb ? 0 : b;
+}
+
+__global__ void k_selftest(uint64_t n, uint64_t seed, unsigned long long *counts) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint64_t a, b;
+  make_pair(i, seed, a, b);
+  // add
+  {
+    bool ok = true;
+    uint64_t r = emu_add_pos(a, b, ok);
+    if (ok) {
+      if (r != dbits(__dadd_rn(bdbl(a), bdbl(b)))) atomicAdd(&counts[0], 1ull);
+    } else {
+      atomicAdd(&counts[3], 1ull);
+    }
+  }
+  // mul
+  {
+    bool ok = true;
+    uint64_t r = emu_mul_pos(a, b, ok);
+    if (ok) {
+      if (r != dbits(__dmul_rn(bdbl(a), bdbl(b)))) atomicAdd(&counts[1], 1ull);
+    } else {
+      atomicAdd(&counts[4], 1ull);
+    }
+  }
+  // div (b > 0)
+  if (b) {
+    bool ok = true;
+    uint64_t r = emu_div_pos(a, b, ok);
+    if (ok) {
+      if (r != dbits(__ddiv_rn(bdbl(a), bdbl(b)))) atomicAdd(&counts[2], 1ull);
+    } else {
+      atomicAdd(&counts[5], 1ull);
+    }
+  }
+}
+
+}  // namespace
+}  // namespace vg
+
+using namespace vg;
+namespace vg {
+void set_last_error(const std::string &m);
+}
+
+extern "C" int vg_selftest_fp64(uint64_t n, uint64_t seed, uint64_t *counts_out) {
+  try {
+    unsigned long long *d = nullptr;
+    VG_CUDA(cudaMalloc(&d, 6 * 8));
+    VG_CUDA(cudaMemset(d, 0, 6 * 8));
+    k_selftest<<<(unsigned)((n + 255) / 256), 256>>>(n, seed, d);
+    VG_CUDA(cudaGetLastError());
+    VG_CUDA(cudaMemcpy(counts_out, d, 6 * 8, cudaMemcpyDeviceToHost));
+    VG_CUDA(cudaFree(d));
+    return VG_OK;
+  } catch (const Error &e) {
+    set_last_error(e.msg);
+    return e.code;
+  }
+}

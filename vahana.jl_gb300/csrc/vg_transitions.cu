@@ -323,91 +323,6 @@ __global__ void k_sir(const uint32_t *__restrict__ rp, const uint32_t *__restric
   d_wr[i] = d;
 }
 
-// ------------------------------------------- bounded confidence (cfg 1)
-// Opinion x (f64), in-edges with weight w (f64).  Sequential over the
-// in-edges in insertion order: neighbours with |x_j - x| < eps contribute
-// w_j to sw and w_j * x_j to swx; x' = a x + b (swx / sw), or x when none
-// qualify.  Degree-bucketed: rows above the hub threshold are processed by
-// one warp each (lanes load and multiply in parallel, lane 0 folds in
-// order), the first blocks of the grid take the hubs so they start first;
-// the other rows are processed by one thread each.
-struct OpinionArgs {
-  const uint32_t *__restrict__ rp;
-  const uint32_t *__restrict__ src;
-  const double *__restrict__ w;
-  const double *__restrict__ x;
-  double *__restrict__ xo;
-  uint64_t n, nrows;
-  const uint32_t *__restrict__ hub_rows;
-  uint64_t nhub;
-  uint32_t hub_thr;
-  unsigned hub_blocks;
-  double eps, a, b;
-};
-
-__device__ __forceinline__ double opinion_finish(const OpinionArgs &p, double xi,
-                                                 double sw, double swx, uint32_t cnt) {
-  return cnt ? __dadd_rn(__dmul_rn(p.a, xi), __dmul_rn(p.b, __ddiv_rn(swx, sw))) : xi;
-}
-
-__global__ void __launch_bounds__(TPB) k_opinion(OpinionArgs p) {
-  if (blockIdx.x < p.hub_blocks) {
-    const int lane = threadIdx.x & 31;
-    uint64_t h = (uint64_t)blockIdx.x * (TPB / 32) + (threadIdx.x >> 5);
-    if (h >= p.nhub) return;
-    uint32_t r = p.hub_rows[h];
-    double xi = p.x[r];
-    double sw = 0.0, swx = 0.0;
-    uint32_t cnt = 0;
-    uint32_t b = p.rp[r], e = p.rp[r + 1];
-    for (uint32_t base = b; base < e; base += 32) {
-      uint32_t k = base + lane;
-      bool q = false;
-      double wk = 0.0, pk = 0.0;
-      if (k < e) {
-        double xj = __ldg(p.x + p.src[k]);
-        q = fabs(__dsub_rn(xj, xi)) < p.eps;
-        wk = p.w[k];
-        pk = __dmul_rn(wk, xj);
-      }
-      unsigned qm = __ballot_sync(0xffffffffu, q);
-      int m = (int)min(32u, e - base);
-      for (int l = 0; l < m; l++) {
-        double wl = __shfl_sync(0xffffffffu, wk, l);
-        double pl = __shfl_sync(0xffffffffu, pk, l);
-        if ((qm >> l) & 1u) {
-          sw = __dadd_rn(sw, wl);
-          swx = __dadd_rn(swx, pl);
-          cnt++;
-        }
-      }
-    }
-    if (lane == 0) p.xo[r] = opinion_finish(p, xi, sw, swx, cnt);
-    return;
-  }
-  uint64_t i = (uint64_t)(blockIdx.x - p.hub_blocks) * TPB + threadIdx.x;
-  if (i >= p.n) return;
-  double xi = p.x[i];
-  if (i >= p.nrows) {
-    p.xo[i] = xi;
-    return;
-  }
-  uint32_t b = p.rp[i], e = p.rp[i + 1];
-  if (e - b > p.hub_thr) return;  // handled by a hub warp
-  double sw = 0.0, swx = 0.0;
-  uint32_t cnt = 0;
-  for (uint32_t k = b; k < e; k++) {
-    double xj = __ldg(p.x + __ldg(p.src + k));
-    if (fabs(__dsub_rn(xj, xi)) < p.eps) {
-      double wk = __ldg(p.w + k);
-      sw = __dadd_rn(sw, wk);
-      swx = __dadd_rn(swx, __dmul_rn(wk, xj));
-      cnt++;
-    }
-  }
-  p.xo[i] = opinion_finish(p, xi, sw, swx, cnt);
-}
-
 // ------------------------------------------------ Life B3/S23 (cfg 2)
 // Cells of a 2-D raster, implicit Moore stencil (chebyshev, distance 1).
 // The count of alive neighbours does not depend on edge order.
@@ -758,54 +673,6 @@ void tr_sir(ApplyCtx &c) {
                                          (int32_t *)a.wr[1], a.n, v.nrows, d_ptab,
                                          (uint32_t)ptab.size(), seed, (uint32_t)c.step, rec,
                                          s.d_status.as<int>());
-  VG_CUDA(cudaGetLastError());
-}
-
-void tr_bounded_confidence(ApplyCtx &c) {
-  Sim &s = *c.sim;
-  const AgentTypeDesc &ad = s.model->at(c.call_type);
-  if (ad.fields.empty() || ad.fields[0].dtype != VG_F64)
-    fail(VG_ERR_ARG, "bounded_confidence: agent field 0 must be Float64");
-  if (!ad.immortal()) fail(VG_ERR_ARG, "bounded_confidence: the opinion type is :Immortal");
-  int e = need_edge_param(c, 0);
-  const EdgeTypeDesc &ed = s.model->et(e);
-  if (!ed.stores_payload() || ed.fields[0].dtype != VG_F64 || !ed.stores_src())
-    fail(VG_ERR_ARG, "bounded_confidence: edges need a source and a Float64 weight");
-  require_edge_read(c, e);
-  require_agent_read(c, c.call_type);
-  if (!c.writes_call()) fail(VG_ERR_ARG, "bounded_confidence: the called type must be in `write`");
-  double eps = c.param(1, 0.3);
-  double a = c.param(2, 0.5);
-  double b = c.nparams > 3 ? c.params[3] : 1.0 - a;
-  uint32_t thr = (uint32_t)c.param(4, 256);
-  EdgeStore &es = s.edges[e];
-  DevCSRView v = csr_view(s, e, c.call_type);
-  if (v.nedges && v.src_type_const != c.call_type)
-    fail(VG_ERR_ARG, "bounded_confidence: sources must be of the called type");
-  DevAgentView av = agent_view(s, c.call_type);
-  if (av.n == 0) return;
-  OpinionArgs p{};
-  p.rp = v.row_ptr;
-  p.src = v.src;
-  p.w = (const double *)v.payload[0];
-  p.x = (const double *)av.rd[0];
-  p.xo = (double *)av.wr[0];
-  p.n = av.n;
-  p.nrows = v.nrows;
-  p.eps = eps;
-  p.a = a;
-  p.b = b;
-  p.hub_thr = 0xffffffffu;
-  if (v.nedges && c.call_type < (int)es.csr.size()) {
-    CSR &cs = es.csr[c.call_type];
-    ensure_schedule(s, cs, thr);
-    p.hub_rows = cs.hub_rows.as<uint32_t>();
-    p.nhub = cs.nhub;
-    p.hub_thr = thr;
-    p.hub_blocks = (unsigned)((cs.nhub + (TPB / 32) - 1) / (TPB / 32));
-  }
-  unsigned grid = p.hub_blocks + nblk(av.n);
-  k_opinion<<<grid, TPB, 0, s.stream>>>(p);
   VG_CUDA(cudaGetLastError());
 }
 
