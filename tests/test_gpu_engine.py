@@ -1,0 +1,536 @@
+"""The reference's known-answer tests through the GPU library (C ABI).
+
+Each test ports a scenario of the reference's test suite (cited) onto the
+product's API with the library's named transitions, and checks the values
+the reference asserts; the last test runs random transition sequences on
+the GPU and on the oracle and compares every state and edge.
+"""
+import functools
+import operator
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+NR = (1 << 36) - 1
+
+
+def nr(id):
+    return int(id) & NR
+
+
+# ---------------------------------------------------------- test/core.jl
+def core_model(vh):
+    return (vh.ModelTypes()
+            .register_agenttype("AMortal", [("foo", "i64")])
+            .register_agenttype("AMortalFixed", [("foo", "i64")])
+            .register_agenttype("AImm", [("foo", "i64")], ":Immortal")
+            .register_agenttype("AImmFixed", [("foo", "i64")], ":Immortal")
+            .register_agenttype("AImmFixedOversize", [("foo", "i64")], ":Immortal")
+            .register_agenttype("ADefault", [("foo", "i64"), ("bool", "bool")])
+            .register_edgetype("ESDict", [("foo", "i64")])
+            .register_edgetype("ESLDict1", [])
+            .register_edgetype("ESLDict2", [], ":SingleType", target="AImm")
+            .create_model("Test Core"))
+
+
+def core_sim(vh, m):
+    sim = vh.create_simulation(m)
+    a1 = vh.add_agent(sim, "AMortal", foo=1)
+    a2, a3 = vh.add_agents(sim, "AMortal", 2, foo=[2, 3])
+    avids = vh.add_agents(sim, "AImm", 10, foo=np.arange(1, 11))
+    avfids = vh.add_agents(sim, "AImmFixed", 10, foo=np.arange(1, 11))
+    vh.add_agents(sim, "AImmFixedOversize", 10, foo=np.arange(1, 11))
+    vh.add_agents(sim, "AMortalFixed", 10, foo=np.arange(1, 11))
+    vh.add_agents(sim, "ADefault", 10, foo=np.arange(1, 11), bool=True)
+    vh.add_edges(sim, "ESDict", [a2, a3, avids[0], avfids[9]], [a1] * 4, foo=[1, 2, 3, 4])
+    vh.add_edges(sim, "ESLDict1", avids, [a1] * 10)
+    vh.add_edges(sim, "ESLDict2", avfids, avids)
+    return sim, a1, a2, a3, avids, avfids
+
+
+ALL = ["AMortal", "AImm", "AImmFixed"]
+
+
+def test_core_accessors(vh):
+    """test/core.jl:161-208, 279-285"""
+    m = core_model(vh)
+    sim, a1, a2, a3, avids, avfids = core_sim(vh, m)
+    vh.finish_init(sim)
+    with pytest.raises(AssertionError):
+        vh.agentstate(sim, a2, "AImm")  # wrong type
+    with pytest.raises(AssertionError):
+        vh.agentstate(sim, a1, "AMortal")  # not readable outside a transition
+    vh.disable_transition_checks(sim, True)
+    assert vh.agentstate(sim, a1, "AMortal") == {"foo": 1}
+    assert vh.agentstate(sim, avfids[9], "AImmFixed") == {"foo": 10}
+    assert len(vh.edges(sim, a1, "ESDict")) == 4
+    assert vh.edges(sim, a2, "ESDict") is None
+    assert len(vh.neighborids(sim, avids[0], "ESLDict2")) == 1
+    ids = vh.neighborids(sim, a1, "ESLDict1")
+    assert ids[0] == avids[0] and ids[9] == avids[9]
+    assert vh.neighborids(sim, avids[9], "ESLDict2")[0] == avfids[9]
+    assert {"foo": 3} in vh.neighborstates_flexible(sim, a1, "ESDict")
+    assert vh.num_edges(sim, a1, "ESDict") == 4
+    assert vh.num_edges(sim, a2, "ESDict") == 0
+    assert vh.num_edges(sim, avids[0], "ESLDict2") == 1
+    sim.close()
+
+
+def test_core_transition_sums(vh):
+    """test/core.jl:289-394"""
+    m = core_model(vh)
+    E1, E2 = m["ESLDict1"].index, m["ESLDict2"].index
+    sim, a1, a2, a3, avids, avfids = core_sim(vh, m)
+    vh.finish_init(sim)
+    with pytest.raises(AssertionError):  # AImmFixed, a source type, is not readable
+        vh.apply_(sim, "neighbor_sum", "AImm", ["ESLDict2"], [], params=[E2, 0, 0])
+    sim.close()
+    sim, a1, a2, a3, avids, avfids = core_sim(vh, m)
+    vh.finish_init(sim)
+    vh.disable_transition_checks(sim, True)
+    vh.add_edge(sim, a1, a1, "ESLDict1")
+    vh.add_edge(sim, avids[0], avids[0], "ESLDict2")
+    vh.add_edge(sim, avfids[0], avfids[0], "ESLDict1")
+    vh.add_edge(sim, avfids[1], avfids[0], "ESLDict1")
+    vh.add_edge(sim, avfids[1], avfids[1], "ESLDict1")
+    vh.disable_transition_checks(sim, False)
+    for expect in (sum(range(1, 11)) + 1, 2 * sum(range(1, 11)) + 1):
+        vh.apply_(sim, "neighbor_sum", ["AMortal"], ALL + ["ESLDict1"], ["AMortal"],
+                  params=[E1, 0, 0])
+        vh.disable_transition_checks(sim, True)
+        assert vh.agentstate(sim, a1, "AMortal") == {"foo": expect}
+        vh.disable_transition_checks(sim, False)
+    sim.close()
+    sim, a1, a2, a3, avids, avfids = core_sim(vh, m)
+    vh.finish_init(sim)
+    vh.disable_transition_checks(sim, True)
+    vh.add_edge(sim, avids[0], avids[0], "ESLDict2")
+    vh.disable_transition_checks(sim, False)
+    for expect in (2, 3, 4):
+        vh.apply_(sim, "neighbor_sum", ["AImm"], ALL + ["ESLDict2"], ["AImm"], params=[E2, 0, 0])
+        vh.disable_transition_checks(sim, True)
+        assert vh.agentstate(sim, avids[0], "AImm") == {"foo": expect}
+        vh.disable_transition_checks(sim, False)
+    sim.close()
+    sim, a1, a2, a3, avids, avfids = core_sim(vh, m)
+    vh.finish_init(sim)
+    vh.disable_transition_checks(sim, True)
+    vh.add_edge(sim, avfids[0], avfids[0], "ESLDict1")
+    vh.add_edge(sim, avfids[1], avfids[0], "ESLDict1")
+    vh.add_edge(sim, avfids[1], avfids[1], "ESLDict1")
+    vh.disable_transition_checks(sim, False)
+    for expect in (3, 5, 7):
+        vh.apply_(sim, "neighbor_sum", ["AImmFixed"], ALL + ["ESLDict1"], ["AImmFixed"],
+                  params=[E1, 0, 0])
+        vh.disable_transition_checks(sim, True)
+        assert vh.agentstate(sim, avfids[0], "AImmFixed") == {"foo": expect}
+        vh.disable_transition_checks(sim, False)
+    sim.close()
+
+
+def test_core_mapreduce(vh):
+    """test/core.jl:87-107, 396-440"""
+    m = core_model(vh)
+    sim = core_sim(vh, m)[0]
+    vh.finish_init(sim)
+    for T in ["AImmFixed", "AImmFixedOversize", "AMortalFixed", "ADefault"]:
+        assert vh.mapreduce(sim, "foo", "+", T) == 55
+        assert vh.mapreduce(sim, "foo", "*", T) == functools.reduce(operator.mul, range(1, 11))
+        assert vh.mapreduce(sim, "foo", "&", T, datatype="i64") == \
+            functools.reduce(operator.and_, range(1, 11))
+        assert vh.mapreduce(sim, "foo", "|", T, datatype="i64") == \
+            functools.reduce(operator.or_, range(1, 11))
+        assert vh.mapreduce(sim, "foo", "max", T) == 10
+        assert vh.mapreduce(sim, "foo", "min", T) == 1
+    vh.apply_(sim, "die_if", ["AMortalFixed"], ["AMortalFixed"], ["AMortalFixed"], params=[0])
+    assert vh.mapreduce(sim, "foo", "+", "AMortalFixed") == 0
+    assert vh.mapreduce(sim, "bool", "&", "ADefault") is True
+    assert vh.mapreduce(sim, "bool", "|", "ADefault") is True
+    vh.apply_(sim, "set_field", ["ADefault"], ["ADefault"], ["ADefault"], params=[1, 0, 0])
+    assert vh.mapreduce(sim, "bool", "&", "ADefault") is False
+    assert vh.mapreduce(sim, "bool", "|", "ADefault") is False
+    vh.apply_(sim, "set_field", ["ADefault"], ["ADefault"], ["ADefault"], params=[1, 1, 0])
+    assert vh.mapreduce(sim, "bool", "&", "ADefault") is False
+    assert vh.mapreduce(sim, "bool", "|", "ADefault") is True
+    sim.close()
+
+
+def test_core_deaths_and_with_edge(vh):
+    """test/core.jl:133-157, 210-277"""
+    m = core_model(vh)
+    sim = core_sim(vh, m)[0]
+    vh.finish_init(sim)
+    c = vh.copy_simulation(sim)
+    assert len(vh.all_agents(c, "AMortalFixed")) == 10
+    vh.apply_(c, "die_if", "AMortalFixed", "AMortalFixed", "AMortalFixed", params=[1, 0, 6])
+    assert vh.num_agents(c, "AMortalFixed") == 5
+    assert sorted(a["foo"] for a in vh.all_agents(c, "AMortalFixed")) == [1, 2, 3, 4, 5]
+    assert vh.num_agents(sim, "AMortalFixed") == 10  # the copy is independent
+    c.close()
+    sim.close()
+    sim = vh.create_simulation(m)
+    aids = vh.add_agents(sim, "AMortal", 100, foo=np.arange(1, 101))
+    vh.add_edge(sim, aids[0], aids[1], "ESLDict1")
+    vh.finish_init(sim)
+    vh.apply_(sim, "die_if", "AMortal", "AMortal", "AMortal", with_edge="ESLDict1", params=[0])
+    assert vh.num_agents(sim, "AMortal") == 99
+    assert len(vh.all_agentids(sim, "AMortal")) == 99
+    sim.close()
+
+
+# ---------------------------------------------------------- test/edges.jl
+STATELESS = ["EdgeS", "EdgeSE", "EdgeST", "EdgeSI", "EdgeSEI", "EdgeSTI", "EdgeSETI", "EdgeSTs",
+             "EdgeSTsI", "EdgeSETsI"]
+STATEFUL = ["EdgeD", "EdgeE", "EdgeT", "EdgeI", "EdgeEI", "EdgeTI", "EdgeTs", "EdgeTsI"]
+
+
+def hashint(t, h):
+    return h in t[4:]
+
+
+def edges_model(vh):
+    m = (vh.ModelTypes().register_agenttype("Agent", [("foo", "i64")])
+         .register_agenttype("AgentB", [("foo", "i64")]))
+    for t in STATELESS + STATEFUL:
+        tag = t[4:]
+        hints = [h for c, h in (("S", ":Stateless"), ("E", ":SingleEdge"), ("I", ":IgnoreFrom"))
+                 if c in tag]
+        kw = {}
+        if "T" in tag:
+            hints.append(":SingleType")
+            kw["target"] = "Agent"
+            if "Ts" in tag:
+                kw["size"] = 10
+        m.register_edgetype(t, [] if t in STATELESS else [("foo", "i64")], *hints, **kw)
+    return m.create_model("Test Edges")
+
+
+def st(t, v):
+    return {} if t in STATELESS else {"foo": v}
+
+
+def test_edges_hint_combinations(vh):
+    """test/edges.jl:68-273"""
+    m = edges_model(vh)
+    sim = vh.create_simulation(m)
+    a1, a2, a3 = vh.add_agents(sim, "Agent", 3, foo=[1, 2, 3])
+    for t in STATELESS + STATEFUL:
+        vh.add_edge(sim, a2, a3, t, **st(t, 1))
+        if hashint(t, "E") and not hashint(t, "T") and not (hashint(t, "S") and hashint(t, "I")):
+            with pytest.raises(AssertionError):
+                vh.add_edge(sim, a1, a3, t, **st(t, 2))
+        elif not hashint(t, "E"):
+            vh.add_edge(sim, a1, a3, t, **st(t, 2))
+        vh.add_edge(sim, a3, a1, t, **st(t, 3))
+    vh.finish_init(sim)
+    vh.disable_transition_checks(sim, True)
+    for t in ["EdgeD", "EdgeT", "EdgeTs"]:
+        e = vh.edges(sim, a3, t)
+        assert e[0] == vh.Edge(a2, {"foo": 1}) and e[1] == vh.Edge(a1, {"foo": 2})
+        assert vh.edges(sim, a2, t) is None
+    assert vh.edges(sim, a3, "EdgeE") == vh.Edge(a2, {"foo": 1})
+    for t in ["EdgeD", "EdgeT", "EdgeTs", "EdgeS", "EdgeST", "EdgeSTs"]:
+        e = vh.neighborids(sim, a3, t)
+        assert e[0] == a2 and e[1] == a1
+        assert vh.neighborids(sim, a2, t) is None
+    for t in ["EdgeE", "EdgeSE"]:
+        assert vh.neighborids(sim, a3, t) == a2
+    for t in ["EdgeD", "EdgeT", "EdgeTs", "EdgeI", "EdgeTI", "EdgeTsI"]:
+        e = vh.edgestates(sim, a3, t)
+        assert e[0] == {"foo": 1} and e[1] == {"foo": 2}
+        assert vh.edgestates(sim, a2, t) is None
+    for t in ["EdgeE", "EdgeEI"]:
+        assert vh.edgestates(sim, a3, t) == {"foo": 1}
+    for t in ["EdgeD", "EdgeT", "EdgeTs", "EdgeI", "EdgeTI", "EdgeTsI", "EdgeS", "EdgeST",
+              "EdgeSTs", "EdgeSTI", "EdgeSTsI"]:
+        assert (vh.num_edges(sim, a1, t), vh.num_edges(sim, a2, t), vh.num_edges(sim, a3, t)) \
+            == (1, 0, 2), t
+    for t in STATELESS + STATEFUL:
+        assert (vh.has_edge(sim, a1, t), vh.has_edge(sim, a2, t), vh.has_edge(sim, a3, t)) \
+            == (True, False, True), t
+    vh.disable_transition_checks(sim, False)
+    for t in ["EdgeI", "EdgeEI", "EdgeTI", "EdgeTsI"] + STATELESS:
+        with pytest.raises(AssertionError):
+            vh.edges(sim, a1, t)
+    for t in ["EdgeI", "EdgeTI", "EdgeTsI", "EdgeSI", "EdgeSTI", "EdgeSTsI", "EdgeEI", "EdgeSEI",
+              "EdgeSETI", "EdgeSETsI"]:
+        with pytest.raises(AssertionError):
+            vh.neighborids(sim, a1, t)
+    for t in STATELESS:
+        with pytest.raises(AssertionError):
+            vh.edgestates(sim, a1, t)
+    for t in ["EdgeE", "EdgeEI", "EdgeSE", "EdgeSETI", "EdgeSETsI"]:
+        with pytest.raises(AssertionError):
+            vh.num_edges(sim, a1, t)
+    for t in ["EdgeD", "EdgeT", "EdgeI", "EdgeTI", "EdgeTs", "EdgeTsI"]:
+        assert vh.mapreduce(sim, "foo", "+", t) == 6, t
+    for t in ["EdgeE", "EdgeEI"]:
+        assert vh.mapreduce(sim, "foo", "+", t) == 4
+    for t in STATELESS + STATEFUL:
+        with pytest.raises(AssertionError):  # add_edge! outside apply! after finish_init!
+            vh.add_edge(sim, a1, a1, t, **st(t, 0))
+    for t in STATELESS + STATEFUL:  # reading an edge type not in `read`
+        with pytest.raises(AssertionError):
+            vh.apply_(sim, "count_edges", "Agent", [], ["Agent"], params=[m[t].index, 0, 0])
+    sim.close()
+
+
+def test_edges_num_edges_write(vh):
+    """test/edges.jl:278-316"""
+    m = edges_model(vh)
+    sim = vh.create_simulation(m)
+    for t in STATELESS + STATEFUL:
+        assert vh.num_edges(sim, t, write=False) == 0
+    id1, id2, id3 = vh.add_agents(sim, "Agent", 3, foo=0)
+    for t in STATELESS + STATEFUL:
+        vh.add_edges(sim, t, [id1, id3], [id1, id3], **st(t, 0))
+    for t in STATELESS + STATEFUL:
+        assert vh.num_edges(sim, t, write=True) == 2, t
+        assert vh.num_edges(sim, t, write=False) == 0
+    vh.finish_init(sim)
+    for t in STATELESS + STATEFUL:
+        assert vh.num_edges(sim, t) == 2
+    sim.close()
+
+
+@pytest.mark.parametrize("ET", ["EdgeD", "EdgeT", "EdgeI", "EdgeTI"])
+def test_edges_transition_readd(vh, ET):
+    """test/edges.jl:319-389 (one process, two agents)"""
+    m = edges_model(vh)
+    e = m[ET].index
+    sim = vh.create_simulation(m)
+    ids = vh.add_agents(sim, "Agent", 2, foo=[1, 2])
+    vh.add_edges(sim, ET, [ids[0], ids[1]], [ids[1], ids[0]], **st(ET, [2, 1]))
+    vh.finish_init(sim)
+
+    def counts():
+        vh.apply_(sim, "count_edges", ["Agent"], [ET], ["Agent"], params=[e, 0, 0])
+        return list(vh.read_agents(sim, "Agent")[0]["foo"])
+    assert counts() == [1, 1]
+    vh.apply_(sim, "keep", ["Agent"], [], [ET], add_existing=[ET])
+    assert counts() == [1, 1]
+    if ET == "EdgeD":
+        vh.apply_(sim, "readd_edges", ["Agent"], [ET], [ET], params=[e])
+        assert counts() == [1, 1]
+        vh.apply_(sim, "readd_edges", ["Agent"], [ET], [ET], add_existing=[ET], params=[e])
+        assert counts() == [2, 2]
+        vh.apply_(sim, "keep", ["Agent"], [], [ET])
+        assert counts() == [0, 0]
+    sim.close()
+
+
+# ---------------------------------------------------- test/remove_agents.jl
+@pytest.mark.parametrize("E", ["DEdge", "DEdgeST"])
+def test_dying_agents(vh, E):
+    """test/remove_agents.jl:22-112 (one process)"""
+    m = (vh.ModelTypes().register_agenttype("DAgent", [("idx", "i64")])
+         .register_agenttype("DAgentRemove", [])
+         .register_edgetype("DEdge", [])
+         .register_edgetype("DEdgeState", [("state", "i64")])
+         .register_edgetype("DSingleEdge", [], ":SingleEdge")
+         .register_edgetype("DEdgeST", [], ":SingleType", target="DAgent")
+         .create_model("remove_agents"))
+    for reps in (1, 2):
+        sim = vh.create_simulation(m)
+        ids = vh.add_agents(sim, "DAgent", 3, idx=[1, 2, 3])
+        rids = vh.add_agents(sim, "DAgentRemove", 1)
+        for _ in range(reps):
+            vh.add_edges(sim, E, ids, [ids[1]] * 3)
+            vh.add_edges(sim, "DEdgeState", rids, [ids[1]], state=0)
+        for _ in range(reps):
+            vh.add_edge(sim, ids[1], ids[2], E)
+        vh.finish_init(sim)
+        assert vh.num_edges(sim, E) == 4 * reps
+        assert vh.num_edges(sim, "DEdgeState") == reps
+        vh.apply_(sim, "die_if", ["DAgentRemove"], [], ["DAgentRemove"], params=[0])
+        assert vh.num_edges(sim, E) == 4 * reps
+        assert vh.num_edges(sim, "DEdgeState") == 0
+        vh.apply_(sim, "die_if", ["DAgent"], ["DAgent", E], ["DAgent"], params=[3, m[E].index])
+        assert vh.num_edges(sim, E) == 3 * reps
+        sim.close()
+
+
+# --------------------------------------------------- test/edgesiterator.jl
+@pytest.mark.parametrize("ET", STATEFUL)
+def test_edges_aggregate_after_deaths(vh, ET):
+    """test/edgesiterator.jl:55-109"""
+    m = edges_model(vh)
+    sim = vh.create_simulation(m)
+    assert vh.mapreduce(sim, "foo", "+", ET) == 0
+    aids = vh.add_agents(sim, "Agent", 10, foo=np.arange(1, 11))
+    vh.add_edges(sim, ET, [aids[0]] * 10, aids, foo=[nr(i) for i in aids])
+    vh.finish_init(sim)
+    assert vh.mapreduce(sim, "foo", "+", ET) == 55
+    vh.apply_(sim, "die_if", ["Agent"], [], ["Agent"], params=[0])
+    assert vh.mapreduce(sim, "foo", "+", ET) == 0
+    sim.close()
+    sim = vh.create_simulation(m)
+    aids = vh.add_agents(sim, "Agent", 10, foo=np.arange(1, 11))
+    bids = vh.add_agents(sim, "AgentB", 10, foo=np.arange(1, 11))
+    vh.add_edges(sim, ET, bids, aids, foo=np.arange(1, 11))
+    vh.finish_init(sim)
+    assert vh.mapreduce(sim, "foo", "+", ET) == 55
+    vh.apply_(sim, "die_if", ["Agent"], [], ["Agent"], params=[0])
+    assert vh.mapreduce(sim, "foo", "+", ET) == 0
+    sim.close()
+
+
+@pytest.mark.parametrize("ET", STATEFUL + STATELESS)
+def test_remove_edges_of_died_agents(vh, ET):
+    """test/edgesiterator.jl:111-217"""
+    m = edges_model(vh)
+    sim = vh.create_simulation(m)
+    aids = vh.add_agents(sim, "Agent", 10, foo=np.arange(1, 11))
+    bids = vh.add_agents(sim, "AgentB", 10, foo=np.arange(1, 11))
+    single_edge, single_type = m.has_hint(ET, ":SingleEdge"), m.has_hint(ET, ":SingleType")
+    vh.add_edges(sim, ET, bids, aids, **st(ET, np.arange(1, 11)))
+    vh.finish_init(sim)
+    assert vh.num_edges(sim, ET) == 10
+    vh.apply_(sim, "die_if", ["Agent"], [], ["Agent"], params=[0])
+    assert vh.num_edges(sim, ET) == 0
+    sim.close()
+    if m.has_hint(ET, ":IgnoreFrom"):
+        return
+    sim = vh.create_simulation(m)
+    aids = vh.add_agents(sim, "Agent", 10, foo=np.arange(1, 11))
+    bids = vh.add_agents(sim, "AgentB", 10, foo=np.arange(1, 11))
+    for i in range(10):
+        v = st(ET, i + 1)
+        if not single_edge:
+            vh.add_edge(sim, aids[i], aids[i], ET, **v)
+            if not single_type:
+                vh.add_edge(sim, aids[i], bids[i], ET, **v)
+        vh.add_edge(sim, bids[i], aids[i], ET, **v)
+        if not single_type:
+            vh.add_edge(sim, bids[i], bids[i], ET, **v)
+    vh.finish_init(sim)
+    vh.apply_(sim, "die_if", "AgentB", "AgentB", "AgentB", params=[2, 0, 2])
+    count = 5 + (10 if not single_edge else 0) + (5 if not single_type else 0) + \
+        (5 if not single_edge and not single_type else 0)
+    assert vh.num_edges(sim, ET) == count
+    sim.close()
+
+
+# --------------------------------------------------------- test/raster.jl
+def raster_model(vh):
+    return (vh.ModelTypes()
+            .register_agenttype("GridA", [("active", "bool")])
+            .register_agenttype("Grid3D", [("active", "bool")])
+            .register_edgetype("GridE", [])
+            .register_agenttype("Position", [("ids_sum", "i64")])
+            .register_agenttype("MovingAgent", [("value", "i64")])
+            .register_edgetype("OnPosition", [])
+            .create_model("Raster_Test"))
+
+
+@pytest.mark.parametrize("dims,start,T,kw,counts", [
+    ((10, 8), (10, 8), "GridA", {}, (1, 9, 25)),
+    ((7, 9), (3, 5), "GridA", {}, (1, 9, 25)),
+    ((17, 6), (9, 1), "GridA", {}, (1, 9, 25)),
+    ((6, 7), (1, 1), "GridA", {}, (1, 9, 25)),
+    ((6, 7, 6), (1, 1, 1), "Grid3D", {}, (1, 27, 125)),
+    ((6, 7, 6), (1, 1, 1), "Grid3D", {"periodic": False}, (1, 8, 27)),
+    ((6, 7, 6), (1, 1, 1), "Grid3D", {"periodic": False, "distance": 2}, (1, 27, 125)),
+    ((6, 7, 6), (1, 1, 1), "Grid3D", {"distance": 1.5, "metric": "euclidean"}, (1, 27 - 8)),
+    ((6, 7, 6), (1, 1, 1), "Grid3D", {"distance": 1.5, "metric": "manhatten"}, (1, 7)),
+    ((6, 7, 6), (1, 1, 1), "Grid3D", {"periodic": False, "distance": 2, "metric": "manhatten"},
+     (1, 10)),
+])
+@pytest.mark.parametrize("implicit", [False, True])
+def test_raster_diffusion(vh, dims, start, T, kw, counts, implicit):
+    """test/raster.jl:34-289 (explicit edges through the generic gather; implicit
+    edges through the stencil kernel with the B1..8/S0..8 rule = diffusion)"""
+    m = raster_model(vh)
+    sim = vh.create_simulation(m)
+    active = np.zeros(dims, dtype=bool)
+    active[tuple(s - 1 for s in start)] = True
+    vh.add_raster(sim, "grid", dims, T, active=active)
+    vh.connect_raster_neighbors(sim, "grid", "GridE", implicit=implicit, **kw)
+    vh.finish_init(sim)
+    E = m["GridE"].index
+    assert vh.mapreduce(sim, "active", "+", T) == counts[0]
+    for c in counts[1:]:
+        if implicit:  # born with >= 1 alive neighbour, always survive
+            vh.apply_(sim, "life", [T], [T, "GridE"], [T], params=[E, 0x7FFFFFFE, 0x7FFFFFFF])
+        else:
+            vh.apply_(sim, "neighbor_or", [T], [T, "GridE"], [T], params=[E, 0, 0])
+        assert vh.mapreduce(sim, "active", "+", T) == c
+    r = vh.rastervalues(sim, "grid", "active")
+    assert r.shape == dims
+    sim.close()
+
+
+def test_raster_move_to_counts(vh):
+    """test/raster.jl:374-436"""
+    m = raster_model(vh)
+    sim = vh.create_simulation(m)
+    vh.add_raster(sim, "raster", (10, 10), "Position", ids_sum=0)
+    p = vh.add_agents(sim, "MovingAgent", 3, value=1)
+    vh.move_to(sim, "raster", p[0], (4, 4), "OnPosition", None, distance=2)
+    vh.move_to(sim, "raster", p[1], (4, 4), "OnPosition", None, distance=2, metric="manhatten")
+    vh.move_to(sim, "raster", p[2], (4, 4), "OnPosition", None, distance=2.5, metric="euclidean")
+    vh.finish_init(sim)
+    vh.disable_transition_checks(sim, True)
+    assert [vh.num_edges(sim, x, "OnPosition") for x in p] == [25, 13, 21]
+    sim.close()
+    sim = vh.create_simulation(m)
+    vh.add_raster(sim, "raster", (10, 10, 10, 10), "Position", ids_sum=0)
+    p = vh.add_agents(sim, "MovingAgent", 2, value=1)
+    vh.move_to(sim, "raster", p[0], (4, 4, 4, 4), "OnPosition", None, distance=1)
+    vh.move_to(sim, "raster", p[1], (4, 4, 4, 4), "OnPosition", None, distance=1,
+               metric="manhatten")
+    vh.finish_init(sim)
+    vh.disable_transition_checks(sim, True)
+    assert [vh.num_edges(sim, x, "OnPosition") for x in p] == [81, 9]
+    assert vh.cellid(sim, "raster", (1, 1, 1, 1)) == vh.agent_id(m["Position"].index, 1)
+    sim.close()
+
+
+# ---------------------------------------------------------- test/graphs.jl
+def test_complete_graph_sum(vh):
+    """test/graphs.jl:237-266"""
+    m = (vh.ModelTypes().register_agenttype("GraphA", [("id", "i64"), ("sum", "i64")])
+         .register_edgetype("GraphE", []).create_model("g"))
+    sim = vh.create_simulation(m)
+    n = 4
+    ids = vh.add_agents(sim, "GraphA", n, id=np.arange(1, n + 1), sum=0)
+    for a in range(n):
+        for b in range(a + 1, n):
+            vh.add_edge(sim, ids[a], ids[b], "GraphE")
+            vh.add_edge(sim, ids[b], ids[a], "GraphE")
+    vh.finish_init(sim)
+    vh.apply_(sim, "neighbor_sum", ["GraphA"], ["GraphA", "GraphE"], ["GraphA"],
+              params=[m["GraphE"].index, 0, 1])
+    assert vh.mapreduce(sim, "sum", "+", "GraphA") == sum(range(1, n + 1)) * (n - 1)
+    sim.close()
+
+
+# ------------------------------------------------------ test/addexisting.jl
+def test_add_existing(vh):
+    """test/addexisting.jl:127-203"""
+    m = (vh.ModelTypes().register_agenttype("ComputeAgent", [])
+         .register_agenttype("ConstructedAgent", []).register_edgetype("Connection", [])
+         .create_model("Test add_existing"))
+    sim = vh.create_simulation(m)
+    c = vh.add_agent(sim, "ComputeAgent")
+    k = vh.add_agent(sim, "ConstructedAgent")
+    vh.add_edge(sim, k, c, "Connection")
+    vh.finish_init(sim)
+    vh.apply_(sim, "keep", "ComputeAgent", [], "Connection", add_existing="Connection")
+    assert vh.num_edges(sim, "Connection") == 1
+    vh.apply_(sim, "keep", ["ComputeAgent"], [], ["ConstructedAgent", "Connection"])
+    assert vh.num_agents(sim, "ComputeAgent") == 1
+    assert vh.num_agents(sim, "ConstructedAgent") == 0
+    assert vh.num_edges(sim, "Connection") == 0
+    sim.close()
+    m2 = (vh.ModelTypes().register_agenttype("ComputeAgent", [])
+          .register_agenttype("ConstructedAgent", [], ":Immortal")
+          .register_edgetype("Connection", []).create_model("imm"))
+    sim = vh.create_simulation(m2)
+    vh.add_agent(sim, "ComputeAgent")
+    vh.finish_init(sim)
+    with pytest.raises(AssertionError):
+        vh.apply_(sim, "keep", ["ComputeAgent"], [], ["ConstructedAgent", "Connection"])
+    sim.close()

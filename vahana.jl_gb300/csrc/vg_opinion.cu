@@ -64,6 +64,12 @@ __device__ __forceinline__ float hi_float(double v, bool &ok) {
   return __int_as_float((int)((h - 0x38000000u) << 3));
 }
 
+// exact binary64 test, out of line so that it is never evaluated
+// speculatively on the FP64 pipe
+__device__ __noinline__ bool within_exact(double xj, double xi, double eps) {
+  return fabs(__dsub_rn(xj, xi)) < eps;
+}
+
 // |x_j - x_i| < eps, exactly as binary64 would decide it
 __device__ __forceinline__ bool within(double xj, double xi, float fxi, bool xi_ok,
                                        const OpinionArgs &p) {
@@ -74,48 +80,96 @@ __device__ __forceinline__ bool within(double xj, double xi, float fxi, bool xi_
     if (fd < p.eps_lo) return true;
     if (fd > p.eps_hi) return false;
   }
-  return fabs(__dsub_rn(xj, xi)) < p.eps;
+  return within_exact(xj, xi, p.eps);
 }
 
-__device__ __forceinline__ uint64_t add_rn(uint64_t a, uint64_t b) {
+__device__ __noinline__ uint64_t add_rn(uint64_t a, uint64_t b) {
   bool ok = ((a | b) >> 63) == 0;
   uint64_t r = ok ? emu_add_pos(a, b, ok) : 0;
-  return ok ? r : bits(__dadd_rn(dbl(a), dbl(b)));
+  if (ok) return r;
+  return bits(__dadd_rn(dbl(a), dbl(b)));
 }
 
-__device__ __forceinline__ uint64_t mul_rn(uint64_t a, uint64_t b) {
+__device__ __noinline__ uint64_t mul_rn(uint64_t a, uint64_t b) {
   bool ok = ((a | b) >> 63) == 0;
   uint64_t r = ok ? emu_mul_pos(a, b, ok) : 0;
-  return ok ? r : bits(__dmul_rn(dbl(a), dbl(b)));
+  if (ok) return r;
+  return bits(__dmul_rn(dbl(a), dbl(b)));
 }
 
-__device__ __forceinline__ uint64_t div_rn(uint64_t a, uint64_t b) {
+__device__ __noinline__ uint64_t div_rn(uint64_t a, uint64_t b) {
   bool ok = ((a | b) >> 63) == 0;
   uint64_t r = ok ? emu_div_pos(a, b, ok) : 0;
-  return ok ? r : bits(__ddiv_rn(dbl(a), dbl(b)));
+  if (ok) return r;
+  return bits(__ddiv_rn(dbl(a), dbl(b)));
+}
+
+// Running sum held decoded: biased exponent e and the 53-bit significand m
+// with its leading bit, value m * 2^(e - 1075).  e = 0 holds the bit
+// pattern itself in m (zero, or a subnormal sum), handled by the general
+// path.
+struct Acc {
+  uint32_t e;
+  uint64_t m;
+};
+
+__device__ __forceinline__ uint64_t acc_bits(const Acc &a) {
+  return a.e ? (((uint64_t)a.e << 52) | (a.m & EMU_M52)) : a.m;
+}
+
+__device__ __noinline__ Acc acc_add_general(Acc a, uint64_t pb) {
+  uint64_t r = add_rn(acc_bits(a), pb);
+  Acc o;
+  o.e = (uint32_t)(r >> 52);
+  o.m = o.e ? ((r & EMU_M52) | EMU_H53) : r;
+  return o;
+}
+
+// a += p (p >= 0 given as bits), correctly rounded.  Fast path: p is 1 to
+// 31 binades below the sum and the sum stays in its binade -- then the sum
+// is m + round(P / 2^d) in units of the sum's ulp, ties to even.
+__device__ __forceinline__ void acc_add(Acc &a, uint64_t pb) {
+  uint32_t phi = (uint32_t)(pb >> 32), plo = (uint32_t)pb;
+  uint32_t ep = phi >> 20;
+  uint32_t d = a.e - ep;
+  if (d - 1u < 31u && ep != 0 && a.e < 2046u) {
+    uint32_t Phi = (phi & 0xFFFFFu) | 0x100000u;
+    uint32_t Qlo = __funnelshift_r(plo, Phi, d);
+    uint32_t Qhi = Phi >> d;
+    uint32_t R = plo & ((1u << d) - 1u);
+    uint32_t half = 1u << (d - 1u);
+    uint64_t M = a.m + (((uint64_t)Qhi << 32) | Qlo);
+    M += (uint64_t)((R > half) | ((R == half) & (uint32_t)M));
+    if (M < (1ull << 53)) {
+      a.m = M;
+      return;
+    }
+  } else if (d - 54u < 2000u && a.e != 0 && ep != 0) {
+    return;  // p < half an ulp of the sum: the sum is unchanged
+  }
+  a = acc_add_general(a, pb);
 }
 
 // x' = a x + b (swx / sw), each operation rounded in this order
-__device__ __forceinline__ double finish(const OpinionArgs &p, double xi, uint64_t sw,
-                                         uint64_t swx, uint32_t cnt) {
-  if (!cnt) return xi;
+__device__ __noinline__ double finish(double pa, double pb_, double xi, uint64_t sw,
+                                      uint64_t swx) {
   uint64_t m = div_rn(swx, sw);
-  uint64_t l = mul_rn(bits(p.a), bits(xi));
-  uint64_t r = mul_rn(bits(p.b), m);
+  uint64_t l = mul_rn(bits(pa), bits(xi));
+  uint64_t r = mul_rn(bits(pb_), m);
   return dbl(add_rn(l, r));
 }
 
 // ordered fold of edges [b, e) of a row into (sw, swx, cnt)
 __device__ __forceinline__ void fold(const OpinionArgs &p, uint32_t b, uint32_t e, double xi,
-                                     float fxi, bool xi_ok, uint64_t &sw, uint64_t &swx,
+                                     float fxi, bool xi_ok, Acc &sw, Acc &swx,
                                      uint32_t &cnt) {
   for (uint32_t k = b; k < e; k++) {
     double xj = __ldg(p.x + __ldg(p.src + k));
     if (within(xj, xi, fxi, xi_ok, p)) {
       double wk = __ldg(p.w + k);
       double pk = __dmul_rn(wk, xj);
-      sw = add_rn(sw, bits(wk));
-      swx = add_rn(swx, bits(pk));
+      acc_add(sw, bits(wk));
+      acc_add(swx, bits(pk));
       cnt++;
     }
   }
@@ -134,22 +188,23 @@ __global__ void __launch_bounds__(TPB) k_opinion(OpinionArgs p) {
     uint32_t b = p.rp[r], e = p.rp[r + 1];
     uint32_t chunk = (e - b + 31) / 32;
     uint32_t cb = min(e, b + lane * chunk), ce = min(e, cb + chunk);
-    uint64_t sw = 0, swx = 0;
+    Acc asw{0, 0}, aswx{0, 0};
     uint32_t cnt = 0;
-    fold(p, cb, ce, xi, fxi, xi_ok, sw, swx, cnt);
+    fold(p, cb, ce, xi, fxi, xi_ok, asw, aswx, cnt);
+    uint64_t sw = acc_bits(asw), swx = acc_bits(aswx);
     // fixed tree: lane l receives lane l + off
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
       uint64_t osw = __shfl_down_sync(0xffffffffu, sw, off);
       uint64_t oswx = __shfl_down_sync(0xffffffffu, swx, off);
       uint32_t ocnt = __shfl_down_sync(0xffffffffu, cnt, off);
-      if ((lane & (2 * off - 1)) == 0) {
+      if ((lane & (2 * off - 1)) == 0 && ocnt) {
         sw = add_rn(sw, osw);
         swx = add_rn(swx, oswx);
         cnt += ocnt;
       }
     }
-    if (lane == 0) p.xo[r] = finish(p, xi, sw, swx, cnt);
+    if (lane == 0) p.xo[r] = cnt ? finish(p.a, p.b, xi, sw, swx) : xi;
     return;
   }
   uint64_t i = (uint64_t)(blockIdx.x - p.hub_blocks) * TPB + threadIdx.x;
@@ -163,10 +218,10 @@ __global__ void __launch_bounds__(TPB) k_opinion(OpinionArgs p) {
   if (e - b > p.hub_thr) return;  // a hub warp writes this row
   bool xi_ok;
   float fxi = hi_float(xi, xi_ok);
-  uint64_t sw = 0, swx = 0;
+  Acc sw{0, 0}, swx{0, 0};
   uint32_t cnt = 0;
   fold(p, b, e, xi, fxi, xi_ok, sw, swx, cnt);
-  p.xo[i] = finish(p, xi, sw, swx, cnt);
+  p.xo[i] = cnt ? finish(p.a, p.b, xi, acc_bits(sw), acc_bits(swx)) : xi;
 }
 
 }  // namespace
