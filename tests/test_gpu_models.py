@@ -54,6 +54,30 @@ def test_opinion_bit_exact(vh):
     run.close()
 
 
+def test_opinion_bit_exact_arbitrary_weights(vh):
+    """Weights that are not multiples of 2^-53 take the kernel's binary64
+    add path for sw; still bit-identical to the sequential fold."""
+    from vahana_gb300 import models
+    rng = np.random.default_rng(5)
+    n, E = 3000, 60000
+    m = models.opinion_model()
+    sim = vh.create_simulation(m)
+    x0 = rng.random(n)
+    ids = vh.add_agents(sim, "Opinion", n, x=x0)
+    frm = ids[rng.integers(0, n, E)]
+    to = ids[np.minimum(rng.zipf(1.8, E) - 1, n - 1)]  # skewed in-degrees
+    w = rng.random(E) * 0.7 + 1e-3                      # off the 2^-53 grid
+    vh.add_edges(sim, "Weight", frm, to, w=w)
+    vh.finish_init(sim)
+    for _ in range(8):
+        vh.apply_(sim, "bounded_confidence", ["Opinion"], ["Opinion", "Weight"], ["Opinion"],
+                  params=[m["Weight"].index, 0.3, 0.5, 0.5, NO_SPLIT])
+    x = vh.read_agents(sim, "Opinion")[0]["x"]
+    ref = om.run_opinion(n, frm, to, w, x0, 0.3, 8)
+    np.testing.assert_array_equal(x.view(np.uint64), ref.view(np.uint64))
+    sim.close()
+
+
 @pytest.mark.parametrize("hub", [256, 16])
 def test_opinion_hub_split(vh, hub):
     """Hub rows (in-degree > hub) are summed in split chunks: within 1e-12

@@ -146,6 +146,9 @@ struct CSR {
   uint64_t nhub = 0;
   uint32_t hub_threshold = 0;
   bool schedule_valid = false;
+  // payload field 0 (Float64) holds only multiples of 2^-53 in (0, 1]:
+  // -1 not checked yet, 0 no, 1 yes (decides the gather kernels' sum path)
+  int unit_grid_weights = -1;
 };
 
 struct StencilDesc {

@@ -19,14 +19,21 @@
 //   The hub warps are the first blocks of the grid so that they start
 //   first.
 //
-// Arithmetic placement on GB300, whose FP64 pipe issues about 2 operations
-// per clock per SM: the threshold test runs on a float filter of the two
-// doubles' high words (exact binary64 test only within 1e-5 of eps); the
-// products w_j * x_j stay on the FP64 pipe; the additions of sw and swx and
-// the per-row division and mixing run as exact round-to-nearest-even
-// integer arithmetic (vg_fp64emu.cuh), falling back to the FP64
-// instruction outside its range.  Every operation is the correctly
-// rounded binary64 result in the reference's order.
+// Arithmetic placement on GB300 (the FP64 pipe issues about 2 operations
+// per clock per SM; the integer ALU pipe is the next scarcest):
+//   threshold test  float filter of the doubles' high words on the FMA
+//                   pipe; the exact binary64 test only within 1e-5 of eps
+//   w_j * x_j       exact round-to-nearest-even product from 32x32-bit
+//                   multiplies (IMAD.WIDE, FMA pipe)
+//   swx += p        the hardware FP64 add (the one FP64 operation per edge)
+//   sw += w         when every weight is a multiple of 2^-53 in (0, 1] (the
+//                   edge type's weights are checked once), sw is kept as an
+//                   integer count K of 2^-53 units and rounded to 53
+//                   significant bits after each addition -- exactly the
+//                   binary64 sum; otherwise the hardware FP64 add
+//   per row         division and mixing as exact integer arithmetic
+// Every operation is the correctly rounded binary64 result, in the
+// reference's order.
 #include <algorithm>
 #include <cmath>
 
@@ -51,6 +58,7 @@ struct OpinionArgs {
   unsigned hub_blocks;
   double eps, a, b;
   float eps_lo, eps_hi;  // float filter: certainly inside / certainly outside
+  int grid;              // all weights are multiples of 2^-53 in (0, 1]
 };
 
 __device__ __forceinline__ uint64_t bits(double v) { return (uint64_t)__double_as_longlong(v); }
@@ -104,50 +112,53 @@ __device__ __noinline__ uint64_t div_rn(uint64_t a, uint64_t b) {
   return bits(__ddiv_rn(dbl(a), dbl(b)));
 }
 
-// Running sum held decoded: biased exponent e and the 53-bit significand m
-// with its leading bit, value m * 2^(e - 1075).  e = 0 holds the bit
-// pattern itself in m (zero, or a subnormal sum), handled by the general
-// path.
-struct Acc {
-  uint32_t e;
-  uint64_t m;
-};
+__device__ __noinline__ double mul_hw(double a, double b) { return __dmul_rn(a, b); }
 
-__device__ __forceinline__ uint64_t acc_bits(const Acc &a) {
-  return a.e ? (((uint64_t)a.e << 52) | (a.m & EMU_M52)) : a.m;
+// a * b for positive normal a, b with a normal result: the 106-bit
+// significand product from four 32x32-bit multiplies, rounded to nearest
+// even.  `ok` is false for other operands (the caller then multiplies on the
+// FP64 pipe).
+__device__ __forceinline__ uint64_t mul_fast(uint64_t a, uint64_t b, bool &ok) {
+  uint32_t ahi = (uint32_t)(a >> 32), alo = (uint32_t)a;
+  uint32_t bhi = (uint32_t)(b >> 32), blo = (uint32_t)b;
+  uint32_t ea = ahi >> 20, eb = bhi >> 20;  // sign bits are 0 here
+  uint32_t mah = (ahi & 0xFFFFFu) | 0x100000u, mbh = (bhi & 0xFFFFFu) | 0x100000u;
+  uint64_t ll = (uint64_t)alo * blo;
+  uint64_t mid = (uint64_t)mah * blo + (uint64_t)alo * mbh;  // < 2^54
+  uint64_t hh = (uint64_t)mah * mbh;                         // < 2^42
+  uint64_t t1 = (ll >> 32) + (mid & 0xFFFFFFFFull);           // < 2^33
+  uint32_t w1 = (uint32_t)t1;
+  uint64_t t2 = (mid >> 32) + hh + (t1 >> 32);  // product bits 64.. (P = t2 2^64 + w1 2^32 + ll.lo)
+  uint32_t big = (uint32_t)(t2 >> 41);          // P >= 2^105
+  uint64_t q = (t2 << (12 - big)) | (uint64_t)(w1 >> (20 + big));
+  uint32_t rb = (w1 >> (19 + big)) & 1u;
+  uint32_t sticky = (w1 & ((1u << (19 + big)) - 1u)) | (uint32_t)ll;
+  q += rb & ((uint32_t)(sticky != 0) | (uint32_t)q);
+  uint32_t c = (uint32_t)(q >> 53);
+  q >>= c;
+  int e = (int)ea + (int)eb - 1023 + (int)big + (int)c;
+  ok = (e > 0) & (e < 2047) & (ea - 1u < 2046u) & (eb - 1u < 2046u);
+  return ((uint64_t)e << 52) | (q & EMU_M52);
 }
 
-__device__ __noinline__ Acc acc_add_general(Acc a, uint64_t pb) {
-  uint64_t r = add_rn(acc_bits(a), pb);
-  Acc o;
-  o.e = (uint32_t)(r >> 52);
-  o.m = o.e ? ((r & EMU_M52) | EMU_H53) : r;
-  return o;
-}
-
-// a += p (p >= 0 given as bits), correctly rounded.  Fast path: p is 1 to
-// 31 binades below the sum and the sum stays in its binade -- then the sum
-// is m + round(P / 2^d) in units of the sum's ulp, ties to even.
-__device__ __forceinline__ void acc_add(Acc &a, uint64_t pb) {
-  uint32_t phi = (uint32_t)(pb >> 32), plo = (uint32_t)pb;
-  uint32_t ep = phi >> 20;
-  uint32_t d = a.e - ep;
-  if (d - 1u < 31u && ep != 0 && a.e < 2046u) {
-    uint32_t Phi = (phi & 0xFFFFFu) | 0x100000u;
-    uint32_t Qlo = __funnelshift_r(plo, Phi, d);
-    uint32_t Qhi = Phi >> d;
-    uint32_t R = plo & ((1u << d) - 1u);
-    uint32_t half = 1u << (d - 1u);
-    uint64_t M = a.m + (((uint64_t)Qhi << 32) | Qlo);
-    M += (uint64_t)((R > half) | ((R == half) & (uint32_t)M));
-    if (M < (1ull << 53)) {
-      a.m = M;
-      return;
-    }
-  } else if (d - 54u < 2000u && a.e != 0 && ep != 0) {
-    return;  // p < half an ulp of the sum: the sum is unchanged
+// sw as an integer K of 2^-53 units: K += w * 2^53, then K rounded to 53
+// significant bits (ties to even) -- the binary64 sum, valid while every
+// weight is a multiple of 2^-53 in (0, 1] and K < 2^64.
+__device__ __forceinline__ void grid_add(uint64_t &K, double w) {
+  uint64_t wb = bits(w);
+  uint32_t ew = (uint32_t)(wb >> 52);
+  uint64_t m = (wb & EMU_M52) | EMU_H53;
+  uint64_t k = ew >= 1023u ? (m << 1) : (m >> (1022u - ew));
+  K += k;
+  uint32_t khi = (uint32_t)(K >> 32);
+  int s = 11 - __clz(khi);  // significant bits beyond 53
+  if (s > 0) {
+    uint32_t lo = (uint32_t)K;
+    uint32_t mask = (1u << s) - 1u, half = 1u << (s - 1);
+    uint32_t rem = lo & mask;
+    K -= rem;
+    if ((rem > half) | ((rem == half) & ((lo >> s) & 1u))) K += (1ull << s);
   }
-  a = acc_add_general(a, pb);
 }
 
 // x' = a x + b (swx / sw), each operation rounded in this order
@@ -160,21 +171,31 @@ __device__ __noinline__ double finish(double pa, double pb_, double xi, uint64_t
 }
 
 // ordered fold of edges [b, e) of a row into (sw, swx, cnt)
+template <bool GRID>
 __device__ __forceinline__ void fold(const OpinionArgs &p, uint32_t b, uint32_t e, double xi,
-                                     float fxi, bool xi_ok, Acc &sw, Acc &swx,
-                                     uint32_t &cnt) {
+                                     float fxi, bool xi_ok, uint64_t &K, double &sw,
+                                     double &swx, uint32_t &cnt) {
   for (uint32_t k = b; k < e; k++) {
     double xj = __ldg(p.x + __ldg(p.src + k));
     if (within(xj, xi, fxi, xi_ok, p)) {
       double wk = __ldg(p.w + k);
-      double pk = __dmul_rn(wk, xj);
-      acc_add(sw, bits(wk));
-      acc_add(swx, bits(pk));
+      bool ok;
+      uint64_t pk = mul_fast(bits(wk), bits(xj), ok);
+      double pkd = ok ? dbl(pk) : mul_hw(wk, xj);
+      swx = __dadd_rn(swx, pkd);
+      if (GRID) grid_add(K, wk);
+      else sw = __dadd_rn(sw, wk);
       cnt++;
     }
   }
 }
 
+template <bool GRID>
+__device__ __forceinline__ double sum_w(uint64_t K, double sw) {
+  return GRID ? __dmul_rn(__ull2double_rn(K), 0x1p-53) : sw;
+}
+
+template <bool GRID>
 __global__ void __launch_bounds__(TPB) k_opinion(OpinionArgs p) {
   if (blockIdx.x < p.hub_blocks) {
     // one warp per hub row: lane l folds the l-th contiguous chunk in order
@@ -188,10 +209,13 @@ __global__ void __launch_bounds__(TPB) k_opinion(OpinionArgs p) {
     uint32_t b = p.rp[r], e = p.rp[r + 1];
     uint32_t chunk = (e - b + 31) / 32;
     uint32_t cb = min(e, b + lane * chunk), ce = min(e, cb + chunk);
-    Acc asw{0, 0}, aswx{0, 0};
+    uint64_t K = 0;
+    double dsw = 0.0, dswx = 0.0;
     uint32_t cnt = 0;
-    fold(p, cb, ce, xi, fxi, xi_ok, asw, aswx, cnt);
-    uint64_t sw = acc_bits(asw), swx = acc_bits(aswx);
+    if (GRID && ce - cb <= 2047) fold<true>(p, cb, ce, xi, fxi, xi_ok, K, dsw, dswx, cnt);
+    else fold<false>(p, cb, ce, xi, fxi, xi_ok, K, dsw, dswx, cnt);
+    uint64_t sw = bits(GRID && ce - cb <= 2047 ? sum_w<true>(K, dsw) : dsw);
+    uint64_t swx = bits(dswx);
     // fixed tree: lane l receives lane l + off
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
@@ -218,10 +242,31 @@ __global__ void __launch_bounds__(TPB) k_opinion(OpinionArgs p) {
   if (e - b > p.hub_thr) return;  // a hub warp writes this row
   bool xi_ok;
   float fxi = hi_float(xi, xi_ok);
-  Acc sw{0, 0}, swx{0, 0};
+  uint64_t K = 0;
+  double dsw = 0.0, swx = 0.0;
   uint32_t cnt = 0;
-  fold(p, b, e, xi, fxi, xi_ok, sw, swx, cnt);
-  p.xo[i] = cnt ? finish(p.a, p.b, xi, acc_bits(sw), acc_bits(swx)) : xi;
+  if (!GRID || e - b > 2047) {  // K would overflow: binary64 adds
+    fold<false>(p, b, e, xi, fxi, xi_ok, K, dsw, swx, cnt);
+    p.xo[i] = cnt ? finish(p.a, p.b, xi, bits(dsw), bits(swx)) : xi;
+    return;
+  }
+  fold<true>(p, b, e, xi, fxi, xi_ok, K, dsw, swx, cnt);
+  p.xo[i] = cnt ? finish(p.a, p.b, xi, bits(sum_w<true>(K, dsw)), bits(swx)) : xi;
+}
+
+// every weight a multiple of 2^-53 in (0, 1]?
+__global__ void k_check_grid(const double *w, uint64_t n, int *bad) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t wb = bits(w[i]);
+    uint32_t ew = (uint32_t)(wb >> 52);
+    bool ok = (wb >> 63) == 0 && ew >= 970u && ew <= 1023u && (ew < 1023u || (wb & EMU_M52) == 0);
+    if (ok && ew < 1022u) {
+      uint64_t m = (wb & EMU_M52) | EMU_H53;
+      ok = (m & ((1ull << (1022u - ew)) - 1ull)) == 0;
+    }
+    if (!ok) atomicExch(bad, 1);
+  }
 }
 
 }  // namespace
@@ -271,16 +316,31 @@ void tr_bounded_confidence(ApplyCtx &c) {
   p.eps_lo = (float)(eps - 1e-5);
   p.eps_hi = (float)(eps + 1e-5);
   p.hub_thr = 0xffffffffu;
-  if (v.nedges && c.call_type < (int)es.csr.size() && thr != 0xffffffffu) {
+  if (v.nedges && c.call_type < (int)es.csr.size()) {
     CSR &cs = es.csr[c.call_type];
-    ensure_schedule(s, cs, thr);
-    p.hub_rows = cs.hub_rows.as<uint32_t>();
-    p.nhub = cs.nhub;
-    p.hub_thr = thr;
-    p.hub_blocks = (unsigned)((cs.nhub + (TPB / 32) - 1) / (TPB / 32));
+    if (cs.unit_grid_weights < 0) {
+      int *bad = nullptr;
+      VG_CUDA(cudaMallocAsync((void **)&bad, 4, s.stream));
+      VG_CUDA(cudaMemsetAsync(bad, 0, 4, s.stream));
+      k_check_grid<<<1024, TPB, 0, s.stream>>>(p.w, v.nedges, bad);
+      int h = 0;
+      VG_CUDA(cudaMemcpyAsync(&h, bad, 4, cudaMemcpyDeviceToHost, s.stream));
+      VG_CUDA(cudaFreeAsync(bad, s.stream));
+      VG_CUDA(cudaStreamSynchronize(s.stream));
+      cs.unit_grid_weights = h ? 0 : 1;
+    }
+    p.grid = cs.unit_grid_weights;
+    if (thr != 0xffffffffu) {
+      ensure_schedule(s, cs, thr);
+      p.hub_rows = cs.hub_rows.as<uint32_t>();
+      p.nhub = cs.nhub;
+      p.hub_thr = thr;
+      p.hub_blocks = (unsigned)((cs.nhub + (TPB / 32) - 1) / (TPB / 32));
+    }
   }
   unsigned grid = p.hub_blocks + (unsigned)((av.n + TPB - 1) / TPB);
-  k_opinion<<<grid, TPB, 0, s.stream>>>(p);
+  if (p.grid) k_opinion<true><<<grid, TPB, 0, s.stream>>>(p);
+  else k_opinion<false><<<grid, TPB, 0, s.stream>>>(p);
   VG_CUDA(cudaGetLastError());
 }
 
