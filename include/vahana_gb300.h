@@ -332,9 +332,16 @@ int vg_batch_step(vg_batch *b, int steps, int mode);
 int vg_batch_step_one(vg_batch *b, int i, int steps);
 int vg_batch_read_states(vg_batch *b, int i, uint8_t *state_out,
                          int32_t *days_out, uint64_t cap, uint64_t *n_out);
+/* which = 0: instance i's state in the batched arena; which = 1: the state
+ * of instance i's own simulation (advanced by vg_batch_step_one). */
+int vg_batch_read_states2(vg_batch *b, int i, int which, uint8_t *state_out,
+                          int32_t *days_out, uint64_t cap, uint64_t *n_out);
 int vg_batch_read_graph(vg_batch *b, int i, uint32_t *row_ptr_out,
                         uint32_t *src_out, uint64_t *nrows_out,
                         uint64_t *nedges_out);
+/* Totals of the arena and the launch shape the autotuner chose. */
+int vg_batch_info(vg_batch *b, uint64_t *agents, uint64_t *edges, int *tpb,
+                  int *apt, uint64_t *device_bytes);
 int vg_batch_destroy(vg_batch *b);
 
 #ifdef __cplusplus

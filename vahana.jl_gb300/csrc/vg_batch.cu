@@ -1,0 +1,510 @@
+// Batched ensemble: many independent SIR simulations stepped together.
+//
+// Each instance is built as an ordinary simulation (the "SIR" model:
+// Person{state::UInt8, days::Int32} :Immortal, Contact :Stateless
+// :SingleType), with its own seeded graph, and then packed into one device
+// arena: the instances' CSRs concatenated (row pointers and source indices
+// offset by the instance's first agent), states concatenated, one row of
+// the infection-probability table per instance.  One kernel launch steps
+// every agent of every instance (per-instance parameters looked up from the
+// agent's instance), so a step costs one launch instead of one per
+// instance; the step loop can be captured once in a CUDA graph and
+// replayed.  Launch shape (block size, agents per thread) comes from a
+// small autotuner keyed on the arena's degree histogram.
+//
+// The plain path of the same instances (vg_batch_step_one) runs apply! on
+// the instance's own simulation; both paths produce bit-identical states.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <vector>
+
+#include "vg_internal.h"
+#include "vg_philox.cuh"
+
+namespace vg {
+void set_last_error(const std::string &m);
+
+namespace {
+
+struct BatchArgs {
+  const uint32_t *__restrict__ rp;      // global row pointers (agents + 1)
+  const uint32_t *__restrict__ src;     // global source agent index
+  const uint16_t *__restrict__ inst;    // instance of each agent
+  const uint64_t *__restrict__ base;    // first global agent of each instance
+  const double *__restrict__ ptab;      // [instance][k], k <= kmax
+  const int32_t *__restrict__ rec;      // recovery steps per instance
+  const uint64_t *__restrict__ seed;    // seed per instance
+  const uint8_t *__restrict__ st_rd;
+  const int32_t *__restrict__ d_rd;
+  uint8_t *__restrict__ st_wr;
+  int32_t *__restrict__ d_wr;
+  uint64_t n;
+  uint32_t kmax1;  // table row length
+  uint32_t step;   // transition number, plus *step_base when step_base is set
+  const int64_t *step_base;
+  int *status;
+};
+
+// the SIR rule of transition "sir" (csrc/vg_transitions.cu), per instance
+template <int APT>
+__global__ void k_batch_sir(BatchArgs a) {
+  if (a.step_base) a.step += (uint32_t)*a.step_base;
+  uint64_t first = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * APT;
+#pragma unroll
+  for (int r = 0; r < APT; r++) {
+    uint64_t i = first + r;
+    if (i >= a.n) return;
+    uint32_t in = a.inst[i];
+    uint8_t s = a.st_rd[i];
+    int32_t d = a.d_rd[i];
+    if (s == 0) {
+      uint32_t k = 0;
+      uint32_t e = a.rp[i + 1];
+      for (uint32_t q = a.rp[i]; q < e; q++) k += (__ldg(a.st_rd + a.src[q]) == 1);
+      if (k > 0) {
+        if (k >= a.kmax1) {
+          atomicCAS(a.status, 0, 402);
+        } else {
+          uint64_t nr = i - a.base[in] + 1;
+          double u = u64_to_unit(philox_u64(philox_draw(a.seed[in], nr, a.step, TAG_INFECT)));
+          if (u < a.ptab[(uint64_t)in * a.kmax1 + k]) {
+            s = 1;
+            d = 0;
+          }
+        }
+      }
+    } else if (s == 1) {
+      d = d + 1;
+      if (d >= a.rec[in]) s = 2;
+    }
+    a.st_wr[i] = s;
+    a.d_wr[i] = d;
+  }
+}
+
+__global__ void k_offset_rp(const uint32_t *rp, uint64_t nrows, uint32_t ebase, uint32_t *out) {
+  uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r <= nrows) out[r] = rp[r] + ebase;
+}
+__global__ void k_offset_src(const uint32_t *src, uint64_t ne, uint32_t abase, uint32_t *out) {
+  uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < ne) out[k] = src[k] + abase;
+}
+__global__ void k_fill_u16(uint16_t *p, uint64_t n, uint16_t v) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = v;
+}
+
+inline unsigned blocks(uint64_t n, int tpb) {
+  return (unsigned)std::max<uint64_t>((n + tpb - 1) / tpb, 1);
+}
+
+}  // namespace
+
+// initial state of an SIR instance: the n_inf agents with the smallest
+// Philox(seed, nr, 0, TAG_INIT) draw (ties by index) start infected
+void sir_initial_state(uint64_t n, uint64_t seed, uint64_t n_inf, std::vector<uint8_t> &state) {
+  std::vector<std::pair<uint64_t, uint64_t>> d(n);
+  for (uint64_t i = 0; i < n; i++) d[i] = {philox_u64(philox_draw(seed, i + 1, 0, TAG_INIT)), i};
+  n_inf = std::min(n_inf, n);
+  std::partial_sort(d.begin(), d.begin() + n_inf, d.end());
+  state.assign(n, 0);
+  for (uint64_t j = 0; j < n_inf; j++) state[d[j].second] = 1;
+}
+
+}  // namespace vg
+
+using namespace vg;
+
+struct vg_batch {
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int n = 0;
+  std::vector<int64_t> N;
+  std::vector<int32_t> deg, rec;
+  std::vector<double> beta;
+  std::vector<uint64_t> seed;
+  vg_model *model = nullptr;
+  std::vector<vg_sim *> sims;
+  int person = 0, contact = 0;
+  uint64_t total = 0, total_edges = 0;
+  uint64_t footprint = 0;
+  DevBuf rp, src, inst, base, ptab, rec_d, seed_d, st[2], dy[2], status;
+  uint32_t kmax1 = 0;
+  int cur = 0;
+  int64_t step = 1;  // transition number of the next step (as after finish_init!)
+  int tpb = 256, apt = 1;
+  bool tuned = false;
+  std::map<uint64_t, std::pair<int, int>> tune_cache;
+  // CUDA graphs of `graph_steps` steps, one per starting buffer parity; the
+  // step number comes from step_base (device) + the node's offset
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  cudaGraph_t graph_def[2] = {nullptr, nullptr};
+  int graph_steps = 0;
+  DevBuf step_base;
+};
+
+namespace {
+
+BatchArgs batch_args(vg_batch *b, int cur, uint32_t step, const int64_t *step_base) {
+  BatchArgs a{};
+  a.rp = b->rp.as<uint32_t>();
+  a.src = b->src.as<uint32_t>();
+  a.inst = b->inst.as<uint16_t>();
+  a.base = b->base.as<uint64_t>();
+  a.ptab = b->ptab.as<double>();
+  a.rec = b->rec_d.as<int32_t>();
+  a.seed = b->seed_d.as<uint64_t>();
+  a.st_rd = b->st[cur].as<uint8_t>();
+  a.d_rd = b->dy[cur].as<int32_t>();
+  a.st_wr = b->st[1 - cur].as<uint8_t>();
+  a.d_wr = b->dy[1 - cur].as<int32_t>();
+  a.n = b->total;
+  a.kmax1 = b->kmax1;
+  a.step = step;
+  a.step_base = step_base;
+  a.status = b->status.as<int>();
+  return a;
+}
+
+void launch_step(vg_batch *b, const BatchArgs &a, int tpb, int apt, cudaStream_t st) {
+  uint64_t threads = (a.n + apt - 1) / apt;
+  unsigned g = blocks(threads, tpb);
+  switch (apt) {
+    case 1: k_batch_sir<1><<<g, tpb, 0, st>>>(a); break;
+    case 2: k_batch_sir<2><<<g, tpb, 0, st>>>(a); break;
+    default: k_batch_sir<4><<<g, tpb, 0, st>>>(a); break;
+  }
+}
+
+// Choose (block size, agents per thread) by timing each candidate on the
+// current step; the trial launches write only the write buffers, which the
+// real step overwrites, so the simulation state is unaffected.
+void autotune(vg_batch *b) {
+  // key: agents, edges and a coarse degree histogram (log2 buckets)
+  std::vector<uint32_t> rp(b->total + 1);
+  VG_CUDA(cudaMemcpyAsync(rp.data(), b->rp.p, rp.size() * 4, cudaMemcpyDeviceToHost, b->stream));
+  VG_CUDA(cudaStreamSynchronize(b->stream));
+  uint64_t hist[16] = {0};
+  for (uint64_t i = 0; i < b->total; i++) {
+    uint32_t d = rp[i + 1] - rp[i];
+    int bkt = 0;
+    while (bkt < 15 && (1u << bkt) <= d) bkt++;
+    hist[bkt]++;
+  }
+  uint64_t key = b->total * 1000003ull + b->total_edges;
+  for (int i = 0; i < 16; i++) key = key * 31 + (hist[i] * 16 / std::max<uint64_t>(b->total, 1));
+  auto it = b->tune_cache.find(key);
+  if (it != b->tune_cache.end()) {
+    b->tpb = it->second.first;
+    b->apt = it->second.second;
+    b->tuned = true;
+    return;
+  }
+  BatchArgs a = batch_args(b, b->cur, (uint32_t)b->step, nullptr);
+  cudaEvent_t e0, e1;
+  VG_CUDA(cudaEventCreate(&e0));
+  VG_CUDA(cudaEventCreate(&e1));
+  float best = 1e30f;
+  int bt = 256, ba = 1;
+  for (int tpb : {128, 256, 512})
+    for (int apt : {1, 2, 4}) {
+      launch_step(b, a, tpb, apt, b->stream);  // warm
+      VG_CUDA(cudaEventRecord(e0, b->stream));
+      for (int r = 0; r < 3; r++) launch_step(b, a, tpb, apt, b->stream);
+      VG_CUDA(cudaEventRecord(e1, b->stream));
+      VG_CUDA(cudaEventSynchronize(e1));
+      float ms = 0;
+      VG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      if (ms < best) {
+        best = ms;
+        bt = tpb;
+        ba = apt;
+      }
+    }
+  VG_CUDA(cudaEventDestroy(e0));
+  VG_CUDA(cudaEventDestroy(e1));
+  b->tpb = bt;
+  b->apt = ba;
+  b->tuned = true;
+  b->tune_cache[key] = {bt, ba};
+}
+
+void check_batch_status(vg_batch *b) {
+  int h = 0;
+  VG_CUDA(cudaMemcpyAsync(&h, b->status.p, 4, cudaMemcpyDeviceToHost, b->stream));
+  VG_CUDA(cudaStreamSynchronize(b->stream));
+  if (h) fail(VG_ERR_DEVICE, "batched SIR step: device status " + std::to_string(h));
+}
+
+}  // namespace
+
+#define API_BEGIN try {
+#define API_END                     \
+  return VG_OK;                     \
+  }                                 \
+  catch (const Error &e) {          \
+    set_last_error(e.msg);          \
+    return e.code;                  \
+  }                                 \
+  catch (const std::exception &e) { \
+    set_last_error(e.what());       \
+    return VG_ERR_ARG;              \
+  }
+
+extern "C" {
+
+int vg_batch_create_sir(int n, const int64_t *N, const int32_t *deg, const double *beta,
+                        const int32_t *rec, const uint64_t *seeds,
+                        int64_t n_init_infected_per_1000, void *stream, vg_batch **out) {
+  API_BEGIN
+  if (n <= 0 || n > 65535) fail(VG_ERR_ARG, "batch: 1..65535 instances");
+  auto b = std::make_unique<vg_batch>();
+  b->n = n;
+  b->N.assign(N, N + n);
+  b->deg.assign(deg, deg + n);
+  b->beta.assign(beta, beta + n);
+  b->rec.assign(rec, rec + n);
+  b->seed.assign(seeds, seeds + n);
+  if (stream) {
+    b->stream = (cudaStream_t)stream;
+  } else {
+    VG_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    b->own_stream = true;
+  }
+  // the "SIR" model
+  int rc = vg_model_create(&b->model);
+  if (rc) fail(rc, vg_last_error());
+  const char *pf[2] = {"state", "days"};
+  int pd[2] = {VG_U8, VG_I32};
+  if ((rc = vg_model_register_agenttype(b->model, "Person", 2, pf, pd, VG_HINT_IMMORTAL,
+                                         &b->person)))
+    fail(rc, vg_last_error());
+  if ((rc = vg_model_register_edgetype(b->model, "Contact", 0, nullptr, nullptr,
+                                        VG_HINT_STATELESS, b->person, 0, &b->contact)))
+    fail(rc, vg_last_error());
+  if ((rc = vg_model_finalize(b->model, "SIR"))) fail(rc, vg_last_error());
+  // instances as plain simulations
+  uint32_t kmax = 0;
+  std::vector<uint64_t> bases(n);
+  for (int i = 0; i < n; i++) {
+    vg_sim *s = nullptr;
+    if ((rc = vg_sim_create(b->model, "instance", b->stream, &s))) fail(rc, vg_last_error());
+    b->sims.push_back(s);
+    uint64_t Ni = (uint64_t)N[i];
+    if (Ni < 2) fail(VG_ERR_ARG, "batch: instances need at least two agents");
+    std::vector<uint8_t> state;
+    uint64_t ninf = (uint64_t)std::max<double>(
+        1.0, std::nearbyint((double)Ni * (double)n_init_infected_per_1000 / 1000.0));
+    sir_initial_state(Ni, seeds[i], ninf, state);
+    std::vector<int32_t> days(Ni, 0);
+    const void *cols[2] = {state.data(), days.data()};
+    if ((rc = vg_add_agents(s, b->person, Ni, cols, nullptr))) fail(rc, vg_last_error());
+    if ((rc = vg_gen_uniform_out_edges(s, b->contact, b->person, (uint32_t)deg[i], seeds[i])))
+      fail(rc, vg_last_error());
+    if ((rc = vg_finish_init(s))) fail(rc, vg_last_error());
+    bases[i] = b->total;
+    b->total += Ni;
+    Sim &S = *s->s;
+    CSR &c = S.edges[b->contact].csr[b->person];
+    b->total_edges += c.nedges;
+    kmax = std::max(kmax, c.max_degree);
+  }
+  if (b->total_edges >= (1ull << 32) || b->total >= (1ull << 32))
+    fail(VG_ERR_NOMEM, "batch: arena indices are 32-bit");
+  // arena
+  cudaStream_t st = b->stream;
+  uint64_t *fp = &b->footprint;
+  b->rp.alloc((b->total + 1) * 4, fp);
+  b->src.alloc(std::max<uint64_t>(b->total_edges, 1) * 4, fp);
+  b->inst.alloc(b->total * 2, fp);
+  for (int k = 0; k < 2; k++) {
+    b->st[k].alloc(b->total, fp);
+    b->dy[k].alloc(b->total * 4, fp);
+  }
+  uint64_t ebase = 0;
+  for (int i = 0; i < n; i++) {
+    Sim &S = *b->sims[i]->s;
+    CSR &c = S.edges[b->contact].csr[b->person];
+    AgentStore &A = S.agents[b->person - 1];
+    uint64_t Ni = A.n, a0 = bases[i];
+    k_offset_rp<<<blocks(Ni + 1, 256), 256, 0, st>>>(c.row_ptr.as<uint32_t>(), Ni, (uint32_t)ebase,
+                                                    b->rp.as<uint32_t>() + a0);
+    if (c.nedges)
+      k_offset_src<<<blocks(c.nedges, 256), 256, 0, st>>>(c.src.as<uint32_t>(), c.nedges,
+                                                         (uint32_t)a0,
+                                                         b->src.as<uint32_t>() + ebase);
+    k_fill_u16<<<blocks(Ni, 256), 256, 0, st>>>(b->inst.as<uint16_t>() + a0, Ni, (uint16_t)i);
+    VG_CUDA(cudaMemcpyAsync(b->st[0].as<uint8_t>() + a0, A.rd[0].p, Ni, cudaMemcpyDeviceToDevice, st));
+    VG_CUDA(cudaMemcpyAsync(b->dy[0].as<int32_t>() + a0, A.rd[1].p, Ni * 4, cudaMemcpyDeviceToDevice, st));
+    ebase += c.nedges;
+    VG_CUDA(cudaGetLastError());
+  }
+  // per-instance tables: p_k = 1 - (1 - beta)^k by repeated multiplication
+  b->kmax1 = kmax + 1;
+  std::vector<double> tab((uint64_t)n * b->kmax1);
+  for (int i = 0; i < n; i++) {
+    double q = 1.0, om = 1.0 - beta[i];
+    tab[(uint64_t)i * b->kmax1] = 0.0;
+    for (uint32_t k = 1; k <= kmax; k++) {
+      q = q * om;
+      tab[(uint64_t)i * b->kmax1 + k] = 1.0 - q;
+    }
+  }
+  b->ptab.alloc(tab.size() * 8, fp);
+  b->base.alloc(n * 8, fp);
+  b->rec_d.alloc(n * 4, fp);
+  b->seed_d.alloc(n * 8, fp);
+  b->status.alloc(16, fp);
+  VG_CUDA(cudaMemcpyAsync(b->ptab.p, tab.data(), tab.size() * 8, cudaMemcpyHostToDevice, st));
+  VG_CUDA(cudaMemcpyAsync(b->base.p, bases.data(), n * 8, cudaMemcpyHostToDevice, st));
+  VG_CUDA(cudaMemcpyAsync(b->rec_d.p, rec, n * 4, cudaMemcpyHostToDevice, st));
+  VG_CUDA(cudaMemcpyAsync(b->seed_d.p, seeds, n * 8, cudaMemcpyHostToDevice, st));
+  VG_CUDA(cudaMemsetAsync(b->status.p, 0, 16, st));
+  VG_CUDA(cudaStreamSynchronize(st));
+  *out = b.release();
+  API_END
+}
+
+// mode 0: one launch per step; mode 1: the `steps` launches captured once in
+// a CUDA graph (re-captured when the step count or phase changes) and
+// replayed.
+int vg_batch_step(vg_batch *b, int steps, int mode) {
+  API_BEGIN
+  if (!b) fail(VG_ERR_ARG, "null batch");
+  if (steps <= 0) return VG_OK;
+  if (!b->tuned) autotune(b);
+  if (mode == 0) {
+    for (int k = 0; k < steps; k++) {
+      BatchArgs a = batch_args(b, b->cur, (uint32_t)b->step, nullptr);
+      launch_step(b, a, b->tpb, b->apt, b->stream);
+      VG_CUDA(cudaGetLastError());
+      b->cur = 1 - b->cur;
+      b->step++;
+    }
+  } else {
+    if (b->graph_steps != steps) {  // (re)capture for this step count
+      for (int p = 0; p < 2; p++)
+        if (b->graph[p]) {
+          cudaGraphExecDestroy(b->graph[p]);
+          cudaGraphDestroy(b->graph_def[p]);
+          b->graph[p] = nullptr;
+        }
+      b->graph_steps = steps;
+    }
+    if (!b->step_base.p) b->step_base.alloc(8, &b->footprint);
+    int p = b->cur;
+    if (!b->graph[p]) {
+      cudaStream_t cs;
+      VG_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+      VG_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+      int cur = p;
+      for (int k = 0; k < steps; k++) {
+        BatchArgs a = batch_args(b, cur, (uint32_t)k, b->step_base.as<int64_t>());
+        launch_step(b, a, b->tpb, b->apt, cs);
+        cur = 1 - cur;
+      }
+      VG_CUDA(cudaStreamEndCapture(cs, &b->graph_def[p]));
+      VG_CUDA(cudaGraphInstantiate(&b->graph[p], b->graph_def[p], 0));
+      VG_CUDA(cudaStreamDestroy(cs));
+    }
+    int64_t s0 = b->step;
+    VG_CUDA(cudaMemcpyAsync(b->step_base.p, &s0, 8, cudaMemcpyHostToDevice, b->stream));
+    VG_CUDA(cudaGraphLaunch(b->graph[p], b->stream));
+    if (steps % 2) b->cur = 1 - b->cur;
+    b->step += steps;
+  }
+  check_batch_status(b);
+  API_END
+}
+
+int vg_batch_step_one(vg_batch *b, int i, int steps) {
+  API_BEGIN
+  if (!b || i < 0 || i >= b->n) fail(VG_ERR_ARG, "batch: instance index");
+  int call = b->person, read[2] = {b->person, VG_EDGE(b->contact)}, write = b->person;
+  double params[4] = {(double)b->contact, b->beta[i], (double)b->rec[i], (double)b->seed[i]};
+  if (b->seed[i] >= (1ull << 53)) fail(VG_ERR_ARG, "batch: seeds below 2^53");
+  for (int k = 0; k < steps; k++) {
+    int rc = vg_apply(b->sims[i], "sir", &call, 1, read, 2, &write, 1, nullptr, 0, -1, params, 4);
+    if (rc) fail(rc, vg_last_error());
+  }
+  API_END
+}
+
+// which = 0: the batched arena; which = 1: the instance's own simulation
+int vg_batch_read_states2(vg_batch *b, int i, int which, uint8_t *state_out,
+                          int32_t *days_out, uint64_t cap, uint64_t *n_out) {
+  API_BEGIN
+  if (!b || i < 0 || i >= b->n) fail(VG_ERR_ARG, "batch: instance index");
+  if (which == 1) {
+    void *cols[2] = {state_out, days_out};
+    int rc = vg_read_agents(b->sims[i], b->person, cols, nullptr, cap, n_out);
+    if (rc) fail(rc, vg_last_error());
+    return VG_OK;
+  }
+  uint64_t a0 = 0;
+  for (int j = 0; j < i; j++) a0 += (uint64_t)b->N[j];
+  uint64_t Ni = (uint64_t)b->N[i];
+  *n_out = Ni;
+  uint64_t m = std::min(cap, Ni);
+  VG_CUDA(cudaStreamSynchronize(b->stream));
+  if (state_out) VG_CUDA(cudaMemcpy(state_out, b->st[b->cur].as<uint8_t>() + a0, m, cudaMemcpyDeviceToHost));
+  if (days_out) VG_CUDA(cudaMemcpy(days_out, b->dy[b->cur].as<int32_t>() + a0, m * 4, cudaMemcpyDeviceToHost));
+  API_END
+}
+
+int vg_batch_read_states(vg_batch *b, int i, uint8_t *state_out, int32_t *days_out,
+                         uint64_t cap, uint64_t *n_out) {
+  return vg_batch_read_states2(b, i, 0, state_out, days_out, cap, n_out);
+}
+
+int vg_batch_read_graph(vg_batch *b, int i, uint32_t *row_ptr_out, uint32_t *src_out,
+                        uint64_t *nrows_out, uint64_t *nedges_out) {
+  API_BEGIN
+  if (!b || i < 0 || i >= b->n) fail(VG_ERR_ARG, "batch: instance index");
+  Sim &S = *b->sims[i]->s;
+  CSR &c = S.edges[b->contact].csr[b->person];
+  *nrows_out = c.nrows;
+  *nedges_out = c.nedges;
+  if (row_ptr_out) VG_CUDA(cudaMemcpy(row_ptr_out, c.row_ptr.p, (c.nrows + 1) * 4, cudaMemcpyDeviceToHost));
+  if (src_out && c.nedges) VG_CUDA(cudaMemcpy(src_out, c.src.p, c.nedges * 4, cudaMemcpyDeviceToHost));
+  API_END
+}
+
+int vg_batch_info(vg_batch *b, uint64_t *agents, uint64_t *edges, int *tpb, int *apt,
+                  uint64_t *device_bytes) {
+  API_BEGIN
+  if (!b) fail(VG_ERR_ARG, "null batch");
+  if (agents) *agents = b->total;
+  if (edges) *edges = b->total_edges;
+  if (tpb) *tpb = b->tpb;
+  if (apt) *apt = b->apt;
+  if (device_bytes) {
+    uint64_t t = b->footprint;
+    for (auto *s : b->sims) t += s->s->footprint;
+    *device_bytes = t;
+  }
+  API_END
+}
+
+int vg_batch_destroy(vg_batch *b) {
+  API_BEGIN
+  if (!b) return VG_OK;
+  cudaStreamSynchronize(b->stream);
+  for (int p = 0; p < 2; p++)
+    if (b->graph[p]) {
+      cudaGraphExecDestroy(b->graph[p]);
+      cudaGraphDestroy(b->graph_def[p]);
+    }
+  for (auto *s : b->sims) vg_sim_destroy(s);
+  if (b->model) vg_model_destroy(b->model);
+  cudaStream_t st = b->stream;
+  bool own = b->own_stream;
+  delete b;
+  if (own) cudaStreamDestroy(st);
+  API_END
+}
+
+}  // extern "C"

@@ -225,16 +225,6 @@ __global__ void k_compact_dest(const uint32_t *keep, const uint32_t *scan,
   if (k < n) dest[k] = keep[k] ? scan[k] : 0xffffffffu;
 }
 
-__global__ void k_hub_rows(const uint32_t *rp, uint64_t nrows, uint32_t thr,
-                           uint32_t *out, unsigned long long *cnt) {
-  uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= nrows) return;
-  if (rp[r + 1] - rp[r] > thr) {
-    unsigned long long i = atomicAdd(cnt, 1ull);
-    out[i] = (uint32_t)r;
-  }
-}
-
 }  // namespace
 
 uint64_t csr_edges_total(const EdgeStore &es) {
@@ -471,27 +461,58 @@ void remove_died_edges(Sim &s, int died_type, const uint8_t *died,
   }
 }
 
-void ensure_schedule(Sim &s, CSR &c, uint32_t thr) {
-  if (c.schedule_valid && c.hub_threshold == thr) return;
+namespace {
+// schedule keys: hub rows first by descending degree (top bit 0), then the
+// other rows window by window, by descending degree inside a window
+__global__ void k_schedule_keys(const uint32_t *rp, uint64_t nrows, uint64_t n, uint32_t thr,
+                                uint32_t wshift, uint32_t *keys, uint32_t *vals,
+                                unsigned long long *nhub) {
+  uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  uint32_t d = r < nrows ? rp[r + 1] - rp[r] : 0;
+  uint32_t key;
+  if (d > thr) {
+    key = 0x7FFFFFFFu - min(d, 0x7FFFFFFFu);
+    atomicAdd(nhub, 1ull);
+  } else {
+    key = 0x80000000u | ((uint32_t)(r >> wshift) << 16) | (0xFFFFu - min(d, 0xFFFFu));
+  }
+  keys[r] = key;
+  vals[r] = (uint32_t)r;
+}
+}  // namespace
+
+void ensure_schedule(Sim &s, CSR &c, uint32_t thr, uint64_t n) {
+  if (c.schedule_valid && c.hub_threshold == thr && c.nhub + c.norder == n) return;
   cudaStream_t st = s.stream;
   c.hub_rows.release();
-  c.nhub = 0;
-  if (c.nrows > 0) {
+  c.row_order.release();
+  c.nhub = c.norder = 0;
+  if (n > 0) {
+    // window of consecutive rows: 8192, or larger so that windows fit 15 bits
+    uint32_t wshift = 13;
+    while ((n >> wshift) >= (1ull << 15)) wshift++;
     Tmp<unsigned long long> cnt(1, st);
     VG_CUDA(cudaMemsetAsync(cnt.p, 0, 8, st));
-    Tmp<uint32_t> tmp(c.nrows, st);
-    k_hub_rows<<<nblk(c.nrows), TPB, 0, st>>>(c.row_ptr.as<uint32_t>(), c.nrows, thr,
-                                              tmp.p, cnt.p);
+    DevBuf order;
+    order.alloc(n * 4, &s.footprint);
+    Tmp<uint32_t> keys(n, st);
+    k_schedule_keys<<<nblk(n), TPB, 0, st>>>(c.row_ptr.as<uint32_t>(), c.nrows, n, thr, wshift,
+                                             keys.p, order.as<uint32_t>(), cnt.p);
+    VG_CUDA(cudaGetLastError());
+    radix_sort_pairs_u32(keys.p, order.as<uint32_t>(), n, 32, st, s);
     unsigned long long h = 0;
     VG_CUDA(cudaMemcpyAsync(&h, cnt.p, 8, cudaMemcpyDeviceToHost, st));
     VG_CUDA(cudaStreamSynchronize(st));
     c.nhub = h;
+    c.norder = n - h;
     if (h) {
       c.hub_rows.alloc(h * 4, &s.footprint);
-      VG_CUDA(cudaMemcpyAsync(c.hub_rows.p, tmp.p, h * 4, cudaMemcpyDeviceToDevice, st));
-      // process the largest hubs first: sort rows by descending degree is
-      // not needed for the result; keep discovery order
+      VG_CUDA(cudaMemcpyAsync(c.hub_rows.p, order.p, h * 4, cudaMemcpyDeviceToDevice, st));
     }
+    c.row_order.alloc(std::max<uint64_t>(c.norder, 1) * 4, &s.footprint);
+    VG_CUDA(cudaMemcpyAsync(c.row_order.p, order.as<uint32_t>() + h, c.norder * 4,
+                            cudaMemcpyDeviceToDevice, st));
     VG_CUDA(cudaStreamSynchronize(st));
   }
   c.hub_threshold = thr;

@@ -144,6 +144,11 @@ struct CSR {
   // derived schedule of the degree-bucketed gather kernels (hub rows)
   DevBuf hub_rows;  // u32 rows with degree above the hub threshold
   uint64_t nhub = 0;
+  // the other rows (and the agents beyond nrows, degree 0) in windows of
+  // consecutive rows, sorted by descending degree inside each window, so
+  // that the rows of one warp have similar degrees
+  DevBuf row_order;
+  uint64_t norder = 0;
   uint32_t hub_threshold = 0;
   bool schedule_valid = false;
   // payload field 0 (Float64) holds only multiples of 2^-53 in (0, 1]:
@@ -305,7 +310,8 @@ void build_csr_from_records(Sim &s, int edge_type, const uint64_t *d_from,
                             const uint64_t *d_key, bool merge_existing);
 void remove_died_edges(Sim &s, int died_type, const uint8_t *died_now,
                        uint64_t n_died);
-void ensure_schedule(Sim &s, CSR &c, uint32_t hub_threshold);
+// hub list and degree-sorted row order over n agent slots (n >= nrows)
+void ensure_schedule(Sim &s, CSR &c, uint32_t hub_threshold, uint64_t n);
 uint64_t csr_edges_total(const EdgeStore &es);
 
 // agents (vg_api.cu)

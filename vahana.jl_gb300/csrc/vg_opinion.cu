@@ -54,6 +54,8 @@ struct OpinionArgs {
   uint64_t n, nrows;
   const uint32_t *__restrict__ hub_rows;
   uint64_t nhub;
+  const uint32_t *__restrict__ order;  // non-hub rows, degree-sorted per window
+  uint64_t norder;
   uint32_t hub_thr;
   unsigned hub_blocks;
   double eps, a, b;
@@ -175,10 +177,20 @@ template <bool GRID>
 __device__ __forceinline__ void fold(const OpinionArgs &p, uint32_t b, uint32_t e, double xi,
                                      float fxi, bool xi_ok, uint64_t &K, double &sw,
                                      double &swx, uint32_t &cnt) {
+  if (b >= e) return;
+  // software pipeline: source index two edges ahead, neighbour state one
+  // edge ahead, so that the dependent gathers overlap the arithmetic
+  uint32_t jn = b + 1 < e ? __ldg(p.src + b + 1) : 0;
+  double xj = __ldg(p.x + __ldg(p.src + b));
   for (uint32_t k = b; k < e; k++) {
-    double xj = __ldg(p.x + __ldg(p.src + k));
-    if (within(xj, xi, fxi, xi_ok, p)) {
-      double wk = __ldg(p.w + k);
+    uint32_t jnn = k + 2 < e ? __ldg(p.src + k + 2) : 0;
+    double xn = k + 1 < e ? __ldg(p.x + jn) : 0.0;
+    double wk = __ldg(p.w + k);
+    double xcur = xj;
+    xj = xn;
+    jn = jnn;
+    if (within(xcur, xi, fxi, xi_ok, p)) {
+      double xj = xcur;
       bool ok;
       uint64_t pk = mul_fast(bits(wk), bits(xj), ok);
       double pkd = ok ? dbl(pk) : mul_hw(wk, xj);
@@ -231,8 +243,9 @@ __global__ void __launch_bounds__(TPB) k_opinion(OpinionArgs p) {
     if (lane == 0) p.xo[r] = cnt ? finish(p.a, p.b, xi, sw, swx) : xi;
     return;
   }
-  uint64_t i = (uint64_t)(blockIdx.x - p.hub_blocks) * TPB + threadIdx.x;
-  if (i >= p.n) return;
+  uint64_t g = (uint64_t)(blockIdx.x - p.hub_blocks) * TPB + threadIdx.x;
+  if (g >= (p.order ? p.norder : p.n)) return;
+  uint64_t i = p.order ? p.order[g] : g;
   double xi = p.x[i];
   if (i >= p.nrows) {
     p.xo[i] = xi;
@@ -330,13 +343,13 @@ void tr_bounded_confidence(ApplyCtx &c) {
       cs.unit_grid_weights = h ? 0 : 1;
     }
     p.grid = cs.unit_grid_weights;
-    if (thr != 0xffffffffu) {
-      ensure_schedule(s, cs, thr);
-      p.hub_rows = cs.hub_rows.as<uint32_t>();
-      p.nhub = cs.nhub;
-      p.hub_thr = thr;
-      p.hub_blocks = (unsigned)((cs.nhub + (TPB / 32) - 1) / (TPB / 32));
-    }
+    ensure_schedule(s, cs, thr, av.n);
+    p.hub_rows = cs.hub_rows.as<uint32_t>();
+    p.nhub = cs.nhub;
+    p.order = cs.row_order.as<uint32_t>();
+    p.norder = cs.norder;
+    p.hub_thr = thr;
+    p.hub_blocks = (unsigned)((cs.nhub + (TPB / 32) - 1) / (TPB / 32));
   }
   unsigned grid = p.hub_blocks + (unsigned)((av.n + TPB - 1) / TPB);
   if (p.grid) k_opinion<true><<<grid, TPB, 0, s.stream>>>(p);

@@ -137,6 +137,8 @@ SIGNATURES = {
     "vg_batch_read_states": (I, [P, I, C.POINTER(C.c_uint8), C.POINTER(C.c_int32), U64, PU64]),
     "vg_batch_read_graph": (I, [P, I, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), PU64, PU64]),
     "vg_batch_destroy": (I, [P]),
+    "vg_batch_read_states2": (I, [P, I, I, C.POINTER(C.c_uint8), C.POINTER(C.c_int32), U64, PU64]),
+    "vg_batch_info": (I, [P, PU64, PU64, PI, PI, PU64]),
 }
 
 

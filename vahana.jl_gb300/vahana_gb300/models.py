@@ -120,6 +120,88 @@ def staged_edges(sim, E):
     return frm, to, {f[0]: c for f, c in zip(t.fields, cols)}
 
 
+# -------------------------------------------------------- batched SIR
+def batch_params(n_instances, n_lo=1_000, n_hi=100_000, deg_lo=5, deg_hi=30, beta_lo=0.01,
+                 beta_hi=0.1, rec_lo=5, rec_hi=10):
+    """Per-instance parameters drawn from Philox(seed = instance index):
+    N log-uniform in [n_lo, n_hi], out-degree uniform in [deg_lo, deg_hi],
+    beta uniform in [beta_lo, beta_hi], recovery uniform in [rec_lo, rec_hi]."""
+    i = np.arange(n_instances, dtype=np.uint64)
+    N = np.empty(n_instances, np.int64)
+    deg = np.empty(n_instances, np.int32)
+    beta = np.empty(n_instances, np.float64)
+    rec = np.empty(n_instances, np.int32)
+    for k in range(n_instances):
+        w = philox.draw(k, 0, 0, philox.TAG_PARAM)
+        u = philox.unit(philox.to_u64(w))
+        N[k] = int(np.floor(n_lo * (n_hi / n_lo) ** float(u)))
+        deg[k] = deg_lo + int(philox.bounded32(w[2], deg_hi - deg_lo + 1))
+        w2 = philox.draw(k, 1, 0, philox.TAG_PARAM)
+        beta[k] = beta_lo + (beta_hi - beta_lo) * float(philox.unit(philox.to_u64(w2)))
+        rec[k] = rec_lo + int(philox.bounded32(w2[2], rec_hi - rec_lo + 1))
+    return N, deg, beta, rec, i.copy()
+
+
+class Batch:
+    """Batched SIR ensemble (vg_batch_*): every instance is also kept as its
+    own simulation for the one-at-a-time path."""
+
+    def __init__(self, N, deg, beta, rec, seeds, infected_per_1000=1, stream=None):
+        self.n = len(N)
+        self.N = np.ascontiguousarray(N, np.int64)
+        h = C.c_void_p()
+        arr = lambda a, t: np.ascontiguousarray(a, t)
+        self._keep = [arr(N, np.int64), arr(deg, np.int32), arr(beta, np.float64),
+                      arr(rec, np.int32), arr(seeds, np.uint64)]
+        k = self._keep
+        check(lib().vg_batch_create_sir(
+            self.n, k[0].ctypes.data_as(C.POINTER(C.c_int64)),
+            k[1].ctypes.data_as(C.POINTER(C.c_int32)), k[2].ctypes.data_as(C.POINTER(C.c_double)),
+            k[3].ctypes.data_as(C.POINTER(C.c_int32)), k[4].ctypes.data_as(C.POINTER(C.c_uint64)),
+            int(infected_per_1000), C.c_void_p(stream) if stream else None, C.byref(h)))
+        self._h = h
+
+    def step(self, steps, mode=1):
+        check(lib().vg_batch_step(self._h, int(steps), int(mode)))
+
+    def step_one(self, i, steps):
+        check(lib().vg_batch_step_one(self._h, int(i), int(steps)))
+
+    def states(self, i, which=0):
+        n = int(self.N[i])
+        s = np.zeros(n, np.uint8)
+        d = np.zeros(n, np.int32)
+        out = C.c_uint64()
+        check(lib().vg_batch_read_states2(self._h, int(i), int(which),
+                                          s.ctypes.data_as(C.POINTER(C.c_uint8)),
+                                          d.ctypes.data_as(C.POINTER(C.c_int32)), n,
+                                          C.byref(out)))
+        return s, d
+
+    def graph(self, i):
+        nr, ne = C.c_uint64(), C.c_uint64()
+        check(lib().vg_batch_read_graph(self._h, int(i), None, None, C.byref(nr), C.byref(ne)))
+        rp = np.zeros(nr.value + 1, np.uint32)
+        src = np.zeros(max(ne.value, 1), np.uint32)
+        check(lib().vg_batch_read_graph(self._h, int(i), rp.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                        src.ctypes.data_as(C.POINTER(C.c_uint32)), C.byref(nr),
+                                        C.byref(ne)))
+        return rp, src[:ne.value]
+
+    def info(self):
+        a, e, db = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        t, p = C.c_int(), C.c_int()
+        check(lib().vg_batch_info(self._h, C.byref(a), C.byref(e), C.byref(t), C.byref(p),
+                                  C.byref(db)))
+        return {"agents": a.value, "edges": e.value, "tpb": t.value, "apt": p.value,
+                "device_bytes": db.value}
+
+    def close(self):
+        if self._h:
+            check(lib().vg_batch_destroy(self._h))
+            self._h = None
+
+
 # ------------------------------------------------------- Life + walkers
 def life_model(name="Life"):
     return (api.ModelTypes()
