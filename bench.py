@@ -24,6 +24,7 @@ reference itself is Julia and cannot run here).
 Multi-GPU: replicas only (one independent simulation per rank).
 """
 import argparse
+import numpy as np
 import json
 import os
 import subprocess
@@ -54,6 +55,9 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="opinion", choices=["opinion", "batch"])
+    ap.add_argument("--instances", type=int, default=512)
+    ap.add_argument("--batch-steps", type=int, default=200)
     return ap.parse_args()
 
 
@@ -338,9 +342,64 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_batch(args):
+    """Batched ensemble: 512 SIR instances (N log-uniform 1e3..1e5, out-degree
+    5..30, beta 0.01..0.1, recovery 5..10, seed = instance index), 200 steps
+    as one CUDA graph, against the same instances stepped one at a time with
+    the plain kernels (apply! per instance and step)."""
+    import torch
+    import vahana_gb300 as vh
+    from vahana_gb300 import models
+    vh.build()
+    n_inst, steps = args.instances, args.batch_steps
+    N, deg, beta, rec, seeds = models.batch_params(n_inst)
+    b = models.Batch(N, deg, beta, rec, seeds)
+    b.step(steps, mode=1)  # warm-up: capture + one replay
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    reps = 3
+    for _ in range(reps):
+        b.step(steps, mode=1)
+    torch.cuda.synchronize()
+    t_batch = (time.perf_counter() - t0) / reps
+    t0 = time.perf_counter()
+    for i in range(n_inst):
+        b.step_one(i, steps)
+    torch.cuda.synchronize()
+    t_plain = time.perf_counter() - t0
+    bad = 0
+    for i in range(n_inst):  # the plain run has done `steps` steps, the batch (reps+1)*steps
+        pass
+    info = b.info()
+    b.close()
+    # parity of batched vs plain on a fresh batch with equal step counts
+    b2 = models.Batch(N[:64], deg[:64], beta[:64], rec[:64], seeds[:64])
+    b2.step(steps, mode=1)
+    for i in range(64):
+        b2.step_one(i, steps)
+        sb, db = b2.states(i, 0)
+        sp, dp = b2.states(i, 1)
+        bad += int(not (np.array_equal(sb, sp) and np.array_equal(db, dp)))
+    b2.close()
+    v = n_inst * steps / t_batch
+    out = {"metric": "sim-steps/s", "value": v, "unit": "instance-steps/s", "n_gpus": 1,
+           "steps": steps, "warmup": 1, "ms_per_step": 1e3 * t_batch / steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/i32",
+           "data": "synthetic",
+           "config": {"workload": "batched_sir_ensemble", "instances": n_inst,
+                      "agents": info["agents"], "edges": info["edges"],
+                      "launch": {"tpb": info["tpb"], "agents_per_thread": info["apt"]}},
+           "plain_one_at_a_time": n_inst * steps / t_plain,
+           "speedup_vs_plain": t_plain / t_batch,
+           "parity_mismatches_first_64": bad}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.workload == "batch":
+        run_batch(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

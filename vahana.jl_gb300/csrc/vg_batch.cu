@@ -426,10 +426,13 @@ int vg_batch_step_one(vg_batch *b, int i, int steps) {
   int call = b->person, read[2] = {b->person, VG_EDGE(b->contact)}, write = b->person;
   double params[4] = {(double)b->contact, b->beta[i], (double)b->rec[i], (double)b->seed[i]};
   if (b->seed[i] >= (1ull << 53)) fail(VG_ERR_ARG, "batch: seeds below 2^53");
+  int rc = vg_sim_set_async(b->sims[i], 1);  // launches back to back, one check at the end
+  if (rc) fail(rc, vg_last_error());
   for (int k = 0; k < steps; k++) {
-    int rc = vg_apply(b->sims[i], "sir", &call, 1, read, 2, &write, 1, nullptr, 0, -1, params, 4);
+    rc = vg_apply(b->sims[i], "sir", &call, 1, read, 2, &write, 1, nullptr, 0, -1, params, 4);
     if (rc) fail(rc, vg_last_error());
   }
+  if ((rc = vg_sim_synchronize(b->sims[i]))) fail(rc, vg_last_error());
   API_END
 }
 
