@@ -1,0 +1,131 @@
+"""CPU tests of the C ABI: the library loads, exports every function
+include/*.h declares, and its host-side logic (model registry, hint
+normalisation, init-phase staging, raster stencils, accessor rules before
+finish_init!) behaves as the reference's, without a GPU."""
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names |= set(re.findall(r"\b(vg_\w+)\s*\(", src))
+    return sorted(names)
+
+
+def test_every_declared_symbol_is_exported(vh):
+    lib = vh.lib()
+    names = declared()
+    assert len(names) > 60
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert missing == []
+
+
+def test_no_gpu_is_reported_not_faked(vh):
+    import ctypes as C
+    n = C.c_int(-1)
+    vh.lib().vg_device_count(C.byref(n))
+    assert n.value >= 0
+
+
+def test_registry_rules(vh):
+    """src/ModelTypes.jl:81-230"""
+    m = vh.ModelTypes().register_agenttype("A", [("foo", "i64")])
+    with pytest.raises(AssertionError):
+        m.register_agenttype("A", [("foo", "i64")])  # already registered
+    with pytest.raises(AssertionError):
+        m.register_agenttype("B", [], ":Bogus")
+    with pytest.raises(AssertionError):  # SingleType+SingleEdge needs Stateless+IgnoreFrom
+        m.register_edgetype("E1", [("w", "f64")], ":SingleType", ":SingleEdge", target="A")
+    m.register_edgetype("E2", [], ":HasEdgeOnly")
+    m.register_edgetype("E3", [], ":NumEdgesOnly")
+    m.register_edgetype("E4", [("w", "f64")], target="A")  # target implies :SingleType
+    m.register_edgetype("E5", [])                          # no field implies :Stateless
+    model = m.create_model("rules")
+    assert model.has_hint("E2", ":Stateless") and model.has_hint("E2", ":IgnoreFrom") \
+        and model.has_hint("E2", ":SingleEdge")
+    assert model.has_hint("E3", ":Stateless") and model.has_hint("E3", ":IgnoreFrom")
+    assert model.has_hint("E4", ":SingleType")
+    assert model.has_hint("E5", ":Stateless")
+
+
+def test_init_phase_staging_and_accessors(vh):
+    """Before finish_init!: add_agent!/add_edge! staging, the :SingleEdge
+    check of _can_add, num_edges(write=true), accessor hint rules."""
+    m = (vh.ModelTypes().register_agenttype("A", [("foo", "i64")])
+         .register_edgetype("D", [("foo", "i64")])
+         .register_edgetype("SE", [("foo", "i64")], ":SingleEdge")
+         .register_edgetype("S", [], ":Stateless")
+         .create_model("stage"))
+    sim = vh.create_simulation(m)
+    a1, a2, a3 = vh.add_agents(sim, "A", 3, foo=[1, 2, 3])
+    assert vh.agent_nr(a3) == 3 and vh.type_nr(a3) == m["A"].index
+    vh.add_edge(sim, a2, a3, "D", foo=1)
+    vh.add_edge(sim, a1, a3, "D", foo=2)
+    vh.add_edge(sim, a2, a3, "SE", foo=1)
+    vh.add_edge(sim, a2, a3, "SE", foo=1)  # identical value: allowed
+    with pytest.raises(AssertionError):
+        vh.add_edge(sim, a1, a3, "SE", foo=2)
+    vh.add_edge(sim, a1, a3, "S")
+    assert vh.num_edges(sim, "D", write=True) == 2
+    assert vh.num_edges(sim, "D", write=False) == 0
+    assert vh.num_edges(sim, "SE", write=True) == 1
+    assert vh.edges(sim, a3, "D") == [vh.Edge(a2, {"foo": 1}), vh.Edge(a1, {"foo": 2})]
+    assert vh.neighborids(sim, a3, "S") == [a1]
+    with pytest.raises(AssertionError):
+        vh.edges(sim, a3, "S")  # stateless: edges is not defined
+    with pytest.raises(AssertionError):
+        vh.num_edges(sim, a3, "SE")  # single edge: num_edges is not defined
+    assert vh.num_agents(sim, "A") == 3
+    assert vh.mapreduce(sim, "foo", "+", "A") == 6
+    assert vh.mapreduce(sim, "foo", "max", "A") == 3
+    with pytest.raises(AssertionError):
+        vh.apply_(sim, "keep", "A", [], [])  # apply! before finish_init!
+    vh.set_param(sim, "beta", 0.5) if False else None
+    sim.close()
+
+
+def test_raster_staging_counts(vh):
+    """move_to! and connect_raster_neighbors! edge counts (test/raster.jl:374-436)
+    on the staged edges, before any device work."""
+    m = (vh.ModelTypes().register_agenttype("Position", [("v", "i64")])
+         .register_agenttype("Mover", [("v", "i64")])
+         .register_edgetype("On", [])
+         .register_edgetype("G", [])
+         .create_model("raster"))
+    sim = vh.create_simulation(m)
+    vh.add_raster(sim, "r", (10, 10), "Position", v=0)
+    p = vh.add_agents(sim, "Mover", 3, v=1)
+    vh.move_to(sim, "r", p[0], (4, 4), "On", None, distance=2)
+    vh.move_to(sim, "r", p[1], (4, 4), "On", None, distance=2, metric="manhatten")
+    vh.move_to(sim, "r", p[2], (4, 4), "On", None, distance=2.5, metric="euclidean")
+    assert [vh.num_edges(sim, x, "On") for x in p] == [25, 13, 21]
+    vh.connect_raster_neighbors(sim, "r", "G")
+    assert vh.num_edges(sim, "G", write=True) == 800
+    c = vh.cellid(sim, "r", (1, 1))
+    ids = vh.neighborids(sim, c, "G")  # insertion order: source column-major
+    assert [vh.agent_nr(i) for i in ids] == [2, 10, 11, 12, 20, 91, 92, 100]
+    sim.close()
+
+
+def test_params_and_globals(vh):
+    m = (vh.ModelTypes().register_agenttype("A", [("foo", "i64")])
+         .register_param("beta", 0.1).register_global("count", 0.0).create_model("pg"))
+    sim = vh.create_simulation(m)
+    assert vh.param(sim, "beta") == 0.1
+    vh.set_param(sim, "beta", 0.2)
+    assert vh.param(sim, "beta") == 0.2
+    vh.set_global(sim, "count", 3.0)
+    vh.push_global(sim, "series", 1.0)
+    vh.push_global(sim, "series", 2.0)
+    assert vh.get_global(sim, "count") == 3.0
+    assert list(vh.global_series(sim, "series")) == [1.0, 2.0]
+    sim.close()
