@@ -315,6 +315,27 @@ int vg_read_staged_edges(vg_sim *s, int edge_type, uint64_t *from_out,
  * number of out-of-range fallbacks of each. */
 int vg_selftest_fp64(uint64_t n, uint64_t seed, uint64_t *counts_out);
 
+/* ---- allocation-free SIR step ---------------------------------------------
+ * No counterpart in the reference.  One step of the "sir" transition on
+ * device buffers the caller owns, for callers that cannot let a library
+ * allocate device memory (a host runtime that owns all device memory and
+ * hands in pre-allocated arrays, or code running while another framework
+ * captures a CUDA graph).  It calls no cudaMalloc, cudaFree or allocating
+ * routine: its only scratch, the table p_k = 1 - (1 - beta)^k, is a fixed
+ * file-scope device array of max_in_degree + 1 <= 4096 entries; larger
+ * max_in_degree is rejected with VG_ERR_ARG.  Calls share that array, so
+ * calls that overlap on the GPU race and must be serialised by the caller.
+ * The first call on a device looks the array's address up and caches it:
+ * make it before any stream capture.  row_ptr u32[n+1] and src u32 (0-based
+ * sources) form the in-edge CSR; state/days are read from the *_in buffers
+ * and written to the *_out buffers; step is the transition number
+ * (num_transitions) that apply! would use; stream is a cudaStream_t. */
+int vg_sir_step_noalloc(const uint32_t *row_ptr, const uint32_t *src,
+                        const uint8_t *state_in, const int32_t *days_in,
+                        uint8_t *state_out, int32_t *days_out, uint64_t n,
+                        uint32_t max_in_degree, double beta, int32_t recovery,
+                        uint64_t seed, uint32_t step, void *stream);
+
 /* ---- batched ensemble (many independent SIR instances in one arena) ----- */
 typedef struct vg_batch vg_batch;
 /* Instances i = 0..n-1 with agent counts N[i], out-degree deg[i], infection
