@@ -55,7 +55,11 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="opinion", choices=["opinion", "batch"])
+    ap.add_argument("--workload", default="opinion", choices=["opinion", "batch", "serve"])
+    ap.add_argument("--jobs", type=int, default=512)
+    ap.add_argument("--rates", default="100,1000")
+    ap.add_argument("--serve-budget-gb", type=float, default=64.0)
+    ap.add_argument("--plain-sample", type=int, default=24)
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=200)
     return ap.parse_args()
@@ -353,34 +357,29 @@ def run_batch(args):
     vh.build()
     n_inst, steps = args.instances, args.batch_steps
     N, deg, beta, rec, seeds = models.batch_params(n_inst)
+    # warm-up on a small batch (graph capture machinery, autotuner)
+    w = models.Batch(N[:8], deg[:8], beta[:8], rec[:8], seeds[:8])
+    w.step(steps, mode=1)
+    w.close()
     b = models.Batch(N, deg, beta, rec, seeds)
-    b.step(steps, mode=1)  # warm-up: capture + one replay
     torch.cuda.synchronize()
+    # both paths step the same fresh instances over the same steps 1..steps
     t0 = time.perf_counter()
-    reps = 3
-    for _ in range(reps):
-        b.step(steps, mode=1)
+    b.step(steps, mode=1)  # autotune + capture + replay, all inside the timed region
     torch.cuda.synchronize()
-    t_batch = (time.perf_counter() - t0) / reps
+    t_batch = time.perf_counter() - t0
     t0 = time.perf_counter()
     for i in range(n_inst):
         b.step_one(i, steps)
     torch.cuda.synchronize()
     t_plain = time.perf_counter() - t0
     bad = 0
-    for i in range(n_inst):  # the plain run has done `steps` steps, the batch (reps+1)*steps
-        pass
+    for i in range(n_inst):  # every instance bit-identical batched vs alone
+        sb, db = b.states(i, 0)
+        sp, dp = b.states(i, 1)
+        bad += int(not (np.array_equal(sb, sp) and np.array_equal(db, dp)))
     info = b.info()
     b.close()
-    # parity of batched vs plain on a fresh batch with equal step counts
-    b2 = models.Batch(N[:64], deg[:64], beta[:64], rec[:64], seeds[:64])
-    b2.step(steps, mode=1)
-    for i in range(64):
-        b2.step_one(i, steps)
-        sb, db = b2.states(i, 0)
-        sp, dp = b2.states(i, 1)
-        bad += int(not (np.array_equal(sb, sp) and np.array_equal(db, dp)))
-    b2.close()
     v = n_inst * steps / t_batch
     out = {"metric": "sim-steps/s", "value": v, "unit": "instance-steps/s", "n_gpus": 1,
            "steps": steps, "warmup": 1, "ms_per_step": 1e3 * t_batch / steps,
@@ -391,7 +390,119 @@ def run_batch(args):
                       "launch": {"tpb": info["tpb"], "agents_per_thread": info["apt"]}},
            "plain_one_at_a_time": n_inst * steps / t_plain,
            "speedup_vs_plain": t_plain / t_batch,
-           "parity_mismatches_first_64": bad}
+           "instances_differing_batched_vs_alone": bad}
+    print(json.dumps(out), flush=True)
+
+
+def serve_jobs(n_jobs, seed):
+    """Job stream: model 50/50 SIR / opinion, N log-uniform in [1e3, 1e6],
+    mean degree in [5, 30], 50..500 steps; SIR beta in [0.01, 0.1] and
+    recovery 5..10; opinion eps 0.3 with the expected degree capped at
+    min(1e4, N / 10)."""
+    from vahana_gb300 import serve
+    rng = np.random.default_rng(seed)
+    specs = []
+    for j in range(n_jobs):
+        n = int(round(10 ** rng.uniform(3, 6)))
+        steps = int(rng.integers(50, 501))
+        if rng.random() < 0.5:
+            specs.append(serve.sir_job(n, degree=int(rng.integers(5, 31)), steps=steps,
+                                       seed=j + 1, beta=float(rng.uniform(0.01, 0.1)),
+                                       recovery=int(rng.integers(5, 11))))
+        else:
+            specs.append(serve.opinion_job(n, mean_degree=float(rng.integers(5, 31)),
+                                           steps=steps, seed=j + 1, eps=0.3,
+                                           wmax=float(min(1e4, n / 10))))
+    return specs
+
+
+def run_serve(args):
+    """Serving stream: args.jobs jobs arriving as a Poisson process at each
+    rate of --rates, admitted by device footprint and stepped together; a
+    sample of the jobs also runs one by one on the plain path (build, then
+    apply! per step) for the throughput ratio and the per-job comparison."""
+    import torch
+    import vahana_gb300 as vh
+    from vahana_gb300 import models, serve
+    vh.build()
+    specs = serve_jobs(args.jobs, args.seed)
+    sample = list(range(min(args.plain_sample, len(specs))))
+    for j in sample:
+        specs[j].keep_state = 1
+    total_steps = sum(s.steps for s in specs)
+    # plain path, one job after the other, on the sample
+    t0 = time.perf_counter()
+    plain_states = {}
+    for j in sample:
+        s = specs[j]
+        if s.model == serve.SIR:
+            run = models.build_sir(n=s.n, degree=int(s.mean_degree), beta=s.beta,
+                                   recovery=s.recovery, seed=s.seed)
+            T = "Person"
+        else:
+            run = models.build_opinion(n=s.n, mean_degree=s.mean_degree, gamma=2.5, wmax=s.wmax,
+                                       eps=s.eps, seed=s.seed, hub_threshold=256)
+            T = "Opinion"
+        vh.finish_init(run.sim)
+        for _ in range(s.steps):
+            run.step()
+        plain_states[j] = vh.read_agents(run.sim, T)[0]
+        run.close()
+    torch.cuda.synchronize()
+    t_plain = time.perf_counter() - t0
+    plain_rate = sum(specs[j].steps for j in sample) / t_plain
+    per_rate = []
+    mismatched = 0
+    rng = np.random.default_rng(args.seed + 1000)
+    for rate in [float(r) for r in args.rates.split(",")]:
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, len(specs)))
+        with serve.Server(budget_bytes=int(args.serve_budget_gb * (1 << 30))) as S:
+            results = {}
+            ids = []
+
+            def feeder():
+                t_start = time.perf_counter()
+                for k, spec in enumerate(specs):
+                    d = arrivals[k] - (time.perf_counter() - t_start)
+                    if d > 0:
+                        time.sleep(d)
+                    ids.append(S.submit(spec))
+            th = threading.Thread(target=feeder)
+            th.start()
+            while len(results) < len(specs):
+                for r in S.poll():
+                    results[r["id"]] = r
+                time.sleep(0.002)
+            th.join()
+            stats = S.stats()
+            lat = np.array([r["finish_s"] - r["arrival_s"] for r in results.values()])
+            wait = np.array([r["admit_s"] - r["arrival_s"] for r in results.values()])
+            t_first = min(r["arrival_s"] for r in results.values())
+            t_last = max(r["finish_s"] for r in results.values())
+            for j in sample:  # the sampled jobs' results equal their plain runs
+                got = S.job_state(ids[j], specs[j])
+                ref = plain_states[j]
+                ok = (np.array_equal(got[0], ref["state"]) and np.array_equal(got[1], ref["days"])
+                      if specs[j].model == serve.SIR
+                      else np.array_equal(got.view(np.uint64), ref["x"].view(np.uint64)))
+                mismatched += int(not ok)
+        per_rate.append({"rate_jobs_per_s": rate, "p50_latency_s": float(np.percentile(lat, 50)),
+                         "p99_latency_s": float(np.percentile(lat, 99)),
+                         "p50_queue_wait_s": float(np.percentile(wait, 50)),
+                         "sim_steps_per_s": total_steps / (t_last - t_first),
+                         "makespan_s": t_last - t_first, "ticks": stats["ticks"]})
+    best = max(per_rate, key=lambda r: r["sim_steps_per_s"])
+    out = {"metric": "sim-steps/s", "value": best["sim_steps_per_s"], "unit": "job-steps/s",
+           "n_gpus": 1, "steps": total_steps, "warmup": 0,
+           "ms_per_step": 1e3 / best["sim_steps_per_s"], "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "u8/i32+f64", "data": "synthetic",
+           "config": {"workload": "serving_stream_sir_opinion", "jobs": len(specs),
+                      "rates": [r["rate_jobs_per_s"] for r in per_rate],
+                      "budget_gb": args.serve_budget_gb},
+           "per_rate": per_rate,
+           "plain_one_by_one": {"sim_steps_per_s": plain_rate, "sample_jobs": len(sample)},
+           "speedup_vs_plain": best["sim_steps_per_s"] / plain_rate,
+           "sample_jobs_differing_served_vs_alone": mismatched}
     print(json.dumps(out), flush=True)
 
 
@@ -399,6 +510,8 @@ def main():
     args = parse()
     if args.workload == "batch":
         run_batch(args)
+    elif args.workload == "serve":
+        run_serve(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

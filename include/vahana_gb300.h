@@ -365,6 +365,55 @@ int vg_batch_info(vg_batch *b, uint64_t *agents, uint64_t *edges, int *tpb,
                   int *apt, uint64_t *device_bytes);
 int vg_batch_destroy(vg_batch *b);
 
+/* ---- serving loop (no reference counterpart) ------------------------------
+ * Simulation jobs of the SIR and the opinion test model arrive over time.
+ * A worker thread admits queued jobs, first come first served, while the sum
+ * of their estimated device footprints stays within budget_bytes and at most
+ * max_active are resident (a job that does not fit an empty server still
+ * runs alone).  Each tick advances every resident job by one transition with
+ * one launch per model over all of them; a job retires after `steps`
+ * transitions.  A job's final state equals the state after `steps` apply!
+ * calls on that job built alone (vahana_gb300 models build_sir /
+ * build_opinion with the same arguments). */
+typedef struct vg_server vg_server;
+typedef struct vg_job_spec {
+  int model;           /* 0 SIR, 1 bounded-confidence opinion              */
+  uint64_t n;          /* agents                                           */
+  double mean_degree;  /* SIR: out-degree (rounded); opinion: mean degree  */
+  int32_t steps;       /* transitions to run                               */
+  uint64_t seed;
+  double beta;         /* SIR infection probability                       */
+  int32_t recovery;    /* SIR recovery steps                              */
+  double eps;          /* opinion confidence bound                        */
+  double wmax;         /* opinion: cap of the expected degree (<=0: 1e4)  */
+  int keep_state;      /* keep the final state for vg_serve_job_state     */
+} vg_job_spec;
+typedef struct vg_job_result {
+  int64_t id;
+  int model;
+  uint64_t n;
+  int32_t steps;
+  double arrival_s, admit_s, finish_s; /* seconds since vg_serve_create   */
+  uint64_t checksum;                   /* FNV-1a 64 of the final state    */
+  double summary;   /* SIR: recovered fraction; opinion: mean opinion      */
+  uint64_t device_bytes;
+} vg_job_result;
+int vg_serve_create(uint64_t budget_bytes, int max_active, vg_server **out);
+int vg_serve_submit(vg_server *s, const vg_job_spec *spec, int64_t *id_out);
+/* Results of jobs finished since the last poll, at most cap. */
+int vg_serve_poll(vg_server *s, vg_job_result *out, uint64_t cap, uint64_t *n_out);
+/* Final state bytes of a finished job submitted with keep_state (SIR: n
+ * state bytes then n Int32 days; opinion: n Float64).  out may be NULL to
+ * query the size. */
+int vg_serve_job_state(vg_server *s, int64_t id, void *out, uint64_t cap,
+                       uint64_t *n_out);
+int vg_serve_stats(vg_server *s, uint64_t *queued, uint64_t *active,
+                   uint64_t *done, uint64_t *ticks, uint64_t *sim_steps,
+                   uint64_t *bytes_in_use);
+/* Stop accepting, finish every queued and resident job. */
+int vg_serve_drain(vg_server *s);
+int vg_serve_destroy(vg_server *s);
+
 #ifdef __cplusplus
 }
 #endif

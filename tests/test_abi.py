@@ -89,7 +89,6 @@ def test_init_phase_staging_and_accessors(vh):
     assert vh.mapreduce(sim, "foo", "max", "A") == 3
     with pytest.raises(AssertionError):
         vh.apply_(sim, "keep", "A", [], [])  # apply! before finish_init!
-    vh.set_param(sim, "beta", 0.5) if False else None
     sim.close()
 
 

@@ -290,6 +290,18 @@ const std::vector<TransitionDef> &transitions();
 // launchers that live in their own translation units
 void tr_bounded_confidence(ApplyCtx &ctx);  // vg_opinion.cu
 
+// one bounded-confidence launch over many simulations (vg_opinion.cu)
+struct OpinionJob {
+  Sim *sim;
+  int edge_type, type_nr;
+  double eps, a, b;
+  uint32_t hub_thr;
+};
+void launch_opinion_jobs(const std::vector<OpinionJob> &jobs, cudaStream_t st, DevBuf &args_buf,
+                         DevBuf &tiles_buf, uint64_t *footprint);
+// initial SIR state: the n_inf agents with the smallest Philox init draw
+void sir_initial_state(uint64_t n, uint64_t seed, uint64_t n_inf, std::vector<uint8_t> &state);
+
 // primitives (vg_sort.cu)
 void exclusive_scan_u32(const uint32_t *in, uint32_t *out, uint64_t n,
                         cudaStream_t st, Sim &s);

@@ -9,11 +9,14 @@
 // x' = a * x + b * (swx / sw), or x when no neighbour qualifies.
 //
 // Degree buckets:
-//   rows with in-degree <= hub_thr: one thread per row, folding in order;
-//     bit-identical to the sequential binary64 computation.
-//   rows above hub_thr ("hubs"): one warp per row, each lane folds a
-//     contiguous chunk in order, the chunk sums are combined in a fixed
-//     lane tree.  The additions are regrouped, so these rows agree with the
+//   rows with in-degree <= hub_thr: 32 rows (of similar degree) per warp.
+//     The warp stages the rows' edges with coalesced loads, tests and
+//     multiplies edge-parallel, and compacts the accepted edges of each row
+//     into a shared-memory column; the row's lane then folds its column in
+//     edge order -- bit-identical to the sequential binary64 computation.
+//   rows above hub_thr ("hubs"): one warp per row, lane l folds the edges
+//     l, l + 32, ... in order and the 32 lane sums are combined in a fixed
+//     tree.  The additions are regrouped, so these rows agree with the
 //     sequential fold to within 1e-12 relative; hub_thr = 2^32-1 disables
 //     the split and keeps every row bit-exact.
 //   The hub warps are the first blocks of the grid so that they start
@@ -146,11 +149,14 @@ __device__ __forceinline__ uint64_t mul_fast(uint64_t a, uint64_t b, bool &ok) {
 // sw as an integer K of 2^-53 units: K += w * 2^53, then K rounded to 53
 // significant bits (ties to even) -- the binary64 sum, valid while every
 // weight is a multiple of 2^-53 in (0, 1] and K < 2^64.
-__device__ __forceinline__ void grid_add(uint64_t &K, double w) {
+__device__ __forceinline__ uint64_t grid_k(double w) {
   uint64_t wb = bits(w);
   uint32_t ew = (uint32_t)(wb >> 52);
   uint64_t m = (wb & EMU_M52) | EMU_H53;
-  uint64_t k = ew >= 1023u ? (m << 1) : (m >> (1022u - ew));
+  return ew >= 1023u ? (m << 1) : (m >> (1022u - ew));
+}
+
+__device__ __forceinline__ void grid_accum(uint64_t &K, uint64_t k) {
   K += k;
   uint32_t khi = (uint32_t)(K >> 32);
   int s = 11 - __clz(khi);  // significant bits beyond 53
@@ -163,6 +169,8 @@ __device__ __forceinline__ void grid_add(uint64_t &K, double w) {
   }
 }
 
+__device__ __forceinline__ void grid_add(uint64_t &K, double w) { grid_accum(K, grid_k(w)); }
+
 // x' = a x + b (swx / sw), each operation rounded in this order
 __device__ __noinline__ double finish(double pa, double pb_, double xi, uint64_t sw,
                                       uint64_t swx) {
@@ -172,61 +180,166 @@ __device__ __noinline__ double finish(double pa, double pb_, double xi, uint64_t
   return dbl(add_rn(l, r));
 }
 
-// ordered fold of edges [b, e) of a row into (sw, swx, cnt)
-template <bool GRID>
-__device__ __forceinline__ void fold(const OpinionArgs &p, uint32_t b, uint32_t e, double xi,
-                                     float fxi, bool xi_ok, uint64_t &K, double &sw,
-                                     double &swx, uint32_t &cnt) {
-  if (b >= e) return;
-  // software pipeline: source index two edges ahead, neighbour state one
-  // edge ahead, so that the dependent gathers overlap the arithmetic
-  uint32_t jn = b + 1 < e ? __ldg(p.src + b + 1) : 0;
-  double xj = __ldg(p.x + __ldg(p.src + b));
-  for (uint32_t k = b; k < e; k++) {
-    uint32_t jnn = k + 2 < e ? __ldg(p.src + k + 2) : 0;
-    double xn = k + 1 < e ? __ldg(p.x + jn) : 0.0;
-    double wk = __ldg(p.w + k);
-    double xcur = xj;
-    xj = xn;
-    jn = jnn;
-    if (within(xcur, xi, fxi, xi_ok, p)) {
-      double xj = xcur;
-      bool ok;
-      uint64_t pk = mul_fast(bits(wk), bits(xj), ok);
-      double pkd = ok ? dbl(pk) : mul_hw(wk, xj);
-      swx = __dadd_rn(swx, pkd);
-      if (GRID) grid_add(K, wk);
-      else sw = __dadd_rn(sw, wk);
-      cnt++;
-    }
-  }
-}
-
 template <bool GRID>
 __device__ __forceinline__ double sum_w(uint64_t K, double sw) {
   return GRID ? __dmul_rn(__ull2double_rn(K), 0x1p-53) : sw;
 }
 
+// Rows of the degree-sorted order, 32 per warp, lane l owning row g0 + l.
+// Rounds of SLOTS edges per row: the warp stages the round's edges of its
+// rows with coalesced loads (SLOTS lanes per row), gathers the neighbours'
+// opinions, applies the threshold test, forms w * x and compacts the
+// accepted edges of each row, in edge order, into a shared-memory column of
+// that row; then each lane folds its own column in order.  The fold is the
+// sequential binary64 computation of the row (bit-identical), and only
+// accepted edges reach the FP64 pipe.
+constexpr int SLOTS = 8;                // edges per row and round
+constexpr int ROWS_PER_IT = 32 / SLOTS;  // rows staged per warp iteration
+constexpr int ITS = 32 / ROWS_PER_IT;    // staging iterations per round
+constexpr uint32_t GRID_MAX_DEG = 2047;  // K < 2^64 for at most 2047 weights <= 1
+
+struct WarpStage {
+  double prod[SLOTS][33];    // accepted w * x, column per row (padded: no bank conflicts)
+  uint64_t wgt[SLOTS][33];   // its weight: K units (grid rows) or binary64 bits
+  uint32_t rb[32], deg[32];  // the rows' first edge and degree (0: nothing to fold)
+  double xi[32];
+  float fxi[32];
+  uint32_t xok[32], cnt[32];
+};
+
 template <bool GRID>
-__global__ void __launch_bounds__(TPB) k_opinion(OpinionArgs p) {
-  if (blockIdx.x < p.hub_blocks) {
-    // one warp per hub row: lane l folds the l-th contiguous chunk in order
-    const int lane = threadIdx.x & 31;
-    uint64_t h = (uint64_t)blockIdx.x * (TPB / 32) + (threadIdx.x >> 5);
+__device__ __forceinline__ void rows_warp(const OpinionArgs &p, uint64_t g0, WarpStage *stage) {
+  WarpStage &S = stage[threadIdx.x >> 5];
+  const unsigned lane = threadIdx.x & 31;
+  const uint64_t total = p.order ? p.norder : p.n;
+  const uint64_t g = g0 + lane;
+  const bool active = g < total;
+  uint64_t i = 0;
+  double xi = 0.0;
+  uint32_t b = 0, deg = 0;
+  bool write = false;
+  if (active) {
+    i = p.order ? p.order[g] : g;
+    xi = p.x[i];
+    write = true;
+    if (i < p.nrows) {
+      b = p.rp[i];
+      deg = p.rp[i + 1] - b;
+      if (deg > p.hub_thr) {  // a hub warp writes this row
+        deg = 0;
+        write = false;
+      }
+    }
+  }
+  bool xi_ok;
+  float fxi = hi_float(xi, xi_ok);
+  S.rb[lane] = b;
+  S.deg[lane] = deg;
+  S.xi[lane] = xi;
+  S.fxi[lane] = fxi;
+  S.xok[lane] = xi_ok;
+  const bool gr = GRID && deg <= GRID_MAX_DEG;
+  const uint32_t maxdeg = __reduce_max_sync(0xffffffffu, deg);
+  __syncwarp();
+  const unsigned sub = lane / SLOTS, t = lane % SLOTS;
+  const unsigned grp = ((1u << SLOTS) - 1u) << (sub * SLOTS);
+  const unsigned lt = (1u << lane) - 1u;
+  uint64_t K = 0;
+  double sw = 0.0, swx = 0.0;
+  uint32_t cnt = 0;
+  for (uint32_t k0 = 0; k0 < maxdeg; k0 += SLOTS) {
+    uint32_t jv[ITS];
+    double wv[ITS], xv[ITS];
+#pragma unroll
+    for (int it = 0; it < ITS; it++) {
+      const unsigned rl = it * ROWS_PER_IT + sub;
+      const uint32_t kk = k0 + t;
+      const bool valid = kk < S.deg[rl];
+      const uint32_t e = S.rb[rl] + kk;
+      jv[it] = valid ? __ldg(p.src + e) : 0xffffffffu;
+      wv[it] = valid ? __ldg(p.w + e) : 0.0;
+    }
+#pragma unroll
+    for (int it = 0; it < ITS; it++) xv[it] = jv[it] != 0xffffffffu ? __ldg(p.x + jv[it]) : 0.0;
+#pragma unroll
+    for (int it = 0; it < ITS; it++) {
+      const unsigned rl = it * ROWS_PER_IT + sub;
+      const bool valid = jv[it] != 0xffffffffu;
+      bool acc = valid && within(xv[it], S.xi[rl], S.fxi[rl], S.xok[rl] != 0, p);
+      const unsigned bal = __ballot_sync(0xffffffffu, acc) & grp;
+      if (acc) {
+        bool ok;
+        uint64_t pk = mul_fast(bits(wv[it]), bits(xv[it]), ok);
+        double pkd = ok ? dbl(pk) : mul_hw(wv[it], xv[it]);
+        const unsigned q = __popc(bal & lt);
+        S.prod[q][rl] = pkd;
+        S.wgt[q][rl] = (GRID && S.deg[rl] <= GRID_MAX_DEG) ? grid_k(wv[it]) : bits(wv[it]);
+      }
+      if (t == 0) S.cnt[rl] = __popc(bal);
+    }
+    __syncwarp();
+    const uint32_t n = S.cnt[lane];
+    for (uint32_t q = 0; q < n; q++) {
+      swx = __dadd_rn(swx, S.prod[q][lane]);
+      if (gr) grid_accum(K, S.wgt[q][lane]);
+      else sw = __dadd_rn(sw, dbl(S.wgt[q][lane]));
+    }
+    cnt += n;
+    __syncwarp();
+  }
+  if (write) {
+    uint64_t swb = bits(gr ? sum_w<true>(K, sw) : sw);
+    p.xo[i] = cnt ? finish(p.a, p.b, xi, swb, bits(swx)) : xi;
+  }
+}
+
+// The work of one block of the gather grid: `blk` < hub_blocks are hub
+// warps, the rest row threads.  Shared by the single-simulation kernel and
+// the multi-job kernel of the serving loop.
+template <bool GRID>
+__device__ __forceinline__ void opinion_block(const OpinionArgs &p, unsigned blk,
+                                              WarpStage *stage) {
+  if (blk < p.hub_blocks) {
+    // one warp per hub row: lane l folds edges l, l + 32, l + 64, ... in
+    // order (coalesced loads), the lane sums are combined in a fixed tree
+    const unsigned lane = threadIdx.x & 31;
+    uint64_t h = (uint64_t)blk * (TPB / 32) + (threadIdx.x >> 5);
     if (h >= p.nhub) return;
     uint32_t r = p.hub_rows[h];
     double xi = p.x[r];
     bool xi_ok;
     float fxi = hi_float(xi, xi_ok);
-    uint32_t b = p.rp[r], e = p.rp[r + 1];
-    uint32_t chunk = (e - b + 31) / 32;
-    uint32_t cb = min(e, b + lane * chunk), ce = min(e, cb + chunk);
+    const uint32_t b = p.rp[r], e = p.rp[r + 1];
+    const bool gr = GRID && (e - b + 31) / 32 <= GRID_MAX_DEG;
     uint64_t K = 0;
     double dsw = 0.0, dswx = 0.0;
     uint32_t cnt = 0;
-    if (GRID && ce - cb <= 2047) fold<true>(p, cb, ce, xi, fxi, xi_ok, K, dsw, dswx, cnt);
-    else fold<false>(p, cb, ce, xi, fxi, xi_ok, K, dsw, dswx, cnt);
-    uint64_t sw = bits(GRID && ce - cb <= 2047 ? sum_w<true>(K, dsw) : dsw);
+    constexpr int U = 4;
+    for (uint32_t k0 = b; k0 < e; k0 += 32 * U) {
+      uint32_t jv[U];
+      double wv[U], xv[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const uint32_t k = k0 + u * 32 + lane;
+        const bool valid = k < e;
+        jv[u] = valid ? __ldg(p.src + k) : 0xffffffffu;
+        wv[u] = valid ? __ldg(p.w + k) : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++) xv[u] = jv[u] != 0xffffffffu ? __ldg(p.x + jv[u]) : 0.0;
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        if (jv[u] != 0xffffffffu && within(xv[u], xi, fxi, xi_ok, p)) {
+          bool ok;
+          uint64_t pk = mul_fast(bits(wv[u]), bits(xv[u]), ok);
+          dswx = __dadd_rn(dswx, ok ? dbl(pk) : mul_hw(wv[u], xv[u]));
+          if (gr) grid_add(K, wv[u]);
+          else dsw = __dadd_rn(dsw, wv[u]);
+          cnt++;
+        }
+      }
+    }
+    uint64_t sw = bits(gr ? sum_w<true>(K, dsw) : dsw);
     uint64_t swx = bits(dswx);
     // fixed tree: lane l receives lane l + off
 #pragma unroll
@@ -243,28 +356,31 @@ __global__ void __launch_bounds__(TPB) k_opinion(OpinionArgs p) {
     if (lane == 0) p.xo[r] = cnt ? finish(p.a, p.b, xi, sw, swx) : xi;
     return;
   }
-  uint64_t g = (uint64_t)(blockIdx.x - p.hub_blocks) * TPB + threadIdx.x;
-  if (g >= (p.order ? p.norder : p.n)) return;
-  uint64_t i = p.order ? p.order[g] : g;
-  double xi = p.x[i];
-  if (i >= p.nrows) {
-    p.xo[i] = xi;
-    return;
-  }
-  uint32_t b = p.rp[i], e = p.rp[i + 1];
-  if (e - b > p.hub_thr) return;  // a hub warp writes this row
-  bool xi_ok;
-  float fxi = hi_float(xi, xi_ok);
-  uint64_t K = 0;
-  double dsw = 0.0, swx = 0.0;
-  uint32_t cnt = 0;
-  if (!GRID || e - b > 2047) {  // K would overflow: binary64 adds
-    fold<false>(p, b, e, xi, fxi, xi_ok, K, dsw, swx, cnt);
-    p.xo[i] = cnt ? finish(p.a, p.b, xi, bits(dsw), bits(swx)) : xi;
-    return;
-  }
-  fold<true>(p, b, e, xi, fxi, xi_ok, K, dsw, swx, cnt);
-  p.xo[i] = cnt ? finish(p.a, p.b, xi, bits(sum_w<true>(K, dsw)), bits(swx)) : xi;
+  rows_warp<GRID>(p, (uint64_t)(blk - p.hub_blocks) * TPB + (threadIdx.x & ~31u), stage);
+}
+
+template <bool GRID>
+__global__ void __launch_bounds__(TPB) k_opinion(OpinionArgs p) {
+  __shared__ WarpStage stage[TPB / 32];
+  opinion_block<GRID>(p, blockIdx.x, stage);
+}
+
+// Many simulations in one launch: block i runs virtual block tiles[i].blk of
+// job tiles[i].job -- the same work, in the same order, as that job's own
+// launch of k_opinion.
+struct JobTile {
+  uint32_t job, blk;
+};
+
+__global__ void __launch_bounds__(TPB) k_opinion_jobs(const OpinionArgs *jobs,
+                                                      const JobTile *tiles) {
+  __shared__ OpinionArgs sp;
+  __shared__ WarpStage stage[TPB / 32];
+  JobTile t = tiles[blockIdx.x];
+  if (threadIdx.x == 0) sp = jobs[t.job];
+  __syncthreads();
+  if (sp.grid) opinion_block<true>(sp, t.blk, stage);
+  else opinion_block<false>(sp, t.blk, stage);
 }
 
 // every weight a multiple of 2^-53 in (0, 1]?
@@ -283,6 +399,9 @@ __global__ void k_check_grid(const double *w, uint64_t n, int *bad) {
 }
 
 }  // namespace
+
+static unsigned opinion_args(Sim &s, int e, int T, double eps, double a, double b,
+                             uint32_t thr, OpinionArgs &p);
 
 // apply!(sim, bounded_confidence, [T], [T, E], [T]; params = [E, eps, a, b,
 // hub_thr]); defaults eps 0.3, a 0.5, b 1 - a, hub_thr 256.
@@ -309,13 +428,24 @@ void tr_bounded_confidence(ApplyCtx &c) {
   double b = c.nparams > 3 ? c.params[3] : 1.0 - a;
   double thr_d = c.param(4, 256);
   uint32_t thr = thr_d >= 4294967295.0 ? 0xffffffffu : (uint32_t)thr_d;
-  EdgeStore &es = s.edges[e];
-  DevCSRView v = csr_view(s, e, c.call_type);
-  if (v.nedges && v.src_type_const != c.call_type)
-    fail(VG_ERR_ARG, "bounded_confidence: sources must be of the called type");
-  DevAgentView av = agent_view(s, c.call_type);
-  if (av.n == 0) return;
   OpinionArgs p{};
+  unsigned grid = opinion_args(s, e, c.call_type, eps, a, b, thr, p);
+  if (!grid) return;
+  if (p.grid) k_opinion<true><<<grid, TPB, 0, s.stream>>>(p);
+  else k_opinion<false><<<grid, TPB, 0, s.stream>>>(p);
+  VG_CUDA(cudaGetLastError());
+}
+
+// arguments and grid size of one simulation's gather launch (0: no agents)
+static unsigned opinion_args(Sim &s, int e, int T, double eps, double a, double b,
+                             uint32_t thr, OpinionArgs &p) {
+  EdgeStore &es = s.edges[e];
+  DevCSRView v = csr_view(s, e, T);
+  if (v.nedges && v.src_type_const != T)
+    fail(VG_ERR_ARG, "bounded_confidence: sources must be of the called type");
+  DevAgentView av = agent_view(s, T);
+  if (av.n == 0) return 0;
+  p = OpinionArgs{};
   p.rp = v.row_ptr;
   p.src = v.src;
   p.w = (const double *)v.payload[0];
@@ -329,8 +459,8 @@ void tr_bounded_confidence(ApplyCtx &c) {
   p.eps_lo = (float)(eps - 1e-5);
   p.eps_hi = (float)(eps + 1e-5);
   p.hub_thr = 0xffffffffu;
-  if (v.nedges && c.call_type < (int)es.csr.size()) {
-    CSR &cs = es.csr[c.call_type];
+  if (v.nedges && T < (int)es.csr.size()) {
+    CSR &cs = es.csr[T];
     if (cs.unit_grid_weights < 0) {
       int *bad = nullptr;
       VG_CUDA(cudaMallocAsync((void **)&bad, 4, s.stream));
@@ -351,10 +481,36 @@ void tr_bounded_confidence(ApplyCtx &c) {
     p.hub_thr = thr;
     p.hub_blocks = (unsigned)((cs.nhub + (TPB / 32) - 1) / (TPB / 32));
   }
-  unsigned grid = p.hub_blocks + (unsigned)((av.n + TPB - 1) / TPB);
-  if (p.grid) k_opinion<true><<<grid, TPB, 0, s.stream>>>(p);
-  else k_opinion<false><<<grid, TPB, 0, s.stream>>>(p);
+  return p.hub_blocks + (unsigned)((av.n + TPB - 1) / TPB);
+}
+
+// One launch for the bounded-confidence step of many simulations (the
+// serving loop's continuous batching).  Each job's blocks do exactly what
+// its own launch would; the caller finishes each job's transition.
+void launch_opinion_jobs(const std::vector<OpinionJob> &jobs, cudaStream_t st, DevBuf &args_buf,
+                         DevBuf &tiles_buf, uint64_t *fp) {
+  std::vector<OpinionArgs> args;
+  std::vector<JobTile> tiles;
+  for (size_t j = 0; j < jobs.size(); j++) {
+    OpinionArgs p{};
+    unsigned g = opinion_args(*jobs[j].sim, jobs[j].edge_type, jobs[j].type_nr, jobs[j].eps,
+                              jobs[j].a, jobs[j].b, jobs[j].hub_thr, p);
+    args.push_back(p);
+    for (unsigned k = 0; k < g; k++) tiles.push_back({(uint32_t)j, k});
+  }
+  if (tiles.empty()) return;
+  if (args_buf.bytes < args.size() * sizeof(OpinionArgs))
+    args_buf.alloc(args.size() * sizeof(OpinionArgs) * 2, fp);
+  if (tiles_buf.bytes < tiles.size() * sizeof(JobTile))
+    tiles_buf.alloc(tiles.size() * sizeof(JobTile) * 2, fp);
+  VG_CUDA(cudaMemcpyAsync(args_buf.p, args.data(), args.size() * sizeof(OpinionArgs),
+                          cudaMemcpyHostToDevice, st));
+  VG_CUDA(cudaMemcpyAsync(tiles_buf.p, tiles.data(), tiles.size() * sizeof(JobTile),
+                          cudaMemcpyHostToDevice, st));
+  k_opinion_jobs<<<(unsigned)tiles.size(), TPB, 0, st>>>(args_buf.as<OpinionArgs>(),
+                                                        tiles_buf.as<JobTile>());
   VG_CUDA(cudaGetLastError());
+  VG_CUDA(cudaStreamSynchronize(st));  // host vectors are released on return
 }
 
 }  // namespace vg

@@ -1,0 +1,501 @@
+// Serving loop: simulation jobs arrive over time, are admitted while their
+// device footprint fits a budget, are stepped together (continuous
+// batching: every tick advances every resident job by one transition in one
+// launch per model), and are retired when their step count is reached.
+//
+// A job is an ordinary simulation (the "SIR" or the opinion model of the
+// test models), built on the server's stream when admitted.  A tick runs
+// the same per-job work as the job's own apply! (the SIR rule with the
+// job's table; the bounded-confidence blocks through launch_opinion_jobs)
+// and then the job's finish of the transition (buffer swap,
+// num_transitions += 1), so each job's state after k ticks equals the
+// state after k apply! calls on that job alone.
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "vg_internal.h"
+#include "vg_philox.cuh"
+
+namespace vg {
+void set_last_error(const std::string &m);
+}  // namespace vg
+
+using namespace vg;
+
+
+namespace {
+
+double now_s(std::chrono::steady_clock::time_point t0) {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+uint64_t fnv1a(const void *p, size_t n, uint64_t h = 1469598103934665603ull) {
+  const uint8_t *b = (const uint8_t *)p;
+  for (size_t i = 0; i < n; i++) {
+    h ^= b[i];
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
+struct Job {
+  int64_t id;
+  vg_job_spec spec;
+  double arrival = 0, admit = 0, finish = 0;
+  vg_sim *sim = nullptr;
+  int done_steps = 0;
+  DevBuf ptab;  // SIR: p_k table
+  uint32_t ptab_n = 0;
+  uint64_t est_bytes = 0;
+  std::vector<uint8_t> final_state;
+  vg_job_result result{};
+};
+
+struct SirJobDesc {
+  const uint32_t *rp;
+  const uint32_t *src;
+  const uint8_t *st_rd;
+  const int32_t *d_rd;
+  uint8_t *st_wr;
+  int32_t *d_wr;
+  uint64_t n, nrows;
+  const double *ptab;
+  uint32_t ptab_n;
+  uint32_t step;
+  uint64_t seed;
+  int32_t recovery;
+};
+
+struct SirTile {
+  uint32_t job;
+  uint32_t start;
+};
+
+// the SIR rule of transition "sir" for the agents of one tile of one job
+__global__ void k_sir_jobs(const SirJobDesc *jobs, const SirTile *tiles, int *status) {
+  SirTile t = tiles[blockIdx.x];
+  const SirJobDesc &j = jobs[t.job];
+  uint64_t i = (uint64_t)t.start + threadIdx.x;
+  if (i >= j.n) return;
+  uint8_t s = j.st_rd[i];
+  int32_t d = j.d_rd[i];
+  if (s == 0) {
+    uint32_t k = 0;
+    if (i < j.nrows) {
+      uint32_t e = j.rp[i + 1];
+      for (uint32_t q = j.rp[i]; q < e; q++) k += (__ldg(j.st_rd + j.src[q]) == 1);
+    }
+    if (k > 0) {
+      if (k >= j.ptab_n) {
+        atomicCAS(status, 0, 401);
+      } else {
+        double u = u64_to_unit(philox_u64(philox_draw(j.seed, i + 1, j.step, TAG_INFECT)));
+        if (u < j.ptab[k]) {
+          s = 1;
+          d = 0;
+        }
+      }
+    }
+  } else if (s == 1) {
+    d = d + 1;
+    if (d >= j.recovery) s = 2;
+  }
+  j.st_wr[i] = s;
+  j.d_wr[i] = d;
+}
+
+}  // namespace
+
+struct vg_server {
+  std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+  uint64_t budget = 0, used = 0;
+  int max_active = 0;
+  cudaStream_t stream = nullptr;
+  vg_model *sir_model = nullptr, *op_model = nullptr;
+  int sir_person = 0, sir_contact = 0, op_agent = 0, op_edge = 0;
+  std::thread worker;
+  std::mutex mu;
+  std::condition_variable cv;
+  bool stop = false;
+  std::string error;
+  int64_t next_id = 1;
+  std::deque<Job *> queue;
+  std::vector<Job *> active;
+  std::vector<Job *> done;
+  uint64_t ticks = 0, sim_steps = 0;
+  uint64_t footprint = 0;
+  DevBuf sir_jobs_buf, sir_tiles_buf, op_args_buf, op_tiles_buf, status;
+};
+
+namespace {
+
+uint64_t estimate_bytes(const vg_job_spec &s) {
+  double n = (double)s.n, e = s.mean_degree * n;
+  if (s.model == 0) {  // state 2x5 B, rows, sources, build staging (16 B/edge + sort)
+    return (uint64_t)(10 * n + 4 * n + 4 * e + 32 * e + 8 * n) + (1 << 20);
+  }
+  // opinion: 2x8 B state, rows + order, 12 B/edge, build staging 24 B/edge + sort
+  return (uint64_t)(16 * n + 12 * n + 12 * e + 40 * e) + (1 << 20);
+}
+
+void build_job(vg_server *S, Job *J) {
+  int rc;
+  const vg_job_spec &sp = J->spec;
+  if (sp.model == 0) {
+    if ((rc = vg_sim_create(S->sir_model, "job", S->stream, &J->sim))) fail(rc, vg_last_error());
+    std::vector<uint8_t> st;
+    uint64_t ninf = (uint64_t)std::max<double>(1.0, std::nearbyint((double)sp.n / 1000.0));
+    sir_initial_state(sp.n, sp.seed, ninf, st);
+    std::vector<int32_t> days(sp.n, 0);
+    const void *cols[2] = {st.data(), days.data()};
+    if ((rc = vg_add_agents(J->sim, S->sir_person, sp.n, cols, nullptr))) fail(rc, vg_last_error());
+    if ((rc = vg_gen_uniform_out_edges(J->sim, S->sir_contact, S->sir_person,
+                                       (uint32_t)std::lround(sp.mean_degree), sp.seed)))
+      fail(rc, vg_last_error());
+    if ((rc = vg_finish_init(J->sim))) fail(rc, vg_last_error());
+    Sim &s = *J->sim->s;
+    uint32_t maxdeg = s.edges[S->sir_contact].csr[S->sir_person].max_degree;
+    std::vector<double> tab(maxdeg + 1);
+    double q = 1.0, om = 1.0 - sp.beta;
+    tab[0] = 0.0;
+    for (uint32_t k = 1; k <= maxdeg; k++) {  // p_k = 1 - (1 - beta)^k, as the "sir" kernel
+      q = q * om;
+      tab[k] = 1.0 - q;
+    }
+    J->ptab.alloc(tab.size() * 8, &S->footprint);
+    VG_CUDA(cudaMemcpyAsync(J->ptab.p, tab.data(), tab.size() * 8, cudaMemcpyHostToDevice, S->stream));
+    VG_CUDA(cudaStreamSynchronize(S->stream));
+    J->ptab_n = (uint32_t)tab.size();
+  } else {
+    if ((rc = vg_sim_create(S->op_model, "job", S->stream, &J->sim))) fail(rc, vg_last_error());
+    std::vector<double> x(sp.n);
+    for (uint64_t i = 0; i < sp.n; i++)
+      x[i] = u64_to_unit(philox_u64(philox_draw(sp.seed, i + 1, 0, TAG_INIT)));
+    const void *cols[1] = {x.data()};
+    if ((rc = vg_add_agents(J->sim, S->op_agent, sp.n, cols, nullptr))) fail(rc, vg_last_error());
+    uint64_t ne = (uint64_t)std::nearbyint(sp.mean_degree * (double)sp.n);
+    if ((rc = vg_gen_chung_lu_edges(J->sim, S->op_edge, S->op_agent, ne, sp.mean_degree, 2.5,
+                                    sp.wmax, sp.seed, 0)))
+      fail(rc, vg_last_error());
+    if ((rc = vg_finish_init(J->sim))) fail(rc, vg_last_error());
+  }
+}
+
+void retire_job(vg_server *S, Job *J) {
+  Sim &s = *J->sim->s;
+  vg_job_result &r = J->result;
+  r.id = J->id;
+  r.model = J->spec.model;
+  r.n = J->spec.n;
+  r.steps = J->spec.steps;
+  r.arrival_s = J->arrival;
+  r.admit_s = J->admit;
+  r.device_bytes = s.footprint;
+  int T = J->spec.model == 0 ? S->sir_person : S->op_agent;
+  AgentStore &A = s.agents[T - 1];
+  std::vector<uint8_t> bytes;
+  if (J->spec.model == 0) {
+    bytes.resize(A.n * 5);
+    VG_CUDA(cudaMemcpyAsync(bytes.data(), A.rd[0].p, A.n, cudaMemcpyDeviceToHost, S->stream));
+    VG_CUDA(cudaMemcpyAsync(bytes.data() + A.n, A.rd[1].p, A.n * 4, cudaMemcpyDeviceToHost,
+                            S->stream));
+    VG_CUDA(cudaStreamSynchronize(S->stream));
+    uint64_t rcount = 0;
+    for (uint64_t i = 0; i < A.n; i++) rcount += bytes[i] == 2;
+    r.summary = A.n ? (double)rcount / (double)A.n : 0.0;
+  } else {
+    bytes.resize(A.n * 8);
+    VG_CUDA(cudaMemcpyAsync(bytes.data(), A.rd[0].p, A.n * 8, cudaMemcpyDeviceToHost, S->stream));
+    VG_CUDA(cudaStreamSynchronize(S->stream));
+    double m = 0;
+    const double *x = (const double *)bytes.data();
+    for (uint64_t i = 0; i < A.n; i++) m += x[i];
+    r.summary = A.n ? m / (double)A.n : 0.0;
+  }
+  r.checksum = fnv1a(bytes.data(), bytes.size());
+  if (J->spec.keep_state) J->final_state = std::move(bytes);
+  vg_sim_destroy(J->sim);
+  J->sim = nullptr;
+  J->ptab.release();
+  r.finish_s = now_s(S->t0);
+  J->finish = r.finish_s;
+}
+
+// one transition of every resident job
+void tick(vg_server *S) {
+  cudaStream_t st = S->stream;
+  std::vector<SirJobDesc> sj;
+  std::vector<SirTile> stiles;
+  std::vector<OpinionJob> oj;
+  std::vector<Job *> sir_jobs, op_jobs;
+  std::vector<Job *> stepping;
+  for (Job *J : S->active)
+    if (J->done_steps < J->spec.steps) stepping.push_back(J);
+  for (Job *J : stepping) {
+    Sim &s = *J->sim->s;
+    if (J->spec.model == 0) {
+      int T = S->sir_person;
+      AgentStore &A = s.agents[T - 1];
+      CSR &c = s.edges[S->sir_contact].csr[T];
+      SirJobDesc d{};
+      d.rp = c.row_ptr.as<uint32_t>();
+      d.src = c.src.as<uint32_t>();
+      d.st_rd = A.rd[0].as<uint8_t>();
+      d.d_rd = A.rd[1].as<int32_t>();
+      d.st_wr = A.wr[0].as<uint8_t>();
+      d.d_wr = A.wr[1].as<int32_t>();
+      d.n = A.n;
+      d.nrows = c.nrows;
+      d.ptab = J->ptab.as<double>();
+      d.ptab_n = J->ptab_n;
+      d.step = (uint32_t)s.num_transitions;
+      d.seed = J->spec.seed;
+      d.recovery = J->spec.recovery;
+      uint32_t ji = (uint32_t)sj.size();
+      sj.push_back(d);
+      for (uint64_t a = 0; a < A.n; a += 256) stiles.push_back({ji, (uint32_t)a});
+      sir_jobs.push_back(J);
+    } else {
+      oj.push_back({&s, S->op_edge, S->op_agent, J->spec.eps, 0.5, 0.5, 256});
+      op_jobs.push_back(J);
+    }
+  }
+  if (!stiles.empty()) {
+    if (S->sir_jobs_buf.bytes < sj.size() * sizeof(SirJobDesc))
+      S->sir_jobs_buf.alloc(sj.size() * sizeof(SirJobDesc) * 2, &S->footprint);
+    if (S->sir_tiles_buf.bytes < stiles.size() * sizeof(SirTile))
+      S->sir_tiles_buf.alloc(stiles.size() * sizeof(SirTile) * 2, &S->footprint);
+    VG_CUDA(cudaMemcpyAsync(S->sir_jobs_buf.p, sj.data(), sj.size() * sizeof(SirJobDesc),
+                            cudaMemcpyHostToDevice, st));
+    VG_CUDA(cudaMemcpyAsync(S->sir_tiles_buf.p, stiles.data(), stiles.size() * sizeof(SirTile),
+                            cudaMemcpyHostToDevice, st));
+    k_sir_jobs<<<(unsigned)stiles.size(), 256, 0, st>>>(
+        S->sir_jobs_buf.as<SirJobDesc>(), S->sir_tiles_buf.as<SirTile>(), S->status.as<int>());
+    VG_CUDA(cudaGetLastError());
+  }
+  if (!oj.empty()) launch_opinion_jobs(oj, st, S->op_args_buf, S->op_tiles_buf, &S->footprint);
+  VG_CUDA(cudaStreamSynchronize(st));
+  int h = 0;
+  VG_CUDA(cudaMemcpy(&h, S->status.p, 4, cudaMemcpyDeviceToHost));
+  if (h) fail(VG_ERR_DEVICE, "serving tick: device status " + std::to_string(h));
+  // finish of the transition of every job (as apply! for its immortal type)
+  for (Job *J : stepping) {
+    Sim &s = *J->sim->s;
+    int T = J->spec.model == 0 ? S->sir_person : S->op_agent;
+    std::swap(s.agents[T - 1].rd, s.agents[T - 1].wr);
+    s.num_transitions++;
+    J->done_steps++;
+  }
+  S->ticks++;
+  S->sim_steps += stepping.size();
+}
+
+void worker_loop(vg_server *S) {
+  try {
+    VG_CUDA(cudaSetDevice(0));
+    while (true) {
+      std::vector<Job *> admit;
+      {
+        std::unique_lock<std::mutex> lk(S->mu);
+        if (S->stop && S->queue.empty() && S->active.empty()) break;
+        while (!S->queue.empty()) {
+          Job *J = S->queue.front();
+          bool fits = S->used + J->est_bytes <= S->budget &&
+                      (int)(S->active.size() + admit.size()) < S->max_active;
+          bool alone = S->active.empty() && admit.empty();  // a lone job always runs
+          if (!fits && !alone) break;
+          S->queue.pop_front();
+          S->used += J->est_bytes;
+          admit.push_back(J);
+        }
+        if (admit.empty() && S->active.empty()) {
+          S->cv.wait_for(lk, std::chrono::milliseconds(2));
+          continue;
+        }
+      }
+      for (Job *J : admit) {
+        J->admit = now_s(S->t0);
+        build_job(S, J);
+        S->active.push_back(J);
+      }
+      tick(S);
+      std::vector<Job *> still, finished;
+      for (Job *J : S->active) (J->done_steps >= J->spec.steps ? finished : still).push_back(J);
+      for (Job *J : finished) retire_job(S, J);
+      {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->active.swap(still);
+        for (Job *J : finished) {
+          S->used -= J->est_bytes;
+          S->done.push_back(J);
+        }
+      }
+    }
+  } catch (const Error &e) {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->error = e.msg;
+    S->stop = true;
+  }
+}
+
+}  // namespace
+
+#define API_BEGIN try {
+#define API_END                     \
+  return VG_OK;                     \
+  }                                 \
+  catch (const Error &e) {          \
+    set_last_error(e.msg);          \
+    return e.code;                  \
+  }                                 \
+  catch (const std::exception &e) { \
+    set_last_error(e.what());       \
+    return VG_ERR_ARG;              \
+  }
+
+extern "C" {
+
+int vg_serve_create(uint64_t budget_bytes, int max_active, vg_server **out) {
+  API_BEGIN
+  auto S = std::make_unique<vg_server>();
+  S->budget = budget_bytes;
+  S->max_active = max_active > 0 ? max_active : 1 << 20;
+  VG_CUDA(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
+  int rc;
+  if ((rc = vg_model_create(&S->sir_model))) fail(rc, vg_last_error());
+  const char *pf[2] = {"state", "days"};
+  int pd[2] = {VG_U8, VG_I32};
+  if ((rc = vg_model_register_agenttype(S->sir_model, "Person", 2, pf, pd, VG_HINT_IMMORTAL,
+                                         &S->sir_person)) ||
+      (rc = vg_model_register_edgetype(S->sir_model, "Contact", 0, nullptr, nullptr,
+                                        VG_HINT_STATELESS, S->sir_person, 0, &S->sir_contact)) ||
+      (rc = vg_model_finalize(S->sir_model, "SIR")))
+    fail(rc, vg_last_error());
+  if ((rc = vg_model_create(&S->op_model))) fail(rc, vg_last_error());
+  const char *of[1] = {"x"};
+  int od[1] = {VG_F64};
+  const char *wf[1] = {"w"};
+  if ((rc = vg_model_register_agenttype(S->op_model, "Opinion", 1, of, od, VG_HINT_IMMORTAL,
+                                         &S->op_agent)) ||
+      (rc = vg_model_register_edgetype(S->op_model, "Weight", 1, wf, od, 0, S->op_agent, 0,
+                                        &S->op_edge)) ||
+      (rc = vg_model_finalize(S->op_model, "Opinion")))
+    fail(rc, vg_last_error());
+  S->status.alloc(16, &S->footprint);
+  VG_CUDA(cudaMemset(S->status.p, 0, 16));
+  vg_server *raw = S.release();
+  raw->worker = std::thread(worker_loop, raw);
+  *out = raw;
+  API_END
+}
+
+int vg_serve_submit(vg_server *S, const vg_job_spec *spec, int64_t *id_out) {
+  API_BEGIN
+  if (!S) fail(VG_ERR_ARG, "null server");
+  if (spec->model != 0 && spec->model != 1) fail(VG_ERR_ARG, "job model 0 (SIR) or 1 (opinion)");
+  if (spec->n < 2 || spec->steps < 0) fail(VG_ERR_ARG, "job size");
+  Job *J = new Job();
+  J->spec = *spec;
+  if (J->spec.model == 1 && J->spec.wmax <= 0) J->spec.wmax = 1e4;
+  J->est_bytes = estimate_bytes(J->spec);
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (!S->error.empty()) {
+      delete J;
+      fail(VG_ERR_STATE, "server stopped: " + S->error);
+    }
+    J->id = S->next_id++;
+    J->arrival = now_s(S->t0);
+    S->queue.push_back(J);
+  }
+  S->cv.notify_one();
+  if (id_out) *id_out = J->id;
+  API_END
+}
+
+// finished jobs since the last poll (at most cap); *n_out = number written
+int vg_serve_poll(vg_server *S, vg_job_result *out, uint64_t cap, uint64_t *n_out) {
+  API_BEGIN
+  std::lock_guard<std::mutex> lk(S->mu);
+  if (!S->error.empty()) fail(VG_ERR_DEVICE, "server stopped: " + S->error);
+  uint64_t k = 0;
+  for (Job *J : S->done) {
+    if (J->result.id == 0) continue;  // already reported
+    if (k >= cap) break;
+    out[k++] = J->result;
+    J->result.id = 0;
+  }
+  *n_out = k;
+  API_END
+}
+
+// the final state bytes of a finished job submitted with keep_state
+int vg_serve_job_state(vg_server *S, int64_t id, void *out, uint64_t cap, uint64_t *n_out) {
+  API_BEGIN
+  std::lock_guard<std::mutex> lk(S->mu);
+  for (Job *J : S->done)
+    if (J->id == id) {
+      *n_out = J->final_state.size();
+      if (out) std::memcpy(out, J->final_state.data(), std::min<uint64_t>(cap, J->final_state.size()));
+      return VG_OK;
+    }
+  fail(VG_ERR_ARG, "no finished job with this id");
+  API_END
+}
+
+int vg_serve_stats(vg_server *S, uint64_t *queued, uint64_t *active, uint64_t *done,
+                   uint64_t *ticks, uint64_t *sim_steps, uint64_t *bytes_in_use) {
+  API_BEGIN
+  std::lock_guard<std::mutex> lk(S->mu);
+  if (queued) *queued = S->queue.size();
+  if (active) *active = S->active.size();
+  if (done) *done = S->done.size();
+  if (ticks) *ticks = S->ticks;
+  if (sim_steps) *sim_steps = S->sim_steps;
+  if (bytes_in_use) *bytes_in_use = S->used;
+  API_END
+}
+
+// stop accepting, finish every queued and resident job, join the worker
+int vg_serve_drain(vg_server *S) {
+  API_BEGIN
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->stop = true;
+  }
+  S->cv.notify_one();
+  if (S->worker.joinable()) S->worker.join();
+  if (!S->error.empty()) fail(VG_ERR_DEVICE, "server stopped: " + S->error);
+  API_END
+}
+
+int vg_serve_destroy(vg_server *S) {
+  API_BEGIN
+  if (!S) return VG_OK;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->stop = true;
+  }
+  S->cv.notify_one();
+  if (S->worker.joinable()) S->worker.join();
+  for (Job *J : S->queue) delete J;
+  for (Job *J : S->active) {
+    if (J->sim) vg_sim_destroy(J->sim);
+    delete J;
+  }
+  for (Job *J : S->done) delete J;
+  vg_model_destroy(S->sir_model);
+  vg_model_destroy(S->op_model);
+  cudaStream_t st = S->stream;
+  delete S;
+  cudaStreamDestroy(st);
+  API_END
+}
+
+}  // extern "C"

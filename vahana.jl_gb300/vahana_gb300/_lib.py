@@ -141,6 +141,13 @@ SIGNATURES = {
     "vg_batch_destroy": (I, [P]),
     "vg_batch_read_states2": (I, [P, I, I, C.POINTER(C.c_uint8), C.POINTER(C.c_int32), U64, PU64]),
     "vg_batch_info": (I, [P, PU64, PU64, PI, PI, PU64]),
+    "vg_serve_create": (I, [U64, I, C.POINTER(P)]),
+    "vg_serve_submit": (I, [P, P, PI64]),
+    "vg_serve_poll": (I, [P, P, U64, PU64]),
+    "vg_serve_job_state": (I, [P, I64, P, U64, PU64]),
+    "vg_serve_stats": (I, [P, PU64, PU64, PU64, PU64, PU64, PU64]),
+    "vg_serve_drain": (I, [P]),
+    "vg_serve_destroy": (I, [P]),
 }
 
 
