@@ -824,3 +824,75 @@ def tr_readd_edges(E):
             add_edges(sim, id, list(es), E)
         return state
     return f
+
+
+def tr_spawn(offsets, E=None):
+    """add_agent! inside a transition (src/AgentMethods.jl:37-89): the agent
+    keeps its state and adds one agent per offset, a copy of its state with
+    field 0 increased by the offset; with E, after each add_agent! the edges
+    new -> caller and caller -> new whose field 0 is the new agent's id
+    (test/independent.jl:167-180)."""
+    def f(state, id, sim):
+        T = sim.tname(type_nr(id))
+        fields = sim.m.atypes[sim.tnr(T) - 1]["fields"]
+        for off in offsets:
+            new = dict(state)
+            if fields:
+                new[fields[0]] = new[fields[0]] + off
+            nid = add_agent(sim, T, new)
+            if E is not None:
+                ef = sim.m.etypes[E]["fields"]
+                st = {ef[0]: nid} if ef else None
+                add_edge(sim, nid, id, E, st)
+                add_edge(sim, id, nid, E, dict(st) if st else None)
+        return state
+    return f
+
+
+def tr_link_neighbors(E, F, die_value=None):
+    """test/independent.jl:66-78: field 0 == die_value returns nothing;
+    otherwise for every source of the in-edges of E, in insertion order,
+    add_edge!(nid, id, F(foo)) and add_edge!(id, nid, F(foo))."""
+    def f(state, id, sim):
+        T = sim.tname(type_nr(id))
+        fields = sim.m.atypes[sim.tnr(T) - 1]["fields"]
+        v = state[fields[0]] if fields else 0
+        if die_value is not None and fields and v == die_value:
+            return None
+        ef = sim.m.etypes[F]["fields"]
+        for nid in neighborids(sim, id, E) or []:
+            add_edge(sim, nid, id, F, {ef[0]: v} if ef else None)
+            add_edge(sim, id, nid, F, {ef[0]: v} if ef else None)
+        return state
+    return f
+
+
+
+def _field_test(kind, arg, v):
+    if kind == 0:
+        return True
+    if kind == 1:
+        return v >= arg
+    return v % int(arg) != 0
+
+
+def tr_remove_edges(E, kind, arg, mode):
+    """remove_edges! inside a transition (src/EdgeMethods.jl:527-599): the
+    agent keeps its state; mode 0: if its field 0 passes the test it calls
+    remove_edges!(sim, id, E); mode 1: for every source nid of its in-edges
+    of E (read container, insertion order) whose field 0 passes the test it
+    calls remove_edges!(sim, nid, id, E)."""
+    def f(state, id, sim):
+        T = sim.tname(type_nr(id))
+        fields = sim.m.atypes[sim.tnr(T) - 1]["fields"]
+        if mode == 0:
+            if not fields or _field_test(kind, arg, state[fields[0]]):
+                remove_edges(sim, id, E)
+            return state
+        for nid in neighborids(sim, id, E) or []:
+            src = agentstate_flexible(sim, nid)
+            sf = sim.m.atypes[type_nr(nid) - 1]["fields"]
+            if _field_test(kind, arg, src[sf[0]]):
+                remove_edges(sim, id, E, frm=nid)
+        return state
+    return f

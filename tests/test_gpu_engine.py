@@ -2,8 +2,8 @@
 
 Each test ports a scenario of the reference's test suite (cited) onto the
 product's API with the library's named transitions, and checks the values
-the reference asserts; the last test runs random transition sequences on
-the GPU and on the oracle and compares every state and edge.
+the reference asserts; where the reference only compares runs with each
+other, the GPU run is compared with the oracle's sequential sweep.
 """
 import functools
 import operator
@@ -534,3 +534,92 @@ def test_add_existing(vh):
     with pytest.raises(AssertionError):
         vh.apply_(sim, "keep", ["ComputeAgent"], [], ["ConstructedAgent", "Connection"])
     sim.close()
+
+
+# ------------------------------------------------------ test/independent.jl
+def _snapshot_product(vh, sim, T, E_ids, E_pl):
+    vh.disable_transition_checks(sim, True)
+    ids = [int(i) for i in vh.all_agentids(sim, T)]
+    states = [vh.agentstate(sim, i, T)["foo"] for i in ids]
+    nb = [[int(x) for x in (vh.neighborids(sim, i, E_ids) or [])] for i in ids]
+    es = [[(int(e.frm), e.state["foo"]) for e in (vh.edges(sim, i, E_pl) or [])] for i in ids]
+    vh.disable_transition_checks(sim, False)
+    return ids, states, nb, es
+
+
+def _snapshot_oracle(R, sim, T, E_ids, E_pl):
+    R.disable_transition_checks(sim, True)
+    ids = [int(i) for i in R.all_agentids(sim, T)]
+    states = [R.agentstate(sim, i, T)["foo"] for i in ids]
+    nb = [[int(x) for x in (R.neighborids(sim, i, E_ids) or [])] for i in ids]
+    es = [[(int(e.frm), e.state["foo"]) for e in (R.edges(sim, i, E_pl) or [])] for i in ids]
+    R.disable_transition_checks(sim, False)
+    return ids, states, nb, es
+
+
+@pytest.mark.parametrize("T,hints", [("AIndependent", [":Independent"]),
+                                     ("ANotIndependent", []),
+                                     ("AIndependentImmortal", [":Independent"])])
+def test_independent_add_agent_in_transition(vh, T, hints):
+    """test/independent.jl:32-216: agents die (foo == 1, then foo == 2) while
+    the others link to and from their neighbours; then every agent calls
+    add_agent! twice inside the transition (states foo + 10 and foo + 20,
+    died slots reused LIFO, then fresh numbers) and links each new agent in
+    both directions with the new id as edge state (add_existing).  Counts
+    are those the reference test compares across the three hint variants;
+    the ids, states and edge lists equal the oracle's sequential sweep."""
+    from oracle import vahana_ref as R
+    results = []
+    for eng in ("product", "oracle"):
+        M = vh if eng == "product" else R
+        m = (M.ModelTypes().register_agenttype(T, [("foo", "i64")], *hints)
+             .register_edgetype("AFooEdge", [("foo", "i64")]).register_edgetype("AEdge", [])
+             .create_model("Test Independent"))
+        sim = M.create_simulation(m)
+        if eng == "product":
+            ids = list(vh.add_agents(sim, T, 10, foo=np.arange(1, 11)))
+            frm = [a for a in ids for _ in ids]
+            to = [b for _ in ids for b in ids]
+            vh.add_edges(sim, "AEdge", frm, to)
+        else:
+            ids = [R.add_agent(sim, T, {"foo": i}) for i in range(1, 11)]
+            for a in ids:
+                for b in ids:
+                    R.add_edge(sim, a, b, "AEdge")
+        M.finish_init(sim)
+        counts = []
+
+        def step(kind, arg):
+            if eng == "product":
+                ei, ef = m["AEdge"].index, m["AFooEdge"].index
+                if kind == "link":
+                    vh.apply_(sim, "link_neighbors", T, [T, "AEdge"], [T, "AFooEdge"],
+                              params=[ei, ef, arg])
+                else:
+                    vh.apply_(sim, "spawn", T, [T, "AEdge"], [T, "AFooEdge"],
+                              add_existing="AFooEdge", params=[2, 10, 20, ef])
+                counts.append((vh.num_agents(sim, T), vh.num_edges(sim, "AEdge"),
+                               vh.num_edges(sim, "AFooEdge")))
+            else:
+                if kind == "link":
+                    R.apply_(sim, R.tr_link_neighbors("AEdge", "AFooEdge", arg), T,
+                             [T, "AEdge"], [T, "AFooEdge"])
+                else:
+                    R.apply_(sim, R.tr_spawn([10, 20], "AFooEdge"), T, [T, "AEdge"],
+                             [T, "AFooEdge"], add_existing="AFooEdge")
+                counts.append((R.num_agents(sim, T), R.num_edges_total(sim, "AEdge"),
+                               R.num_edges_total(sim, "AFooEdge")))
+        step("link", 1)
+        step("link", 2)
+        step("spawn", None)
+        snap = (_snapshot_product(vh, sim, T, "AEdge", "AFooEdge") if eng == "product"
+                else _snapshot_oracle(R, sim, T, "AEdge", "AFooEdge"))
+        results.append((counts, snap))
+        if eng == "product":
+            sim.close()
+    (c_p, s_p), (c_o, s_o) = results
+    assert c_p == c_o == [(9, 81, 162), (8, 64, 128), (24, 64, 160)]
+    assert s_p[0] == s_o[0]  # ids: died slots 2 and 1 reused first, then 11..
+    assert s_p[1] == s_o[1]
+    assert s_p[2] == s_o[2]
+    assert s_p[3] == s_o[3]

@@ -50,6 +50,25 @@ EdgeAppend *ApplyCtx::append_for(int e, uint64_t capacity, bool ordered) {
   return appends.back().get();
 }
 
+EdgeRemoval *ApplyCtx::removal_for(int e, uint64_t capacity) {
+  for (auto &r : removals)
+    if (r->edge_type == e) {
+      if (r->cap < capacity) fail(VG_ERR_ARG, "removal buffer sized by the first call type");
+      return r.get();
+    }
+  Sim &s = *sim;
+  auto r = std::make_unique<EdgeRemoval>();
+  r->edge_type = e;
+  r->cap = std::max<uint64_t>(capacity, 1);
+  r->to.alloc(r->cap * 8, &s.footprint);
+  r->from.alloc(r->cap * 8, &s.footprint);
+  r->key.alloc(r->cap * 8, &s.footprint);
+  r->counter.alloc(8, &s.footprint);
+  VG_CUDA(cudaMemsetAsync(r->counter.p, 0, 8, s.stream));
+  removals.push_back(std::move(r));
+  return removals.back().get();
+}
+
 namespace {
 
 constexpr int TPB = 256;
@@ -491,10 +510,12 @@ int vg_apply(vg_sim *h, const char *tname, const int *call, int ncall, const int
       }
       if (n > ap->cap) fail(VG_ERR_DEVICE, "edge append buffer overflow");
     }
+    bool merge = s.edges[e].add_existing;
+    for (auto &r : ctx.removals)
+      if (r->edge_type == e) apply_edge_removals(s, e, *r, ap, n, merge);
     std::vector<const void *> pl;
     if (ap)
       for (auto &b : ap->payload) pl.push_back(b.p);
-    bool merge = s.edges[e].add_existing;
     build_csr_from_records(s, e, ap ? ap->from.as<uint64_t>() : nullptr,
                            ap ? ap->to.as<uint64_t>() : nullptr, pl, n,
                            ap ? ap->ordered : true, ap ? ap->key.as<uint64_t>() : nullptr,
@@ -506,6 +527,7 @@ int vg_apply(vg_sim *h, const char *tname, const int *call, int ncall, const int
     remove_died_edges(s, T, a.died_rd.as<uint8_t>(), a.n);
   }
   ctx.appends.clear();
+  ctx.removals.clear();
   s.num_transitions++;
   API_END
 }

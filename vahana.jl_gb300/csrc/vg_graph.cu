@@ -404,6 +404,41 @@ void build_csr_from_records(Sim &s, int e, const uint64_t *d_from,
   VG_CUDA(cudaStreamSynchronize(st));
 }
 
+// Replace c by its edges with keep[k] = 1 (scan = exclusive scan of keep,
+// newtotal = kept edges), rows and order unchanged.
+static void compact_csr(Sim &s, const EdgeTypeDesc &ed, CSR &c, const uint32_t *keep,
+                        const uint32_t *scan, uint32_t newtotal) {
+  cudaStream_t st = s.stream;
+  uint64_t ne = c.nedges;
+  CSR n2;
+  n2.nrows = c.nrows;
+  n2.nedges = newtotal;
+  n2.src_type_const = c.src_type_const;
+  n2.row_ptr.alloc((c.nrows + 1) * 4, &s.footprint);
+  k_new_rowptr<<<nblk(c.nrows + 1), TPB, 0, st>>>(c.row_ptr.as<uint32_t>(), c.nrows, scan,
+                                                  n2.row_ptr.as<uint32_t>());
+  Tmp<uint32_t> dest(ne, st);
+  k_compact_dest<<<nblk(ne), TPB, 0, st>>>(keep, scan, ne, dest.p);
+  uint64_t alloc_n = std::max<uint64_t>(newtotal, 1);
+  if (c.src.p) {
+    n2.src.alloc(alloc_n * 4, &s.footprint);
+    scatter_column(4, c.src.p, nullptr, dest.p, ne, n2.src.p, st);
+  }
+  if (c.src_type.p) {
+    n2.src_type.alloc(alloc_n, &s.footprint);
+    scatter_column(1, c.src_type.p, nullptr, dest.p, ne, n2.src_type.p, st);
+  }
+  n2.payload.resize(c.payload.size());
+  for (size_t f = 0; f < c.payload.size(); f++) {
+    n2.payload[f].alloc(alloc_n * ed.fields[f].size, &s.footprint);
+    scatter_column(ed.fields[f].size, c.payload[f].p, nullptr, dest.p, ne, n2.payload[f].p, st);
+  }
+  n2.max_degree = c.max_degree;
+  VG_CUDA(cudaGetLastError());
+  VG_CUDA(cudaStreamSynchronize(st));
+  c = std::move(n2);
+}
+
 void remove_died_edges(Sim &s, int died_type, const uint8_t *died,
                        uint64_t died_n) {
   cudaStream_t st = s.stream;
@@ -430,91 +465,294 @@ void remove_died_edges(Sim &s, int died_type, const uint8_t *died,
       VG_CUDA(cudaMemcpyAsync(&newtotal, scan.p + ne, 4, cudaMemcpyDeviceToHost, st));
       VG_CUDA(cudaStreamSynchronize(st));
       if (newtotal == ne) continue;
-      CSR n2;
-      n2.nrows = c.nrows;
-      n2.nedges = newtotal;
-      n2.src_type_const = c.src_type_const;
-      n2.row_ptr.alloc((c.nrows + 1) * 4, &s.footprint);
-      k_new_rowptr<<<nblk(c.nrows + 1), TPB, 0, st>>>(c.row_ptr.as<uint32_t>(), c.nrows,
-                                                      scan.p, n2.row_ptr.as<uint32_t>());
-      Tmp<uint32_t> dest(ne, st);
-      k_compact_dest<<<nblk(ne), TPB, 0, st>>>(keep.p, scan.p, ne, dest.p);
-      uint64_t alloc_n = std::max<uint64_t>(newtotal, 1);
-      if (c.src.p) {
-        n2.src.alloc(alloc_n * 4, &s.footprint);
-        scatter_column(4, c.src.p, nullptr, dest.p, ne, n2.src.p, st);
-      }
-      if (c.src_type.p) {
-        n2.src_type.alloc(alloc_n, &s.footprint);
-        scatter_column(1, c.src_type.p, nullptr, dest.p, ne, n2.src_type.p, st);
-      }
-      n2.payload.resize(c.payload.size());
-      for (size_t f = 0; f < c.payload.size(); f++) {
-        n2.payload[f].alloc(alloc_n * ed.fields[f].size, &s.footprint);
-        scatter_column(ed.fields[f].size, c.payload[f].p, nullptr, dest.p, ne,
-                       n2.payload[f].p, st);
-      }
-      n2.max_degree = c.max_degree;
-      VG_CUDA(cudaStreamSynchronize(st));
-      c = std::move(n2);
+      compact_csr(s, ed, c, keep.p, scan.p, newtotal);
     }
   }
 }
 
 namespace {
-// schedule keys: hub rows first by descending degree (top bit 0), then the
-// other rows window by window, by descending degree inside a window
-__global__ void k_schedule_keys(const uint32_t *rp, uint64_t nrows, uint64_t n, uint32_t thr,
-                                uint32_t wshift, uint32_t *keys, uint32_t *vals,
-                                unsigned long long *nhub) {
+// remove_edges! records sorted by (to, from); from = REMOVE_ALL sorts last
+struct RemovalTable {
+  const uint64_t *to, *from, *key;
+  uint64_t n;
+};
+
+__device__ uint64_t removal_key(const RemovalTable &R, uint64_t to, uint64_t from) {
+  uint64_t lo = 0, hi = R.n;
+  while (lo < hi) {
+    uint64_t mid = (lo + hi) >> 1;
+    if (R.to[mid] < to || (R.to[mid] == to && R.from[mid] < from)) lo = mid + 1;
+    else hi = mid;
+  }
+  uint64_t mx = 0;
+  for (uint64_t k = lo; k < R.n && R.to[k] == to && R.from[k] == from; k++)
+    mx = R.key[k] > mx ? R.key[k] : mx;
+  return mx;
+}
+
+// an edge (to, from) added with key k is gone when a later removal hit it
+__device__ __forceinline__ bool removed_edge(const RemovalTable &R, uint64_t to, uint64_t from,
+                                             uint64_t k, bool has_from) {
+  if (removal_key(R, to, REMOVE_ALL) > k) return true;
+  return has_from && removal_key(R, to, from) > k;
+}
+
+__global__ void k_removal_keep_old(const uint32_t *rp, uint64_t nrows, const uint32_t *src,
+                                   const uint8_t *src_type, int src_type_const, int target_type,
+                                   RemovalTable R, uint32_t *keep) {
+  uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  const uint64_t to = ((uint64_t)target_type << SHIFT_TYPE) | (r + 1);
+  for (uint32_t k = rp[r]; k < rp[r + 1]; k++) {
+    uint64_t from = REMOVE_ALL;
+    if (src) {
+      int ty = src_type ? (int)src_type[k] : src_type_const;
+      from = ((uint64_t)ty << SHIFT_TYPE) | ((uint64_t)src[k] + 1);
+    }
+    keep[k] = removed_edge(R, to, from, 0, src != nullptr) ? 0u : 1u;
+  }
+}
+
+__global__ void k_removal_keep_new(const uint64_t *to, const uint64_t *from, const uint64_t *key,
+                                   uint64_t n, int has_from, RemovalTable R, uint32_t *keep) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  keep[i] = removed_edge(R, to[i], from[i], key[i] + 1, has_from != 0) ? 0u : 1u;
+}
+
+__global__ void k_gather_u64(const uint64_t *in, const uint32_t *perm, uint64_t n, uint64_t *out) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = in[perm[i]];
+}
+}  // namespace
+
+void apply_edge_removals(Sim &s, int e, EdgeRemoval &rm, EdgeAppend *ap, uint64_t &n_records,
+                         bool merge_existing) {
+  cudaStream_t st = s.stream;
+  const EdgeTypeDesc &ed = s.model->et(e);
+  EdgeStore &es = s.edges[e];
+  uint64_t r = 0;
+  VG_CUDA(cudaMemcpyAsync(&r, rm.counter.p, 8, cudaMemcpyDeviceToHost, st));
+  VG_CUDA(cudaStreamSynchronize(st));
+  if (r > rm.cap) fail(VG_ERR_DEVICE, "remove_edges! record buffer overflow");
+  if (r == 0) return;
+  if (r >= (1ull << 31)) fail(VG_ERR_NOMEM, "more than 2^31 remove_edges! calls in one apply!");
+  // the table sorted by (to, from): stable LSD passes, from first
+  Tmp<uint32_t> perm(r, st);
+  k_iota<<<nblk(r), TPB, 0, st>>>(perm.p, r);
+  Tmp<uint64_t> k1(r, st), tto(r, st), tfrom(r, st), tkey(r, st);
+  k_copy_u64<<<nblk(r), TPB, 0, st>>>(rm.from.as<uint64_t>(), k1.p, r);
+  radix_sort_pairs_u64(k1.p, perm.p, r, 64, st, s);
+  k_gather_u64<<<nblk(r), TPB, 0, st>>>(rm.to.as<uint64_t>(), perm.p, r, tto.p);
+  radix_sort_pairs_u64(tto.p, perm.p, r, 64, st, s);
+  k_gather_u64<<<nblk(r), TPB, 0, st>>>(rm.from.as<uint64_t>(), perm.p, r, tfrom.p);
+  k_gather_u64<<<nblk(r), TPB, 0, st>>>(rm.key.as<uint64_t>(), perm.p, r, tkey.p);
+  VG_CUDA(cudaGetLastError());
+  RemovalTable R{tto.p, tfrom.p, tkey.p, r};
+  // the old edges that add_existing carries over
+  if (merge_existing) {
+    for (int T = 1; T < (int)es.csr.size(); T++) {
+      CSR &c = es.csr[T];
+      if (c.nedges == 0 || !c.row_ptr.p) continue;
+      uint64_t ne = c.nedges;
+      Tmp<uint32_t> keep(ne + 1, st), scan(ne + 1, st);
+      VG_CUDA(cudaMemsetAsync(keep.p + ne, 0, 4, st));
+      k_removal_keep_old<<<nblk(c.nrows), TPB, 0, st>>>(
+          c.row_ptr.as<uint32_t>(), c.nrows, ed.stores_src() ? c.src.as<uint32_t>() : nullptr,
+          c.src_type.as<uint8_t>(), c.src_type_const, T, R, keep.p);
+      exclusive_scan_u32(keep.p, scan.p, ne + 1, st, s);
+      uint32_t newtotal = 0;
+      VG_CUDA(cudaMemcpyAsync(&newtotal, scan.p + ne, 4, cudaMemcpyDeviceToHost, st));
+      VG_CUDA(cudaStreamSynchronize(st));
+      if (newtotal != ne) compact_csr(s, ed, c, keep.p, scan.p, newtotal);
+    }
+  }
+  // the edges appended in this transition
+  if (ap && n_records > 0) {
+    if (ap->key.p == nullptr)
+      fail(VG_ERR_ARG, "remove_edges! with edges appended in a fixed order is not supported");
+    uint64_t n = n_records;
+    Tmp<uint32_t> keep(n + 1, st), scan(n + 1, st);
+    VG_CUDA(cudaMemsetAsync(keep.p + n, 0, 4, st));
+    k_removal_keep_new<<<nblk(n), TPB, 0, st>>>(ap->to.as<uint64_t>(), ap->from.as<uint64_t>(),
+                                                ap->key.as<uint64_t>(), n,
+                                                ed.stores_src() ? 1 : 0, R, keep.p);
+    exclusive_scan_u32(keep.p, scan.p, n + 1, st, s);
+    uint32_t kept = 0;
+    VG_CUDA(cudaMemcpyAsync(&kept, scan.p + n, 4, cudaMemcpyDeviceToHost, st));
+    VG_CUDA(cudaStreamSynchronize(st));
+    if (kept != n) {
+      Tmp<uint32_t> dest(n, st);
+      k_compact_dest<<<nblk(n), TPB, 0, st>>>(keep.p, scan.p, n, dest.p);
+      auto squeeze = [&](DevBuf &b, int esz) {
+        DevBuf nb;
+        nb.alloc(std::max<uint64_t>(kept, 1) * esz, &s.footprint);
+        scatter_column(esz, b.p, nullptr, dest.p, n, nb.p, st);
+        b = std::move(nb);
+      };
+      squeeze(ap->to, 8);
+      squeeze(ap->from, 8);
+      squeeze(ap->key, 8);
+      for (size_t f = 0; f < ap->payload.size(); f++) squeeze(ap->payload[f], ed.fields[f].size);
+      ap->cap = std::max<uint64_t>(kept, 1);
+      VG_CUDA(cudaGetLastError());
+      VG_CUDA(cudaStreamSynchronize(st));
+      n_records = kept;
+    }
+  }
+}
+
+namespace {
+__device__ __forceinline__ uint32_t row_degree(const uint32_t *rp, uint64_t nrows, uint64_t r) {
+  return r < nrows ? rp[r + 1] - rp[r] : 0u;
+}
+
+// flag rows with lo < degree <= hi
+__global__ void k_flag_degree(const uint32_t *rp, uint64_t nrows, uint64_t n, uint32_t lo,
+                              uint32_t hi, uint32_t *flag) {
   uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n) return;
-  uint32_t d = r < nrows ? rp[r + 1] - rp[r] : 0;
-  uint32_t key;
-  if (d > thr) {
-    key = 0x7FFFFFFFu - min(d, 0x7FFFFFFFu);
-    atomicAdd(nhub, 1ull);
-  } else {
-    key = 0x80000000u | ((uint32_t)(r >> wshift) << 16) | (0xFFFFu - min(d, 0xFFFFu));
-  }
-  keys[r] = key;
+  uint32_t d = row_degree(rp, nrows, r);
+  flag[r] = (d > lo && d <= hi) ? 1u : 0u;
+}
+
+__global__ void k_compact_rows(const uint32_t *flag, const uint32_t *pos, uint64_t n,
+                               uint32_t *rows) {
+  uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < n && flag[r]) rows[pos[r]] = (uint32_t)r;
+}
+
+// sort key of a hub row: descending degree
+__global__ void k_hub_keys(const uint32_t *rp, const uint32_t *rows, uint64_t m, uint32_t *keys) {
+  uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < m) keys[k] = 0xFFFFFFFFu - (rp[rows[k] + 1] - rp[rows[k]]);
+}
+
+// order keys: rows with degree <= cap by window, then descending degree
+// (stable sort: ties by index); the others sort last
+__global__ void k_order_keys(const uint32_t *rp, uint64_t nrows, uint64_t n, uint32_t cap,
+                             uint32_t wshift, uint32_t *keys, uint32_t *vals) {
+  uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  uint32_t d = row_degree(rp, nrows, r);
+  keys[r] = d > cap ? 0xFFFFFFFFu : (((uint32_t)(r >> wshift) << 16) | (0xFFFFu - min(d, 0xFFFFu)));
   vals[r] = (uint32_t)r;
+}
+
+
+
+
+// largest degree of each slice of 32 order positions
+__global__ void k_slice_deg(const uint32_t *rp, uint64_t nrows, const uint32_t *order, uint64_t m,
+                            uint64_t nslices, uint32_t *sdeg, uint64_t *slots) {
+  uint64_t sl = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (sl >= nslices) return;
+  uint32_t dm = 0;
+  for (uint64_t k = sl * 32; k < min(m, sl * 32 + 32); k++)
+    dm = max(dm, row_degree(rp, nrows, order[k]));
+  sdeg[sl] = dm;
+  slots[sl] = 32ull * dm;
+}
+
+// copy each row's edges into its slice, column-major; padding source 0,
+// weight 0
+__global__ void k_sell_fill(const uint32_t *rp, uint64_t nrows, const uint32_t *src,
+                            const double *w, const uint32_t *order, uint64_t m,
+                            const uint64_t *base, const uint32_t *sdeg, uint32_t *ssrc,
+                            double *sw) {
+  uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t nslices_pos = (m + 31) / 32 * 32;
+  if (k >= nslices_pos) return;
+  const uint64_t sl = k >> 5, lane = k & 31;
+  uint32_t b = 0, d = 0;
+  if (k < m) {
+    uint32_t r = order[k];
+    if (r < nrows) {
+      b = rp[r];
+      d = rp[r + 1] - b;
+    }
+  }
+  const uint64_t o = base[sl] + lane;
+  for (uint32_t q = 0; q < sdeg[sl]; q++) {
+    ssrc[o + 32ull * q] = q < d ? src[b + q] : 0u;
+    sw[o + 32ull * q] = q < d ? w[b + q] : 0.0;
+  }
+}
+
+// rows with lo < degree <= hi, in index order
+uint64_t select_rows(Sim &s, const CSR &c, uint64_t n, uint32_t lo, uint32_t hi, DevBuf &out) {
+  cudaStream_t st = s.stream;
+  Tmp<uint32_t> flag(n + 1, st), pos(n + 1, st);
+  VG_CUDA(cudaMemsetAsync(flag.p + n, 0, 4, st));
+  k_flag_degree<<<nblk(n), TPB, 0, st>>>(c.row_ptr.as<uint32_t>(), c.nrows, n, lo, hi, flag.p);
+  exclusive_scan_u32(flag.p, pos.p, n + 1, st, s);
+  uint32_t m = 0;
+  VG_CUDA(cudaMemcpyAsync(&m, pos.p + n, 4, cudaMemcpyDeviceToHost, st));
+  VG_CUDA(cudaStreamSynchronize(st));
+  if (m) {
+    out.alloc((uint64_t)m * 4, &s.footprint);
+    k_compact_rows<<<nblk(n), TPB, 0, st>>>(flag.p, pos.p, n, out.as<uint32_t>());
+    VG_CUDA(cudaGetLastError());
+  }
+  return m;
 }
 }  // namespace
 
 void ensure_schedule(Sim &s, CSR &c, uint32_t thr, uint64_t n) {
-  if (c.schedule_valid && c.hub_threshold == thr && c.nhub + c.norder == n) return;
+  if (c.schedule_valid && c.hub_threshold == thr && c.sched_n == n) return;
   cudaStream_t st = s.stream;
   c.hub_rows.release();
-  c.row_order.release();
-  c.nhub = c.norder = 0;
-  if (n > 0) {
-    // window of consecutive rows: 8192, or larger so that windows fit 15 bits
-    uint32_t wshift = 13;
-    while ((n >> wshift) >= (1ull << 15)) wshift++;
-    Tmp<unsigned long long> cnt(1, st);
-    VG_CUDA(cudaMemsetAsync(cnt.p, 0, 8, st));
-    DevBuf order;
-    order.alloc(n * 4, &s.footprint);
-    Tmp<uint32_t> keys(n, st);
-    k_schedule_keys<<<nblk(n), TPB, 0, st>>>(c.row_ptr.as<uint32_t>(), c.nrows, n, thr, wshift,
-                                             keys.p, order.as<uint32_t>(), cnt.p);
-    VG_CUDA(cudaGetLastError());
-    radix_sort_pairs_u32(keys.p, order.as<uint32_t>(), n, 32, st, s);
-    unsigned long long h = 0;
-    VG_CUDA(cudaMemcpyAsync(&h, cnt.p, 8, cudaMemcpyDeviceToHost, st));
-    VG_CUDA(cudaStreamSynchronize(st));
-    c.nhub = h;
-    c.norder = n - h;
-    if (h) {
-      c.hub_rows.alloc(h * 4, &s.footprint);
-      VG_CUDA(cudaMemcpyAsync(c.hub_rows.p, order.p, h * 4, cudaMemcpyDeviceToDevice, st));
+  c.order.release();
+  c.slice_base.release();
+  c.slice_deg.release();
+  c.sell_src.release();
+  c.sell_w.release();
+  c.nhub = c.norder = c.nslices = 0;
+  if (n > 0 && c.row_ptr.p) {
+    const uint32_t *rp = c.row_ptr.as<uint32_t>();
+    // hub rows by descending degree
+    c.nhub = select_rows(s, c, n, thr, 0xFFFFFFFFu, c.hub_rows);
+    if (c.nhub > 1) {
+      Tmp<uint32_t> keys(c.nhub, st);
+      k_hub_keys<<<nblk(c.nhub), TPB, 0, st>>>(rp, c.hub_rows.as<uint32_t>(), c.nhub, keys.p);
+      radix_sort_pairs_u32(keys.p, c.hub_rows.as<uint32_t>(), c.nhub, 32, st, s);
     }
-    c.row_order.alloc(std::max<uint64_t>(c.norder, 1) * 4, &s.footprint);
-    VG_CUDA(cudaMemcpyAsync(c.row_order.p, order.as<uint32_t>() + h, c.norder * 4,
-                            cudaMemcpyDeviceToDevice, st));
+    // the other rows by descending degree in windows of 2^16 rows (or
+    // more, so that the window number stays below the sentinel)
+    uint32_t wshift = 16;
+    while ((n >> wshift) >= 0xFFFFull) wshift++;
+    Tmp<uint32_t> keys(n, st);
+    c.order.alloc(n * 4, &s.footprint);
+    k_order_keys<<<nblk(n), TPB, 0, st>>>(rp, c.nrows, n, thr, wshift, keys.p,
+                                          c.order.as<uint32_t>());
+    radix_sort_pairs_u32(keys.p, c.order.as<uint32_t>(), n, 32, st, s);
+    const uint64_t m = n - c.nhub;
+    c.norder = m;
+    const uint64_t ns = (m + 31) / 32;
+    c.nslices = ns;
+    if (ns > 0) {
+      c.slice_deg.alloc(ns * 4, &s.footprint);
+      c.slice_base.alloc((ns + 1) * 8, &s.footprint);
+      Tmp<uint64_t> slots(ns + 1, st);
+      VG_CUDA(cudaMemsetAsync(slots.p + ns, 0, 8, st));
+      k_slice_deg<<<nblk(ns), TPB, 0, st>>>(rp, c.nrows, c.order.as<uint32_t>(), m, ns,
+                                            c.slice_deg.as<uint32_t>(), slots.p);
+      exclusive_scan_u64(slots.p, c.slice_base.as<uint64_t>(), ns + 1, st, s);
+      uint64_t total = 0;
+      VG_CUDA(cudaMemcpyAsync(&total, c.slice_base.as<uint64_t>() + ns, 8, cudaMemcpyDeviceToHost,
+                              st));
+      VG_CUDA(cudaStreamSynchronize(st));
+      c.sell_src.alloc(std::max<uint64_t>(total, 1) * 4, &s.footprint);
+      c.sell_w.alloc(std::max<uint64_t>(total, 1) * 8, &s.footprint);
+      k_sell_fill<<<nblk(ns * 32), TPB, 0, st>>>(
+          rp, c.nrows, c.src.as<uint32_t>(), c.payload[0].as<double>(), c.order.as<uint32_t>(), m,
+          c.slice_base.as<uint64_t>(), c.slice_deg.as<uint32_t>(), c.sell_src.as<uint32_t>(),
+          c.sell_w.as<double>());
+    }
+    VG_CUDA(cudaGetLastError());
     VG_CUDA(cudaStreamSynchronize(st));
   }
+  c.sched_n = n;
   c.hub_threshold = thr;
   c.schedule_valid = true;
 }

@@ -141,14 +141,24 @@ struct CSR {
   int src_type_const = 0;  // >0 all sources of that type, 0 none, -1 mixed
   std::vector<DevBuf> payload;
   uint32_t max_degree = 0;
-  // derived schedule of the degree-bucketed gather kernels (hub rows)
-  DevBuf hub_rows;  // u32 rows with degree above the hub threshold
+  // derived gather layout of the Float64 payload column 0 (built on first
+  // use by the gather kernels, cached until the CSR changes):
+  // hub rows (degree > hub threshold) by descending degree; the other rows
+  // (agents beyond the CSR's rows included) in `order`, by descending
+  // degree inside windows of 2^16 consecutive rows, cut into slices of 32;
+  // the edges of a slice stored column-major (SELL-C-sigma): edge k of the
+  // slice's lane l at slice_base + 32 k + l, padded to the slice's largest
+  // degree (padding: source 0, weight 0)
+  DevBuf hub_rows;  // u32
   uint64_t nhub = 0;
-  // the other rows (and the agents beyond nrows, degree 0) in windows of
-  // consecutive rows, sorted by descending degree inside each window, so
-  // that the rows of one warp have similar degrees
-  DevBuf row_order;
+  DevBuf order;     // u32 rows, position = 32 slice + lane
   uint64_t norder = 0;
+  DevBuf slice_base;  // u64 [nslices + 1]: first column-major slot of each slice
+  DevBuf slice_deg;   // u32 [nslices]: the slice's largest degree
+  uint64_t nslices = 0;
+  DevBuf sell_src;  // u32 [slots]
+  DevBuf sell_w;    // f64 [slots]
+  uint64_t sched_n = 0;  // agent count the layout covers
   uint32_t hub_threshold = 0;
   bool schedule_valid = false;
   // payload field 0 (Float64) holds only multiples of 2^-53 in (0, 1]:
@@ -259,6 +269,22 @@ struct EdgeAppend {
   uint64_t fixed_count = 0;  // when the count is known on the host
 };
 
+// remove_edges! calls recorded by a transition (src/EdgeMethods.jl:527-599):
+// (to, from, key); from = REMOVE_ALL for remove_edges!(sim, to, T).  At the
+// end of apply! a record of the written container (old edges kept by
+// add_existing: key 0; appended edges: order key + 1) is dropped when a
+// removal of its target (all sources, or its source) carries a larger key,
+// i.e. was called after the edge was added in the sequential sweep.
+constexpr uint64_t REMOVE_ALL = ~0ull;
+struct EdgeRemoval {
+  int edge_type = -1;
+  uint64_t cap = 0;
+  DevBuf to, from, key;
+  DevBuf counter;  // u64 device counter
+};
+void apply_edge_removals(Sim &s, int edge_type, EdgeRemoval &rm, EdgeAppend *ap,
+                         uint64_t &n_records, bool merge_existing);
+
 // Apply context handed to a transition launcher.
 struct ApplyCtx {
   Sim *sim;
@@ -278,6 +304,8 @@ struct ApplyCtx {
   // edge records appended by the launchers, per written edge type
   std::vector<std::unique_ptr<EdgeAppend>> appends;
   EdgeAppend *append_for(int edge_type, uint64_t capacity, bool ordered);
+  std::vector<std::unique_ptr<EdgeRemoval>> removals;
+  EdgeRemoval *removal_for(int edge_type, uint64_t capacity);
 };
 
 

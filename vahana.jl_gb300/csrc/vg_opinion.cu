@@ -55,10 +55,15 @@ struct OpinionArgs {
   const double *__restrict__ x;
   double *__restrict__ xo;
   uint64_t n, nrows;
-  const uint32_t *__restrict__ hub_rows;
+  const uint32_t *__restrict__ hub_rows;  // degree > hub_thr, split over a warp
   uint64_t nhub;
-  const uint32_t *__restrict__ order;  // non-hub rows, degree-sorted per window
+  const uint32_t *__restrict__ order;  // the other rows, degree-sorted windows
   uint64_t norder;
+  const uint64_t *__restrict__ slice_base;  // column-major slices of 32 rows
+  const uint32_t *__restrict__ slice_deg;
+  const uint32_t *__restrict__ sell_src;
+  const double *__restrict__ sell_w;
+  uint64_t nslices;
   uint32_t hub_thr;
   unsigned hub_blocks;
   double eps, a, b;
@@ -67,6 +72,36 @@ struct OpinionArgs {
 };
 
 __device__ __forceinline__ uint64_t bits(double v) { return (uint64_t)__double_as_longlong(v); }
+
+// L2 policies: the edge columns stream through once per step (evict first);
+// the opinions, gathered once per edge, should stay resident (evict last).
+__device__ __forceinline__ uint64_t policy_evict_first() {
+  uint64_t p;
+  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t policy_evict_last() {
+  uint64_t p;
+  asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint32_t ld_stream(const uint32_t *a, uint64_t pol) {
+  uint32_t v;
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.b32 %0, [%1], %2;"
+               : "=r"(v) : "l"(a), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ double ld_stream(const double *a, uint64_t pol) {
+  double v;
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.f64 %0, [%1], %2;"
+               : "=d"(v) : "l"(a), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ double ld_keep(const double *a, uint64_t pol) {
+  double v;
+  asm("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(a), "l"(pol));
+  return v;
+}
 __device__ __forceinline__ double dbl(uint64_t v) { return __longlong_as_double((long long)v); }
 
 // float image of a double in [2^-126, 2) from its high word (exponent
@@ -185,184 +220,133 @@ __device__ __forceinline__ double sum_w(uint64_t K, double sw) {
   return GRID ? __dmul_rn(__ull2double_rn(K), 0x1p-53) : sw;
 }
 
-// Rows of the degree-sorted order, 32 per warp, lane l owning row g0 + l.
-// Rounds of SLOTS edges per row: the warp stages the round's edges of its
-// rows with coalesced loads (SLOTS lanes per row), gathers the neighbours'
-// opinions, applies the threshold test, forms w * x and compacts the
-// accepted edges of each row, in edge order, into a shared-memory column of
-// that row; then each lane folds its own column in order.  The fold is the
-// sequential binary64 computation of the row (bit-identical), and only
-// accepted edges reach the FP64 pipe.
-constexpr int SLOTS = 8;                // edges per row and round
-constexpr int ROWS_PER_IT = 32 / SLOTS;  // rows staged per warp iteration
-constexpr int ITS = 32 / ROWS_PER_IT;    // staging iterations per round
 constexpr uint32_t GRID_MAX_DEG = 2047;  // K < 2^64 for at most 2047 weights <= 1
-
-struct WarpStage {
-  double prod[SLOTS][33];    // accepted w * x, column per row (padded: no bank conflicts)
-  uint64_t wgt[SLOTS][33];   // its weight: K units (grid rows) or binary64 bits
-  uint32_t rb[32], deg[32];  // the rows' first edge and degree (0: nothing to fold)
-  double xi[32];
-  float fxi[32];
-  uint32_t xok[32], cnt[32];
-};
-
+// One slice of 32 rows of similar degree, lane l owning row order[32 s +
+// l]: the lanes walk their rows' edges in insertion order in lock-step; the
+// column-major slice layout makes every load of a source index or weight
+// one coalesced 128 or 256-byte access.  Branch-free fold: a rejected edge
+// adds +0 to swx and 0 K units to sw, which leaves both sums unchanged, so
+// the FP64 pipe sees one add per slot and no lane is masked off.
 template <bool GRID>
-__device__ __forceinline__ void rows_warp(const OpinionArgs &p, uint64_t g0, WarpStage *stage) {
-  WarpStage &S = stage[threadIdx.x >> 5];
+__device__ __forceinline__ void sell_slice(const OpinionArgs &p, uint64_t sl) {
   const unsigned lane = threadIdx.x & 31;
-  const uint64_t total = p.order ? p.norder : p.n;
-  const uint64_t g = g0 + lane;
-  const bool active = g < total;
-  uint64_t i = 0;
-  double xi = 0.0;
-  uint32_t b = 0, deg = 0;
-  bool write = false;
-  if (active) {
-    i = p.order ? p.order[g] : g;
-    xi = p.x[i];
-    write = true;
-    if (i < p.nrows) {
-      b = p.rp[i];
-      deg = p.rp[i + 1] - b;
-      if (deg > p.hub_thr) {  // a hub warp writes this row
-        deg = 0;
-        write = false;
-      }
-    }
+  const uint64_t pos = sl * 32 + lane;
+  uint32_t r = 0, d = 0;
+  bool live = pos < p.norder;
+  if (live) {
+    r = p.order[pos];
+    if (r < p.nrows) d = p.rp[r + 1] - p.rp[r];
   }
+  const double xi = live ? p.x[r] : 0.0;
   bool xi_ok;
-  float fxi = hi_float(xi, xi_ok);
-  S.rb[lane] = b;
-  S.deg[lane] = deg;
-  S.xi[lane] = xi;
-  S.fxi[lane] = fxi;
-  S.xok[lane] = xi_ok;
-  const bool gr = GRID && deg <= GRID_MAX_DEG;
-  const uint32_t maxdeg = __reduce_max_sync(0xffffffffu, deg);
-  __syncwarp();
-  const unsigned sub = lane / SLOTS, t = lane % SLOTS;
-  const unsigned grp = ((1u << SLOTS) - 1u) << (sub * SLOTS);
-  const unsigned lt = (1u << lane) - 1u;
+  const float fxi = hi_float(xi, xi_ok);
+  const bool gr = GRID && d <= GRID_MAX_DEG;
+  const uint32_t D = p.slice_deg[sl];
+  const uint32_t *__restrict__ cs = p.sell_src + p.slice_base[sl] + lane;
+  const double *__restrict__ cw = p.sell_w + p.slice_base[sl] + lane;
+  const uint64_t pol_stream = policy_evict_first(), pol_keep = policy_evict_last();
   uint64_t K = 0;
   double sw = 0.0, swx = 0.0;
   uint32_t cnt = 0;
-  for (uint32_t k0 = 0; k0 < maxdeg; k0 += SLOTS) {
-    uint32_t jv[ITS];
-    double wv[ITS], xv[ITS];
-#pragma unroll
-    for (int it = 0; it < ITS; it++) {
-      const unsigned rl = it * ROWS_PER_IT + sub;
-      const uint32_t kk = k0 + t;
-      const bool valid = kk < S.deg[rl];
-      const uint32_t e = S.rb[rl] + kk;
-      jv[it] = valid ? __ldg(p.src + e) : 0xffffffffu;
-      wv[it] = valid ? __ldg(p.w + e) : 0.0;
+  // software pipeline: the next slot's source, weight and opinion are in
+  // flight while the current one is folded
+  uint32_t jn = D > 0 ? ld_stream(cs, pol_stream) : 0;
+  double wn = D > 0 ? ld_stream(cw, pol_stream) : 0.0;
+  double xn = D > 0 ? ld_keep(p.x + jn, pol_keep) : 0.0;
+  for (uint32_t q = 0; q < D; q++) {
+    const double wv = wn, xj = xn;
+    if (q + 1 < D) {
+      jn = ld_stream(cs + 32ull * (q + 1), pol_stream);
+      wn = ld_stream(cw + 32ull * (q + 1), pol_stream);
+      xn = ld_keep(p.x + jn, pol_keep);
     }
-#pragma unroll
-    for (int it = 0; it < ITS; it++) xv[it] = jv[it] != 0xffffffffu ? __ldg(p.x + jv[it]) : 0.0;
-#pragma unroll
-    for (int it = 0; it < ITS; it++) {
-      const unsigned rl = it * ROWS_PER_IT + sub;
-      const bool valid = jv[it] != 0xffffffffu;
-      bool acc = valid && within(xv[it], S.xi[rl], S.fxi[rl], S.xok[rl] != 0, p);
-      const unsigned bal = __ballot_sync(0xffffffffu, acc) & grp;
-      if (acc) {
-        bool ok;
-        uint64_t pk = mul_fast(bits(wv[it]), bits(xv[it]), ok);
-        double pkd = ok ? dbl(pk) : mul_hw(wv[it], xv[it]);
-        const unsigned q = __popc(bal & lt);
-        S.prod[q][rl] = pkd;
-        S.wgt[q][rl] = (GRID && S.deg[rl] <= GRID_MAX_DEG) ? grid_k(wv[it]) : bits(wv[it]);
-      }
-      if (t == 0) S.cnt[rl] = __popc(bal);
-    }
-    __syncwarp();
-    const uint32_t n = S.cnt[lane];
-    for (uint32_t q = 0; q < n; q++) {
-      swx = __dadd_rn(swx, S.prod[q][lane]);
-      if (gr) grid_accum(K, S.wgt[q][lane]);
-      else sw = __dadd_rn(sw, dbl(S.wgt[q][lane]));
-    }
-    cnt += n;
-    __syncwarp();
+    const bool acc = q < d && within(xj, xi, fxi, xi_ok, p);
+    bool ok;
+    uint64_t pk = mul_fast(bits(wv), bits(xj), ok);
+    double pkd = ok ? dbl(pk) : (acc ? mul_hw(wv, xj) : 0.0);
+    swx = __dadd_rn(swx, acc ? pkd : 0.0);
+    if (gr) grid_accum(K, acc ? grid_k(wv) : 0ull);
+    else sw = __dadd_rn(sw, acc ? wv : 0.0);
+    cnt += acc;
   }
-  if (write) {
-    uint64_t swb = bits(gr ? sum_w<true>(K, sw) : sw);
-    p.xo[i] = cnt ? finish(p.a, p.b, xi, swb, bits(swx)) : xi;
-  }
+  if (live) p.xo[r] = cnt ? finish(p.a, p.b, xi, bits(gr ? sum_w<true>(K, sw) : sw), bits(swx)) : xi;
 }
 
-// The work of one block of the gather grid: `blk` < hub_blocks are hub
-// warps, the rest row threads.  Shared by the single-simulation kernel and
-// the multi-job kernel of the serving loop.
+// One warp per hub row (degree > hub_thr): lane l folds edges l, l + 32,
+// l + 64, ... in order (coalesced loads), the 32 lane sums are combined in a
+// fixed tree.
 template <bool GRID>
-__device__ __forceinline__ void opinion_block(const OpinionArgs &p, unsigned blk,
-                                              WarpStage *stage) {
+__device__ __forceinline__ void hub_warp(const OpinionArgs &p, uint32_t r) {
+  const unsigned lane = threadIdx.x & 31;
+  double xi = p.x[r];
+  bool xi_ok;
+  float fxi = hi_float(xi, xi_ok);
+  const uint32_t b = p.rp[r], e = p.rp[r + 1];
+  const bool gr = GRID && (e - b + 31) / 32 <= GRID_MAX_DEG;
+  uint64_t K = 0;
+  double dsw = 0.0, dswx = 0.0;
+  uint32_t cnt = 0;
+  constexpr int U = 4;
+  const uint64_t pol_stream = policy_evict_first(), pol_keep = policy_evict_last();
+  for (uint32_t k0 = b; k0 < e; k0 += 32 * U) {
+    uint32_t jv[U];
+    double wv[U], xv[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const uint32_t k = k0 + u * 32 + lane;
+      const bool valid = k < e;
+      jv[u] = valid ? ld_stream(p.src + k, pol_stream) : 0xffffffffu;
+      wv[u] = valid ? ld_stream(p.w + k, pol_stream) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++)
+      xv[u] = jv[u] != 0xffffffffu ? ld_keep(p.x + jv[u], pol_keep) : 0.0;
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      if (jv[u] != 0xffffffffu && within(xv[u], xi, fxi, xi_ok, p)) {
+        bool ok;
+        uint64_t pk = mul_fast(bits(wv[u]), bits(xv[u]), ok);
+        dswx = __dadd_rn(dswx, ok ? dbl(pk) : mul_hw(wv[u], xv[u]));
+        if (gr) grid_add(K, wv[u]);
+        else dsw = __dadd_rn(dsw, wv[u]);
+        cnt++;
+      }
+    }
+  }
+  uint64_t sw = bits(gr ? sum_w<true>(K, dsw) : dsw);
+  uint64_t swx = bits(dswx);
+  // fixed tree: lane l receives lane l + off
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    uint64_t osw = __shfl_down_sync(0xffffffffu, sw, off);
+    uint64_t oswx = __shfl_down_sync(0xffffffffu, swx, off);
+    uint32_t ocnt = __shfl_down_sync(0xffffffffu, cnt, off);
+    if ((lane & (2 * off - 1)) == 0 && ocnt) {
+      sw = add_rn(sw, osw);
+      swx = add_rn(swx, oswx);
+      cnt += ocnt;
+    }
+  }
+  if (lane == 0) p.xo[r] = cnt ? finish(p.a, p.b, xi, sw, swx) : xi;
+}
+
+// The work of one block of the gather grid: hub warps, then slices (one
+// per warp).  Shared by the single-simulation kernel and the multi-job
+// kernel of the serving loop.
+template <bool GRID>
+__device__ __forceinline__ void opinion_block(const OpinionArgs &p, unsigned blk) {
+  const uint64_t warp = (uint64_t)blk * (TPB / 32) + (threadIdx.x >> 5);
   if (blk < p.hub_blocks) {
-    // one warp per hub row: lane l folds edges l, l + 32, l + 64, ... in
-    // order (coalesced loads), the lane sums are combined in a fixed tree
-    const unsigned lane = threadIdx.x & 31;
-    uint64_t h = (uint64_t)blk * (TPB / 32) + (threadIdx.x >> 5);
-    if (h >= p.nhub) return;
-    uint32_t r = p.hub_rows[h];
-    double xi = p.x[r];
-    bool xi_ok;
-    float fxi = hi_float(xi, xi_ok);
-    const uint32_t b = p.rp[r], e = p.rp[r + 1];
-    const bool gr = GRID && (e - b + 31) / 32 <= GRID_MAX_DEG;
-    uint64_t K = 0;
-    double dsw = 0.0, dswx = 0.0;
-    uint32_t cnt = 0;
-    constexpr int U = 4;
-    for (uint32_t k0 = b; k0 < e; k0 += 32 * U) {
-      uint32_t jv[U];
-      double wv[U], xv[U];
-#pragma unroll
-      for (int u = 0; u < U; u++) {
-        const uint32_t k = k0 + u * 32 + lane;
-        const bool valid = k < e;
-        jv[u] = valid ? __ldg(p.src + k) : 0xffffffffu;
-        wv[u] = valid ? __ldg(p.w + k) : 0.0;
-      }
-#pragma unroll
-      for (int u = 0; u < U; u++) xv[u] = jv[u] != 0xffffffffu ? __ldg(p.x + jv[u]) : 0.0;
-#pragma unroll
-      for (int u = 0; u < U; u++) {
-        if (jv[u] != 0xffffffffu && within(xv[u], xi, fxi, xi_ok, p)) {
-          bool ok;
-          uint64_t pk = mul_fast(bits(wv[u]), bits(xv[u]), ok);
-          dswx = __dadd_rn(dswx, ok ? dbl(pk) : mul_hw(wv[u], xv[u]));
-          if (gr) grid_add(K, wv[u]);
-          else dsw = __dadd_rn(dsw, wv[u]);
-          cnt++;
-        }
-      }
-    }
-    uint64_t sw = bits(gr ? sum_w<true>(K, dsw) : dsw);
-    uint64_t swx = bits(dswx);
-    // fixed tree: lane l receives lane l + off
-#pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-      uint64_t osw = __shfl_down_sync(0xffffffffu, sw, off);
-      uint64_t oswx = __shfl_down_sync(0xffffffffu, swx, off);
-      uint32_t ocnt = __shfl_down_sync(0xffffffffu, cnt, off);
-      if ((lane & (2 * off - 1)) == 0 && ocnt) {
-        sw = add_rn(sw, osw);
-        swx = add_rn(swx, oswx);
-        cnt += ocnt;
-      }
-    }
-    if (lane == 0) p.xo[r] = cnt ? finish(p.a, p.b, xi, sw, swx) : xi;
+    if (warp < p.nhub) hub_warp<GRID>(p, p.hub_rows[warp]);
     return;
   }
-  rows_warp<GRID>(p, (uint64_t)(blk - p.hub_blocks) * TPB + (threadIdx.x & ~31u), stage);
+  const uint64_t sl = warp - (uint64_t)p.hub_blocks * (TPB / 32);
+  if (sl < p.nslices) sell_slice<GRID>(p, sl);
 }
 
 template <bool GRID>
 __global__ void __launch_bounds__(TPB) k_opinion(OpinionArgs p) {
-  __shared__ WarpStage stage[TPB / 32];
-  opinion_block<GRID>(p, blockIdx.x, stage);
+  opinion_block<GRID>(p, blockIdx.x);
 }
 
 // Many simulations in one launch: block i runs virtual block tiles[i].blk of
@@ -375,13 +359,13 @@ struct JobTile {
 __global__ void __launch_bounds__(TPB) k_opinion_jobs(const OpinionArgs *jobs,
                                                       const JobTile *tiles) {
   __shared__ OpinionArgs sp;
-  __shared__ WarpStage stage[TPB / 32];
   JobTile t = tiles[blockIdx.x];
   if (threadIdx.x == 0) sp = jobs[t.job];
   __syncthreads();
-  if (sp.grid) opinion_block<true>(sp, t.blk, stage);
-  else opinion_block<false>(sp, t.blk, stage);
+  if (sp.grid) opinion_block<true>(sp, t.blk);
+  else opinion_block<false>(sp, t.blk);
 }
+
 
 // every weight a multiple of 2^-53 in (0, 1]?
 __global__ void k_check_grid(const double *w, uint64_t n, int *bad) {
@@ -436,7 +420,8 @@ void tr_bounded_confidence(ApplyCtx &c) {
   VG_CUDA(cudaGetLastError());
 }
 
-// arguments and grid size of one simulation's gather launch (0: no agents)
+// arguments and grid size of one simulation's gather launch; 0 when there
+// is nothing to launch (no agents, or no edges: then x' = x, copied here)
 static unsigned opinion_args(Sim &s, int e, int T, double eps, double a, double b,
                              uint32_t thr, OpinionArgs &p) {
   EdgeStore &es = s.edges[e];
@@ -458,30 +443,36 @@ static unsigned opinion_args(Sim &s, int e, int T, double eps, double a, double 
   p.b = b;
   p.eps_lo = (float)(eps - 1e-5);
   p.eps_hi = (float)(eps + 1e-5);
-  p.hub_thr = 0xffffffffu;
-  if (v.nedges && T < (int)es.csr.size()) {
-    CSR &cs = es.csr[T];
-    if (cs.unit_grid_weights < 0) {
-      int *bad = nullptr;
-      VG_CUDA(cudaMallocAsync((void **)&bad, 4, s.stream));
-      VG_CUDA(cudaMemsetAsync(bad, 0, 4, s.stream));
-      k_check_grid<<<1024, TPB, 0, s.stream>>>(p.w, v.nedges, bad);
-      int h = 0;
-      VG_CUDA(cudaMemcpyAsync(&h, bad, 4, cudaMemcpyDeviceToHost, s.stream));
-      VG_CUDA(cudaFreeAsync(bad, s.stream));
-      VG_CUDA(cudaStreamSynchronize(s.stream));
-      cs.unit_grid_weights = h ? 0 : 1;
-    }
-    p.grid = cs.unit_grid_weights;
-    ensure_schedule(s, cs, thr, av.n);
-    p.hub_rows = cs.hub_rows.as<uint32_t>();
-    p.nhub = cs.nhub;
-    p.order = cs.row_order.as<uint32_t>();
-    p.norder = cs.norder;
-    p.hub_thr = thr;
-    p.hub_blocks = (unsigned)((cs.nhub + (TPB / 32) - 1) / (TPB / 32));
+  p.hub_thr = thr;
+  if (!v.nedges || T >= (int)es.csr.size() || !v.row_ptr) {
+    VG_CUDA(cudaMemcpyAsync(p.xo, p.x, av.n * 8, cudaMemcpyDeviceToDevice, s.stream));
+    return 0;
   }
-  return p.hub_blocks + (unsigned)((av.n + TPB - 1) / TPB);
+  CSR &cs = es.csr[T];
+  if (cs.unit_grid_weights < 0) {
+    int *bad = nullptr;
+    VG_CUDA(cudaMallocAsync((void **)&bad, 4, s.stream));
+    VG_CUDA(cudaMemsetAsync(bad, 0, 4, s.stream));
+    k_check_grid<<<1024, TPB, 0, s.stream>>>(p.w, v.nedges, bad);
+    int h = 0;
+    VG_CUDA(cudaMemcpyAsync(&h, bad, 4, cudaMemcpyDeviceToHost, s.stream));
+    VG_CUDA(cudaFreeAsync(bad, s.stream));
+    VG_CUDA(cudaStreamSynchronize(s.stream));
+    cs.unit_grid_weights = h ? 0 : 1;
+  }
+  p.grid = cs.unit_grid_weights;
+  ensure_schedule(s, cs, thr, av.n);
+  p.hub_rows = cs.hub_rows.as<uint32_t>();
+  p.nhub = cs.nhub;
+  p.order = cs.order.as<uint32_t>();
+  p.norder = cs.norder;
+  p.slice_base = cs.slice_base.as<uint64_t>();
+  p.slice_deg = cs.slice_deg.as<uint32_t>();
+  p.sell_src = cs.sell_src.as<uint32_t>();
+  p.sell_w = cs.sell_w.as<double>();
+  p.nslices = cs.nslices;
+  p.hub_blocks = (unsigned)((cs.nhub + (TPB / 32) - 1) / (TPB / 32));
+  return p.hub_blocks + (unsigned)((cs.nslices + (TPB / 32) - 1) / (TPB / 32));
 }
 
 // One launch for the bounded-confidence step of many simulations (the

@@ -284,6 +284,161 @@ __global__ void k_readd_edges(Sweep s, DevCSRView c, Append ap, int call_pos) {
   }
 }
 
+// remove_edges!: a swept agent keeps its state; mode 0: when its field 0
+// passes the test (kind 0 always, 1 field >= arg, 2 field % arg != 0) it
+// calls remove_edges!(sim, id, E); mode 1: for every source nid of its
+// in-edges of E (read container, insertion order) whose field 0 passes the
+// test it calls remove_edges!(sim, nid, id, E).
+struct Removal {
+  uint64_t *to, *from, *key;
+  unsigned long long *counter;
+  uint64_t cap;
+};
+
+__device__ __forceinline__ bool field_test(int kind, double arg, const void *p, int dt,
+                                           uint64_t i) {
+  if (kind == 0) return true;
+  if (kind == 1) return ld_f64(p, dt, i) >= arg;
+  return (ld_i64(p, dt, i) % (int64_t)arg) != 0;
+}
+
+__device__ __forceinline__ bool push_removal(const Removal &r, uint64_t to, uint64_t from,
+                                             uint64_t key, int *status) {
+  unsigned long long k = atomicAdd(r.counter, 1ull);
+  if (k >= r.cap) {
+    set_status(status, 302);  // removal buffer overflow
+    return false;
+  }
+  r.to[k] = to;
+  r.from[k] = from;
+  r.key[k] = key;
+  return true;
+}
+
+__global__ void k_remove_edges(Sweep s, DevCSRView c, SrcTable t, int kind, double arg, int mode,
+                               Removal rm, int call_pos) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s.a.n || !sw_begin(s, i)) return;
+  if (s.writes) sw_copy(s, i);
+  const uint64_t id = ((uint64_t)s.type_nr << SHIFT_TYPE) | (i + 1);
+  if (mode == 0) {
+    if (s.nfields > 0 && !field_test(kind, arg, s.a.rd[0], s.fdt[0], i)) return;
+    push_removal(rm, id, REMOVE_ALL, order_key(call_pos, i, 0) + 1, s.status);
+    return;
+  }
+  if (i >= c.nrows) return;
+  uint32_t q = 0;
+  for (uint32_t e = c.row_ptr[i]; e < c.row_ptr[i + 1]; e++) {
+    int ty = edge_src_type(c, e);
+    uint32_t j = c.src[e];
+    if (ty <= 0 || ty >= MAX_AGENT_TYPES || !t.ptr[ty]) {
+      set_status(s.status, 202);  // source type not readable
+      continue;
+    }
+    if (!field_test(kind, arg, t.ptr[ty], t.dt[ty], j)) continue;
+    const uint64_t nid = ((uint64_t)ty << SHIFT_TYPE) | ((uint64_t)j + 1);
+    if (!push_removal(rm, id, nid, order_key(call_pos, i, q++) + 1, s.status)) return;
+  }
+}
+
+// ------------------------------------------- add_agent! within a transition
+// spawn: every swept agent keeps its state and calls add_agent! k times
+// (src/AgentMethods.jl:37-89) with a copy of its state whose field 0 is
+// increased by offset j; with a link edge type, after each add_agent! it
+// adds the edges new -> caller and caller -> new, payload field 0 = the new
+// agent's id.  Pass 1 keeps the callers and flags them; the callers' rank
+// (an exclusive scan in index order) numbers the new agents in the order of
+// the sequential sweep: new agent s takes the s-th slot popped from the
+// reuse stack (LIFO) and, when the stack is empty, the next fresh number.
+constexpr int SPAWN_MAX = 8;
+struct SpawnArgs {
+  int k;
+  double off[SPAWN_MAX];
+  const uint64_t *reuse;  // 1-based agent numbers, top at nreuse - 1
+  uint64_t nreuse, take;  // stack height, slots taken from it
+  uint64_t n_old;         // nextid - 1 before the transition
+};
+
+__global__ void k_spawn_flags(Sweep s, uint32_t *flag) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s.a.n) return;
+  bool swept = sw_begin(s, i);
+  flag[i] = swept ? 1u : 0u;
+  if (swept && s.writes) sw_copy(s, i);
+}
+
+__global__ void k_spawn_new(Sweep s, uint64_t n_callers_scope, const uint32_t *flag,
+                            const uint32_t *pos, SpawnArgs g, Append ap, int link_dt,
+                            int call_pos) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_callers_scope || !flag[i]) return;
+  const uint64_t id = ((uint64_t)s.type_nr << SHIFT_TYPE) | (i + 1);
+  for (int j = 0; j < g.k; j++) {
+    const uint64_t q = (uint64_t)pos[i] * g.k + j;
+    const uint64_t nr = q < g.take ? g.reuse[g.nreuse - 1 - q] : g.n_old + 1 + (q - g.take);
+    const uint64_t t = nr - 1;
+    for (int f = 0; f < s.nfields; f++) {
+      switch (s.fsize[f]) {
+        case 1: ((uint8_t *)s.a.wr[f])[t] = ((const uint8_t *)s.a.rd[f])[i]; break;
+        case 2: ((uint16_t *)s.a.wr[f])[t] = ((const uint16_t *)s.a.rd[f])[i]; break;
+        case 4: ((uint32_t *)s.a.wr[f])[t] = ((const uint32_t *)s.a.rd[f])[i]; break;
+        case 8: ((uint64_t *)s.a.wr[f])[t] = ((const uint64_t *)s.a.rd[f])[i]; break;
+      }
+    }
+    if (s.nfields > 0) {
+      int dt = s.fdt[0];
+      if (is_float(dt)) st_f64(s.a.wr[0], dt, t, ld_f64(s.a.rd[0], dt, i) + g.off[j]);
+      else st_i64(s.a.wr[0], dt, t, ld_i64(s.a.rd[0], dt, i) + (int64_t)g.off[j]);
+    }
+    if (s.mortal) s.a.died_wr[t] = 0;
+    if (link_dt < 0) continue;
+    const uint64_t nid = ((uint64_t)s.type_nr << SHIFT_TYPE) | nr;
+    for (int d = 0; d < 2; d++) {
+      int64_t k = append_slot(ap, s.status);
+      if (k < 0) return;
+      ap.from[k] = d == 0 ? nid : id;
+      ap.to[k] = d == 0 ? id : nid;
+      ap.key[k] = order_key(call_pos, i, 2 * j + d);
+      if (ap.npayload > 0) st_i64(ap.payload[0], link_dt, k, (int64_t)nid);
+    }
+  }
+}
+
+// link_neighbors: an agent whose field 0 equals die_value returns nothing;
+// every other agent keeps its state and, for each source nid of its
+// in-edges of type E in insertion order, adds nid -> id and id -> nid of
+// type F with payload field 0 = its own field 0.
+__global__ void k_link_neighbors(Sweep s, DevCSRView c, Append ap, int pl_dt, int has_die,
+                                 double die_value, int call_pos) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s.a.n || !sw_begin(s, i)) return;
+  const int dt0 = s.fdt[0];
+  const double v = s.nfields > 0 ? ld_f64(s.a.rd[0], dt0, i) : 0.0;
+  if (has_die && s.nfields > 0 && v == die_value) {
+    if (s.writes) sw_die(s, i);
+    return;
+  }
+  if (s.writes) sw_copy(s, i);
+  if (i >= c.nrows) return;
+  const uint64_t id = ((uint64_t)s.type_nr << SHIFT_TYPE) | (i + 1);
+  const int64_t vi = s.nfields > 0 ? ld_i64(s.a.rd[0], dt0, i) : 0;
+  uint32_t q = 0;
+  for (uint32_t e = c.row_ptr[i]; e < c.row_ptr[i + 1]; e++) {
+    const uint64_t nid = ((uint64_t)edge_src_type(c, e) << SHIFT_TYPE) | ((uint64_t)c.src[e] + 1);
+    for (int d = 0; d < 2; d++, q++) {
+      int64_t k = append_slot(ap, s.status);
+      if (k < 0) return;
+      ap.from[k] = d == 0 ? nid : id;
+      ap.to[k] = d == 0 ? id : nid;
+      ap.key[k] = order_key(call_pos, i, q);
+      if (ap.npayload > 0) {
+        if (is_float(pl_dt)) st_f64(ap.payload[0], pl_dt, k, v);
+        else st_i64(ap.payload[0], pl_dt, k, vi);
+      }
+    }
+  }
+}
+
 // ---------------------------------------------------------- SIR (cfg 0)
 // Person{state::UInt8 (0 S, 1 I, 2 R), days::Int32}.  A susceptible agent
 // with k infected in-neighbours is infected with p_k = 1 - (1 - beta)^k
@@ -638,6 +793,114 @@ void tr_readd_edges(ApplyCtx &c) {
   VG_CUDA(cudaGetLastError());
 }
 
+void tr_remove_edges(ApplyCtx &c) {
+  Sim &s = *c.sim;
+  const int E = need_edge_param(c, 0);
+  const EdgeTypeDesc &ed = s.model->et(E);
+  const int kind = (int)c.param(1, 0);
+  const double arg = c.param(2, 0);
+  const int mode = (int)c.param(3, 0);
+  if (kind < 0 || kind > 2 || mode < 0 || mode > 1) fail(VG_ERR_ARG, "remove_edges: kind 0..2, mode 0..1");
+  if (kind == 2 && arg == 0) fail(VG_ERR_ARG, "remove_edges: modulus 0");
+  if (!c.in_write(VG_EDGE(E)) && s.check_readable)
+    fail(VG_ERR_ASSERT, ed.name + " must be in the `write` argument of the transition function.");
+  Sweep w = make_sweep(c);
+  DevCSRView v = csr_view(s, E, c.call_type);
+  SrcTable t{};
+  uint64_t cap = w.a.n;
+  if (mode == 1) {
+    if (ed.ignorefrom())
+      fail(VG_ERR_ASSERT, "remove_edges! with a source agent is not defined for edgetypes "
+                          "with the :IgnoreFrom hint.");
+    require_edge_read(c, E);
+    require_sources_read(c, E, c.call_type);
+    t = make_src_table(c, 0);
+    cap = v.nedges;
+  } else if (kind != 0) {
+    require_agent_read(c, c.call_type);
+  }
+  if (w.a.n == 0) return;
+  EdgeRemoval *r = c.removal_for(E, std::max<uint64_t>(cap, 1));
+  Removal rm{r->to.as<uint64_t>(), r->from.as<uint64_t>(), r->key.as<uint64_t>(),
+             r->counter.as<unsigned long long>(), r->cap};
+  k_remove_edges<<<nblk(w.a.n), TPB, 0, s.stream>>>(w, v, t, kind, arg, mode, rm, c.call_pos);
+  VG_CUDA(cudaGetLastError());
+}
+
+void tr_spawn(ApplyCtx &c) {
+  Sim &s = *c.sim;
+  const int T = c.call_type;
+  const AgentTypeDesc &ad = s.model->at(T);
+  const int k = (int)c.param(0, 1);
+  if (k < 0 || k > SPAWN_MAX) fail(VG_ERR_ARG, "spawn: 0..8 new agents per caller");
+  if (!c.writes_call())
+    fail(VG_ERR_ASSERT, ad.name + " must be in the `write` argument of the transition function.");
+  if (!ad.fields.empty()) require_agent_read(c, T);
+  SpawnArgs g{};
+  g.k = k;
+  for (int j = 0; j < k; j++) g.off[j] = c.param(1 + j, 0);
+  const int link = c.nparams > 1 + k ? (int)c.params[1 + k] : -1;
+  int link_dt = -1;
+  if (link >= 0) {
+    const EdgeTypeDesc &ed = s.model->et(link);
+    link_dt = ed.stores_payload() ? ed.fields[0].dtype : VG_I64;
+    if (ed.stores_payload() && (link_dt == VG_F32 || link_dt == VG_F64))
+      fail(VG_ERR_ARG, "spawn: the link edge's field 0 holds an agent id (an integer)");
+  }
+  Sweep w = make_sweep(c);
+  const uint64_t n = w.a.n;
+  if (n == 0) return;
+  uint32_t *flag = nullptr, *pos = nullptr;
+  VG_CUDA(cudaMallocAsync((void **)&flag, (n + 1) * 4, s.stream));
+  VG_CUDA(cudaMallocAsync((void **)&pos, (n + 1) * 4, s.stream));
+  k_spawn_flags<<<nblk(n), TPB, 0, s.stream>>>(w, flag);
+  VG_CUDA(cudaGetLastError());
+  VG_CUDA(cudaMemsetAsync(flag + n, 0, 4, s.stream));
+  exclusive_scan_u32(flag, pos, n + 1, s.stream, s);
+  uint32_t m = 0;
+  VG_CUDA(cudaMemcpyAsync(&m, pos + n, 4, cudaMemcpyDeviceToHost, s.stream));
+  VG_CUDA(cudaStreamSynchronize(s.stream));
+  AgentStore &a = s.agents[T - 1];
+  const uint64_t total = (uint64_t)m * k;
+  g.nreuse = ad.immortal() ? 0 : a.nreuse;
+  g.take = std::min<uint64_t>(total, g.nreuse);
+  g.reuse = a.reuse.as<uint64_t>();
+  g.n_old = a.n;
+  const uint64_t n_new = a.n + (total - g.take);
+  agent_reserve(s, T, n_new);  // may move the columns: take the views after it
+  Sweep w2 = make_sweep(c);
+  Append ap{};
+  if (link >= 0 && total > 0) ap = make_append(c, link, 2 * total);
+  if (total > 0)
+    k_spawn_new<<<nblk(n), TPB, 0, s.stream>>>(w2, n, flag, pos, g, ap, link >= 0 ? link_dt : -1,
+                                               c.call_pos);
+  VG_CUDA(cudaGetLastError());
+  VG_CUDA(cudaFreeAsync(flag, s.stream));
+  VG_CUDA(cudaFreeAsync(pos, s.stream));
+  a.nreuse = g.nreuse - g.take;
+  a.n = n_new;
+  a.nliving += total;
+}
+
+void tr_link_neighbors(ApplyCtx &c) {
+  Sim &s = *c.sim;
+  const int E = (int)c.param(0, -1), F = (int)c.param(1, -1);
+  s.model->et(E);
+  const EdgeTypeDesc &fd = s.model->et(F);
+  require_edge_read(c, E);
+  Sweep w = make_sweep(c);
+  if (w.nfields > 0) require_agent_read(c, c.call_type);
+  const int has_die = c.nparams > 2;
+  const double die_value = c.param(2, 0);
+  DevCSRView v = csr_view(s, E, c.call_type);
+  if (w.a.n == 0) return;
+  Append ap = make_append(c, F, std::max<uint64_t>(2 * v.nedges, 1));
+  const int pl_dt = fd.stores_payload() ? fd.fields[0].dtype : -1;
+  k_link_neighbors<<<nblk(w.a.n), TPB, 0, s.stream>>>(w, v, ap, pl_dt, has_die, die_value,
+                                                      c.call_pos);
+  VG_CUDA(cudaGetLastError());
+}
+
 void tr_sir(ApplyCtx &c) {
   Sim &s = *c.sim;
   const AgentTypeDesc &ad = s.model->at(c.call_type);
@@ -765,6 +1028,9 @@ const std::vector<TransitionDef> &transitions() {
       {"keep", tr_keep},
       {"self_edge", tr_self_edge},
       {"readd_edges", tr_readd_edges},
+      {"spawn", tr_spawn},
+      {"link_neighbors", tr_link_neighbors},
+      {"remove_edges", tr_remove_edges},
   };
   return defs;
 }
