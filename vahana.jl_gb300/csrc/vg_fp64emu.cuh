@@ -129,4 +129,54 @@ __device__ __forceinline__ uint64_t emu_div_pos(uint64_t a, uint64_t b, bool &ok
   return ((uint64_t)e << 52) | (q & EMU_M52);
 }
 
+// a * b for positive doubles given as bit patterns, the form the gather
+// kernels use: correctly rounded when both operands are normal and the
+// product is normal (ok = false otherwise, and the caller multiplies on the
+// FP64 pipe).  The significand product comes from four 32x32-bit multiplies
+// with 64-bit addends; the rounded significand q (hidden bit included) is
+// packed by adding it to (exponent - 1) << 52, so that a carry out of the
+// rounding (q = 2^53) raises the exponent by itself.
+__device__ __forceinline__ uint64_t emu_mul_fast(uint64_t a, uint64_t b, bool &ok) {
+  const uint32_t ahi = (uint32_t)(a >> 32), alo = (uint32_t)a;
+  const uint32_t bhi = (uint32_t)(b >> 32), blo = (uint32_t)b;
+  const uint32_t ea = ahi >> 20, eb = bhi >> 20;
+  const uint32_t mah = (ahi & 0xFFFFFu) | 0x100000u, mbh = (bhi & 0xFFFFFu) | 0x100000u;
+  const uint64_t L = (uint64_t)alo * blo;                 // product bits 0..63
+  uint64_t S = (uint64_t)mah * blo + (L >> 32);           // < 2^53 + 2^32
+  S += (uint64_t)alo * mbh;                               // bits 32.. (< 2^55)
+  const uint64_t U = (uint64_t)mah * mbh + (S >> 32);     // bits 64.. (< 2^42 + 2^23)
+  const uint32_t ul = (uint32_t)S;                        // bits 32..63
+  const uint32_t big = (uint32_t)(U >> 41);               // product >= 2^105
+  const uint32_t sh = 20u + big;
+  uint64_t q = (U << (32u - sh)) | (uint64_t)(ul >> sh);  // 53 significant bits
+  const uint32_t rb = (ul >> (sh - 1u)) & 1u;
+  const uint32_t st = (ul & ((1u << (sh - 1u)) - 1u)) | (uint32_t)L;
+  q += rb & ((uint32_t)(st != 0u) | (uint32_t)q);
+  const int e = (int)ea + (int)eb - 1023 + (int)big;  // biased exponent before rounding
+  ok = (e > 0) & (e < 2046) & (ea - 1u < 2046u) & (eb - 1u < 2046u);
+  return ((uint64_t)(e - 1) << 52) + q;
+}
+
+// A weight w that is a multiple of 2^-53 in (0, 1] as the integer w * 2^53.
+__device__ __forceinline__ uint64_t emu_grid_units(uint64_t wb) {
+  const uint32_t ew = (uint32_t)(wb >> 52);
+  const uint64_t m = (wb & EMU_M52) | EMU_H53;
+  return ew >= 1023u ? (EMU_H53 << 1) : (m >> (1022u - ew));
+}
+
+// K + k for integers K, k that hold multiples of 2^-53 in units of 2^-53,
+// rounded to 53 significant bits, ties to even: the binary64 sum of the two
+// values (valid while K + k < 2^64).  Round to nearest even at bit s by
+// adding 2^(s-1) - 1 plus the bit at s, then clearing the low s bits.
+__device__ __forceinline__ uint64_t emu_grid_add(uint64_t K, uint64_t k) {
+  K += k;
+  const int s = 11 - __clz((uint32_t)(K >> 32));  // significant bits beyond 53
+  if (s > 0) {
+    const uint32_t lo = (uint32_t)K;
+    K += ((1u << (s - 1)) - 1u) + ((lo >> s) & 1u);
+    K &= ~(uint64_t)((1u << s) - 1u);
+  }
+  return K;
+}
+
 }  // namespace vg

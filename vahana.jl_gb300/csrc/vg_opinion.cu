@@ -118,16 +118,17 @@ __device__ __noinline__ bool within_exact(double xj, double xi, double eps) {
   return fabs(__dsub_rn(xj, xi)) < eps;
 }
 
-// |x_j - x_i| < eps, exactly as binary64 would decide it
+// |x_j - x_i| < eps, exactly as binary64 would decide it: the float
+// filter decides unless |fd - eps| < 1e-5 or an opinion is outside the
+// filter's range; then the exact test runs (out of line, so that its FP64
+// subtraction is never issued for the lanes the filter decided)
 __device__ __forceinline__ bool within(double xj, double xi, float fxi, bool xi_ok,
                                        const OpinionArgs &p) {
   bool ok;
-  float fxj = hi_float(xj, ok);
-  if (ok && xi_ok) {
-    float fd = fabsf(fxj - fxi);
-    if (fd < p.eps_lo) return true;
-    if (fd > p.eps_hi) return false;
-  }
+  const float fxj = hi_float(xj, ok);
+  const float fd = fabsf(fxj - fxi);
+  const bool sure = ok && xi_ok && (fd < p.eps_lo || fd > p.eps_hi);
+  if (__builtin_expect(sure, 1)) return fd < p.eps_lo;
   return within_exact(xj, xi, p.eps);
 }
 
@@ -138,81 +139,28 @@ __device__ __noinline__ uint64_t add_rn(uint64_t a, uint64_t b) {
   return bits(__dadd_rn(dbl(a), dbl(b)));
 }
 
-__device__ __noinline__ uint64_t mul_rn(uint64_t a, uint64_t b) {
-  bool ok = ((a | b) >> 63) == 0;
-  uint64_t r = ok ? emu_mul_pos(a, b, ok) : 0;
-  if (ok) return r;
-  return bits(__dmul_rn(dbl(a), dbl(b)));
-}
 
-__device__ __noinline__ uint64_t div_rn(uint64_t a, uint64_t b) {
-  bool ok = ((a | b) >> 63) == 0;
-  uint64_t r = ok ? emu_div_pos(a, b, ok) : 0;
-  if (ok) return r;
-  return bits(__ddiv_rn(dbl(a), dbl(b)));
-}
 
 __device__ __noinline__ double mul_hw(double a, double b) { return __dmul_rn(a, b); }
 
-// a * b for positive normal a, b with a normal result: the 106-bit
-// significand product from four 32x32-bit multiplies, rounded to nearest
-// even.  `ok` is false for other operands (the caller then multiplies on the
-// FP64 pipe).
 __device__ __forceinline__ uint64_t mul_fast(uint64_t a, uint64_t b, bool &ok) {
-  uint32_t ahi = (uint32_t)(a >> 32), alo = (uint32_t)a;
-  uint32_t bhi = (uint32_t)(b >> 32), blo = (uint32_t)b;
-  uint32_t ea = ahi >> 20, eb = bhi >> 20;  // sign bits are 0 here
-  uint32_t mah = (ahi & 0xFFFFFu) | 0x100000u, mbh = (bhi & 0xFFFFFu) | 0x100000u;
-  uint64_t ll = (uint64_t)alo * blo;
-  uint64_t mid = (uint64_t)mah * blo + (uint64_t)alo * mbh;  // < 2^54
-  uint64_t hh = (uint64_t)mah * mbh;                         // < 2^42
-  uint64_t t1 = (ll >> 32) + (mid & 0xFFFFFFFFull);           // < 2^33
-  uint32_t w1 = (uint32_t)t1;
-  uint64_t t2 = (mid >> 32) + hh + (t1 >> 32);  // product bits 64.. (P = t2 2^64 + w1 2^32 + ll.lo)
-  uint32_t big = (uint32_t)(t2 >> 41);          // P >= 2^105
-  uint64_t q = (t2 << (12 - big)) | (uint64_t)(w1 >> (20 + big));
-  uint32_t rb = (w1 >> (19 + big)) & 1u;
-  uint32_t sticky = (w1 & ((1u << (19 + big)) - 1u)) | (uint32_t)ll;
-  q += rb & ((uint32_t)(sticky != 0) | (uint32_t)q);
-  uint32_t c = (uint32_t)(q >> 53);
-  q >>= c;
-  int e = (int)ea + (int)eb - 1023 + (int)big + (int)c;
-  ok = (e > 0) & (e < 2047) & (ea - 1u < 2046u) & (eb - 1u < 2046u);
-  return ((uint64_t)e << 52) | (q & EMU_M52);
+  return emu_mul_fast(a, b, ok);
 }
 
-// sw as an integer K of 2^-53 units: K += w * 2^53, then K rounded to 53
-// significant bits (ties to even) -- the binary64 sum, valid while every
-// weight is a multiple of 2^-53 in (0, 1] and K < 2^64.
-__device__ __forceinline__ uint64_t grid_k(double w) {
-  uint64_t wb = bits(w);
-  uint32_t ew = (uint32_t)(wb >> 52);
-  uint64_t m = (wb & EMU_M52) | EMU_H53;
-  return ew >= 1023u ? (m << 1) : (m >> (1022u - ew));
-}
-
-__device__ __forceinline__ void grid_accum(uint64_t &K, uint64_t k) {
-  K += k;
-  uint32_t khi = (uint32_t)(K >> 32);
-  int s = 11 - __clz(khi);  // significant bits beyond 53
-  if (s > 0) {
-    uint32_t lo = (uint32_t)K;
-    uint32_t mask = (1u << s) - 1u, half = 1u << (s - 1);
-    uint32_t rem = lo & mask;
-    K -= rem;
-    if ((rem > half) | ((rem == half) & ((lo >> s) & 1u))) K += (1ull << s);
-  }
-}
-
+// sw as an integer K of 2^-53 units (weights that are multiples of 2^-53 in
+// (0, 1]), rounded to 53 significant bits after every addition: the
+// binary64 sum (vg_fp64emu.cuh)
+__device__ __forceinline__ uint64_t grid_k(double w) { return emu_grid_units(bits(w)); }
+__device__ __forceinline__ void grid_accum(uint64_t &K, uint64_t k) { K = emu_grid_add(K, k); }
 __device__ __forceinline__ void grid_add(uint64_t &K, double w) { grid_accum(K, grid_k(w)); }
 
-// x' = a x + b (swx / sw), each operation rounded in this order
-__device__ __noinline__ double finish(double pa, double pb_, double xi, uint64_t sw,
-                                      uint64_t swx) {
-  uint64_t m = div_rn(swx, sw);
-  uint64_t l = mul_rn(bits(pa), bits(xi));
-  uint64_t r = mul_rn(bits(pb_), m);
-  return dbl(add_rn(l, r));
+// x' = a x + b (swx / sw), each operation correctly rounded, in this order.
+// Once per row: the hardware binary64 instructions (the FP64 pipe has room
+// for them; the integer pipes, busy with the per-edge work, do not).
+__device__ __forceinline__ double finish(double pa, double pb, double xi, uint64_t sw,
+                                         uint64_t swx) {
+  const double m = __ddiv_rn(dbl(swx), dbl(sw));
+  return __dadd_rn(__dmul_rn(pa, xi), __dmul_rn(pb, m));
 }
 
 template <bool GRID>
