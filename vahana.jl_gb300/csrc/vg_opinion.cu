@@ -46,7 +46,7 @@
 namespace vg {
 namespace {
 
-constexpr int TPB = 256;
+constexpr int TPB = 128;
 
 struct OpinionArgs {
   const uint32_t *__restrict__ rp;
@@ -172,15 +172,37 @@ constexpr uint32_t GRID_MAX_DEG = 2047;  // K < 2^64 for at most 2047 weights <=
 // One slice of 32 rows of similar degree, lane l owning row order[32 s +
 // l]: the lanes walk their rows' edges in insertion order in lock-step; the
 // column-major slice layout makes every load of a source index or weight
-// one coalesced 128 or 256-byte access.  Branch-free fold: a rejected edge
-// adds +0 to swx and 0 K units to sw, which leaves both sums unchanged, so
-// the FP64 pipe sees one add per slot and no lane is masked off.
+// one coalesced 128 or 256-byte access.  Slots are taken in groups of
+// SELL_U with a two-stage software pipeline (while group g is folded, the
+// opinions of group g + 1 and the sources and weights of group g + 2 are in
+// flight), so that each warp keeps 2 SELL_U slots per lane outstanding.
+// Branch-free fold: a rejected edge adds +0 to swx and 0 K units to sw,
+// which leaves both sums unchanged, so no lane is masked off.
+constexpr uint32_t SELL_U = 2;
+
+struct SellCursor {
+  const uint32_t *__restrict__ cs;
+  const double *__restrict__ cw;
+  uint32_t D;
+  uint64_t pol;
+  __device__ __forceinline__ void load(uint32_t g, uint32_t (&j)[SELL_U],
+                                       double (&w)[SELL_U]) const {
+#pragma unroll
+    for (uint32_t u = 0; u < SELL_U; u++) {
+      const uint32_t q = g * SELL_U + u;
+      const bool v = q < D;
+      j[u] = v ? ld_stream(cs + 32ull * q, pol) : 0u;
+      w[u] = v ? ld_stream(cw + 32ull * q, pol) : 0.0;
+    }
+  }
+};
+
 template <bool GRID>
 __device__ __forceinline__ void sell_slice(const OpinionArgs &p, uint64_t sl) {
   const unsigned lane = threadIdx.x & 31;
   const uint64_t pos = sl * 32 + lane;
   uint32_t r = 0, d = 0;
-  bool live = pos < p.norder;
+  const bool live = pos < p.norder;
   if (live) {
     r = p.order[pos];
     if (r < p.nrows) d = p.rp[r + 1] - p.rp[r];
@@ -189,33 +211,48 @@ __device__ __forceinline__ void sell_slice(const OpinionArgs &p, uint64_t sl) {
   bool xi_ok;
   const float fxi = hi_float(xi, xi_ok);
   const bool gr = GRID && d <= GRID_MAX_DEG;
-  const uint32_t D = p.slice_deg[sl];
-  const uint32_t *__restrict__ cs = p.sell_src + p.slice_base[sl] + lane;
-  const double *__restrict__ cw = p.sell_w + p.slice_base[sl] + lane;
-  const uint64_t pol_stream = policy_evict_first(), pol_keep = policy_evict_last();
+  const uint64_t pol_keep = policy_evict_last();
+  SellCursor cur{p.sell_src + p.slice_base[sl] + lane, p.sell_w + p.slice_base[sl] + lane,
+                 p.slice_deg[sl], policy_evict_first()};
+  const uint32_t G = (cur.D + SELL_U - 1) / SELL_U;
   uint64_t K = 0;
   double sw = 0.0, swx = 0.0;
   uint32_t cnt = 0;
-  // software pipeline: the next slot's source, weight and opinion are in
-  // flight while the current one is folded
-  uint32_t jn = D > 0 ? ld_stream(cs, pol_stream) : 0;
-  double wn = D > 0 ? ld_stream(cw, pol_stream) : 0.0;
-  double xn = D > 0 ? ld_keep(p.x + jn, pol_keep) : 0.0;
-  for (uint32_t q = 0; q < D; q++) {
-    const double wv = wn, xj = xn;
-    if (q + 1 < D) {
-      jn = ld_stream(cs + 32ull * (q + 1), pol_stream);
-      wn = ld_stream(cw + 32ull * (q + 1), pol_stream);
-      xn = ld_keep(p.x + jn, pol_keep);
+  uint32_t j0[SELL_U], j1[SELL_U];
+  double w0[SELL_U], w1[SELL_U], x0[SELL_U];
+  cur.load(0, j0, w0);
+#pragma unroll
+  for (uint32_t u = 0; u < SELL_U; u++) x0[u] = u < cur.D ? ld_keep(p.x + j0[u], pol_keep) : 0.0;
+  cur.load(1, j1, w1);
+  for (uint32_t g = 0; g < G; g++) {
+    double x1[SELL_U];
+#pragma unroll
+    for (uint32_t u = 0; u < SELL_U; u++)
+      x1[u] = (g + 1) * SELL_U + u < cur.D ? ld_keep(p.x + j1[u], pol_keep) : 0.0;
+    uint32_t j2[SELL_U];
+    double w2[SELL_U];
+    cur.load(g + 2, j2, w2);
+#pragma unroll
+    for (uint32_t u = 0; u < SELL_U; u++) {
+      const uint32_t q = g * SELL_U + u;
+      if (q >= cur.D) break;  // warp-uniform: the slice's padding to a whole group
+      const double wv = w0[u], xj = x0[u];
+      const bool acc = q < d && within(xj, xi, fxi, xi_ok, p);
+      bool ok;
+      const uint64_t pk = mul_fast(bits(wv), bits(xj), ok);
+      const double pkd = ok ? dbl(pk) : (acc ? mul_hw(wv, xj) : 0.0);
+      swx = __dadd_rn(swx, acc ? pkd : 0.0);
+      if (gr) grid_accum(K, acc ? grid_k(wv) : 0ull);
+      else sw = __dadd_rn(sw, acc ? wv : 0.0);
+      cnt += acc;
     }
-    const bool acc = q < d && within(xj, xi, fxi, xi_ok, p);
-    bool ok;
-    uint64_t pk = mul_fast(bits(wv), bits(xj), ok);
-    double pkd = ok ? dbl(pk) : (acc ? mul_hw(wv, xj) : 0.0);
-    swx = __dadd_rn(swx, acc ? pkd : 0.0);
-    if (gr) grid_accum(K, acc ? grid_k(wv) : 0ull);
-    else sw = __dadd_rn(sw, acc ? wv : 0.0);
-    cnt += acc;
+#pragma unroll
+    for (uint32_t u = 0; u < SELL_U; u++) {
+      w0[u] = w1[u];
+      x0[u] = x1[u];
+      j1[u] = j2[u];
+      w1[u] = w2[u];
+    }
   }
   if (live) p.xo[r] = cnt ? finish(p.a, p.b, xi, bits(gr ? sum_w<true>(K, sw) : sw), bits(swx)) : xi;
 }
