@@ -311,10 +311,10 @@ int vg_read_staged_edges(vg_sim *s, int edge_type, uint64_t *from_out,
 /* ---- self test ----------------------------------------------------------
  * Compares the integer-pipe binary64 add/mul/div used by the gather kernels
  * with the hardware instructions on n generated operand pairs (no reference
- * counterpart).  counts_out[6]: mismatches of add (including the partial
- * sums of 24 grid weights per pair, summed in 2^-53 units), mul (both the
- * general and the gather kernels' form), div, then the number of
- * out-of-range fallbacks of the general add, mul and div. */
+ * counterpart).  counts_out[6]: mismatches of add, mul (the general and the
+ * gather kernels' form, and scaling by powers of two), div (the general and
+ * the gather kernels' form), then the number of out-of-range fallbacks of
+ * the general add, mul and div. */
 int vg_selftest_fp64(uint64_t n, uint64_t seed, uint64_t *counts_out);
 
 /* ---- allocation-free SIR step ---------------------------------------------

@@ -136,7 +136,8 @@ __device__ __forceinline__ uint64_t emu_div_pos(uint64_t a, uint64_t b, bool &ok
 // with 64-bit addends; the rounded significand q (hidden bit included) is
 // packed by adding it to (exponent - 1) << 52, so that a carry out of the
 // rounding (q = 2^53) raises the exponent by itself.
-__device__ __forceinline__ uint64_t emu_mul_fast(uint64_t a, uint64_t b, bool &ok) {
+template <bool GRID_A>
+__device__ __forceinline__ uint64_t emu_mul_fast_t(uint64_t a, uint64_t b, bool &ok) {
   const uint32_t ahi = (uint32_t)(a >> 32), alo = (uint32_t)a;
   const uint32_t bhi = (uint32_t)(b >> 32), blo = (uint32_t)b;
   const uint32_t ea = ahi >> 20, eb = bhi >> 20;
@@ -153,30 +154,75 @@ __device__ __forceinline__ uint64_t emu_mul_fast(uint64_t a, uint64_t b, bool &o
   const uint32_t st = (ul & ((1u << (sh - 1u)) - 1u)) | (uint32_t)L;
   q += rb & ((uint32_t)(st != 0u) | (uint32_t)q);
   const int e = (int)ea + (int)eb - 1023 + (int)big;  // biased exponent before rounding
+  if (GRID_A)  // a's exponent is 970..1023: only b's needs a check
+    ok = (eb - 54u) <= 1990u;
+  else
+    ok = (e > 0) & (e < 2046) & (ea - 1u < 2046u) & (eb - 1u < 2046u);
+  return ((uint64_t)(e - 1) << 52) + q;
+}
+__device__ __forceinline__ uint64_t emu_mul_fast(uint64_t a, uint64_t b, bool &ok) {
+  return emu_mul_fast_t<false>(a, b, ok);
+}
+// the same for a weight a that is a multiple of 2^-53 in (0, 1]
+__device__ __forceinline__ uint64_t emu_mul_grid(uint64_t a, uint64_t b, bool &ok) {
+  return emu_mul_fast_t<true>(a, b, ok);
+}
+
+// a / b for positive doubles given as bit patterns, the per-row division of
+// the gather kernels: correctly rounded when both operands are normal and
+// the quotient is normal (ok = false otherwise, and the caller divides on
+// the FP64 pipe).  Significands A in [B, 2B), B in [2^52, 2^53); quotient
+// q = floor(A 2^52 / B).  A float reciprocal of B >> 29 gives y0 ~ 2^83/B
+// (relative error < 2^-22), one Newton step gives Y ~ 2^115/B (< 2^-43),
+// the quotient estimate from Y is corrected once through its remainder (the
+// remainder stays below 2^62 in magnitude) and then exactly: the remainder
+// N - q B is small enough to be exact in 64-bit two's complement.  The
+// remainder decides the rounding (ties to even).  Newton-Raphson reciprocal
+// refinement and remainder correction as in P. Markstein, IBM J. Res. Dev.
+// 34(1), 1990.
+__device__ __forceinline__ uint64_t emu_div_fast(uint64_t a, uint64_t b, bool &ok) {
+  const uint32_t ea = (uint32_t)(a >> 52), eb = (uint32_t)(b >> 52);
+  uint64_t A = (a & EMU_M52) | EMU_H53;
+  const uint64_t B = (b & EMU_M52) | EMU_H53;
+  int e = (int)ea - (int)eb + 1023;
+  if (A < B) {
+    A <<= 1;
+    e--;
+  }
+  const float fb = __uint_as_float((150u << 23) | ((uint32_t)(B >> 29) & 0x7FFFFFu));  // B >> 29
+  const uint32_t ub = __float_as_uint(__frcp_rn(fb));
+  const uint64_t y0 = (uint64_t)((ub & 0x7FFFFFu) | 0x800000u) << ((ub >> 23) - 96u);
+  const int64_t e1 = (int64_t)(0ull - B * y0);  // 2^83 - B y0 (fits: |.| < 2^62)
+  const uint64_t Y = (y0 << 32) + (uint64_t)__mul64hi((long long)(y0 << 13), (long long)e1);
+  const uint64_t N = A << 52;  // A 2^52 mod 2^64
+  uint64_t q = __umul64hi(A << 1, Y);
+  const int64_t r1 = (int64_t)(N - q * B);
+  q += (uint64_t)(__mul64hi((long long)r1, (long long)(Y >> 1)) >> 50);
+  int64_t r = (int64_t)(N - q * B);
+#pragma unroll
+  for (int k = 0; k < 2; k++)
+    if (r < 0) {
+      q--;
+      r += (int64_t)B;
+    }
+#pragma unroll
+  for (int k = 0; k < 2; k++)
+    if (r >= (int64_t)B) {
+      q++;
+      r -= (int64_t)B;
+    }
+  const uint64_t r2 = (uint64_t)r << 1;
+  q += (r2 > B) || (r2 == B && (q & 1));
   ok = (e > 0) & (e < 2046) & (ea - 1u < 2046u) & (eb - 1u < 2046u);
   return ((uint64_t)(e - 1) << 52) + q;
 }
 
-// A weight w that is a multiple of 2^-53 in (0, 1] as the integer w * 2^53.
-__device__ __forceinline__ uint64_t emu_grid_units(uint64_t wb) {
-  const uint32_t ew = (uint32_t)(wb >> 52);
-  const uint64_t m = (wb & EMU_M52) | EMU_H53;
-  return ew >= 1023u ? (EMU_H53 << 1) : (m >> (1022u - ew));
-}
-
-// K + k for integers K, k that hold multiples of 2^-53 in units of 2^-53,
-// rounded to 53 significant bits, ties to even: the binary64 sum of the two
-// values (valid while K + k < 2^64).  Round to nearest even at bit s by
-// adding 2^(s-1) - 1 plus the bit at s, then clearing the low s bits.
-__device__ __forceinline__ uint64_t emu_grid_add(uint64_t K, uint64_t k) {
-  K += k;
-  const int s = 11 - __clz((uint32_t)(K >> 32));  // significant bits beyond 53
-  if (s > 0) {
-    const uint32_t lo = (uint32_t)K;
-    K += ((1u << (s - 1)) - 1u) + ((lo >> s) & 1u);
-    K &= ~(uint64_t)((1u << s) - 1u);
-  }
-  return K;
+// x * 2^k for a positive double x (bit pattern) when x and the result are
+// normal: exact; ok = false otherwise.
+__device__ __forceinline__ uint64_t emu_scale2(uint64_t x, int k, bool &ok) {
+  const int ex = (int)(x >> 52);
+  ok = (ex >= 1) & (ex <= 2046) & (ex + k >= 1) & (ex + k <= 2046) & ((x >> 63) == 0);
+  return x + ((uint64_t)(int64_t)k << 52);
 }
 
 }  // namespace vg

@@ -39,6 +39,7 @@
 // reference's order.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 
 #include "vg_fp64emu.cuh"
 #include "vg_internal.h"
@@ -67,8 +68,9 @@ struct OpinionArgs {
   uint32_t hub_thr;
   unsigned hub_blocks;
   double eps, a, b;
+  int a_pow2, b_pow2, a_k, b_k;  // a = 2^a_k, b = 2^b_k (positive normal powers of two)
   float eps_lo, eps_hi;  // float filter: certainly inside / certainly outside
-  int grid;              // all weights are multiples of 2^-53 in (0, 1]
+  int grid;              // all weights are multiples of 2^-53 in (0, 1] (exponent 970..1023)
 };
 
 __device__ __forceinline__ uint64_t bits(double v) { return (uint64_t)__double_as_longlong(v); }
@@ -143,32 +145,29 @@ __device__ __noinline__ uint64_t add_rn(uint64_t a, uint64_t b) {
 
 __device__ __noinline__ double mul_hw(double a, double b) { return __dmul_rn(a, b); }
 
-__device__ __forceinline__ uint64_t mul_fast(uint64_t a, uint64_t b, bool &ok) {
-  return emu_mul_fast(a, b, ok);
-}
 
-// sw as an integer K of 2^-53 units (weights that are multiples of 2^-53 in
-// (0, 1]), rounded to 53 significant bits after every addition: the
-// binary64 sum (vg_fp64emu.cuh)
-__device__ __forceinline__ uint64_t grid_k(double w) { return emu_grid_units(bits(w)); }
-__device__ __forceinline__ void grid_accum(uint64_t &K, uint64_t k) { K = emu_grid_add(K, k); }
-__device__ __forceinline__ void grid_add(uint64_t &K, double w) { grid_accum(K, grid_k(w)); }
+__device__ __noinline__ double div_hw(double a, double b) { return __ddiv_rn(a, b); }
 
 // x' = a x + b (swx / sw), each operation correctly rounded, in this order.
-// Once per row: the hardware binary64 instructions (the FP64 pipe has room
-// for them; the integer pipes, busy with the per-edge work, do not).
-__device__ __forceinline__ double finish(double pa, double pb, double xi, uint64_t sw,
+// Once per row.  The division runs on the integer pipes (exact, with the
+// hardware instruction for out-of-range operands); a and b that are powers
+// of two (the model's 0.5) scale by their exponent, other values multiply on
+// the FP64 pipe; the final addition is the hardware add.
+__device__ __forceinline__ double finish(const OpinionArgs &p, double xi, uint64_t sw,
                                          uint64_t swx) {
-  const double m = __ddiv_rn(dbl(swx), dbl(sw));
-  return __dadd_rn(__dmul_rn(pa, xi), __dmul_rn(pb, m));
+  bool ok;
+  const uint64_t m = emu_div_fast(swx, sw, ok);
+  const double md = ok ? dbl(m) : div_hw(dbl(swx), dbl(sw));
+  bool okl = false, okr = false;
+  double l = 0.0, r = 0.0;
+  if (p.a_pow2) l = dbl(emu_scale2(bits(xi), p.a_k, okl));
+  if (!okl) l = mul_hw(p.a, xi);
+  if (p.b_pow2) r = dbl(emu_scale2(bits(md), p.b_k, okr));
+  if (!okr) r = mul_hw(p.b, md);
+  return __dadd_rn(l, r);
 }
 
-template <bool GRID>
-__device__ __forceinline__ double sum_w(uint64_t K, double sw) {
-  return GRID ? __dmul_rn(__ull2double_rn(K), 0x1p-53) : sw;
-}
 
-constexpr uint32_t GRID_MAX_DEG = 2047;  // K < 2^64 for at most 2047 weights <= 1
 // One slice of 32 rows of similar degree, lane l owning row order[32 s +
 // l]: the lanes walk their rows' edges in insertion order in lock-step; the
 // column-major slice layout makes every load of a source index or weight
@@ -180,23 +179,82 @@ constexpr uint32_t GRID_MAX_DEG = 2047;  // K < 2^64 for at most 2047 weights <=
 // which leaves both sums unchanged, so no lane is masked off.
 constexpr uint32_t SELL_U = 2;
 
+struct SellGroup {
+  uint32_t j[SELL_U];
+  double w[SELL_U], x[SELL_U];
+};
+
 struct SellCursor {
   const uint32_t *__restrict__ cs;
   const double *__restrict__ cw;
   uint32_t D;
   uint64_t pol;
-  __device__ __forceinline__ void load(uint32_t g, uint32_t (&j)[SELL_U],
-                                       double (&w)[SELL_U]) const {
+  __device__ __forceinline__ void load(uint32_t g, SellGroup &G) const {
 #pragma unroll
     for (uint32_t u = 0; u < SELL_U; u++) {
       const uint32_t q = g * SELL_U + u;
       const bool v = q < D;
-      j[u] = v ? ld_stream(cs + 32ull * q, pol) : 0u;
-      w[u] = v ? ld_stream(cw + 32ull * q, pol) : 0.0;
+      G.j[u] = v ? ld_stream(cs + 32ull * q, pol) : 0u;
+      G.w[u] = v ? ld_stream(cw + 32ull * q, pol) : 0.0;
     }
   }
 };
 
+struct RowAcc {
+  double sw, swx;
+  uint32_t cnt;
+};
+
+template <bool GRID>
+struct SliceCtx {
+  const OpinionArgs &p;
+  SellCursor cur;
+  uint64_t pol_keep;
+  double xi;
+  float fxi;
+  bool xi_ok;
+  uint32_t d, G;
+
+  __device__ __forceinline__ void gather(uint32_t g, SellGroup &N) const {
+#pragma unroll
+    for (uint32_t u = 0; u < SELL_U; u++)
+      N.x[u] = g * SELL_U + u < cur.D ? ld_keep(p.x + N.j[u], pol_keep) : 0.0;
+  }
+  __device__ __forceinline__ void fold(uint32_t g, const SellGroup &C, RowAcc &a) const {
+#pragma unroll
+    for (uint32_t u = 0; u < SELL_U; u++) {
+      const uint32_t q = g * SELL_U + u;
+      if (q >= cur.D) break;  // warp-uniform: the slice's padding to a whole group
+      const double wv = C.w[u], xj = C.x[u];
+      const bool acc = q < d && within(xj, xi, fxi, xi_ok, p);
+      bool ok;
+      const uint64_t pk = GRID ? emu_mul_grid(bits(wv), bits(xj), ok)
+                               : emu_mul_fast(bits(wv), bits(xj), ok);
+      const double pkd = ok ? dbl(pk) : (acc ? mul_hw(wv, xj) : 0.0);
+      a.swx = __dadd_rn(a.swx, acc ? pkd : 0.0);
+      a.sw = __dadd_rn(a.sw, acc ? wv : 0.0);
+      a.cnt += acc;
+    }
+  }
+  // one pipeline step: group g is folded while the opinions of group g + 1
+  // and the sources and weights of group g + 2 are requested
+  __device__ __forceinline__ void step(uint32_t g, const SellGroup &C, SellGroup &N,
+                                       SellGroup &NN, RowAcc &a) const {
+    gather(g + 1, N);
+    cur.load(g + 2, NN);
+    fold(g, C, a);
+  }
+};
+
+// One slice of 32 rows of similar degree, lane l owning row order[32 s +
+// l]: the lanes walk their rows' edges in insertion order in lock-step; the
+// column-major slice layout makes every load of a source index or weight
+// one coalesced 128 or 256-byte access.  Slots are taken in groups of
+// SELL_U with a two-stage software pipeline over three rotating buffers
+// (while group g is folded, the opinions of group g + 1 and the sources and
+// weights of group g + 2 are in flight).  Branch-free fold: a rejected edge
+// adds +0 to swx and 0 to sw, which leaves both sums unchanged, so no lane
+// is masked off.
 template <bool GRID>
 __device__ __forceinline__ void sell_slice(const OpinionArgs &p, uint64_t sl) {
   const unsigned lane = threadIdx.x & 31;
@@ -210,51 +268,24 @@ __device__ __forceinline__ void sell_slice(const OpinionArgs &p, uint64_t sl) {
   const double xi = live ? p.x[r] : 0.0;
   bool xi_ok;
   const float fxi = hi_float(xi, xi_ok);
-  const bool gr = GRID && d <= GRID_MAX_DEG;
-  const uint64_t pol_keep = policy_evict_last();
   SellCursor cur{p.sell_src + p.slice_base[sl] + lane, p.sell_w + p.slice_base[sl] + lane,
                  p.slice_deg[sl], policy_evict_first()};
-  const uint32_t G = (cur.D + SELL_U - 1) / SELL_U;
-  uint64_t K = 0;
-  double sw = 0.0, swx = 0.0;
-  uint32_t cnt = 0;
-  uint32_t j0[SELL_U], j1[SELL_U];
-  double w0[SELL_U], w1[SELL_U], x0[SELL_U];
-  cur.load(0, j0, w0);
-#pragma unroll
-  for (uint32_t u = 0; u < SELL_U; u++) x0[u] = u < cur.D ? ld_keep(p.x + j0[u], pol_keep) : 0.0;
-  cur.load(1, j1, w1);
-  for (uint32_t g = 0; g < G; g++) {
-    double x1[SELL_U];
-#pragma unroll
-    for (uint32_t u = 0; u < SELL_U; u++)
-      x1[u] = (g + 1) * SELL_U + u < cur.D ? ld_keep(p.x + j1[u], pol_keep) : 0.0;
-    uint32_t j2[SELL_U];
-    double w2[SELL_U];
-    cur.load(g + 2, j2, w2);
-#pragma unroll
-    for (uint32_t u = 0; u < SELL_U; u++) {
-      const uint32_t q = g * SELL_U + u;
-      if (q >= cur.D) break;  // warp-uniform: the slice's padding to a whole group
-      const double wv = w0[u], xj = x0[u];
-      const bool acc = q < d && within(xj, xi, fxi, xi_ok, p);
-      bool ok;
-      const uint64_t pk = mul_fast(bits(wv), bits(xj), ok);
-      const double pkd = ok ? dbl(pk) : (acc ? mul_hw(wv, xj) : 0.0);
-      swx = __dadd_rn(swx, acc ? pkd : 0.0);
-      if (gr) grid_accum(K, acc ? grid_k(wv) : 0ull);
-      else sw = __dadd_rn(sw, acc ? wv : 0.0);
-      cnt += acc;
-    }
-#pragma unroll
-    for (uint32_t u = 0; u < SELL_U; u++) {
-      w0[u] = w1[u];
-      x0[u] = x1[u];
-      j1[u] = j2[u];
-      w1[u] = w2[u];
-    }
+  const SliceCtx<GRID> c{p, cur, policy_evict_last(), xi, fxi, xi_ok, d,
+                         (cur.D + SELL_U - 1) / SELL_U};
+  RowAcc a{0.0, 0.0, 0};
+  SellGroup X, Y, Z;
+  cur.load(0, X);
+  c.gather(0, X);
+  cur.load(1, Y);
+  for (uint32_t g = 0; g < c.G; g += 3) {
+    c.step(g, X, Y, Z, a);
+    if (g + 1 >= c.G) break;
+    c.step(g + 1, Y, Z, X, a);
+    if (g + 2 >= c.G) break;
+    c.step(g + 2, Z, X, Y, a);
   }
-  if (live) p.xo[r] = cnt ? finish(p.a, p.b, xi, bits(gr ? sum_w<true>(K, sw) : sw), bits(swx)) : xi;
+  if (!live) return;
+  p.xo[r] = a.cnt ? finish(p, xi, bits(a.sw), bits(a.swx)) : xi;
 }
 
 // One warp per hub row (degree > hub_thr): lane l folds edges l, l + 32,
@@ -267,8 +298,6 @@ __device__ __forceinline__ void hub_warp(const OpinionArgs &p, uint32_t r) {
   bool xi_ok;
   float fxi = hi_float(xi, xi_ok);
   const uint32_t b = p.rp[r], e = p.rp[r + 1];
-  const bool gr = GRID && (e - b + 31) / 32 <= GRID_MAX_DEG;
-  uint64_t K = 0;
   double dsw = 0.0, dswx = 0.0;
   uint32_t cnt = 0;
   constexpr int U = 4;
@@ -290,15 +319,15 @@ __device__ __forceinline__ void hub_warp(const OpinionArgs &p, uint32_t r) {
     for (int u = 0; u < U; u++) {
       if (jv[u] != 0xffffffffu && within(xv[u], xi, fxi, xi_ok, p)) {
         bool ok;
-        uint64_t pk = mul_fast(bits(wv[u]), bits(xv[u]), ok);
+        const uint64_t pk = GRID ? emu_mul_grid(bits(wv[u]), bits(xv[u]), ok)
+                                 : emu_mul_fast(bits(wv[u]), bits(xv[u]), ok);
         dswx = __dadd_rn(dswx, ok ? dbl(pk) : mul_hw(wv[u], xv[u]));
-        if (gr) grid_add(K, wv[u]);
-        else dsw = __dadd_rn(dsw, wv[u]);
+        dsw = __dadd_rn(dsw, wv[u]);
         cnt++;
       }
     }
   }
-  uint64_t sw = bits(gr ? sum_w<true>(K, dsw) : dsw);
+  uint64_t sw = bits(dsw);
   uint64_t swx = bits(dswx);
   // fixed tree: lane l receives lane l + off
 #pragma unroll
@@ -312,7 +341,7 @@ __device__ __forceinline__ void hub_warp(const OpinionArgs &p, uint32_t r) {
       cnt += ocnt;
     }
   }
-  if (lane == 0) p.xo[r] = cnt ? finish(p.a, p.b, xi, sw, swx) : xi;
+  if (lane == 0) p.xo[r] = cnt ? finish(p, xi, sw, swx) : xi;
 }
 
 // The work of one block of the gather grid: hub warps, then slices (one
@@ -428,6 +457,15 @@ static unsigned opinion_args(Sim &s, int e, int T, double eps, double a, double 
   p.b = b;
   p.eps_lo = (float)(eps - 1e-5);
   p.eps_hi = (float)(eps + 1e-5);
+  auto pow2 = [](double v, int &k) {
+    uint64_t u;
+    std::memcpy(&u, &v, 8);
+    const int ev = (int)(u >> 52);
+    k = ev - 1023;
+    return (u & EMU_M52) == 0 && ev >= 1 && ev <= 2046;  // positive, normal, no fraction bits
+  };
+  p.a_pow2 = pow2(a, p.a_k);
+  p.b_pow2 = pow2(b, p.b_k);
   p.hub_thr = thr;
   if (!v.nedges || T >= (int)es.csr.size() || !v.row_ptr) {
     VG_CUDA(cudaMemcpyAsync(p.xo, p.x, av.n * 8, cudaMemcpyDeviceToDevice, s.stream));

@@ -72,40 +72,38 @@ __global__ void k_selftest(uint64_t n, uint64_t seed, unsigned long long *counts
     uint64_t r2 = emu_mul_fast(a, b, ok2);
     if (ok2 && r2 != hw) atomicAdd(&counts[1], 1ull);
   }
-  // grid sums: 24 weights that are multiples of 2^-53 in (0, 1] (uniform,
-  // tiny, 1.0 and all-ones significands), summed in units of 2^-53 and with
-  // the hardware add; every partial sum must agree
-  {
-    uint64_t K = 0;
-    double d = 0.0;
-    for (int j = 0; j < 24; j++) {
-      Philox4 g = philox_draw(seed, i, 2 + j, 12);
-      uint64_t u = ((uint64_t)g.v[1] << 32 | g.v[0]) >> 11;  // [0, 2^53)
-      switch (g.v[2] % 5) {
-        case 1: u >>= (g.v[3] % 50); break;
-        case 2: u = 1ull << 53; break;
-        case 3: u = (1ull << 53) - 1 - (g.v[3] & 3); break;
-        default: break;
-      }
-      if (u == 0) u = 1;
-      const double w = (double)u * 0x1p-53;  // exact: u < 2^54
-      K = emu_grid_add(K, emu_grid_units(dbits(w)));
-      d = __dadd_rn(d, w);
-      if (dbits(__dmul_rn(__ull2double_rn(K), 0x1p-53)) != dbits(d)) {
-        atomicAdd(&counts[0], 1ull);
-        break;
-      }
-    }
-  }
-  // div (b > 0)
+  // div (b > 0): the general emulation and the gather kernels' form
   if (b) {
     bool ok = true;
     uint64_t r = emu_div_pos(a, b, ok);
+    const uint64_t hw = dbits(__ddiv_rn(bdbl(a), bdbl(b)));
     if (ok) {
-      if (r != dbits(__ddiv_rn(bdbl(a), bdbl(b)))) atomicAdd(&counts[2], 1ull);
+      if (r != hw) atomicAdd(&counts[2], 1ull);
     } else {
       atomicAdd(&counts[5], 1ull);
     }
+    bool ok2 = true;
+    uint64_t r2 = emu_div_fast(a, b, ok2);
+    if (ok2 && r2 != hw) atomicAdd(&counts[2], 1ull);
+  }
+  // the gather kernels' product for a weight that is a multiple of 2^-53 in
+  // (0, 1] (only the other operand's exponent is checked)
+  {
+    Philox4 g = philox_draw(seed, i, 2, 12);
+    uint64_t u = (((uint64_t)g.v[1] << 32 | g.v[0]) >> 11) >> (g.v[2] % 53);
+    if (g.v[3] % 17 == 0) u = 1ull << 53;
+    if (u == 0) u = 1;
+    const double w = (double)u * 0x1p-53;  // exact
+    bool ok = true;
+    uint64_t r = emu_mul_grid(dbits(w), b, ok);
+    if (ok && r != dbits(__dmul_rn(w, bdbl(b)))) atomicAdd(&counts[1], 1ull);
+  }
+  // exact scaling by powers of two
+  {
+    bool ok = true;
+    const int k = (int)(a % 7) - 3;
+    uint64_t r = emu_scale2(b, k, ok);
+    if (ok && r != dbits(__dmul_rn(bdbl(b), ldexp(1.0, k)))) atomicAdd(&counts[1], 1ull);
   }
 }
 
