@@ -8,12 +8,13 @@
 // |x_j - x| < eps adds w_j to sw and w_j * x_j to swx; then
 // x' = a * x + b * (swx / sw), or x when no neighbour qualifies.
 //
-// Degree buckets:
-//   rows with in-degree <= hub_thr: 32 rows (of similar degree) per warp.
-//     The warp stages the rows' edges with coalesced loads, tests and
-//     multiplies edge-parallel, and compacts the accepted edges of each row
-//     into a shared-memory column; the row's lane then folds its column in
-//     edge order -- bit-identical to the sequential binary64 computation.
+// Row classes:
+//   rows with in-degree <= hub_thr, and agents with no in-edge: slices of
+//     32 rows of similar degree (degree-sorted windows) whose edges sit in
+//     a column-major copy of the CSR (SELL-C-sigma, built once per graph by
+//     ensure_schedule): lane l of a warp folds its row's edges in insertion
+//     order while every load of the warp is one coalesced access --
+//     bit-identical to the sequential binary64 computation.
 //   rows above hub_thr ("hubs"): one warp per row, lane l folds the edges
 //     l, l + 32, ... in order and the 32 lane sums are combined in a fixed
 //     tree.  The additions are regrouped, so these rows agree with the
@@ -22,19 +23,16 @@
 //   The hub warps are the first blocks of the grid so that they start
 //   first.
 //
-// Arithmetic placement on GB300 (the FP64 pipe issues about 2 operations
-// per clock per SM; the integer ALU pipe is the next scarcest):
-//   threshold test  float filter of the doubles' high words on the FMA
-//                   pipe; the exact binary64 test only within 1e-5 of eps
+// Arithmetic placement on GB300 (the FP64 pipe executes about 5e11 binary64
+// operations per second, far below the integer pipes):
+//   threshold test  float filter of the opinions' high words; the exact
+//                   binary64 test only within 1e-5 of eps
 //   w_j * x_j       exact round-to-nearest-even product from 32x32-bit
-//                   multiplies (IMAD.WIDE, FMA pipe)
-//   swx += p        the hardware FP64 add (the one FP64 operation per edge)
-//   sw += w         when every weight is a multiple of 2^-53 in (0, 1] (the
-//                   edge type's weights are checked once), sw is kept as an
-//                   integer count K of 2^-53 units and rounded to 53
-//                   significant bits after each addition -- exactly the
-//                   binary64 sum; otherwise the hardware FP64 add
-//   per row         division and mixing as exact integer arithmetic
+//                   multiplies (vg_fp64emu.cuh)
+//   swx += p,       the hardware binary64 adds, branch-free (a rejected
+//   sw += w         edge adds +0): two FP64 operations per edge
+//   per row         exact integer division, exponent scaling for mixing
+//                   weights that are powers of two, one hardware add
 // Every operation is the correctly rounded binary64 result, in the
 // reference's order.
 #include <algorithm>
