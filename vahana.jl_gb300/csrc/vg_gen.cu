@@ -32,8 +32,9 @@ __global__ void k_gen_uniform_out(uint64_t N, uint32_t k, uint64_t seed, int typ
 }
 
 // smallest index i with cdf[i] > u (cdf inclusive prefix sums of weights)
-__device__ __forceinline__ uint64_t sample_cdf(const double *cdf, uint64_t n, double u) {
-  uint64_t lo = 0, hi = n - 1;
+// first i in [lo, hi] with cdf[i] > u, else hi
+__device__ __forceinline__ uint64_t sample_cdf_in(const double *cdf, uint64_t lo, uint64_t hi,
+                                                  double u) {
   while (lo < hi) {
     uint64_t mid = (lo + hi) >> 1;
     if (cdf[mid] > u) hi = mid; else lo = mid + 1;
@@ -41,16 +42,42 @@ __device__ __forceinline__ uint64_t sample_cdf(const double *cdf, uint64_t n, do
   return lo;
 }
 
+__device__ __forceinline__ uint64_t sample_cdf(const double *cdf, uint64_t n, double u) {
+  return sample_cdf_in(cdf, 0, n - 1, u);
+}
+
+// guide table: guide[b] = sample_cdf(b * total / G), b = 0..G.  The sample
+// of u lies between the entries of the buckets around u * G / total
+// (widened by one bucket on each side against rounding of the bucket
+// index), so the search over that range returns the full search's index.
+constexpr uint32_t GUIDE_BITS = 20;
+__global__ void k_cdf_guide(const double *cdf, uint64_t n, double total, uint32_t *guide) {
+  uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint64_t G = 1ull << GUIDE_BITS;
+  if (b > G) return;
+  guide[b] = (uint32_t)sample_cdf(cdf, n, (double)b * (total / (double)G));
+}
+
+__device__ __forceinline__ uint64_t sample_guided(const double *cdf, const uint32_t *guide,
+                                                  double total, double u) {
+  const uint64_t G = 1ull << GUIDE_BITS;
+  double fb = u * ((double)G / total);
+  uint64_t b = fb <= 0.0 ? 0 : (fb >= (double)G ? G - 1 : (uint64_t)fb);
+  const uint64_t lo = guide[b > 0 ? b - 1 : 0];
+  const uint64_t hi = guide[b + 2 <= G ? b + 2 : G];
+  return sample_cdf_in(cdf, lo, hi, u);
+}
+
 // directed Chung-Lu: edge e draws source and target proportional to the
 // expected degrees and a weight in (0, 1]
-__global__ void k_gen_chung_lu(uint64_t E, const double *cdf, uint64_t N, double total,
-                               uint64_t seed, int type_nr, uint64_t first_nr, uint64_t *from,
-                               uint64_t *to, double *w) {
+__global__ void k_gen_chung_lu(uint64_t E, const double *cdf, const uint32_t *guide,
+                               double total, uint64_t seed, int type_nr, uint64_t first_nr,
+                               uint64_t *from, uint64_t *to, double *w) {
   uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= E) return;
   double us = u64_to_unit(philox_u64(philox_draw(seed, e, 0, TAG_SRC))) * total;
   double ud = u64_to_unit(philox_u64(philox_draw(seed, e, 0, TAG_DST))) * total;
-  uint64_t s = sample_cdf(cdf, N, us), d = sample_cdf(cdf, N, ud);
+  uint64_t s = sample_guided(cdf, guide, total, us), d = sample_guided(cdf, guide, total, ud);
   from[e] = ((uint64_t)type_nr << SHIFT_TYPE) | (first_nr + s);
   to[e] = ((uint64_t)type_nr << SHIFT_TYPE) | (first_nr + d);
   if (w) w[e] = u64_to_unit_open0(philox_u64(philox_draw(seed, e, 0, TAG_WEIGHT)));
@@ -179,10 +206,15 @@ int vg_gen_chung_lu_edges(vg_sim *h, int e, int type_nr, uint64_t nedges, double
       fail(VG_ERR_ARG, "weight field must be a Float64 edge field");
     wp = seg.d_payload[weight_field].as<double>();
   }
-  k_gen_chung_lu<<<nblk(nedges), TPB, 0, s.stream>>>(nedges, d_cdf, N, acc, seed, type_nr, 1,
+  uint32_t *d_guide = nullptr;
+  const uint64_t G = 1ull << GUIDE_BITS;
+  VG_CUDA(cudaMallocAsync((void **)&d_guide, (G + 1) * 4, s.stream));
+  k_cdf_guide<<<nblk(G + 1), TPB, 0, s.stream>>>(d_cdf, N, acc, d_guide);
+  k_gen_chung_lu<<<nblk(nedges), TPB, 0, s.stream>>>(nedges, d_cdf, d_guide, acc, seed, type_nr, 1,
                                                      seg.d_from.as<uint64_t>(),
                                                      seg.d_to.as<uint64_t>(), wp);
   VG_CUDA(cudaGetLastError());
+  VG_CUDA(cudaFreeAsync(d_guide, s.stream));
   VG_CUDA(cudaFreeAsync(d_cdf, s.stream));
   VG_CUDA(cudaStreamSynchronize(s.stream));
   API_END

@@ -32,16 +32,25 @@ __global__ void k_type_hist(const uint64_t *to, const uint64_t *from, uint64_t n
   if (threadIdx.x < MAX_AGENT_TYPES) sc[threadIdx.x] = 0;
   if (threadIdx.x == 0) sm = 0;
   __syncthreads();
-  unsigned mymask = 0;
+  // records mostly share one target type: count runs of equal types in a
+  // register and flush a run to shared memory when the type changes
+  unsigned mymask = 0, run_t = 0xFFFFFFFFu;
+  unsigned long long run_n = 0;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (uint64_t)gridDim.x * blockDim.x) {
     unsigned t = (unsigned)(to[i] >> SHIFT_TYPE);
-    if (t < MAX_AGENT_TYPES) atomicAdd(&sc[t], 1ull);
+    if (t != run_t) {
+      if (run_n && run_t < MAX_AGENT_TYPES) atomicAdd(&sc[run_t], run_n);
+      run_t = t;
+      run_n = 0;
+    }
+    run_n++;
     if (from) {
       unsigned f = (unsigned)(from[i] >> SHIFT_TYPE);
       if (f < 32) mymask |= 1u << f;
     }
   }
+  if (run_n && run_t < MAX_AGENT_TYPES) atomicAdd(&sc[run_t], run_n);
   if (mymask) atomicOr(&sm, mymask);
   __syncthreads();
   if (threadIdx.x < MAX_AGENT_TYPES && sc[threadIdx.x])
