@@ -469,9 +469,12 @@ def run_serve(args):
                     ids.append(S.submit(spec))
             th = threading.Thread(target=feeder)
             th.start()
+            deadline = time.perf_counter() + 1800
             while len(results) < len(specs):
                 for r in S.poll():
                     results[r["id"]] = r
+                if time.perf_counter() > deadline:
+                    raise RuntimeError("serving stream did not finish within 30 minutes")
                 time.sleep(0.002)
             th.join()
             stats = S.stats()

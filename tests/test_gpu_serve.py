@@ -4,7 +4,7 @@ through apply! (bit-identical, both models), whatever the admission budget."""
 import numpy as np
 import pytest
 
-pytestmark = pytest.mark.gpu
+pytestmark = [pytest.mark.gpu, pytest.mark.timeout(600)]
 
 
 def _alone(spec):

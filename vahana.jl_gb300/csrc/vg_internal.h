@@ -327,6 +327,7 @@ struct OpinionJob {
 };
 void launch_opinion_jobs(const std::vector<OpinionJob> &jobs, cudaStream_t st, DevBuf &args_buf,
                          DevBuf &tiles_buf, uint64_t *footprint);
+void prepare_opinion_job(const OpinionJob &job);
 // initial SIR state: the n_inf agents with the smallest Philox init draw
 void sir_initial_state(uint64_t n, uint64_t seed, uint64_t n_inf, std::vector<uint8_t> &state);
 

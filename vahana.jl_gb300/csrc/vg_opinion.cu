@@ -397,7 +397,7 @@ __global__ void k_check_grid(const double *w, uint64_t n, int *bad) {
 }  // namespace
 
 static unsigned opinion_args(Sim &s, int e, int T, double eps, double a, double b,
-                             uint32_t thr, OpinionArgs &p);
+                             uint32_t thr, OpinionArgs &p, cudaStream_t launch_stream);
 
 // apply!(sim, bounded_confidence, [T], [T, E], [T]; params = [E, eps, a, b,
 // hub_thr]); defaults eps 0.3, a 0.5, b 1 - a, hub_thr 256.
@@ -425,7 +425,7 @@ void tr_bounded_confidence(ApplyCtx &c) {
   double thr_d = c.param(4, 256);
   uint32_t thr = thr_d >= 4294967295.0 ? 0xffffffffu : (uint32_t)thr_d;
   OpinionArgs p{};
-  unsigned grid = opinion_args(s, e, c.call_type, eps, a, b, thr, p);
+  unsigned grid = opinion_args(s, e, c.call_type, eps, a, b, thr, p, s.stream);
   if (!grid) return;
   if (p.grid) k_opinion<true><<<grid, TPB, 0, s.stream>>>(p);
   else k_opinion<false><<<grid, TPB, 0, s.stream>>>(p);
@@ -433,9 +433,10 @@ void tr_bounded_confidence(ApplyCtx &c) {
 }
 
 // arguments and grid size of one simulation's gather launch; 0 when there
-// is nothing to launch (no agents, or no edges: then x' = x, copied here)
+// is nothing to launch (no agents, or no edges: then x' = x, copied here on
+// the stream the launch would use)
 static unsigned opinion_args(Sim &s, int e, int T, double eps, double a, double b,
-                             uint32_t thr, OpinionArgs &p) {
+                             uint32_t thr, OpinionArgs &p, cudaStream_t launch_stream) {
   EdgeStore &es = s.edges[e];
   DevCSRView v = csr_view(s, e, T);
   if (v.nedges && v.src_type_const != T)
@@ -466,7 +467,7 @@ static unsigned opinion_args(Sim &s, int e, int T, double eps, double a, double 
   p.b_pow2 = pow2(b, p.b_k);
   p.hub_thr = thr;
   if (!v.nedges || T >= (int)es.csr.size() || !v.row_ptr) {
-    VG_CUDA(cudaMemcpyAsync(p.xo, p.x, av.n * 8, cudaMemcpyDeviceToDevice, s.stream));
+    VG_CUDA(cudaMemcpyAsync(p.xo, p.x, av.n * 8, cudaMemcpyDeviceToDevice, launch_stream));
     return 0;
   }
   CSR &cs = es.csr[T];
@@ -496,6 +497,16 @@ static unsigned opinion_args(Sim &s, int e, int T, double eps, double a, double 
   return p.hub_blocks + (unsigned)((cs.nslices + (TPB / 32) - 1) / (TPB / 32));
 }
 
+// Builds what a job's launches need ahead of its first step (the weight
+// check and the gather layout), on the simulation's own stream.
+void prepare_opinion_job(const OpinionJob &j) {
+  OpinionArgs p{};
+  DevCSRView v = csr_view(*j.sim, j.edge_type, j.type_nr);
+  if (v.nedges == 0) return;  // nothing to prepare (and no copy to queue)
+  opinion_args(*j.sim, j.edge_type, j.type_nr, j.eps, j.a, j.b, j.hub_thr, p, j.sim->stream);
+  VG_CUDA(cudaStreamSynchronize(j.sim->stream));
+}
+
 // One launch for the bounded-confidence step of many simulations (the
 // serving loop's continuous batching).  Each job's blocks do exactly what
 // its own launch would; the caller finishes each job's transition.
@@ -506,7 +517,7 @@ void launch_opinion_jobs(const std::vector<OpinionJob> &jobs, cudaStream_t st, D
   for (size_t j = 0; j < jobs.size(); j++) {
     OpinionArgs p{};
     unsigned g = opinion_args(*jobs[j].sim, jobs[j].edge_type, jobs[j].type_nr, jobs[j].eps,
-                              jobs[j].a, jobs[j].b, jobs[j].hub_thr, p);
+                              jobs[j].a, jobs[j].b, jobs[j].hub_thr, p, st);
     args.push_back(p);
     for (unsigned k = 0; k < g; k++) tiles.push_back({(uint32_t)j, k});
   }

@@ -112,21 +112,34 @@ __global__ void k_sir_jobs(const SirJobDesc *jobs, const SirTile *tiles, int *st
 
 }  // namespace
 
+// Threads: one worker admits jobs and ticks the resident ones on the
+// server's stream; BUILDERS builder threads (each with its own stream) build
+// admitted jobs -- graph generation, CSR and gather layout -- while the
+// worker keeps ticking, and hand them over through `ready`.
+constexpr int BUILDERS = 4;
+
 struct vg_server {
   std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
   uint64_t budget = 0, used = 0;
   int max_active = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t build_stream[BUILDERS] = {};
   vg_model *sir_model = nullptr, *op_model = nullptr;
   int sir_person = 0, sir_contact = 0, op_agent = 0, op_edge = 0;
   std::thread worker;
+  std::thread builders[BUILDERS];
   std::mutex mu;
-  std::condition_variable cv;
-  bool stop = false;
+  std::condition_variable cv;        // worker: submissions, finished builds
+  std::condition_variable build_cv;  // builders: admitted jobs
+  bool stop = false;           // no more submissions: finish every job, then exit
+  bool builders_stop = false;  // set once the worker has exited
   std::string error;
   int64_t next_id = 1;
-  std::deque<Job *> queue;
-  std::vector<Job *> active;
+  std::deque<Job *> queue;      // submitted, not admitted
+  std::deque<Job *> to_build;   // admitted, not yet picked by a builder
+  int building = 0;             // picked by a builder
+  std::vector<Job *> ready;     // built, not yet resident
+  std::vector<Job *> active;    // resident: stepped every tick
   std::vector<Job *> done;
   uint64_t ticks = 0, sim_steps = 0;
   uint64_t footprint = 0;
@@ -144,11 +157,11 @@ uint64_t estimate_bytes(const vg_job_spec &s) {
   return (uint64_t)(16 * n + 12 * n + 12 * e + 40 * e) + (1 << 20);
 }
 
-void build_job(vg_server *S, Job *J) {
+void build_job(vg_server *S, Job *J, cudaStream_t bst) {
   int rc;
   const vg_job_spec &sp = J->spec;
   if (sp.model == 0) {
-    if ((rc = vg_sim_create(S->sir_model, "job", S->stream, &J->sim))) fail(rc, vg_last_error());
+    if ((rc = vg_sim_create(S->sir_model, "job", bst, &J->sim))) fail(rc, vg_last_error());
     std::vector<uint8_t> st;
     uint64_t ninf = (uint64_t)std::max<double>(1.0, std::nearbyint((double)sp.n / 1000.0));
     sir_initial_state(sp.n, sp.seed, ninf, st);
@@ -168,12 +181,12 @@ void build_job(vg_server *S, Job *J) {
       q = q * om;
       tab[k] = 1.0 - q;
     }
-    J->ptab.alloc(tab.size() * 8, &S->footprint);
-    VG_CUDA(cudaMemcpyAsync(J->ptab.p, tab.data(), tab.size() * 8, cudaMemcpyHostToDevice, S->stream));
-    VG_CUDA(cudaStreamSynchronize(S->stream));
+    J->ptab.alloc(tab.size() * 8, &s.footprint);
+    VG_CUDA(cudaMemcpyAsync(J->ptab.p, tab.data(), tab.size() * 8, cudaMemcpyHostToDevice, bst));
+    VG_CUDA(cudaStreamSynchronize(bst));
     J->ptab_n = (uint32_t)tab.size();
   } else {
-    if ((rc = vg_sim_create(S->op_model, "job", S->stream, &J->sim))) fail(rc, vg_last_error());
+    if ((rc = vg_sim_create(S->op_model, "job", bst, &J->sim))) fail(rc, vg_last_error());
     std::vector<double> x(sp.n);
     for (uint64_t i = 0; i < sp.n; i++)
       x[i] = u64_to_unit(philox_u64(philox_draw(sp.seed, i + 1, 0, TAG_INIT)));
@@ -184,6 +197,7 @@ void build_job(vg_server *S, Job *J) {
                                     sp.wmax, sp.seed, 0)))
       fail(rc, vg_last_error());
     if ((rc = vg_finish_init(J->sim))) fail(rc, vg_last_error());
+    prepare_opinion_job({J->sim->s.get(), S->op_edge, S->op_agent, J->spec.eps, 0.5, 0.5, 256});
   }
 }
 
@@ -220,9 +234,9 @@ void retire_job(vg_server *S, Job *J) {
   }
   r.checksum = fnv1a(bytes.data(), bytes.size());
   if (J->spec.keep_state) J->final_state = std::move(bytes);
+  J->ptab.release();  // before the simulation whose byte counter it updates
   vg_sim_destroy(J->sim);
   J->sim = nullptr;
-  J->ptab.release();
   r.finish_s = now_s(S->t0);
   J->finish = r.finish_s;
 }
@@ -296,34 +310,75 @@ void tick(vg_server *S) {
   S->sim_steps += stepping.size();
 }
 
+void fail_server(vg_server *S, const std::string &msg) {
+  std::lock_guard<std::mutex> lk(S->mu);
+  if (S->error.empty()) S->error = msg;
+  S->stop = true;
+  S->builders_stop = true;
+  S->cv.notify_all();
+  S->build_cv.notify_all();
+}
+
+void builder_loop(vg_server *S, int b) {
+  try {
+    VG_CUDA(cudaSetDevice(0));
+    while (true) {
+      Job *J = nullptr;
+      {
+        std::unique_lock<std::mutex> lk(S->mu);
+        // builders outlive the worker's admissions: they leave only after the
+        // worker has exited (or on an error)
+        S->build_cv.wait(lk, [&] { return !S->to_build.empty() || S->builders_stop; });
+        if (S->to_build.empty()) return;
+        J = S->to_build.front();
+        S->to_build.pop_front();
+        S->building++;
+      }
+      build_job(S, J, S->build_stream[b]);
+      {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->building--;
+        S->ready.push_back(J);
+      }
+      S->cv.notify_one();
+    }
+  } catch (const Error &e) {
+    fail_server(S, e.msg);
+  }
+}
+
 void worker_loop(vg_server *S) {
   try {
     VG_CUDA(cudaSetDevice(0));
     while (true) {
-      std::vector<Job *> admit;
+      std::vector<Job *> arrived;
       {
         std::unique_lock<std::mutex> lk(S->mu);
-        if (S->stop && S->queue.empty() && S->active.empty()) break;
+        if (!S->error.empty()) return;
+        // admission, first come first served, by estimated footprint
+        bool admitted = false;
         while (!S->queue.empty()) {
           Job *J = S->queue.front();
-          bool fits = S->used + J->est_bytes <= S->budget &&
-                      (int)(S->active.size() + admit.size()) < S->max_active;
-          bool alone = S->active.empty() && admit.empty();  // a lone job always runs
+          const size_t inflight = S->active.size() + S->ready.size() + S->to_build.size() +
+                                  (size_t)S->building;
+          bool fits = S->used + J->est_bytes <= S->budget && (int)inflight < S->max_active;
+          bool alone = inflight == 0;  // a lone job always runs
           if (!fits && !alone) break;
           S->queue.pop_front();
           S->used += J->est_bytes;
-          admit.push_back(J);
+          J->admit = now_s(S->t0);
+          S->to_build.push_back(J);
+          admitted = true;
         }
-        if (admit.empty() && S->active.empty()) {
+        if (admitted) S->build_cv.notify_all();
+        arrived.swap(S->ready);
+        if (arrived.empty() && S->active.empty()) {
+          if (S->stop && S->queue.empty() && S->to_build.empty() && S->building == 0) break;
           S->cv.wait_for(lk, std::chrono::milliseconds(2));
           continue;
         }
       }
-      for (Job *J : admit) {
-        J->admit = now_s(S->t0);
-        build_job(S, J);
-        S->active.push_back(J);
-      }
+      for (Job *J : arrived) S->active.push_back(J);
       tick(S);
       std::vector<Job *> still, finished;
       for (Job *J : S->active) (J->done_steps >= J->spec.steps ? finished : still).push_back(J);
@@ -338,9 +393,7 @@ void worker_loop(vg_server *S) {
       }
     }
   } catch (const Error &e) {
-    std::lock_guard<std::mutex> lk(S->mu);
-    S->error = e.msg;
-    S->stop = true;
+    fail_server(S, e.msg);
   }
 }
 
@@ -389,8 +442,11 @@ int vg_serve_create(uint64_t budget_bytes, int max_active, vg_server **out) {
     fail(rc, vg_last_error());
   S->status.alloc(16, &S->footprint);
   VG_CUDA(cudaMemset(S->status.p, 0, 16));
+  for (int b = 0; b < BUILDERS; b++)
+    VG_CUDA(cudaStreamCreateWithFlags(&S->build_stream[b], cudaStreamNonBlocking));
   vg_server *raw = S.release();
   raw->worker = std::thread(worker_loop, raw);
+  for (int b = 0; b < BUILDERS; b++) raw->builders[b] = std::thread(builder_loop, raw, b);
   *out = raw;
   API_END
 }
@@ -463,14 +519,25 @@ int vg_serve_stats(vg_server *S, uint64_t *queued, uint64_t *active, uint64_t *d
 }
 
 // stop accepting, finish every queued and resident job, join the worker
-int vg_serve_drain(vg_server *S) {
-  API_BEGIN
+static void stop_threads(vg_server *S) {
   {
     std::lock_guard<std::mutex> lk(S->mu);
     S->stop = true;
   }
-  S->cv.notify_one();
-  if (S->worker.joinable()) S->worker.join();
+  S->cv.notify_all();
+  if (S->worker.joinable()) S->worker.join();  // every admitted job built, stepped, retired
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->builders_stop = true;
+  }
+  S->build_cv.notify_all();
+  for (auto &t : S->builders)
+    if (t.joinable()) t.join();
+}
+
+int vg_serve_drain(vg_server *S) {
+  API_BEGIN
+  stop_threads(S);
   if (!S->error.empty()) fail(VG_ERR_DEVICE, "server stopped: " + S->error);
   API_END
 }
@@ -478,23 +545,24 @@ int vg_serve_drain(vg_server *S) {
 int vg_serve_destroy(vg_server *S) {
   API_BEGIN
   if (!S) return VG_OK;
-  {
-    std::lock_guard<std::mutex> lk(S->mu);
-    S->stop = true;
-  }
-  S->cv.notify_one();
-  if (S->worker.joinable()) S->worker.join();
-  for (Job *J : S->queue) delete J;
-  for (Job *J : S->active) {
-    if (J->sim) vg_sim_destroy(J->sim);
-    delete J;
-  }
+  stop_threads(S);
+  for (auto *q : {&S->queue, &S->to_build})
+    for (Job *J : *q) delete J;
+  for (auto *v : {&S->ready, &S->active})
+    for (Job *J : *v) {
+      J->ptab.release();
+      if (J->sim) vg_sim_destroy(J->sim);
+      delete J;
+    }
   for (Job *J : S->done) delete J;
   vg_model_destroy(S->sir_model);
   vg_model_destroy(S->op_model);
   cudaStream_t st = S->stream;
+  cudaStream_t bst[BUILDERS];
+  for (int b = 0; b < BUILDERS; b++) bst[b] = S->build_stream[b];
   delete S;
   cudaStreamDestroy(st);
+  for (int b = 0; b < BUILDERS; b++) cudaStreamDestroy(bst[b]);
   API_END
 }
 
