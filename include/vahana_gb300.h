@@ -173,6 +173,17 @@ int vg_push_global(vg_sim *s, const char *name, double v);
 int vg_global_series(vg_sim *s, const char *name, double *out, uint64_t cap,
                      uint64_t *n_out);
 
+/* Checkpoint / restore of an initialized simulation (the reference's
+ * write_snapshot / read_snapshot!, src/HDF5.jl:688-715, 1594-1660, write
+ * HDF5; this is the library's own binary format, no HDF5 library is used).
+ * The file holds every agent type's read state, died flags, reuse stack
+ * and nextid, every edge type's CSR (or implicit stencil), rasters, params,
+ * globals and num_transitions, with a fingerprint of the model: loading
+ * into a different model fails with VG_ERR_ASSERT.  A loaded simulation
+ * continues bit-identically to the saved one. */
+int vg_sim_save(vg_sim *s, const char *path);
+int vg_sim_load(vg_model *m, const char *path, void *stream, vg_sim **out);
+
 /* ---- agents ------------------------------------------------------------ */
 /* add_agents!(sim, agents) / add_agent! -- src/Agent.jl:174-180,
  * src/AgentMethods.jl:65-89.  fields[i] points to n values of field i
@@ -207,6 +218,17 @@ int vg_agent_field_device_ptr(vg_sim *s, int type_nr, int field, void **out);
  * types).  Edges are appended in array order. */
 int vg_add_edges(vg_sim *s, int edge_type, uint64_t n, const uint64_t *from,
                  const uint64_t *to, const void *const *payload);
+/* add_graph!(sim, graph, agent_constructor, edge_constructor) --
+ * src/GraphsSupport.jl:34-57, before finish_init!.  The graph's nv vertices
+ * become agents of type_nr (fields: nv values per field, vertex order);
+ * its ne edges, in the graph's edge order as 1-based vertex numbers
+ * src[k] -> dst[k] with payload columns of ne values, are added as
+ * add_edge!(agent[src], agent[dst]) and, when directed == 0, then
+ * add_edge!(agent[dst], agent[src]) with the same state.  ids_out (nv
+ * entries, may be NULL) receives the agents' ids. */
+int vg_add_graph(vg_sim *s, int type_nr, uint64_t nv, const void *const *fields,
+                 int edge_type, uint64_t ne, const uint64_t *src, const uint64_t *dst,
+                 int directed, const void *const *payload, uint64_t *ids_out);
 /* remove_edges!(sim, to, T) and remove_edges!(sim, from, to, T) --
  * src/EdgeMethods.jl:527-599.  from may be NULL (remove all edges to `to`). */
 int vg_remove_edges(vg_sim *s, int edge_type, uint64_t n, const uint64_t *from,

@@ -489,21 +489,50 @@ def test_raster_move_to_counts(vh):
 
 
 # ---------------------------------------------------------- test/graphs.jl
+def complete_graph_edges(n):
+    """Edges of SimpleGraphs.complete_graph(n) in Graphs.jl's order."""
+    return [(i, j) for i in range(1, n + 1) for j in range(i + 1, n + 1)]
+
+
 def test_complete_graph_sum(vh):
-    """test/graphs.jl:237-266"""
+    """test/graphs.jl:16-45: add_graph! of an undirected complete graph"""
     m = (vh.ModelTypes().register_agenttype("GraphA", [("id", "i64"), ("sum", "i64")])
          .register_edgetype("GraphE", []).create_model("g"))
     sim = vh.create_simulation(m)
     n = 4
-    ids = vh.add_agents(sim, "GraphA", n, id=np.arange(1, n + 1), sum=0)
-    for a in range(n):
-        for b in range(a + 1, n):
-            vh.add_edge(sim, ids[a], ids[b], "GraphE")
-            vh.add_edge(sim, ids[b], ids[a], "GraphE")
+    src, dst = zip(*complete_graph_edges(n))
+    ids = vh.add_graph(sim, "GraphA", "GraphE", n, src, dst, directed=False,
+                       agent_fields={"id": np.arange(1, n + 1), "sum": 0})
+    assert [nr(i) for i in ids] == [1, 2, 3, 4]
+    # both directions of each graph edge, src -> dst first
+    assert vh.num_edges(sim, "GraphE", write=True) == n * (n - 1)
     vh.finish_init(sim)
     vh.apply_(sim, "neighbor_sum", ["GraphA"], ["GraphA", "GraphE"], ["GraphA"],
               params=[m["GraphE"].index, 0, 1])
     assert vh.mapreduce(sim, "sum", "+", "GraphA") == sum(range(1, n + 1)) * (n - 1)
+    vh.disable_transition_checks(sim, True)
+    assert [nr(x) for x in vh.neighborids(sim, ids[0], "GraphE")] == [2, 3, 4]
+    assert [nr(x) for x in vh.neighborids(sim, ids[2], "GraphE")] == [1, 2, 4]
+    sim.close()
+
+
+@pytest.mark.parametrize("ET", ["EdgeD", "EdgeE", "EdgeT", "EdgeI", "EdgeEI", "EdgeTI"])
+def test_add_graph_edge_types(vh, ET):
+    """test/edges.jl:319-345: add_graph! of complete_graph(2) with the edge
+    state ET(e.dst); every agent has nagents - 1 edges, twice"""
+    m = edges_model(vh)
+    if m.has_hint(ET, ":SingleEdge"):
+        pytest.skip("the reference test skips :SingleEdge types")
+    e = m[ET].index
+    sim = vh.create_simulation(m)
+    nagents = 2
+    src, dst = zip(*complete_graph_edges(nagents))
+    vh.add_graph(sim, "Agent", ET, nagents, src, dst, directed=False,
+                 agent_fields={"foo": np.arange(1, nagents + 1)}, edge_fields=st(ET, np.array(dst)))
+    vh.finish_init(sim)
+    for _ in range(2):
+        vh.apply_(sim, "count_edges", ["Agent"], [ET], ["Agent"], params=[e, 0, 0])
+        assert list(vh.read_agents(sim, "Agent")[0]["foo"]) == [nagents - 1] * nagents
     sim.close()
 
 

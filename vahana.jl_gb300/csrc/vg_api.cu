@@ -896,6 +896,63 @@ int vg_add_edges(vg_sim *h, int e, uint64_t n, const uint64_t *from,
   API_END
 }
 
+int vg_add_graph(vg_sim *h, int type_nr, uint64_t nv, const void *const *fields, int e,
+                 uint64_t ne, const uint64_t *src, const uint64_t *dst, int directed,
+                 const void *const *payload, uint64_t *ids_out) {
+  API_BEGIN
+  Sim &s = S(h);
+  const EdgeTypeDesc &ed = s.model->et(e);
+  if (s.initialized)
+    fail(VG_ERR_ASSERT, "add_graph! adds agents: only in the initialization phase (until "
+                        "`finish_init!` is called).");
+  for (uint64_t k = 0; k < ne; k++)
+    if (src[k] < 1 || src[k] > nv || dst[k] < 1 || dst[k] > nv)
+      fail(VG_ERR_ARG, "graph edge " + std::to_string(k + 1) + " names a vertex outside 1.." +
+                           std::to_string(nv));
+  std::vector<uint64_t> ids(nv);
+  int rc = vg_add_agents(h, type_nr, nv, fields, ids.data());
+  if (rc) fail(rc, vg_last_error());
+  // for each graph edge in order: add_edge!(src, dst) and, undirected,
+  // add_edge!(dst, src) with the same state
+  const uint64_t m = directed ? ne : 2 * ne;
+  std::vector<uint64_t> from(m), to(m);
+  const int nf = ed.stores_payload() ? (int)ed.fields.size() : 0;
+  std::vector<std::vector<uint8_t>> cols(nf);
+  std::vector<const void *> pl(nf);
+  for (int f = 0; f < nf; f++) {
+    const size_t sz = ed.fields[f].size;
+    cols[f].resize(m * sz);
+    for (uint64_t k = 0; k < ne; k++) {
+      const uint8_t *v = (const uint8_t *)payload[f] + k * sz;
+      if (directed) {
+        std::memcpy(cols[f].data() + k * sz, v, sz);
+      } else {
+        std::memcpy(cols[f].data() + 2 * k * sz, v, sz);
+        std::memcpy(cols[f].data() + (2 * k + 1) * sz, v, sz);
+      }
+    }
+    pl[f] = cols[f].data();
+  }
+  for (uint64_t k = 0; k < ne; k++) {
+    const uint64_t a = ids[src[k] - 1], b = ids[dst[k] - 1];
+    if (directed) {
+      from[k] = a;
+      to[k] = b;
+    } else {
+      from[2 * k] = a;
+      to[2 * k] = b;
+      from[2 * k + 1] = b;
+      to[2 * k + 1] = a;
+    }
+  }
+  if (m) {
+    rc = vg_add_edges(h, e, m, from.data(), to.data(), nf ? pl.data() : nullptr);
+    if (rc) fail(rc, vg_last_error());
+  }
+  if (ids_out) std::memcpy(ids_out, ids.data(), nv * 8);
+  API_END
+}
+
 int vg_remove_edges(vg_sim *h, int e, uint64_t n, const uint64_t *from,
                     const uint64_t *to) {
   API_BEGIN

@@ -141,6 +141,9 @@ SIGNATURES = {
     "vg_batch_destroy": (I, [P]),
     "vg_batch_read_states2": (I, [P, I, I, C.POINTER(C.c_uint8), C.POINTER(C.c_int32), U64, PU64]),
     "vg_batch_info": (I, [P, PU64, PU64, PI, PI, PU64]),
+    "vg_add_graph": (I, [P, I, U64, PP, I, U64, PU64, PU64, I, PP, PU64]),
+    "vg_sim_save": (I, [P, CP]),
+    "vg_sim_load": (I, [P, CP, P, C.POINTER(P)]),
     "vg_serve_create": (I, [U64, I, C.POINTER(P)]),
     "vg_serve_submit": (I, [P, P, PI64]),
     "vg_serve_poll": (I, [P, P, U64, PU64]),

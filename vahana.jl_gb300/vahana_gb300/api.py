@@ -9,6 +9,7 @@ library, named by string (`transition_names()` lists them).
 Errors: where the reference raises AssertionError, so does this module.
 """
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -201,6 +202,21 @@ def copy_simulation(sim):
     c = Simulation(sim.model, name=sim.name, _handle=h)
     c.rasters = dict(sim.rasters)
     return c
+
+
+def save_simulation(sim, path):
+    """Checkpoint of an initialized simulation (the role of write_snapshot,
+    src/HDF5.jl:688-715; the library's own file format)."""
+    check(lib().vg_sim_save(sim._h, os.fsencode(path)))
+
+
+def load_simulation(model, path, stream=None):
+    """Restore a checkpoint written by save_simulation for the same model
+    (the role of read_snapshot!, src/HDF5.jl:1594-1660)."""
+    h = C.c_void_p()
+    check(lib().vg_sim_load(model.types._h, os.fsencode(path),
+                            C.c_void_p(stream) if stream else None, C.byref(h)))
+    return Simulation(model, _handle=h)
 
 
 def finish_init(sim):
@@ -410,6 +426,30 @@ def add_edges(sim, T, frm, to, **payload):
 def add_edge(sim, frm, to, T, **payload):
     """add_edge!(sim, from, to, state)"""
     add_edges(sim, T, [frm], [to], **payload)
+
+
+def add_graph(sim, T, E, nv, src, dst, directed=True, agent_fields=None, edge_fields=None):
+    """add_graph!(sim, graph, agent_constructor, edge_constructor) --
+    src/GraphsSupport.jl:34-57.  nv vertices become agents of type T
+    (agent_fields: name -> nv values, or a constant); the edges src[k] ->
+    dst[k] (1-based vertex numbers, in the graph's edge order) become edges
+    of type E with edge_fields (name -> one value per graph edge, or a
+    constant); an undirected graph adds both directions, src -> dst first.
+    Returns the new agents' ids."""
+    t, e = sim.T(T), sim.T(E)
+    src = np.ascontiguousarray(np.asarray(src, dtype=np.uint64).ravel())
+    dst = np.ascontiguousarray(np.asarray(dst, dtype=np.uint64).ravel())
+    if src.size != dst.size:
+        raise ValueError("src and dst differ in length")
+    acols, aptrs = _columns(t, nv, agent_fields or {})
+    ecols, eptrs = _columns(e, src.size, edge_fields or {})
+    ids = np.zeros(nv, dtype=np.uint64)
+    check(lib().vg_add_graph(sim._h, t.index, nv, aptrs, e.index, src.size,
+                             src.ctypes.data_as(C.POINTER(C.c_uint64)),
+                             dst.ctypes.data_as(C.POINTER(C.c_uint64)), 1 if directed else 0,
+                             eptrs if e.fields else None,
+                             ids.ctypes.data_as(C.POINTER(C.c_uint64))))
+    return ids
 
 
 def remove_edges(sim, to, T, frm=None):
@@ -698,9 +738,18 @@ def cellid(sim, name, pos):
     return np.uint64(out.value)
 
 
+def _raster_dims(sim, name):
+    if name not in sim.rasters:  # e.g. a simulation restored from a checkpoint
+        dims = (C.c_int64 * 4)()
+        nd = C.c_int()
+        check(lib().vg_raster_dims(sim._h, name.encode(), dims, C.byref(nd)))
+        sim.rasters[name] = tuple(dims[k] for k in range(nd.value))
+    return sim.rasters[name]
+
+
 def rastervalues(sim, name, field):
     """rastervalues(sim, name, field) -- src/Raster.jl:353-387 (array of shape dims)"""
-    dims = sim.rasters[name]
+    dims = _raster_dims(sim, name)
     ids = cellid(sim, name, [1] * len(dims))
     t = [x for x in sim.model.types.agent_types if x.index == type_nr(ids)][0]
     f = t.field_index(field)
