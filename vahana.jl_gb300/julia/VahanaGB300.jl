@@ -20,7 +20,8 @@ export ModelTypes, register_agenttype!, register_edgetype!, register_param!,
        neighborstates, edgestates, num_edges, has_edge, num_agents, all_agents,
        all_agentids, add_raster!, connect_raster_neighbors!, move_to!, cellid,
        rastervalues, calc_rasterstate, param, set_param!, get_global, set_global!,
-       push_global!, disable_transition_checks, transition_names, Edge, AgentID
+       push_global!, disable_transition_checks, transition_names, Edge, AgentID,
+       add_graph!, remove_edges!, add_agent_per_process!, write_snapshot, read_snapshot
 
 const LIB = get(ENV, "VAHANA_GB300_LIB",
                 joinpath(@__DIR__, "..", "libvahana_gb300.so"))
@@ -408,8 +409,18 @@ function cellid(sim::Simulation, name::Symbol, pos)
 end
 
 "rastervalues(sim, name, field) -- src/Raster.jl:353-387"
+function raster_dims(sim::Simulation, name::Symbol)
+    get!(sim.rasters, name) do  # a simulation read from a snapshot knows no names yet
+        d = zeros(Int64, 4)
+        nd = Ref{Cint}(0)
+        check(ccall((:vg_raster_dims, LIB), Cint, (Ptr{Cvoid}, Cstring, Ptr{Int64}, Ptr{Cint}),
+                    sim.h, String(name), d, nd))
+        Tuple(d[1:nd[]])
+    end
+end
+
 function rastervalues(sim::Simulation, name::Symbol, field::Symbol)
-    dims = sim.rasters[name]
+    dims = raster_dims(sim, name)
     T = agentstate_type(sim, cellid(sim, name, ntuple(_ -> 1, length(dims))))
     FT = fieldtype(T, field)
     out = Vector{FT}(undef, prod(dims))
@@ -432,5 +443,70 @@ set_global!(sim::Simulation, name::Symbol, v) =
     check(ccall((:vg_set_global, LIB), Cint, (Ptr{Cvoid}, Cstring, Cdouble), sim.h, String(name), v))
 push_global!(sim::Simulation, name::Symbol, v) =
     check(ccall((:vg_push_global, LIB), Cint, (Ptr{Cvoid}, Cstring, Cdouble), sim.h, String(name), v))
+
+"""
+    add_graph!(sim, nv, edges, agent_constructor, edge_constructor; directed)
+
+add_graph! -- src/GraphsSupport.jl:34-57, with the graph given as its vertex
+count and its edge list `(src, dst)` in the graph's edge order (so that no
+Graphs.jl import is needed).  Returns the new agents' ids.
+"""
+function add_graph!(sim::Simulation, nv::Integer, edges::Vector{Tuple{Int,Int}},
+                    agent_constructor, edge_constructor; directed::Bool = true)
+    agents = [agent_constructor(v) for v in 1:nv]
+    states = [edge_constructor(e) for e in edges]
+    T = eltype(agents)
+    acols = columns(agents)
+    aptrs = Ptr{Cvoid}[pointer(c) for c in acols]
+    E = eltype(states)
+    ecols = columns(states)
+    eptrs = Ptr{Cvoid}[pointer(c) for c in ecols]
+    src = UInt64[e[1] for e in edges]
+    dst = UInt64[e[2] for e in edges]
+    ids = Vector{AgentID}(undef, nv)
+    GC.@preserve acols ecols check(ccall((:vg_add_graph, LIB), Cint,
+        (Ptr{Cvoid}, Cint, UInt64, Ptr{Ptr{Cvoid}}, Cint, UInt64, Ptr{UInt64}, Ptr{UInt64},
+         Cint, Ptr{Ptr{Cvoid}}, Ptr{UInt64}),
+        sim.h, sim.model.agents[T], nv, aptrs, sim.model.edges[E], length(edges), src, dst,
+        directed ? 1 : 0, isempty(eptrs) ? C_NULL : eptrs, ids))
+    ids
+end
+
+"remove_edges!(sim, to, T) / remove_edges!(sim, from, to, T) -- src/EdgeMethods.jl:527-599"
+remove_edges!(sim::Simulation, to::AgentID, ::Type{T}) where T =
+    check(ccall((:vg_remove_edges, LIB), Cint,
+                (Ptr{Cvoid}, Cint, UInt64, Ptr{UInt64}, Ptr{UInt64}),
+                sim.h, sim.model.edges[T], 1, C_NULL, [to]))
+remove_edges!(sim::Simulation, from::AgentID, to::AgentID, ::Type{T}) where T =
+    check(ccall((:vg_remove_edges, LIB), Cint,
+                (Ptr{Cvoid}, Cint, UInt64, Ptr{UInt64}, Ptr{UInt64}),
+                sim.h, sim.model.edges[T], 1, [from], [to]))
+
+"add_agent_per_process!(sim, agent) -- src/Agent.jl:367-388"
+function add_agent_per_process!(sim::Simulation, agent::T) where T
+    cols = columns([agent])
+    ptrs = Ptr{Cvoid}[pointer(c) for c in cols]
+    id = Ref{UInt64}(0)
+    GC.@preserve cols check(ccall((:vg_add_agent_per_process, LIB), Cint,
+        (Ptr{Cvoid}, Cint, Ptr{Ptr{Cvoid}}, Ptr{UInt64}), sim.h, sim.model.agents[T], ptrs, id))
+    id[]
+end
+
+"""
+    write_snapshot(sim, path) / read_snapshot(model, path)
+
+The role of write_snapshot / read_snapshot! (src/HDF5.jl:688-715,
+1594-1660) in the library's own checkpoint format (not HDF5).
+"""
+write_snapshot(sim::Simulation, path::AbstractString) =
+    check(ccall((:vg_sim_save, LIB), Cint, (Ptr{Cvoid}, Cstring), sim.h, path))
+function read_snapshot(model::ModelTypes, path::AbstractString; stream = C_NULL)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:vg_sim_load, LIB), Cint, (Ptr{Cvoid}, Cstring, Ptr{Cvoid}, Ptr{Ptr{Cvoid}}),
+                model.h, path, stream, h))
+    sim = Simulation(h[], model, Dict{Symbol, Tuple}())
+    finalizer(s -> s.h == C_NULL || ccall((:vg_sim_destroy, LIB), Cint, (Ptr{Cvoid},), s.h), sim)
+    sim
+end
 
 end # module
