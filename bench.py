@@ -55,7 +55,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="opinion", choices=["opinion", "batch", "serve"])
+    ap.add_argument("--workload", default="opinion",
+                    choices=["opinion", "batch", "serve", "sir", "life"])
     ap.add_argument("--jobs", type=int, default=512)
     ap.add_argument("--rates", default="100,1000")
     ap.add_argument("--serve-budget-gb", type=float, default=64.0)
@@ -509,12 +510,116 @@ def run_serve(args):
     print(json.dumps(out), flush=True)
 
 
+def _timed_steps(step, stream, K, clk):
+    """K steps between events on the simulation's stream; per-step events."""
+    import torch
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(K)]
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    clk.start()
+    time.sleep(0.3)
+    start.record(stream)
+    for k in range(K):
+        ev[k][0].record(stream)
+        step()
+        ev[k][1].record(stream)
+    end.record(stream)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    per = sorted(a.elapsed_time(b) for a, b in ev)
+    return start.elapsed_time(end), per, clocks
+
+
+def run_model(args):
+    """Config 0 (SIR, N = 10^5, out-degree 10, 100 steps) or config 2 (Life
+    B3/S23 on a 4096 x 4096 periodic raster with 10^6 random walkers whose
+    walker -> cell edges are rebuilt every step, 1000 steps): the same
+    metric, edge-updates/s, for these parity workloads (the per-agent loop
+    of apply! on each), with the oracle's C restatement timed beside."""
+    import torch
+    import vahana_gb300 as vh
+    from vahana_gb300 import models
+    from oracle import models as om
+    vh.build()
+    stream = torch.cuda.Stream()
+    peak, kind = peaks()
+    if args.workload == "sir":
+        N, deg, steps = 100_000, 10, 100
+        run = models.build_sir(n=N, degree=deg, beta=0.05, recovery=7, seed=args.seed,
+                               stream=stream.cuda_stream)
+        frm, to, _ = models.staged_edges(run.sim, "Contact")
+        st0, d0 = vh.read_agents(run.sim, "Person")[0].values()
+        st0, d0 = st0.copy(), d0.copy()
+        E = N * deg
+        alg = 4 * E + 14 * N + 4
+        cfg = {"workload": "sir_uniform_out_degree", "agents": N, "edges": E,
+               "out_degree": deg, "beta": 0.05, "recovery": 7, "model_steps_reference": steps,
+               "l2": "L2-resident (5.4 MB per step): latency bound"}
+        kern = "k_sir"
+    else:
+        W = H = 4096
+        nw, steps = 1_000_000, 1000
+        run = models.build_life(W, H, nw, 0.3, args.seed, stream=stream.cuda_stream)
+        a0 = vh.read_agents(run.sim, "Cell")[0]["alive"].copy()
+        wc = vh.read_agents(run.sim, "Walker")[0]
+        x0, y0 = wc["x"].copy(), wc["y"].copy()
+        E = 8 * W * H + nw
+        alg = 2 * W * H + 16 * nw + 4 * (W * H + 1) + 4 * nw
+        cfg = {"workload": "life_b3s23_raster_walkers", "raster": [W, H], "cells": W * H,
+               "walkers": nw, "edges_per_step": E, "model_steps_reference": steps,
+               "l2": "inputs larger than L2 (121 MB per step)"}
+        kern = "k_life2d + k_random_walk + walker edge rebuild"
+    vh.finish_init(run.sim)
+    vh.set_async(run.sim, True)
+    for _ in range(args.warmup):
+        run.step()
+    vh.synchronize(run.sim)
+    K = steps
+    total_ms, per, clocks = _timed_steps(run.step, stream, K, Clocks(0))
+    vh.synchronize(run.sim)
+    mean_ms = sum(per) / len(per)
+    out = {"metric": METRIC, "value": E * K / (total_ms * 1e-3), "unit": "edge-updates/s",
+           "n_gpus": 1, "steps": K, "warmup": args.warmup, "ms_per_step": total_ms / K,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "u8/i32" if args.workload == "sir" else "bool/i32", "data": "synthetic",
+           "config": cfg,
+           "roofline": {"bound": "hbm", "achieved": alg / (mean_ms * 1e-3) / 1e9, "peak": peak,
+                        "unit": "GB/s", "frac": alg / (mean_ms * 1e-3) / 1e9 / peak,
+                        "peak_kind": kind, "traffic": None, "algorithmic_bytes_per_step": alg,
+                        "kernel": kern, "step_ms_mean": mean_ms},
+           "clocks": clocks}
+    if not args.no_cpu_baseline:
+        t0 = time.perf_counter()
+        done = 0
+        if args.workload == "sir":
+            g = om.build_inedges(N, frm, to)
+            s_, d_ = st0, d0
+            while done < K and time.perf_counter() - t0 < args.cpu_seconds:
+                s_, d_ = om.sir_step(g, s_, d_, 0.05, 7, args.seed, 1 + done)
+                done += 1
+        else:
+            a_, x_, y_ = a0, x0, y0
+            while done < K and time.perf_counter() - t0 < args.cpu_seconds:
+                a_ = om.life_step(a_, W, H)
+                x_, y_, _ = om.walk_step(x_, y_, W, H, args.seed, 2 + 2 * done)
+                done += 1
+        el = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": E * done / el, "unit": "edge-updates/s",
+                               "cores": om.threads(), "kind": "port",
+                               "sample": "%d steps (%.1f s) of the oracle's C restatement" % (done, el)}
+    run.close()
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     if args.workload == "batch":
         run_batch(args)
     elif args.workload == "serve":
         run_serve(args)
+    elif args.workload in ("sir", "life"):
+        run_model(args)
     elif args.impl == "reference":
         run_reference(args)
     else:
