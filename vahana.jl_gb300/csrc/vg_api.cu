@@ -488,7 +488,7 @@ int vg_sim_copy(vg_sim *h, vg_sim **out) {
     for (size_t T = 0; T < a.csr.size(); T++) {
       CSR &x = a.csr[T], &y = b.csr[T];
       y.nrows = x.nrows; y.nedges = x.nedges; y.src_type_const = x.src_type_const;
-      y.max_degree = x.max_degree;
+      y.max_degree = csr_max_degree(s, x);
       copy_buf(*c, y.row_ptr, x.row_ptr, c->stream);
       copy_buf(*c, y.src, x.src, c->stream);
       copy_buf(*c, y.src_type, x.src_type, c->stream);

@@ -511,8 +511,13 @@ int vg_apply(vg_sim *h, const char *tname, const int *call, int ncall, const int
       if (n > ap->cap) fail(VG_ERR_DEVICE, "edge append buffer overflow");
     }
     bool merge = s.edges[e].add_existing;
+    bool removals = false;
     for (auto &r : ctx.removals)
-      if (r->edge_type == e) apply_edge_removals(s, e, *r, ap, n, merge);
+      if (r->edge_type == e) {
+        apply_edge_removals(s, e, *r, ap, n, merge);
+        removals = true;
+      }
+    if (ap && !removals && build_csr_typed(s, e, *ap, n)) continue;
     std::vector<const void *> pl;
     if (ap)
       for (auto &b : ap->payload) pl.push_back(b.p);

@@ -310,7 +310,7 @@ int vg_batch_create_sir(int n, const int64_t *N, const int32_t *deg, const doubl
     Sim &S = *s->s;
     CSR &c = S.edges[b->contact].csr[b->person];
     b->total_edges += c.nedges;
-    kmax = std::max(kmax, c.max_degree);
+    kmax = std::max(kmax, csr_max_degree(S, c));
   }
   if (b->total_edges >= (1ull << 32) || b->total >= (1ull << 32))
     fail(VG_ERR_NOMEM, "batch: arena indices are 32-bit");

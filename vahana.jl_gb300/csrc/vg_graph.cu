@@ -168,8 +168,10 @@ template <class E>
 __global__ void k_scatter_col(const E *in, const uint32_t *rec,
                               const uint32_t *dest, uint64_t m, E *out) {
   uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= m || dest[j] == 0xffffffffu) return;
-  out[dest[j]] = rec ? in[rec[j]] : in[j];
+  if (j >= m) return;
+  const uint32_t dj = dest ? dest[j] : (uint32_t)j;  // no dest: a gather in place order
+  if (dj == 0xffffffffu) return;
+  out[dj] = rec ? in[rec[j]] : in[j];
 }
 
 __global__ void k_fill_u8(uint8_t *p, uint8_t v, const uint32_t *dest,
@@ -240,6 +242,138 @@ uint64_t csr_edges_total(const EdgeStore &es) {
   uint64_t t = 0;
   for (auto &c : es.csr) t += c.nedges;
   return t;
+}
+
+// ---------------------------------------- fast rebuild from typed records
+namespace {
+// row key of each record (target agent_nr - 1); a record of another type or
+// beyond the rows sets the status word (the records come from kernels that
+// declare their types)
+__global__ void k_typed_keys(const uint64_t *to, const uint64_t *from, uint64_t n,
+                             uint32_t target_type, uint32_t src_type, uint64_t nrows,
+                             uint32_t *keys, uint32_t *vals, int *status) {
+  uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const uint64_t t = to[k];
+  uint64_t r = (t & NR_MASK) - 1;
+  bool bad = (uint32_t)(t >> SHIFT_TYPE) != target_type || r >= nrows;
+  if (from && (uint32_t)(from[k] >> SHIFT_TYPE) != src_type) bad = true;
+  if (bad) {
+    atomicCAS(status, 0, 501);
+    r = 0;
+  }
+  keys[k] = (uint32_t)r;
+  vals[k] = (uint32_t)k;
+}
+
+// row_ptr of the rows 0..nrows from the sorted row keys: a merge path over
+// the rows and the records (record k precedes row r iff keys[k] < r), each
+// thread taking `items` consecutive steps of the merged sequence, so the
+// work is balanced whatever the distribution of the keys
+__global__ void k_coo_rowptr(const uint32_t *keys, uint64_t n, uint64_t nrows, uint32_t items,
+                             uint32_t *rp) {
+  const uint64_t nb = nrows + 1, total = nb + n;
+  const uint64_t d = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * items;
+  if (d >= total) return;
+  uint64_t lo = d > nb ? d - nb : 0, hi = d < n ? d : n;
+  while (lo < hi) {  // smallest k with keys[k] >= row d - 1 - k
+    const uint64_t mid = (lo + hi) >> 1;
+    if ((uint64_t)keys[mid] < d - 1 - mid) lo = mid + 1;
+    else hi = mid;
+  }
+  uint64_t k = lo, r = d - lo;
+  const uint64_t end = d + items < total ? d + items : total;
+  for (uint64_t q = d; q < end; q++) {
+    if (k < n && (r >= nb || (uint64_t)keys[k] < r)) {
+      k++;
+    } else {
+      rp[r] = (uint32_t)k;
+      r++;
+    }
+  }
+}
+
+// the largest row length: at the first record of each row
+__global__ void k_run_maxdeg(const uint32_t *keys, uint64_t n, const uint32_t *rp,
+                             unsigned *maxdeg) {
+  uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n || (k > 0 && keys[k - 1] == keys[k])) return;
+  atomicMax(maxdeg, rp[keys[k] + 1] - rp[keys[k]]);
+}
+
+__global__ void k_gather_src(const uint64_t *from, const uint32_t *vals, uint64_t n,
+                             uint32_t *src) {
+  uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) src[k] = (uint32_t)((from[vals[k]] & NR_MASK) - 1);
+}
+}  // namespace
+
+uint32_t csr_max_degree(Sim &s, CSR &c) {
+  if (c.max_degree_pending) {
+    VG_CUDA(cudaMemcpyAsync(&c.max_degree, c.d_max_degree.p, 4, cudaMemcpyDeviceToHost, s.stream));
+    VG_CUDA(cudaStreamSynchronize(s.stream));
+    c.max_degree_pending = false;
+  }
+  return c.max_degree;
+}
+
+bool build_csr_typed(Sim &s, int e, const EdgeAppend &ap, uint64_t n) {
+  const EdgeTypeDesc &ed = s.model->et(e);
+  EdgeStore &es = s.edges[e];
+  if (!ap.ordered || ap.target_type <= 0 || (ed.stores_src() && ap.src_type <= 0) ||
+      ed.bool_only() || ed.singleedge() || es.add_existing || n >= (1ull << 31))
+    return false;
+  const int T = ap.target_type;
+  if (T > (int)s.model->atypes.size() || (ed.singletype() && T != ed.target)) return false;
+  cudaStream_t st = s.stream;
+  if (es.csr.size() < (size_t)MAX_AGENT_TYPES) es.csr.resize(MAX_AGENT_TYPES);
+  for (int U = 1; U < (int)es.csr.size(); U++)
+    if (U != T && es.csr[U].row_ptr.p) es.csr[U] = CSR();
+  CSR &c = es.csr[T];
+  const uint64_t nrows = s.agents[T - 1].n;
+  // buffers of the previous container are reused when large enough (the
+  // stream orders every earlier reader before these writes)
+  auto ensure = [&](DevBuf &b, uint64_t bytes) {
+    if (b.bytes < bytes || !b.p) b.alloc(std::max<uint64_t>(bytes, 16), &s.footprint);
+  };
+  ensure(c.row_ptr, (nrows + 1) * 4);
+  if (ed.stores_src()) ensure(c.src, std::max<uint64_t>(n, 1) * 4);
+  else c.src.release();
+  c.src_type.release();
+  const int nf = ed.stores_payload() ? (int)ed.fields.size() : 0;
+  c.payload.resize(nf);
+  for (int f = 0; f < nf; f++) ensure(c.payload[f], std::max<uint64_t>(n, 1) * ed.fields[f].size);
+  ensure(c.d_max_degree, 4);
+  VG_CUDA(cudaMemsetAsync(c.d_max_degree.p, 0, 4, st));
+  Tmp<uint32_t> keys(n, st), vals(n, st);
+  if (n) {
+    k_typed_keys<<<nblk(n), TPB, 0, st>>>(ap.to.as<uint64_t>(),
+                                           ed.stores_src() ? ap.from.as<uint64_t>() : nullptr, n,
+                                           (uint32_t)T, (uint32_t)ap.src_type, nrows, keys.p,
+                                           vals.p, s.d_status.as<int>());
+    radix_sort_pairs_u32(keys.p, vals.p, n, bits_for(nrows ? nrows - 1 : 0), st, s);
+  }
+  const uint32_t items = 16;
+  const uint64_t total = nrows + 1 + n;
+  k_coo_rowptr<<<nblk((total + items - 1) / items), TPB, 0, st>>>(keys.p, n, nrows, items,
+                                                                  c.row_ptr.as<uint32_t>());
+  if (n) {
+    k_run_maxdeg<<<nblk(n), TPB, 0, st>>>(keys.p, n, c.row_ptr.as<uint32_t>(),
+                                           c.d_max_degree.as<unsigned>());
+    if (ed.stores_src())
+      k_gather_src<<<nblk(n), TPB, 0, st>>>(ap.from.as<uint64_t>(), vals.p, n,
+                                             c.src.as<uint32_t>());
+    for (int f = 0; f < nf; f++)
+      scatter_column(ed.fields[f].size, ap.payload[f].p, vals.p, nullptr, n, c.payload[f].p, st);
+  }
+  VG_CUDA(cudaGetLastError());
+  c.nrows = nrows;
+  c.nedges = n;
+  c.src_type_const = ed.stores_src() ? ap.src_type : 0;
+  c.max_degree_pending = true;
+  c.schedule_valid = false;
+  c.unit_grid_weights = -1;
+  return true;
 }
 
 void build_csr_from_records(Sim &s, int e, const uint64_t *d_from,
@@ -442,7 +576,7 @@ static void compact_csr(Sim &s, const EdgeTypeDesc &ed, CSR &c, const uint32_t *
     n2.payload[f].alloc(alloc_n * ed.fields[f].size, &s.footprint);
     scatter_column(ed.fields[f].size, c.payload[f].p, nullptr, dest.p, ne, n2.payload[f].p, st);
   }
-  n2.max_degree = c.max_degree;
+  n2.max_degree = csr_max_degree(s, c);
   VG_CUDA(cudaGetLastError());
   VG_CUDA(cudaStreamSynchronize(st));
   c = std::move(n2);

@@ -140,7 +140,9 @@ struct CSR {
   DevBuf src_type; // u8[nedges] when src_type_const < 0
   int src_type_const = 0;  // >0 all sources of that type, 0 none, -1 mixed
   std::vector<DevBuf> payload;
-  uint32_t max_degree = 0;
+  uint32_t max_degree = 0;  // read through csr_max_degree()
+  DevBuf d_max_degree;      // device value while max_degree_pending
+  bool max_degree_pending = false;
   // derived gather layout of the Float64 payload column 0 (built on first
   // use by the gather kernels, cached until the CSR changes):
   // hub rows (degree > hub threshold) by descending degree; the other rows
@@ -267,6 +269,10 @@ struct EdgeAppend {
   DevBuf counter;  // u64 device counter
   bool ordered = false;  // records already in order-key order
   uint64_t fixed_count = 0;  // when the count is known on the host
+  // declared by kernels whose records are typed by construction: every
+  // target of agent type target_type, every source of type src_type
+  // (0: unknown) -- allows the typed fast rebuild (build_csr_typed)
+  int target_type = 0, src_type = 0;
 };
 
 // remove_edges! calls recorded by a transition (src/EdgeMethods.jl:527-599):
@@ -353,6 +359,11 @@ void remove_died_edges(Sim &s, int died_type, const uint8_t *died_now,
                        uint64_t n_died);
 // hub list and degree-sorted row order over n agent slots (n >= nrows)
 void ensure_schedule(Sim &s, CSR &c, uint32_t hub_threshold, uint64_t n);
+// largest row length (synchronises when the value is still on the device)
+uint32_t csr_max_degree(Sim &s, CSR &c);
+// rebuild of an edge type's container from typed, ordered records without
+// host synchronisation; false when the generic build must run
+bool build_csr_typed(Sim &s, int edge_type, const EdgeAppend &ap, uint64_t n);
 uint64_t csr_edges_total(const EdgeStore &es);
 
 // agents (vg_api.cu)

@@ -173,7 +173,7 @@ void build_job(vg_server *S, Job *J, cudaStream_t bst) {
       fail(rc, vg_last_error());
     if ((rc = vg_finish_init(J->sim))) fail(rc, vg_last_error());
     Sim &s = *J->sim->s;
-    uint32_t maxdeg = s.edges[S->sir_contact].csr[S->sir_person].max_degree;
+    uint32_t maxdeg = csr_max_degree(s, s.edges[S->sir_contact].csr[S->sir_person]);
     std::vector<double> tab(maxdeg + 1);
     double q = 1.0, om = 1.0 - sp.beta;
     tab[0] = 0.0;

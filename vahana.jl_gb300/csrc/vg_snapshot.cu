@@ -204,7 +204,7 @@ int vg_sim_save(vg_sim *h, const char *path) {
       F.put<uint64_t>(c.nrows);
       F.put<uint64_t>(c.nedges);
       F.put<int32_t>(c.src_type_const);
-      F.put<uint32_t>(c.max_degree);
+      F.put<uint32_t>(csr_max_degree(s, c));
       put_dev(F, c.row_ptr, (c.nrows + 1) * 4, s.stream);
       put_dev(F, c.src, c.src.p ? c.nedges * 4 : 0, s.stream);
       put_dev(F, c.src_type, c.src_type.p ? c.nedges : 0, s.stream);

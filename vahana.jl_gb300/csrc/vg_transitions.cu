@@ -918,7 +918,7 @@ void tr_sir(ApplyCtx &c) {
   DevCSRView v = csr_view(s, e, c.call_type);
   if (v.nedges && v.src_type_const != c.call_type)
     fail(VG_ERR_ARG, "sir: contact sources must be of the called type");
-  uint32_t maxdeg = c.call_type < (int)es.csr.size() ? es.csr[c.call_type].max_degree : 0;
+  uint32_t maxdeg = c.call_type < (int)es.csr.size() ? csr_max_degree(s, es.csr[c.call_type]) : 0;
   // p_k = 1 - q^k by repeated multiplication, k = 0..maxdeg
   std::vector<double> ptab(maxdeg + 1);
   double q = 1.0, om = 1.0 - beta;
@@ -1005,6 +1005,8 @@ void tr_random_walk(ApplyCtx &c) {
   if (a.n == 0) return;
   EdgeAppend *ap = c.append_for(e, a.n, true);
   ap->fixed_count = a.n;
+  ap->target_type = R.type_nr;  // walker -> cell records, typed by construction
+  ap->src_type = c.call_type;
   k_random_walk<<<nblk(a.n), TPB, 0, s.stream>>>(
       (const int32_t *)a.rd[0], (const int32_t *)a.rd[1], (int32_t *)a.wr[0],
       (int32_t *)a.wr[1], a.n, R.dims[0], R.dims[1], seed, (uint32_t)c.step,
