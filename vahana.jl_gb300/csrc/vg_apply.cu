@@ -34,6 +34,17 @@ EdgeAppend *ApplyCtx::append_for(int e, uint64_t capacity, bool ordered) {
     }
   Sim &s = *sim;
   const EdgeTypeDesc &ed = s.model->et(e);
+  auto it = s.append_spare.find(e);
+  if (it != s.append_spare.end() && it->second->cap >= capacity &&
+      it->second->ordered == ordered) {
+    std::unique_ptr<EdgeAppend> a = std::move(it->second);
+    s.append_spare.erase(it);
+    a->fixed_count = 0;
+    a->target_type = a->src_type = 0;
+    VG_CUDA(cudaMemsetAsync(a->counter.p, 0, 8, s.stream));
+    appends.push_back(std::move(a));
+    return appends.back().get();
+  }
   auto a = std::make_unique<EdgeAppend>();
   a->edge_type = e;
   a->cap = std::max<uint64_t>(capacity, 1);
@@ -531,6 +542,7 @@ int vg_apply(vg_sim *h, const char *tname, const int *call, int ncall, const int
     AgentStore &a = s.agents[T - 1];
     remove_died_edges(s, T, a.died_rd.as<uint8_t>(), a.n);
   }
+  for (auto &a : ctx.appends) s.append_spare[a->edge_type] = std::move(a);
   ctx.appends.clear();
   ctx.removals.clear();
   s.num_transitions++;

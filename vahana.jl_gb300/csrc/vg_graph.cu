@@ -267,30 +267,51 @@ __global__ void k_typed_keys(const uint64_t *to, const uint64_t *from, uint64_t 
 }
 
 // row_ptr of the rows 0..nrows from the sorted row keys: a merge path over
-// the rows and the records (record k precedes row r iff keys[k] < r), each
-// thread taking `items` consecutive steps of the merged sequence, so the
-// work is balanced whatever the distribution of the keys
-__global__ void k_coo_rowptr(const uint32_t *keys, uint64_t n, uint64_t nrows, uint32_t items,
-                             uint32_t *rp) {
-  const uint64_t nb = nrows + 1, total = nb + n;
-  const uint64_t d = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * items;
-  if (d >= total) return;
+// the rows and the records (record k precedes row r iff keys[k] < r).  A
+// block takes COO_SPAN consecutive steps of the merged sequence, each
+// thread COO_ITEMS of them; the block's rows are collected in shared memory
+// and stored contiguously (coalesced), whatever the distribution of keys.
+constexpr uint32_t COO_ITEMS = 16;
+constexpr uint32_t COO_SPAN = COO_ITEMS * TPB;
+
+__device__ __forceinline__ uint64_t coo_split(const uint32_t *keys, uint64_t n, uint64_t nb,
+                                              uint64_t d) {
   uint64_t lo = d > nb ? d - nb : 0, hi = d < n ? d : n;
   while (lo < hi) {  // smallest k with keys[k] >= row d - 1 - k
     const uint64_t mid = (lo + hi) >> 1;
     if ((uint64_t)keys[mid] < d - 1 - mid) lo = mid + 1;
     else hi = mid;
   }
-  uint64_t k = lo, r = d - lo;
-  const uint64_t end = d + items < total ? d + items : total;
-  for (uint64_t q = d; q < end; q++) {
-    if (k < n && (r >= nb || (uint64_t)keys[k] < r)) {
-      k++;
-    } else {
-      rp[r] = (uint32_t)k;
-      r++;
+  return lo;  // records among the first d merged items
+}
+
+__global__ void __launch_bounds__(TPB) k_coo_rowptr(const uint32_t *keys, uint64_t n,
+                                                    uint64_t nrows, uint32_t *rp) {
+  __shared__ uint32_t rows[COO_SPAN];
+  __shared__ uint64_t r_begin, r_end;
+  const uint64_t nb = nrows + 1, total = nb + n;
+  const uint64_t d0 = (uint64_t)blockIdx.x * COO_SPAN;
+  const uint64_t d1 = d0 + COO_SPAN < total ? d0 + COO_SPAN : total;
+  if (threadIdx.x == 0) {
+    r_begin = d0 - coo_split(keys, n, nb, d0);
+    r_end = d1 - coo_split(keys, n, nb, d1);
+  }
+  __syncthreads();
+  const uint64_t d = d0 + (uint64_t)threadIdx.x * COO_ITEMS;
+  if (d < d1) {
+    uint64_t k = coo_split(keys, n, nb, d), r = d - k;
+    const uint64_t end = d + COO_ITEMS < d1 ? d + COO_ITEMS : d1;
+    for (uint64_t q = d; q < end; q++) {
+      if (k < n && (r >= nb || (uint64_t)keys[k] < r)) {
+        k++;
+      } else {
+        rows[r - r_begin] = (uint32_t)k;
+        r++;
+      }
     }
   }
+  __syncthreads();
+  for (uint64_t i = threadIdx.x; i < r_end - r_begin; i += TPB) rp[r_begin + i] = rows[i];
 }
 
 // the largest row length: at the first record of each row
@@ -353,10 +374,9 @@ bool build_csr_typed(Sim &s, int e, const EdgeAppend &ap, uint64_t n) {
                                            vals.p, s.d_status.as<int>());
     radix_sort_pairs_u32(keys.p, vals.p, n, bits_for(nrows ? nrows - 1 : 0), st, s);
   }
-  const uint32_t items = 16;
   const uint64_t total = nrows + 1 + n;
-  k_coo_rowptr<<<nblk((total + items - 1) / items), TPB, 0, st>>>(keys.p, n, nrows, items,
-                                                                  c.row_ptr.as<uint32_t>());
+  k_coo_rowptr<<<(unsigned)((total + COO_SPAN - 1) / COO_SPAN), TPB, 0, st>>>(
+      keys.p, n, nrows, c.row_ptr.as<uint32_t>());
   if (n) {
     k_run_maxdeg<<<nblk(n), TPB, 0, st>>>(keys.p, n, c.row_ptr.as<uint32_t>(),
                                            c.d_max_degree.as<unsigned>());

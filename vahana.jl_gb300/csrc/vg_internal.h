@@ -210,6 +210,8 @@ struct Raster {
   uint64_t ncells = 0;
 };
 
+struct EdgeAppend;
+
 struct Sim {
   std::shared_ptr<Model> model;
   std::string name;
@@ -238,6 +240,9 @@ struct Sim {
   // asynchronous mode: apply! does not wait for the device; the kernels'
   // status word is checked at the next synchronizing call
   bool async = false;
+  // edge-append buffers of earlier transitions, by edge type, reused by the
+  // next apply! that appends to the same type (no allocation per step)
+  std::map<int, std::unique_ptr<EdgeAppend>> append_spare;
 };
 
 // ---------------------------------------------------------------- kernels
