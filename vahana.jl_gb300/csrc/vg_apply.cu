@@ -651,7 +651,6 @@ int vg_mapreduce_edges(vg_sim *h, int e, int field, int map_kind, double map_arg
   // fold over the CSR of every target type in (type, row, insertion) order
   int64_t ai = r.init_i;
   double af = r.init_f;
-  bool any = false;
   for (int T = 1; T < (int)es.csr.size(); T++) {
     CSR &c = es.csr[T];
     if (!c.nedges) continue;
@@ -674,9 +673,7 @@ int vg_mapreduce_edges(vg_sim *h, int e, int field, int map_kind, double map_arg
       run_reduce(s, q, VG_I64, ordered, &v);
       ai = v;
     }
-    any = true;
   }
-  (void)any;
   if (out_dtype == VG_F64) *(double *)out = r.float_acc ? af : (double)ai;
   else if (out_dtype == VG_BOOL) *(uint8_t *)out = (r.float_acc ? af : (double)ai) != 0;
   else *(int64_t *)out = r.float_acc ? (int64_t)af : ai;
