@@ -339,6 +339,15 @@ int vg_read_staged_edges(vg_sim *s, int edge_type, uint64_t *from_out,
  * the general add, mul and div. */
 int vg_selftest_fp64(uint64_t n, uint64_t seed, uint64_t *counts_out);
 
+/* Sorts n generated (key, index) pairs with the library's device radix sort
+ * (32-bit keys, or 64-bit keys when wide != 0, key_bits significant bits,
+ * bits [const_lo, const_hi) equal in every key) and compares keys and
+ * indices with a stable host sort; *mismatch_out = mismatching positions.
+ * The sort is what rebuilds every CSR in insertion order (no reference
+ * counterpart: Vahana appends to per-agent vectors). */
+int vg_selftest_sort(uint64_t n, int key_bits, int wide, int const_lo, int const_hi,
+                     uint64_t seed, uint64_t *mismatch_out);
+
 /* ---- allocation-free SIR step ---------------------------------------------
  * No counterpart in the reference.  One step of the "sir" transition on
  * device buffers the caller owns, for callers that cannot let a library

@@ -266,60 +266,68 @@ __global__ void k_typed_keys(const uint64_t *to, const uint64_t *from, uint64_t 
   vals[k] = (uint32_t)k;
 }
 
-// row_ptr of the rows 0..nrows from the sorted row keys: a merge path over
-// the rows and the records (record k precedes row r iff keys[k] < r).  A
-// block takes COO_SPAN consecutive steps of the merged sequence, each
-// thread COO_ITEMS of them; the block's rows are collected in shared memory
-// and stored contiguously (coalesced), whatever the distribution of keys.
-constexpr uint32_t COO_ITEMS = 16;
-constexpr uint32_t COO_SPAN = COO_ITEMS * TPB;
+// row_ptr of the rows 0..nrows from the sorted row keys: rp[r] = the
+// number of keys below r.  Rows are cut into blocks of RP_ROWS; a first
+// pass over the records finds, for every block boundary j * RP_ROWS, the
+// first record at or above it (record k owns the boundaries in
+// (keys[k-1], keys[k]]); then each block stages its records' keys in
+// shared memory, finds every row's first record by a short search there,
+// stores its rows contiguously and reduces the largest row length of the
+// block into *maxdeg.  Blocks whose records do not fit in shared memory
+// search in global memory instead.
+constexpr uint32_t RP_ROWS = 4096;
+constexpr uint32_t RP_CAP = 4096;
+constexpr uint32_t RP_PER_THREAD = RP_ROWS / TPB;
 
-__device__ __forceinline__ uint64_t coo_split(const uint32_t *keys, uint64_t n, uint64_t nb,
-                                              uint64_t d) {
-  uint64_t lo = d > nb ? d - nb : 0, hi = d < n ? d : n;
-  while (lo < hi) {  // smallest k with keys[k] >= row d - 1 - k
-    const uint64_t mid = (lo + hi) >> 1;
-    if ((uint64_t)keys[mid] < d - 1 - mid) lo = mid + 1;
-    else hi = mid;
-  }
-  return lo;  // records among the first d merged items
+__global__ void k_rp_bounds(const uint32_t *keys, uint64_t n, uint64_t nbr, uint32_t *bstart) {
+  const uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k > n) return;
+  const uint64_t jlo = k == 0 ? 0 : (uint64_t)keys[k - 1] / RP_ROWS + 1;
+  const uint64_t jhi = k == n ? nbr : (uint64_t)keys[k] / RP_ROWS;
+  for (uint64_t j = jlo; j <= jhi; j++) bstart[j] = (uint32_t)k;
 }
 
-__global__ void __launch_bounds__(TPB) k_coo_rowptr(const uint32_t *keys, uint64_t n,
-                                                    uint64_t nrows, uint32_t *rp) {
-  __shared__ uint32_t rows[COO_SPAN];
-  __shared__ uint64_t r_begin, r_end;
-  const uint64_t nb = nrows + 1, total = nb + n;
-  const uint64_t d0 = (uint64_t)blockIdx.x * COO_SPAN;
-  const uint64_t d1 = d0 + COO_SPAN < total ? d0 + COO_SPAN : total;
-  if (threadIdx.x == 0) {
-    r_begin = d0 - coo_split(keys, n, nb, d0);
-    r_end = d1 - coo_split(keys, n, nb, d1);
-  }
+__global__ void __launch_bounds__(TPB) k_rp_fill(const uint32_t *keys, uint64_t nrows,
+                                                 const uint32_t *bstart, uint32_t *rp,
+                                                 unsigned *maxdeg) {
+  __shared__ uint32_t sk[RP_CAP];
+  __shared__ uint32_t rows[RP_ROWS + 1];
+  const uint64_t r0 = (uint64_t)blockIdx.x * RP_ROWS;
+  const uint64_t r1 = r0 + RP_ROWS < nrows + 1 ? r0 + RP_ROWS : nrows + 1;
+  const uint32_t k0 = bstart[blockIdx.x], k1 = bstart[blockIdx.x + 1];
+  const uint32_t m = k1 - k0;
+  const bool fits = m <= RP_CAP;
+  if (fits)
+    for (uint32_t i = threadIdx.x; i < m; i += TPB) sk[i] = keys[k0 + i];
   __syncthreads();
-  const uint64_t d = d0 + (uint64_t)threadIdx.x * COO_ITEMS;
-  if (d < d1) {
-    uint64_t k = coo_split(keys, n, nb, d), r = d - k;
-    const uint64_t end = d + COO_ITEMS < d1 ? d + COO_ITEMS : d1;
-    for (uint64_t q = d; q < end; q++) {
-      if (k < n && (r >= nb || (uint64_t)keys[k] < r)) {
-        k++;
-      } else {
-        rows[r - r_begin] = (uint32_t)k;
-        r++;
-      }
+  const uint32_t *ks = fits ? sk : keys + k0;
+  // thread t: rows r0 + t * RP_PER_THREAD ... (+ RP_PER_THREAD), one search
+  // for the first, then a forward walk
+  const uint64_t ra = r0 + (uint64_t)threadIdx.x * RP_PER_THREAD;
+  if (ra < r1) {
+    uint32_t lo = 0, hi = m;
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if ((uint64_t)ks[mid] < ra) lo = mid + 1;
+      else hi = mid;
+    }
+    const uint64_t re = ra + RP_PER_THREAD < r1 ? ra + RP_PER_THREAD : r1;
+    for (uint64_t r = ra; r < re; r++) {
+      while (lo < m && (uint64_t)ks[lo] < r) lo++;
+      rows[r - r0] = k0 + lo;
     }
   }
+  if (threadIdx.x == 0) rows[r1 - r0] = k1;
   __syncthreads();
-  for (uint64_t i = threadIdx.x; i < r_end - r_begin; i += TPB) rp[r_begin + i] = rows[i];
-}
-
-// the largest row length: at the first record of each row
-__global__ void k_run_maxdeg(const uint32_t *keys, uint64_t n, const uint32_t *rp,
-                             unsigned *maxdeg) {
-  uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n || (k > 0 && keys[k - 1] == keys[k])) return;
-  atomicMax(maxdeg, rp[keys[k] + 1] - rp[keys[k]]);
+  unsigned dmax = 0;
+  const uint32_t nr = (uint32_t)(r1 - r0);
+  for (uint32_t i = threadIdx.x; i < nr; i += TPB) {
+    rp[r0 + i] = rows[i];
+    if (r0 + i < nrows) dmax = max(dmax, rows[i + 1] - rows[i]);
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) dmax = max(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+  if ((threadIdx.x & 31) == 0 && dmax) atomicMax(maxdeg, dmax);
 }
 
 __global__ void k_gather_src(const uint64_t *from, const uint32_t *vals, uint64_t n,
@@ -374,12 +382,14 @@ bool build_csr_typed(Sim &s, int e, const EdgeAppend &ap, uint64_t n) {
                                            vals.p, s.d_status.as<int>());
     radix_sort_pairs_u32(keys.p, vals.p, n, bits_for(nrows ? nrows - 1 : 0), st, s);
   }
-  const uint64_t total = nrows + 1 + n;
-  k_coo_rowptr<<<(unsigned)((total + COO_SPAN - 1) / COO_SPAN), TPB, 0, st>>>(
-      keys.p, n, nrows, c.row_ptr.as<uint32_t>());
+  {
+    const uint64_t nbr = (nrows + 1 + RP_ROWS - 1) / RP_ROWS;
+    Tmp<uint32_t> bstart(nbr + 1, st);
+    k_rp_bounds<<<nblk(n + 1), TPB, 0, st>>>(keys.p, n, nbr, bstart.p);
+    k_rp_fill<<<(unsigned)nbr, TPB, 0, st>>>(keys.p, nrows, bstart.p, c.row_ptr.as<uint32_t>(),
+                                             c.d_max_degree.as<unsigned>());
+  }
   if (n) {
-    k_run_maxdeg<<<nblk(n), TPB, 0, st>>>(keys.p, n, c.row_ptr.as<uint32_t>(),
-                                           c.d_max_degree.as<unsigned>());
     if (ed.stores_src())
       k_gather_src<<<nblk(n), TPB, 0, st>>>(ap.from.as<uint64_t>(), vals.p, n,
                                              c.src.as<uint32_t>());

@@ -4,6 +4,10 @@
 // (src/EdgeMethods.jl:495-496): records arrive in insertion order (or carry
 // an order key), and a stable sort by target row keeps that order inside
 // each row.
+#include <algorithm>
+#include <numeric>
+#include <vector>
+
 #include "vg_internal.h"
 
 namespace vg {
@@ -107,114 +111,229 @@ void exclusive_scan_impl(const T *in, T *out, uint64_t n, cudaStream_t st) {
 }
 
 // ------------------------------------------------------------ radix sort
+// LSD radix sort with 8-bit digits in one launch per digit: the digit
+// counts of every pass come from one upfront read of the keys, and each
+// pass ranks its tiles locally and finds the tile's offset for every digit
+// by a chained scan with decoupled look-back over the tiles' published
+// counts (D. Merrill and M. Garland, "Single-pass parallel prefix scan with
+// decoupled look-back", NVIDIA NVR-2016-002; A. Adinets and D. Merrill,
+// "Onesweep: a faster least significant digit radix sort for GPUs",
+// arXiv:2206.01784, 2022).  Tiles take their index from a counter in the
+// order the blocks start, so a tile only waits for tiles that are already
+// running.
 constexpr int RS_TPB = 256;
 constexpr int RS_WARPS = RS_TPB / 32;
-constexpr int RS_IPT = 8;                    // items per lane
-constexpr int RS_WARP_ITEMS = 32 * RS_IPT;  // 256
+constexpr int RS_IPT = 8;                          // items per lane
+constexpr int RS_WARP_ITEMS = 32 * RS_IPT;         // 256
 constexpr int RS_TILE = RS_WARPS * RS_WARP_ITEMS;  // 2048
+constexpr int RS_MAXPASS = 8;
+// look-back polls of one tile's status before the pass gives up, records an
+// error in the simulation's status word and treats the count as zero
+// (every write is bounds-checked, so a failed pass stays in bounds)
+constexpr uint32_t RS_SPIN_LIMIT = 1u << 21;
+constexpr int RS_ERR_LOOKBACK = 0x5e01;
 
-template <class K>
-__global__ void rs_hist(const K *keys, uint64_t n, int shift, uint32_t *hist,
-                        uint32_t ntiles) {
-  __shared__ uint32_t s[256];
-  s[threadIdx.x] = 0;
-  __syncthreads();
-  uint64_t base = (uint64_t)blockIdx.x * RS_TILE;
-#pragma unroll
-  for (int k = 0; k < RS_TILE / RS_TPB; k++) {
-    uint64_t i = base + (uint64_t)k * RS_TPB + threadIdx.x;
-    if (i < n) atomicAdd(&s[(unsigned)((keys[i] >> shift) & 255u)], 1u);
-  }
-  __syncthreads();
-  hist[(uint64_t)threadIdx.x * ntiles + blockIdx.x] = s[threadIdx.x];
+// status word of (tile, digit): count in bits 0..31, flag in bits 32..33
+// (1: the tile's own count, 2: inclusive prefix over tiles 0..tile), pass
+// tag (pass + 1) in bits 34..; words of an earlier pass read as not ready
+__device__ __forceinline__ void st_status(unsigned long long *a, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(a), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_status(const unsigned long long *a) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(a) : "memory");
+  return v;
 }
 
-// Stable scatter: the tile's logical item order is (warp, k, lane), and
-// ranks are accumulated in that order.
 template <class K>
-__global__ void rs_scatter(const K *kin, const uint32_t *vin, K *kout,
-                           uint32_t *vout, uint64_t n, int shift,
-                           const uint32_t *offs, uint32_t ntiles) {
-  __shared__ uint32_t wcnt[RS_WARPS][256];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int d = threadIdx.x; d < RS_WARPS * 256; d += RS_TPB)
-    (&wcnt[0][0])[d] = 0;
+__global__ void __launch_bounds__(RS_TPB) rs_upfront(const K *keys, uint64_t n, int passes,
+                                                      uint32_t *ghist) {
+  __shared__ uint32_t h[RS_MAXPASS][256];
+  for (int i = threadIdx.x; i < RS_MAXPASS * 256; i += RS_TPB) (&h[0][0])[i] = 0;
   __syncthreads();
+  for (uint64_t i = (uint64_t)blockIdx.x * RS_TPB + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * RS_TPB) {
+    const K k = keys[i];
+    for (int p = 0; p < passes; p++) atomicAdd(&h[p][(unsigned)(k >> (8 * p)) & 255u], 1u);
+  }
+  __syncthreads();
+  for (int p = 0; p < passes; p++) {
+    const uint32_t c = h[p][threadIdx.x];
+    if (c) atomicAdd(&ghist[p * 256 + threadIdx.x], c);
+  }
+}
+
+template <class K>
+struct RsShared {
+  uint32_t wcnt[RS_WARPS][256];
+  uint32_t dstart[256];
+  uint32_t gbase[256];
+  uint32_t ws[32];
+  uint32_t tile;
+  int trivial;
+  K key[RS_TILE];
+  uint32_t val[RS_TILE];
+};
+
+// One pass: tile `tile` (from the ticket counter) is ranked stably (item
+// order = warp, slot, lane = input order), published, offset by the
+// look-back, staged in shared memory in digit order and written out in
+// runs of consecutive positions.
+template <class K>
+__global__ void __launch_bounds__(RS_TPB) rs_pass(const K *kin, const uint32_t *vin, K *kout,
+                                                   uint32_t *vout, uint64_t n, int pass,
+                                                   const uint32_t *ghist,
+                                                   unsigned long long *status,
+                                                   uint32_t *ticket, int *err) {
+  __shared__ RsShared<K> S;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int shift = 8 * pass;
+  const uint32_t gcount = ghist[pass * 256 + threadIdx.x];
+  if (threadIdx.x == 0) {
+    S.tile = atomicAdd(ticket, 1u);
+    S.trivial = 0;
+  }
+  for (int d = threadIdx.x; d < RS_WARPS * 256; d += RS_TPB) (&S.wcnt[0][0])[d] = 0;
+  __syncthreads();
+  if (gcount == n) S.trivial = 1;  // every key has this digit: the pass keeps the order
+  const uint32_t tile = S.tile;
+  const uint64_t t0 = (uint64_t)tile * RS_TILE;
+  const uint32_t m = (uint32_t)(n - t0 < (uint64_t)RS_TILE ? n - t0 : (uint64_t)RS_TILE);
+  __syncthreads();
+  if (S.trivial) {
+    for (uint32_t i = threadIdx.x; i < m; i += RS_TPB) {
+      kout[t0 + i] = kin[t0 + i];
+      vout[t0 + i] = vin[t0 + i];
+    }
+    return;
+  }
   const unsigned lt = (1u << lane) - 1u;
-  uint64_t base = (uint64_t)blockIdx.x * RS_TILE + (uint64_t)w * RS_WARP_ITEMS;
+  const uint32_t wbase = (uint32_t)w * RS_WARP_ITEMS;
   K key[RS_IPT];
   uint32_t val[RS_IPT], rank[RS_IPT];
   int dig[RS_IPT];
 #pragma unroll
   for (int k = 0; k < RS_IPT; k++) {
-    uint64_t i = base + (uint64_t)k * 32 + lane;
-    bool valid = i < n;
-    key[k] = valid ? kin[i] : K(0);
-    val[k] = valid ? vin[i] : 0u;
-    int d = valid ? (int)((key[k] >> shift) & 255u) : 256;
+    const uint32_t i = wbase + (uint32_t)k * 32 + lane;
+    const bool valid = i < m;
+    key[k] = valid ? kin[t0 + i] : K(0);
+    val[k] = valid ? vin[t0 + i] : 0u;
+    const int d = valid ? (int)((key[k] >> shift) & 255u) : 256;
     dig[k] = d;
-    unsigned peers = __match_any_sync(0xffffffffu, d);
-    uint32_t b = valid ? wcnt[w][d] : 0u;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const uint32_t b = valid ? S.wcnt[w][d] : 0u;
     rank[k] = b + __popc(peers & lt);
     __syncwarp();
-    if (valid && lane == __ffs(peers) - 1) wcnt[w][d] = b + __popc(peers);
+    if (valid && lane == __ffs(peers) - 1) S.wcnt[w][d] = b + __popc(peers);
     __syncwarp();
   }
   __syncthreads();
-  {
-    int d = threadIdx.x;
-    uint32_t run = 0;
+  // thread d: exclusive counts of digit d over the warps, the tile's count
+  const int d = threadIdx.x;
+  uint32_t c = 0;
 #pragma unroll
-    for (int w2 = 0; w2 < RS_WARPS; w2++) {
-      uint32_t t = wcnt[w2][d];
-      wcnt[w2][d] = run;
-      run += t;
-    }
+  for (int w2 = 0; w2 < RS_WARPS; w2++) {
+    const uint32_t t = S.wcnt[w2][d];
+    S.wcnt[w2][d] = c;
+    c += t;
   }
+  const unsigned long long tag = (unsigned long long)(pass + 1) << 34;
+  unsigned long long *my = status + (uint64_t)tile * 256 + d;
+  st_status(my, tag | ((tile ? 1ull : 2ull) << 32) | c);
+  const uint32_t ds = block_exclusive_scan<uint32_t>(c, S.ws, (uint32_t *)nullptr);
+  const uint32_t gex = block_exclusive_scan<uint32_t>(gcount, S.ws, (uint32_t *)nullptr);
+  uint32_t excl = 0;
+  if (tile) {
+    uint32_t t = tile - 1, spins = 0;
+    for (;;) {
+      const unsigned long long v = ld_status(status + (uint64_t)t * 256 + d);
+      const uint32_t flag = (v >> 34) == (unsigned long long)(pass + 1) ? (uint32_t)(v >> 32) & 3u : 0u;
+      if (!flag) {
+        if (++spins > RS_SPIN_LIMIT) {
+          atomicCAS(err, 0, RS_ERR_LOOKBACK);
+          break;
+        }
+        if (spins > 16) __nanosleep(64);
+        continue;
+      }
+      spins = 0;
+      excl += (uint32_t)v;
+      if (flag == 2u || t == 0) break;
+      t--;
+    }
+    st_status(my, tag | (2ull << 32) | (excl + c));
+  }
+  S.dstart[d] = ds;
+  S.gbase[d] = gex + excl;
   __syncthreads();
 #pragma unroll
   for (int k = 0; k < RS_IPT; k++) {
     if (dig[k] < 256) {
-      uint64_t pos = (uint64_t)offs[(uint64_t)dig[k] * ntiles + blockIdx.x] +
-                     wcnt[w][dig[k]] + rank[k];
-      kout[pos] = key[k];
-      vout[pos] = val[k];
+      const uint32_t pos = S.dstart[dig[k]] + S.wcnt[w][dig[k]] + rank[k];
+      S.key[pos] = key[k];
+      S.val[pos] = val[k];
+    }
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < m; i += RS_TPB) {
+    const K kk = S.key[i];
+    const uint32_t dd = (uint32_t)(kk >> shift) & 255u;
+    const uint64_t pos = (uint64_t)S.gbase[dd] + (i - S.dstart[dd]);
+    if (pos < n) {
+      kout[pos] = kk;
+      vout[pos] = S.val[i];
     }
   }
 }
 
 template <class K>
-void radix_sort_impl(K *keys, uint32_t *vals, uint64_t n, int bits,
-                     cudaStream_t st) {
+void radix_sort_impl(K *keys, uint32_t *vals, uint64_t n, int bits, cudaStream_t st,
+                     int *err) {
   if (n <= 1 || bits <= 0) return;
   if (n >= (1ull << 32)) fail(VG_ERR_NOMEM, "radix sort: more than 2^32 items");
-  uint32_t ntiles = (uint32_t)((n + RS_TILE - 1) / RS_TILE);
-  K *kalt = nullptr;
-  uint32_t *valt = nullptr, *hist = nullptr;
-  VG_CUDA(cudaMallocAsync((void **)&kalt, n * sizeof(K), st));
-  VG_CUDA(cudaMallocAsync((void **)&valt, n * sizeof(uint32_t), st));
-  VG_CUDA(cudaMallocAsync((void **)&hist, (uint64_t)256 * ntiles * 4, st));
-  K *ki = keys, *ko = kalt;
-  uint32_t *vi = vals, *vo = valt;
-  int passes = (bits + 7) / 8;
+  const int passes = std::min((bits + 7) / 8, (int)sizeof(K));
+  const uint64_t ntiles = (n + RS_TILE - 1) / RS_TILE;
+  // scratch: digit counts [passes][256], tickets [passes], tile status
+  // words, then one or two alternate key/value buffers (two for an odd
+  // number of passes above one, so that the last pass lands in `keys`)
+  const int nalt = (passes % 2 == 1 && passes > 1) ? 2 : 1;
+  const uint64_t head = RS_MAXPASS * 256 * 4 + 64;
+  const uint64_t stat = ntiles * 256 * 8;
+  const uint64_t kb = (n * sizeof(K) + 255) & ~255ull, vb = (n * 4 + 255) & ~255ull;
+  char *buf = nullptr;
+  VG_CUDA(cudaMallocAsync((void **)&buf, head + stat + nalt * (kb + vb), st));
+  VG_CUDA(cudaMemsetAsync(buf, 0, head + stat, st));
+  uint32_t *ghist = (uint32_t *)buf;
+  uint32_t *tickets = (uint32_t *)(buf + RS_MAXPASS * 256 * 4);
+  unsigned long long *status = (unsigned long long *)(buf + head);
+  K *ka = (K *)(buf + head + stat);
+  uint32_t *va = (uint32_t *)(buf + head + stat + kb);
+  K *kb2 = nalt == 2 ? (K *)(buf + head + stat + kb + vb) : nullptr;
+  uint32_t *vb2 = nalt == 2 ? (uint32_t *)(buf + head + stat + 2 * kb + vb) : nullptr;
+  const unsigned hblocks = (unsigned)std::min<uint64_t>(ntiles, 152 * 4);
+  rs_upfront<K><<<hblocks, RS_TPB, 0, st>>>(keys, n, passes, ghist);
+  VG_CUDA(cudaGetLastError());
+  // buffer sequence: keys -> a -> keys ... for an even number of passes;
+  // keys -> a -> b -> keys -> ... with three buffers for an odd number
+  K *kbufs[3] = {keys, ka, kb2};
+  uint32_t *vbufs[3] = {vals, va, vb2};
+  int cur = 0;
   for (int p = 0; p < passes; p++) {
-    int shift = 8 * p;
-    rs_hist<K><<<ntiles, RS_TPB, 0, st>>>(ki, n, shift, hist, ntiles);
+    int nxt;
+    if (nalt == 1) nxt = cur == 0 ? 1 : 0;
+    else if (p == passes - 1) nxt = 0;
+    else nxt = cur == 0 ? 1 : (cur == 1 ? 2 : 1);
+    rs_pass<K><<<(unsigned)ntiles, RS_TPB, 0, st>>>(kbufs[cur], vbufs[cur], kbufs[nxt],
+                                                    vbufs[nxt], n, p, ghist, status,
+                                                    tickets + p, err);
     VG_CUDA(cudaGetLastError());
-    exclusive_scan_impl<uint32_t>(hist, hist, (uint64_t)256 * ntiles, st);
-    rs_scatter<K><<<ntiles, RS_TPB, 0, st>>>(ki, vi, ko, vo, n, shift, hist,
-                                             ntiles);
-    VG_CUDA(cudaGetLastError());
-    std::swap(ki, ko);
-    std::swap(vi, vo);
+    cur = nxt;
   }
-  if (ki != keys) {
-    VG_CUDA(cudaMemcpyAsync(keys, ki, n * sizeof(K), cudaMemcpyDeviceToDevice, st));
-    VG_CUDA(cudaMemcpyAsync(vals, vi, n * 4, cudaMemcpyDeviceToDevice, st));
+  if (cur != 0) {  // one pass only
+    VG_CUDA(cudaMemcpyAsync(keys, kbufs[cur], n * sizeof(K), cudaMemcpyDeviceToDevice, st));
+    VG_CUDA(cudaMemcpyAsync(vals, vbufs[cur], n * 4, cudaMemcpyDeviceToDevice, st));
   }
-  VG_CUDA(cudaFreeAsync(kalt, st));
-  VG_CUDA(cudaFreeAsync(valt, st));
-  VG_CUDA(cudaFreeAsync(hist, st));
+  VG_CUDA(cudaFreeAsync(buf, st));
 }
 
 }  // namespace
@@ -229,13 +348,91 @@ void exclusive_scan_u64(const uint64_t *in, uint64_t *out, uint64_t n,
                                           (unsigned long long *)out, n, st);
 }
 void radix_sort_pairs_u32(uint32_t *keys, uint32_t *vals, uint64_t n, int bits,
-                          cudaStream_t st, Sim &) {
-  radix_sort_impl<uint32_t>(keys, vals, n, bits, st);
+                          cudaStream_t st, Sim &s) {
+  radix_sort_impl<uint32_t>(keys, vals, n, bits, st, s.d_status.as<int>());
 }
 void radix_sort_pairs_u64(uint64_t *keys, uint32_t *vals, uint64_t n, int bits,
-                          cudaStream_t st, Sim &) {
-  radix_sort_impl<unsigned long long>((unsigned long long *)keys, vals, n, bits,
-                                      st);
+                          cudaStream_t st, Sim &s) {
+  radix_sort_impl<unsigned long long>((unsigned long long *)keys, vals, n, bits, st,
+                                      s.d_status.as<int>());
 }
 
+void set_last_error(const std::string &m);
+
 }  // namespace vg
+
+// Sorts n generated (key, index) pairs on the device and compares the result
+// with a stable sort on the host.  Keys: splitmix64 of (seed, i), masked to
+// key_bits, with bits [const_lo, const_hi) forced to one (a digit that all
+// keys share exercises the pass that keeps the order).  Returns the number of
+// mismatching positions in *mismatch_out (keys or values).
+extern "C" int vg_selftest_sort(uint64_t n, int key_bits, int wide, int const_lo, int const_hi,
+                                uint64_t seed, uint64_t *mismatch_out) {
+  using namespace vg;
+  try {
+    if (key_bits < 1 || key_bits > (wide ? 64 : 32) || const_lo < 0 || const_hi > key_bits)
+      fail(VG_ERR_ARG, "vg_selftest_sort: bad key bits");
+    std::vector<unsigned long long> k(n);
+    uint64_t cmask = 0;
+    for (int b = const_lo; b < const_hi; b++) cmask |= 1ull << b;
+    const uint64_t kmask = key_bits == 64 ? ~0ull : (1ull << key_bits) - 1;
+    for (uint64_t i = 0; i < n; i++) {
+      uint64_t z = seed + (i + 1) * 0x9E3779B97F4A7C15ull;
+      z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+      z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+      z ^= z >> 31;
+      // clustered keys: a quarter of the keys repeat a small set of values
+      if ((z & 3) == 0) z = (z >> 8) % 7;
+      k[i] = ((z & kmask) | cmask) & kmask;
+    }
+    std::vector<uint32_t> idx(n);
+    std::iota(idx.begin(), idx.end(), 0u);
+    std::vector<uint32_t> ref = idx;
+    std::stable_sort(ref.begin(), ref.end(), [&](uint32_t a, uint32_t b) { return k[a] < k[b]; });
+    cudaStream_t st;
+    VG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    void *dk = nullptr, *dv = nullptr;
+    int *derr = nullptr;
+    VG_CUDA(cudaMalloc(&dk, std::max<uint64_t>(n, 1) * 8));
+    VG_CUDA(cudaMalloc(&dv, std::max<uint64_t>(n, 1) * 4));
+    VG_CUDA(cudaMalloc(&derr, 4));
+    VG_CUDA(cudaMemset(derr, 0, 4));
+    std::vector<uint32_t> k32(wide ? 0 : n);
+    for (uint64_t i = 0; i < k32.size(); i++) k32[i] = (uint32_t)k[i];
+    if (wide)
+      VG_CUDA(cudaMemcpy(dk, k.data(), n * 8, cudaMemcpyHostToDevice));
+    else
+      VG_CUDA(cudaMemcpy(dk, k32.data(), n * 4, cudaMemcpyHostToDevice));
+    VG_CUDA(cudaMemcpy(dv, idx.data(), n * 4, cudaMemcpyHostToDevice));
+    if (wide)
+      radix_sort_impl<unsigned long long>((unsigned long long *)dk, (uint32_t *)dv, n, key_bits,
+                                          st, derr);
+    else
+      radix_sort_impl<uint32_t>((uint32_t *)dk, (uint32_t *)dv, n, key_bits, st, derr);
+    VG_CUDA(cudaStreamSynchronize(st));
+    std::vector<unsigned long long> ok(n);
+    std::vector<uint32_t> ok32(wide ? 0 : n), ov(n);
+    int herr = 0;
+    if (wide)
+      VG_CUDA(cudaMemcpy(ok.data(), dk, n * 8, cudaMemcpyDeviceToHost));
+    else
+      VG_CUDA(cudaMemcpy(ok32.data(), dk, n * 4, cudaMemcpyDeviceToHost));
+    VG_CUDA(cudaMemcpy(ov.data(), dv, n * 4, cudaMemcpyDeviceToHost));
+    VG_CUDA(cudaMemcpy(&herr, derr, 4, cudaMemcpyDeviceToHost));
+    VG_CUDA(cudaFree(dk));
+    VG_CUDA(cudaFree(dv));
+    VG_CUDA(cudaFree(derr));
+    VG_CUDA(cudaStreamDestroy(st));
+    if (herr) fail(VG_ERR_DEVICE, "vg_selftest_sort: device status " + std::to_string(herr));
+    uint64_t bad = 0;
+    for (uint64_t i = 0; i < n; i++) {
+      const unsigned long long kk = wide ? ok[i] : ok32[i];
+      bad += (ov[i] != ref[i]) || (kk != k[ref[i]]);
+    }
+    *mismatch_out = bad;
+    return VG_OK;
+  } catch (const Error &e) {
+    set_last_error(e.msg);
+    return e.code;
+  }
+}
