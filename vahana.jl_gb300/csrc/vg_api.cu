@@ -95,6 +95,18 @@ void *Sim::scratch(size_t bytes) {
   return d_scratch.p;
 }
 
+const void *Sim::const_table(const std::string &key, const void *host, size_t bytes) {
+  ConstTable &t = const_tables[key];
+  const uint8_t *h = (const uint8_t *)host;
+  if (t.dev.p && t.host.size() == bytes && std::equal(t.host.begin(), t.host.end(), h))
+    return t.dev.p;
+  if (!t.dev.p || t.dev.bytes < bytes) t.dev.alloc(std::max<size_t>(bytes, 16), &footprint);
+  t.host.assign(h, h + bytes);
+  // from the kept host copy, which outlives the asynchronous transfer
+  VG_CUDA(cudaMemcpyAsync(t.dev.p, t.host.data(), bytes, cudaMemcpyHostToDevice, stream));
+  return t.dev.p;
+}
+
 void Sim::ensure_device() {
   if (device_ready) return;
   if (!stream) {

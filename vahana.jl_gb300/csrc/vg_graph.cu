@@ -291,7 +291,9 @@ __global__ void __launch_bounds__(TPB) k_rp_fill(const uint32_t *keys, uint64_t 
                                                  const uint32_t *bstart, uint32_t *rp,
                                                  unsigned *maxdeg) {
   __shared__ uint32_t sk[RP_CAP];
-  __shared__ uint32_t rows[RP_ROWS + 1];
+  // row i at rows[i + i / 16]: a thread's 16 consecutive rows and a warp's
+  // 32 consecutive rows both fall in distinct banks
+  __shared__ uint32_t rows[RP_ROWS + 1 + (RP_ROWS + 1) / 16 + 1];
   const uint64_t r0 = (uint64_t)blockIdx.x * RP_ROWS;
   const uint64_t r1 = r0 + RP_ROWS < nrows + 1 ? r0 + RP_ROWS : nrows + 1;
   const uint32_t k0 = bstart[blockIdx.x], k1 = bstart[blockIdx.x + 1];
@@ -314,16 +316,18 @@ __global__ void __launch_bounds__(TPB) k_rp_fill(const uint32_t *keys, uint64_t 
     const uint64_t re = ra + RP_PER_THREAD < r1 ? ra + RP_PER_THREAD : r1;
     for (uint64_t r = ra; r < re; r++) {
       while (lo < m && (uint64_t)ks[lo] < r) lo++;
-      rows[r - r0] = k0 + lo;
+      const uint32_t i = (uint32_t)(r - r0);
+      rows[i + i / 16] = k0 + lo;
     }
   }
-  if (threadIdx.x == 0) rows[r1 - r0] = k1;
+  const uint32_t nr = (uint32_t)(r1 - r0);
+  if (threadIdx.x == 0) rows[nr + nr / 16] = k1;
   __syncthreads();
   unsigned dmax = 0;
-  const uint32_t nr = (uint32_t)(r1 - r0);
   for (uint32_t i = threadIdx.x; i < nr; i += TPB) {
-    rp[r0 + i] = rows[i];
-    if (r0 + i < nrows) dmax = max(dmax, rows[i + 1] - rows[i]);
+    const uint32_t v = rows[i + i / 16];
+    rp[r0 + i] = v;
+    if (r0 + i < nrows) dmax = max(dmax, rows[i + 1 + (i + 1) / 16] - v);
   }
 #pragma unroll
   for (int o = 16; o; o >>= 1) dmax = max(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
@@ -373,29 +377,76 @@ bool build_csr_typed(Sim &s, int e, const EdgeAppend &ap, uint64_t n) {
   c.payload.resize(nf);
   for (int f = 0; f < nf; f++) ensure(c.payload[f], std::max<uint64_t>(n, 1) * ed.fields[f].size);
   ensure(c.d_max_degree, 4);
-  VG_CUDA(cudaMemsetAsync(c.d_max_degree.p, 0, 4, st));
-  Tmp<uint32_t> keys(n, st), vals(n, st);
-  if (n) {
-    k_typed_keys<<<nblk(n), TPB, 0, st>>>(ap.to.as<uint64_t>(),
-                                           ed.stores_src() ? ap.from.as<uint64_t>() : nullptr, n,
-                                           (uint32_t)T, (uint32_t)ap.src_type, nrows, keys.p,
-                                           vals.p, s.d_status.as<int>());
-    radix_sort_pairs_u32(keys.p, vals.p, n, bits_for(nrows ? nrows - 1 : 0), st, s);
+  if (!c.rebuild) c.rebuild.reset(new RebuildCache());
+  RebuildCache &rc = *c.rebuild;
+  const int bits = bits_for(nrows ? nrows - 1 : 0);
+  const uint64_t nbr = (nrows + 1 + RP_ROWS - 1) / RP_ROWS;
+  const uint64_t sort_bytes = radix_sort_scratch_bytes(n, 4, bits);
+  ensure(rc.keys, std::max<uint64_t>(n, 1) * 4);
+  ensure(rc.vals, std::max<uint64_t>(n, 1) * 4);
+  ensure(rc.bstart, (nbr + 1) * 4);
+  if (sort_bytes) ensure(rc.sort, sort_bytes);
+  uint32_t *keys = rc.keys.as<uint32_t>(), *vals = rc.vals.as<uint32_t>();
+  const uint64_t *from = ed.stores_src() ? ap.from.as<uint64_t>() : nullptr;
+  // the launch sequence, a function of these arguments only
+  std::vector<uint64_t> args = {(uint64_t)ap.to.p, (uint64_t)from, n, nrows, (uint64_t)T,
+                                (uint64_t)ap.src_type, (uint64_t)c.row_ptr.p,
+                                (uint64_t)c.src.p, (uint64_t)c.d_max_degree.p,
+                                (uint64_t)keys, (uint64_t)vals, (uint64_t)rc.sort.p,
+                                (uint64_t)rc.bstart.p, (uint64_t)s.d_status.p, (uint64_t)nf};
+  for (int f = 0; f < nf; f++) {
+    args.push_back((uint64_t)ap.payload[f].p);
+    args.push_back((uint64_t)c.payload[f].p);
   }
-  {
-    const uint64_t nbr = (nrows + 1 + RP_ROWS - 1) / RP_ROWS;
-    Tmp<uint32_t> bstart(nbr + 1, st);
-    k_rp_bounds<<<nblk(n + 1), TPB, 0, st>>>(keys.p, n, nbr, bstart.p);
-    k_rp_fill<<<(unsigned)nbr, TPB, 0, st>>>(keys.p, nrows, bstart.p, c.row_ptr.as<uint32_t>(),
+  auto enqueue = [&]() {
+    VG_CUDA(cudaMemsetAsync(c.d_max_degree.p, 0, 4, st));
+    if (n) {
+      k_typed_keys<<<nblk(n), TPB, 0, st>>>(ap.to.as<uint64_t>(), from, n, (uint32_t)T,
+                                             (uint32_t)ap.src_type, nrows, keys, vals,
+                                             s.d_status.as<int>());
+      radix_sort_pairs_u32_in(keys, vals, n, bits, st, s.d_status.as<int>(), rc.sort.p);
+    }
+    k_rp_bounds<<<nblk(n + 1), TPB, 0, st>>>(keys, n, nbr, rc.bstart.as<uint32_t>());
+    k_rp_fill<<<(unsigned)nbr, TPB, 0, st>>>(keys, nrows, rc.bstart.as<uint32_t>(),
+                                             c.row_ptr.as<uint32_t>(),
                                              c.d_max_degree.as<unsigned>());
+    if (n) {
+      if (from) k_gather_src<<<nblk(n), TPB, 0, st>>>(from, vals, n, c.src.as<uint32_t>());
+      for (int f = 0; f < nf; f++)
+        scatter_column(ed.fields[f].size, ap.payload[f].p, vals, nullptr, n, c.payload[f].p, st);
+    }
+    VG_CUDA(cudaGetLastError());
+  };
+  const bool graphable = st != nullptr && st != cudaStreamLegacy && st != cudaStreamPerThread;
+  if (rc.exec && args == rc.graph_args) {
+    VG_CUDA(cudaGraphLaunch(rc.exec, st));
+  } else if (graphable && args == rc.last) {
+    // the same rebuild twice in a row: record it once, replay from now on
+    if (rc.exec) {
+      cudaGraphExecDestroy(rc.exec);
+      rc.exec = nullptr;
+      rc.graph_args.clear();
+    }
+    cudaGraph_t g = nullptr;
+    VG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    try {
+      enqueue();
+    } catch (...) {
+      cudaStreamEndCapture(st, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    VG_CUDA(cudaStreamEndCapture(st, &g));
+    const cudaError_t ie = cudaGraphInstantiate(&rc.exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) rc.exec = nullptr;
+    VG_CUDA(ie);
+    rc.graph_args = args;
+    VG_CUDA(cudaGraphLaunch(rc.exec, st));
+  } else {
+    enqueue();
   }
-  if (n) {
-    if (ed.stores_src())
-      k_gather_src<<<nblk(n), TPB, 0, st>>>(ap.from.as<uint64_t>(), vals.p, n,
-                                             c.src.as<uint32_t>());
-    for (int f = 0; f < nf; f++)
-      scatter_column(ed.fields[f].size, ap.payload[f].p, vals.p, nullptr, n, c.payload[f].p, st);
-  }
+  rc.last = std::move(args);
   VG_CUDA(cudaGetLastError());
   c.nrows = nrows;
   c.nedges = n;

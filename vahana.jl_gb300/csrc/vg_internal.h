@@ -133,8 +133,25 @@ struct AgentStore {
   bool readable = false, writeable = false;
 };
 
+// Persistent scratch of the typed rebuild (the per-step edge rebuild from
+// records whose types the emitting kernel declares) and a CUDA graph of its
+// launch sequence: recorded when the same arguments (sizes and buffers)
+// repeat on consecutive rebuilds, replayed while they stay the same.
+struct RebuildCache {
+  DevBuf keys, vals, sort, bstart;
+  std::vector<uint64_t> last, graph_args;
+  cudaGraphExec_t exec = nullptr;
+  RebuildCache() = default;
+  RebuildCache(const RebuildCache &) = delete;
+  RebuildCache &operator=(const RebuildCache &) = delete;
+  ~RebuildCache() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+};
+
 struct CSR {
   uint64_t nrows = 0, nedges = 0;
+  std::unique_ptr<RebuildCache> rebuild;
   DevBuf row_ptr;  // u32[nrows + 1]
   DevBuf src;      // u32[nedges] source agent_nr - 1
   DevBuf src_type; // u8[nedges] when src_type_const < 0
@@ -232,6 +249,15 @@ struct Sim {
   DevBuf d_scratch;
   size_t scratch_bytes = 0;
   void *scratch(size_t bytes);
+  // constant tables of the transitions (e.g. infection probabilities per
+  // infected-neighbour count), uploaded once per distinct content; the key
+  // names the table, the bytes decide whether the copy is current
+  struct ConstTable {
+    DevBuf dev;
+    std::vector<uint8_t> host;
+  };
+  std::map<std::string, ConstTable> const_tables;
+  const void *const_table(const std::string &key, const void *host, size_t bytes);
   int raster_index(const std::string &n) const;
   // stream and status word are created on first device use, so that the
   // init phase (registry, staging) runs without a GPU
@@ -352,6 +378,10 @@ void radix_sort_pairs_u32(uint32_t *keys, uint32_t *vals, uint64_t n,
                           int bits, cudaStream_t st, Sim &s);
 void radix_sort_pairs_u64(uint64_t *keys, uint32_t *vals, uint64_t n,
                           int bits, cudaStream_t st, Sim &s);
+// caller-owned scratch of radix_sort_scratch_bytes() bytes: no allocation
+uint64_t radix_sort_scratch_bytes(uint64_t n, int key_size, int bits);
+void radix_sort_pairs_u32_in(uint32_t *keys, uint32_t *vals, uint64_t n, int bits,
+                             cudaStream_t st, int *err, void *scratch);
 int bits_for(uint64_t maxval);
 
 // graph building (vg_graph.cu)

@@ -286,22 +286,40 @@ __global__ void __launch_bounds__(RS_TPB) rs_pass(const K *kin, const uint32_t *
   }
 }
 
+// scratch: digit counts [passes][256], tickets [passes], tile status
+// words, then one or two alternate key/value buffers (two for an odd number
+// of passes above one, so that the last pass lands in `keys`)
+struct RsLayout {
+  int passes, nalt;
+  uint64_t ntiles, head, stat, kb, vb;
+  uint64_t bytes() const { return head + stat + nalt * (kb + vb); }
+};
+RsLayout rs_layout(uint64_t n, int key_size, int bits) {
+  RsLayout L;
+  L.passes = std::min((bits + 7) / 8, key_size);
+  L.ntiles = (n + RS_TILE - 1) / RS_TILE;
+  L.nalt = (L.passes % 2 == 1 && L.passes > 1) ? 2 : 1;
+  L.head = RS_MAXPASS * 256 * 4 + 64;
+  L.stat = L.ntiles * 256 * 8;
+  L.kb = (n * key_size + 255) & ~255ull;
+  L.vb = (n * 4 + 255) & ~255ull;
+  return L;
+}
+
+// `scratch`: null (allocated on the stream here) or at least
+// radix_sort_scratch_bytes(n, sizeof(K), bits) bytes owned by the caller;
+// with caller scratch the sort makes no allocation, so it can be recorded
+// into a CUDA graph
 template <class K>
 void radix_sort_impl(K *keys, uint32_t *vals, uint64_t n, int bits, cudaStream_t st,
-                     int *err) {
+                     int *err, void *scratch = nullptr) {
   if (n <= 1 || bits <= 0) return;
   if (n >= (1ull << 32)) fail(VG_ERR_NOMEM, "radix sort: more than 2^32 items");
-  const int passes = std::min((bits + 7) / 8, (int)sizeof(K));
-  const uint64_t ntiles = (n + RS_TILE - 1) / RS_TILE;
-  // scratch: digit counts [passes][256], tickets [passes], tile status
-  // words, then one or two alternate key/value buffers (two for an odd
-  // number of passes above one, so that the last pass lands in `keys`)
-  const int nalt = (passes % 2 == 1 && passes > 1) ? 2 : 1;
-  const uint64_t head = RS_MAXPASS * 256 * 4 + 64;
-  const uint64_t stat = ntiles * 256 * 8;
-  const uint64_t kb = (n * sizeof(K) + 255) & ~255ull, vb = (n * 4 + 255) & ~255ull;
-  char *buf = nullptr;
-  VG_CUDA(cudaMallocAsync((void **)&buf, head + stat + nalt * (kb + vb), st));
+  const RsLayout L = rs_layout(n, (int)sizeof(K), bits);
+  const int passes = L.passes, nalt = L.nalt;
+  const uint64_t ntiles = L.ntiles, head = L.head, stat = L.stat, kb = L.kb, vb = L.vb;
+  char *buf = (char *)scratch;
+  if (!buf) VG_CUDA(cudaMallocAsync((void **)&buf, L.bytes(), st));
   VG_CUDA(cudaMemsetAsync(buf, 0, head + stat, st));
   uint32_t *ghist = (uint32_t *)buf;
   uint32_t *tickets = (uint32_t *)(buf + RS_MAXPASS * 256 * 4);
@@ -333,7 +351,7 @@ void radix_sort_impl(K *keys, uint32_t *vals, uint64_t n, int bits, cudaStream_t
     VG_CUDA(cudaMemcpyAsync(keys, kbufs[cur], n * sizeof(K), cudaMemcpyDeviceToDevice, st));
     VG_CUDA(cudaMemcpyAsync(vals, vbufs[cur], n * 4, cudaMemcpyDeviceToDevice, st));
   }
-  VG_CUDA(cudaFreeAsync(buf, st));
+  if (!scratch) VG_CUDA(cudaFreeAsync(buf, st));
 }
 
 }  // namespace
@@ -350,6 +368,14 @@ void exclusive_scan_u64(const uint64_t *in, uint64_t *out, uint64_t n,
 void radix_sort_pairs_u32(uint32_t *keys, uint32_t *vals, uint64_t n, int bits,
                           cudaStream_t st, Sim &s) {
   radix_sort_impl<uint32_t>(keys, vals, n, bits, st, s.d_status.as<int>());
+}
+uint64_t radix_sort_scratch_bytes(uint64_t n, int key_size, int bits) {
+  if (n <= 1 || bits <= 0) return 0;
+  return rs_layout(n, key_size, bits).bytes();
+}
+void radix_sort_pairs_u32_in(uint32_t *keys, uint32_t *vals, uint64_t n, int bits,
+                             cudaStream_t st, int *err, void *scratch) {
+  radix_sort_impl<uint32_t>(keys, vals, n, bits, st, err, scratch);
 }
 void radix_sort_pairs_u64(uint64_t *keys, uint32_t *vals, uint64_t n, int bits,
                           cudaStream_t st, Sim &s) {

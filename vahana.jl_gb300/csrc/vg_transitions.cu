@@ -953,8 +953,7 @@ void tr_sir(ApplyCtx &c) {
     q = q * om;
     ptab[k] = 1.0 - q;
   }
-  double *d_ptab = (double *)s.scratch(ptab.size() * 8);
-  VG_CUDA(cudaMemcpyAsync(d_ptab, ptab.data(), ptab.size() * 8, cudaMemcpyHostToDevice, s.stream));
+  const double *d_ptab = (const double *)s.const_table("sir.p_infect", ptab.data(), ptab.size() * 8);
   DevAgentView a = agent_view(s, c.call_type);
   if (a.n == 0) return;
   k_sir<<<nblk(a.n), TPB, 0, s.stream>>>(v.row_ptr, v.src, (const uint8_t *)a.rd[0],

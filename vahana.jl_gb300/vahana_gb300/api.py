@@ -631,15 +631,44 @@ def _refs(sim, xs):
     return [sim.T(x).ref for x in xs]
 
 
-def apply_(sim, transition, call, read, write, add_existing=(), with_edge=None, params=()):
-    """apply!(sim, f, call, read, write; add_existing, with_edge) -- src/Simulation.jl:720-821"""
+def _apply_args(sim, transition, call, read, write, add_existing, with_edge, params):
     c, r, w, a = (_refs(sim, call), _refs(sim, read), _refs(sim, write),
                   _refs(sim, add_existing))
     arr = lambda v: (C.c_int * max(len(v), 1))(*v)
     p = (C.c_double * max(len(params), 1))(*[float(x) for x in params])
     we = sim.T(with_edge).index if with_edge is not None else -1
-    check(lib().vg_apply(sim._h, transition.encode(), arr(c), len(c), arr(r), len(r), arr(w),
-                         len(w), arr(a), len(a), we, p, len(params)))
+    return (transition.encode(), arr(c), len(c), arr(r), len(r), arr(w), len(w), arr(a),
+            len(a), we, p, len(params))
+
+
+def _key(x):
+    if x is None or isinstance(x, (str, int, float)):
+        return x
+    if isinstance(x, TypeInfo):
+        return ("T", x.kind, x.name)
+    return tuple(_key(v) for v in x)
+
+
+def apply_(sim, transition, call, read, write, add_existing=(), with_edge=None, params=()):
+    """apply!(sim, f, call, read, write; add_existing, with_edge) -- src/Simulation.jl:720-821
+
+    The marshalled C arguments of a call are kept per simulation, keyed by
+    the arguments, so that a step loop repeating the same apply! pays the
+    conversion once."""
+    cache = sim.__dict__.setdefault("_apply_cache", {})
+    try:
+        key = (transition, _key(call), _key(read), _key(write), _key(add_existing),
+               _key(with_edge), _key(params))
+        args = cache.get(key)
+    except TypeError:  # an unhashable argument: marshal every time
+        key, args = None, None
+    if args is None:
+        args = _apply_args(sim, transition, call, read, write, add_existing, with_edge, params)
+        if key is not None:
+            if len(cache) >= 64:
+                cache.clear()
+            cache[key] = args
+    check(lib().vg_apply(sim._h, *args))
     return sim
 
 
