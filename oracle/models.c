@@ -159,9 +159,13 @@ void or_opinion_step(int64_t n, const uint64_t *rowptr, const uint32_t *src, con
   }
 }
 
-/* ---- Life B3/S23 on a periodic 2-D raster (column-major, first index
- * fastest: cell (x, y) 1-based has linear index (x-1) + (y-1) W) -------- */
-void or_life_step(int64_t W, int64_t H, const uint8_t *a, uint8_t *o, int nthreads) {
+/* ---- Life B3/S23 on a 2-D raster (column-major, first index fastest:
+ * cell (x, y) 1-based has linear index (x-1) + (y-1) W), Moore
+ * neighbourhood as connect_raster_neighbors! builds it (src/Raster.jl:82-167):
+ * periodic wraps (mod1), otherwise positions outside the raster are dropped
+ * (src/Raster.jl:479-499) ------------------------------------------------ */
+void or_life_step_p(int64_t W, int64_t H, int periodic, const uint8_t *a, uint8_t *o,
+                    int nthreads) {
 #pragma omp parallel for schedule(static) num_threads(nthreads)
   for (int64_t y = 0; y < H; y++) {
     for (int64_t x = 0; x < W; x++) {
@@ -169,13 +173,22 @@ void or_life_step(int64_t W, int64_t H, const uint8_t *a, uint8_t *o, int nthrea
       for (int dy = -1; dy <= 1; dy++)
         for (int dx = -1; dx <= 1; dx++) {
           if (!dx && !dy) continue;
-          int64_t xx = (x + dx + W) % W, yy = (y + dy + H) % H;
+          int64_t xx = x + dx, yy = y + dy;
+          if (xx < 0 || xx >= W || yy < 0 || yy >= H) {
+            if (!periodic) continue;
+            xx = (xx + W) % W;
+            yy = (yy + H) % H;
+          }
           cnt += a[yy * W + xx];
         }
       uint8_t al = a[y * W + x];
       o[y * W + x] = (cnt == 3 || (al && cnt == 2)) ? 1 : 0;
     }
   }
+}
+
+void or_life_step(int64_t W, int64_t H, const uint8_t *a, uint8_t *o, int nthreads) {
+  or_life_step_p(W, H, 1, a, o, nthreads);
 }
 
 /* ---- walkers: one Moore offset (stencil order, first dimension fastest,

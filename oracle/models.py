@@ -24,6 +24,8 @@ def lib():
         _L.or_opinion_step.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int]
         _L.or_life_step.argtypes = [C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_int]
+        _L.or_life_step_p.argtypes = [C.c_int64, C.c_int64, C.c_int, C.c_void_p, C.c_void_p,
+                                      C.c_int]
         _L.or_walk_step.argtypes = [C.c_int64, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p,
                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32,
                                     C.c_int]
@@ -117,10 +119,10 @@ def run_opinion(n, frm, to, w, x, eps, steps, a=0.5, b=0.5):
     return x
 
 
-def life_step(alive, W, H, nthreads=None):
+def life_step(alive, W, H, nthreads=None, periodic=True):
     a = np.ascontiguousarray(alive, dtype=np.uint8)
     o = np.empty_like(a)
-    lib().or_life_step(W, H, _p(a), _p(o), nthreads or threads())
+    lib().or_life_step_p(W, H, int(bool(periodic)), _p(a), _p(o), nthreads or threads())
     return o
 
 

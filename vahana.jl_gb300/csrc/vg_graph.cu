@@ -249,35 +249,45 @@ namespace {
 // row key of each record (target agent_nr - 1); a record of another type or
 // beyond the rows sets the status word (the records come from kernels that
 // declare their types)
+// vals: the record number k, or (src_vals) the source's agent_nr - 1, which
+// the stable sort then carries straight into the CSR's source column
 __global__ void k_typed_keys(const uint64_t *to, const uint64_t *from, uint64_t n,
                              uint32_t target_type, uint32_t src_type, uint64_t nrows,
-                             uint32_t *keys, uint32_t *vals, int *status) {
+                             uint32_t *keys, uint32_t *vals, int src_vals, int *status) {
   uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   const uint64_t t = to[k];
   uint64_t r = (t & NR_MASK) - 1;
   bool bad = (uint32_t)(t >> SHIFT_TYPE) != target_type || r >= nrows;
-  if (from && (uint32_t)(from[k] >> SHIFT_TYPE) != src_type) bad = true;
+  uint64_t f = 0;
+  if (from) {
+    f = from[k];
+    if ((uint32_t)(f >> SHIFT_TYPE) != src_type) bad = true;
+  }
   if (bad) {
     atomicCAS(status, 0, 501);
     r = 0;
   }
   keys[k] = (uint32_t)r;
-  vals[k] = (uint32_t)k;
+  vals[k] = src_vals ? (uint32_t)((f & NR_MASK) - 1) : (uint32_t)k;
 }
 
 // row_ptr of the rows 0..nrows from the sorted row keys: rp[r] = the
-// number of keys below r.  Rows are cut into blocks of RP_ROWS; a first
-// pass over the records finds, for every block boundary j * RP_ROWS, the
-// first record at or above it (record k owns the boundaries in
-// (keys[k-1], keys[k]]); then each block stages its records' keys in
-// shared memory, finds every row's first record by a short search there,
-// stores its rows contiguously and reduces the largest row length of the
-// block into *maxdeg.  Blocks whose records do not fit in shared memory
-// search in global memory instead.
-constexpr uint32_t RP_ROWS = 4096;
-constexpr uint32_t RP_CAP = 4096;
-constexpr uint32_t RP_PER_THREAD = RP_ROWS / TPB;
+// number of keys below r.  Rows are cut into spans of RP_ROWS, one block
+// each; a first pass over the records finds, for every span boundary
+// j * RP_ROWS, the first record at or above it (record k owns the boundaries
+// in (keys[k-1], keys[k]]).  In the block, the last record of each row's run
+// stores its end position (relative to the span's first record) at the
+// row's slot in shared memory -- one plain store per non-empty row, however
+// long the run.  Since the ends grow with the row, rp of a row is the
+// largest end stored before it: an exclusive max-scan (each thread 32
+// consecutive rows, then across the threads), which also gives every
+// non-empty row's length for the block's largest degree.  The rows leave
+// shared memory as coalesced 16-byte stores.  Shared rows are swizzled in
+// 16-byte chunks (chunk q of thread t at q ^ (t & 7)) so that both the
+// per-thread and the per-warp access patterns avoid bank conflicts.
+constexpr uint32_t RP_ROWS = 8192;
+constexpr uint32_t RP_PER_THREAD = RP_ROWS / TPB;  // 32
 
 __global__ void k_rp_bounds(const uint32_t *keys, uint64_t n, uint64_t nbr, uint32_t *bstart) {
   const uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -287,51 +297,82 @@ __global__ void k_rp_bounds(const uint32_t *keys, uint64_t n, uint64_t nbr, uint
   for (uint64_t j = jlo; j <= jhi; j++) bstart[j] = (uint32_t)k;
 }
 
+// shared word of row i of the span (32 rows per thread, 8 chunks of 4)
+__device__ __forceinline__ uint32_t rp_slot(uint32_t i) {
+  const uint32_t t = i >> 5, q = (i >> 2) & 7u;
+  return (t << 5) | ((q ^ (t & 7u)) << 2) | (i & 3u);
+}
+
 __global__ void __launch_bounds__(TPB) k_rp_fill(const uint32_t *keys, uint64_t nrows,
                                                  const uint32_t *bstart, uint32_t *rp,
                                                  unsigned *maxdeg) {
-  __shared__ uint32_t sk[RP_CAP];
-  // row i at rows[i + i / 16]: a thread's 16 consecutive rows and a warp's
-  // 32 consecutive rows both fall in distinct banks
-  __shared__ uint32_t rows[RP_ROWS + 1 + (RP_ROWS + 1) / 16 + 1];
-  const uint64_t r0 = (uint64_t)blockIdx.x * RP_ROWS;
-  const uint64_t r1 = r0 + RP_ROWS < nrows + 1 ? r0 + RP_ROWS : nrows + 1;
+  __shared__ __align__(16) uint32_t E[RP_ROWS];
+  __shared__ uint32_t ws[32];
+  const uint32_t tid = threadIdx.x;
+  const uint64_t R0 = (uint64_t)blockIdx.x * RP_ROWS;
+  const uint64_t R1 = R0 + RP_ROWS < nrows + 1 ? R0 + RP_ROWS : nrows + 1;
   const uint32_t k0 = bstart[blockIdx.x], k1 = bstart[blockIdx.x + 1];
-  const uint32_t m = k1 - k0;
-  const bool fits = m <= RP_CAP;
-  if (fits)
-    for (uint32_t i = threadIdx.x; i < m; i += TPB) sk[i] = keys[k0 + i];
+  uint4 *E4 = reinterpret_cast<uint4 *>(E);
+  for (uint32_t i = tid; i < RP_ROWS / 4; i += TPB) E4[i] = make_uint4(0, 0, 0, 0);
   __syncthreads();
-  const uint32_t *ks = fits ? sk : keys + k0;
-  // thread t: rows r0 + t * RP_PER_THREAD ... (+ RP_PER_THREAD), one search
-  // for the first, then a forward walk
-  const uint64_t ra = r0 + (uint64_t)threadIdx.x * RP_PER_THREAD;
-  if (ra < r1) {
-    uint32_t lo = 0, hi = m;
-    while (lo < hi) {
-      const uint32_t mid = (lo + hi) >> 1;
-      if ((uint64_t)ks[mid] < ra) lo = mid + 1;
-      else hi = mid;
-    }
-    const uint64_t re = ra + RP_PER_THREAD < r1 ? ra + RP_PER_THREAD : r1;
-    for (uint64_t r = ra; r < re; r++) {
-      while (lo < m && (uint64_t)ks[lo] < r) lo++;
-      const uint32_t i = (uint32_t)(r - r0);
-      rows[i + i / 16] = k0 + lo;
-    }
+  for (uint32_t k = k0 + tid; k < k1; k += TPB) {
+    const uint32_t key = keys[k];
+    if (k + 1 == k1 || keys[k + 1] != key) E[rp_slot(key - (uint32_t)R0)] = k + 1 - k0;
   }
-  const uint32_t nr = (uint32_t)(r1 - r0);
-  if (threadIdx.x == 0) rows[nr + nr / 16] = k1;
   __syncthreads();
+  // pass 1: the largest end in the thread's 32 rows (its last stored end)
+  uint4 v[RP_PER_THREAD / 4];
+  uint32_t m = 0;
+#pragma unroll
+  for (uint32_t q = 0; q < RP_PER_THREAD / 4; q++) {
+    v[q] = E4[(tid << 3) | (q ^ (tid & 7u))];
+    m = max(m, max(max(v[q].x, v[q].y), max(v[q].z, v[q].w)));
+  }
+  // exclusive max-scan over the threads
+  const uint32_t lane = tid & 31, wid = tid >> 5;
+  uint32_t incl = m;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= (uint32_t)o) incl = max(incl, y);
+  }
+  if (lane == 31) ws[wid] = incl;
+  __syncthreads();
+  uint32_t before = 0;
+  for (uint32_t w2 = 0; w2 < wid; w2++) before = max(before, ws[w2]);
+  const uint32_t excl_lane = __shfl_up_sync(0xffffffffu, incl, 1);
+  uint32_t run = max(before, lane ? excl_lane : 0u);
+  // pass 2: rp of each row = the largest end before it; row lengths
   unsigned dmax = 0;
-  for (uint32_t i = threadIdx.x; i < nr; i += TPB) {
-    const uint32_t v = rows[i + i / 16];
-    rp[r0 + i] = v;
-    if (r0 + i < nrows) dmax = max(dmax, rows[i + 1 + (i + 1) / 16] - v);
+  const uint32_t row0 = tid * RP_PER_THREAD;
+#pragma unroll
+  for (uint32_t q = 0; q < RP_PER_THREAD / 4; q++) {
+    uint32_t e[4] = {v[q].x, v[q].y, v[q].z, v[q].w}, o[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      o[j] = k0 + run;
+      if (e[j]) {
+        if (R0 + row0 + q * 4 + j < nrows) dmax = max(dmax, e[j] - run);
+        run = e[j];
+      }
+    }
+    v[q] = make_uint4(o[0], o[1], o[2], o[3]);
+  }
+  __syncthreads();  // every thread has read its ends
+#pragma unroll
+  for (uint32_t q = 0; q < RP_PER_THREAD / 4; q++) E4[(tid << 3) | (q ^ (tid & 7u))] = v[q];
+  __syncthreads();
+  const uint32_t nr = (uint32_t)(R1 - R0);
+  if (nr == RP_ROWS && ((uintptr_t)(rp + R0) & 15) == 0) {
+    uint4 *out = reinterpret_cast<uint4 *>(rp + R0);
+    for (uint32_t c = tid; c < RP_ROWS / 4; c += TPB)
+      out[c] = E4[((c >> 3) << 3) | ((c & 7u) ^ ((c >> 3) & 7u))];
+  } else {
+    for (uint32_t i = tid; i < nr; i += TPB) rp[R0 + i] = E[rp_slot(i)];
   }
 #pragma unroll
-  for (int o = 16; o; o >>= 1) dmax = max(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
-  if ((threadIdx.x & 31) == 0 && dmax) atomicMax(maxdeg, dmax);
+  for (int off = 16; off; off >>= 1) dmax = max(dmax, __shfl_xor_sync(0xffffffffu, dmax, off));
+  if (lane == 0 && dmax) atomicMax(maxdeg, dmax);
 }
 
 __global__ void k_gather_src(const uint64_t *from, const uint32_t *vals, uint64_t n,
@@ -386,8 +427,11 @@ bool build_csr_typed(Sim &s, int e, const EdgeAppend &ap, uint64_t n) {
   ensure(rc.vals, std::max<uint64_t>(n, 1) * 4);
   ensure(rc.bstart, (nbr + 1) * 4);
   if (sort_bytes) ensure(rc.sort, sort_bytes);
-  uint32_t *keys = rc.keys.as<uint32_t>(), *vals = rc.vals.as<uint32_t>();
   const uint64_t *from = ed.stores_src() ? ap.from.as<uint64_t>() : nullptr;
+  // without payload columns the sorted values are the source column itself
+  const bool src_vals = from && nf == 0;
+  uint32_t *keys = rc.keys.as<uint32_t>();
+  uint32_t *vals = src_vals ? c.src.as<uint32_t>() : rc.vals.as<uint32_t>();
   // the launch sequence, a function of these arguments only
   std::vector<uint64_t> args = {(uint64_t)ap.to.p, (uint64_t)from, n, nrows, (uint64_t)T,
                                 (uint64_t)ap.src_type, (uint64_t)c.row_ptr.p,
@@ -403,7 +447,7 @@ bool build_csr_typed(Sim &s, int e, const EdgeAppend &ap, uint64_t n) {
     if (n) {
       k_typed_keys<<<nblk(n), TPB, 0, st>>>(ap.to.as<uint64_t>(), from, n, (uint32_t)T,
                                              (uint32_t)ap.src_type, nrows, keys, vals,
-                                             s.d_status.as<int>());
+                                             (int)src_vals, s.d_status.as<int>());
       radix_sort_pairs_u32_in(keys, vals, n, bits, st, s.d_status.as<int>(), rc.sort.p);
     }
     k_rp_bounds<<<nblk(n + 1), TPB, 0, st>>>(keys, n, nbr, rc.bstart.as<uint32_t>());
@@ -411,7 +455,8 @@ bool build_csr_typed(Sim &s, int e, const EdgeAppend &ap, uint64_t n) {
                                              c.row_ptr.as<uint32_t>(),
                                              c.d_max_degree.as<unsigned>());
     if (n) {
-      if (from) k_gather_src<<<nblk(n), TPB, 0, st>>>(from, vals, n, c.src.as<uint32_t>());
+      if (from && !src_vals)
+        k_gather_src<<<nblk(n), TPB, 0, st>>>(from, vals, n, c.src.as<uint32_t>());
       for (int f = 0; f < nf; f++)
         scatter_column(ed.fields[f].size, ap.payload[f].p, vals, nullptr, n, c.payload[f].p, st);
     }

@@ -132,6 +132,7 @@ constexpr int RS_MAXPASS = 8;
 // (every write is bounds-checked, so a failed pass stays in bounds)
 constexpr uint32_t RS_SPIN_LIMIT = 1u << 21;
 constexpr int RS_ERR_LOOKBACK = 0x5e01;
+constexpr int RS_LOOK = 8;  // predecessor tiles read per look-back round trip
 
 // status word of (tile, digit): count in bits 0..31, flag in bits 32..33
 // (1: the tile's own count, 2: inclusive prefix over tiles 0..tile), pass
@@ -180,7 +181,7 @@ struct RsShared {
 // look-back, staged in shared memory in digit order and written out in
 // runs of consecutive positions.
 template <class K>
-__global__ void __launch_bounds__(RS_TPB) rs_pass(const K *kin, const uint32_t *vin, K *kout,
+__global__ void __launch_bounds__(RS_TPB, 4) rs_pass(const K *kin, const uint32_t *vin, K *kout,
                                                    uint32_t *vout, uint64_t n, int pass,
                                                    const uint32_t *ghist,
                                                    unsigned long long *status,
@@ -244,22 +245,41 @@ __global__ void __launch_bounds__(RS_TPB) rs_pass(const K *kin, const uint32_t *
   const uint32_t gex = block_exclusive_scan<uint32_t>(gcount, S.ws, (uint32_t *)nullptr);
   uint32_t excl = 0;
   if (tile) {
-    uint32_t t = tile - 1, spins = 0;
-    for (;;) {
-      const unsigned long long v = ld_status(status + (uint64_t)t * 256 + d);
-      const uint32_t flag = (v >> 34) == (unsigned long long)(pass + 1) ? (uint32_t)(v >> 32) & 3u : 0u;
-      if (!flag) {
+    // RS_LOOK predecessors per round trip: their words are loaded together
+    // and consumed in order until a prefix, or a word not yet published
+    int64_t t = (int64_t)tile - 1;
+    uint32_t spins = 0;
+    bool done = false;
+    while (!done) {
+      unsigned long long v[RS_LOOK];
+#pragma unroll
+      for (int i = 0; i < RS_LOOK; i++)
+        v[i] = t - i >= 0 ? ld_status(status + (uint64_t)(t - i) * 256 + d) : 0ull;
+      int used = 0;
+#pragma unroll
+      for (int i = 0; i < RS_LOOK; i++) {
+        if (used != i || t - i < 0) break;
+        const uint32_t flag =
+            (v[i] >> 34) == (unsigned long long)(pass + 1) ? (uint32_t)(v[i] >> 32) & 3u : 0u;
+        if (!flag) break;
+        excl += (uint32_t)v[i];
+        used++;
+        if (flag == 2u || t - i == 0) {
+          done = true;
+          break;
+        }
+      }
+      if (done) break;
+      t -= used;
+      if (used) {
+        spins = 0;
+      } else {
         if (++spins > RS_SPIN_LIMIT) {
           atomicCAS(err, 0, RS_ERR_LOOKBACK);
           break;
         }
         if (spins > 16) __nanosleep(64);
-        continue;
       }
-      spins = 0;
-      excl += (uint32_t)v;
-      if (flag == 2u || t == 0) break;
-      t--;
     }
     st_status(my, tag | (2ull << 32) | (excl + c));
   }

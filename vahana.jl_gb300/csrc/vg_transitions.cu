@@ -485,26 +485,60 @@ __global__ void k_sir(const uint32_t *__restrict__ rp, const uint32_t *__restric
 // x + i): per row the sum of left, centre and right neighbours in every
 // byte lane, three rows added and the centre subtracted; a lane never
 // exceeds 8, so no byte lane carries into the next.
-__device__ __forceinline__ uint32_t life_rowsum(const uint32_t *__restrict__ row, int64_t qx,
-                                                int64_t Wq, int periodic) {
-  const uint32_t c = row[qx];
-  const uint32_t lw = qx > 0 ? row[qx - 1] : (periodic ? row[Wq - 1] : 0u);
-  const uint32_t rw = qx + 1 < Wq ? row[qx + 1] : (periodic ? row[0] : 0u);
+// Moore neighbourhood of 2-D Life with four cells per 32-bit word (one
+// byte each, 0 or 1): the sums of three horizontally adjacent cells of a
+// row for all four bytes at once (no byte exceeds 3, so no carries cross
+// bytes).  A warp holds 32 consecutive words of a row; the neighbouring
+// words come from the adjacent lanes, and only the warp's edge lanes load.
+// Row y of the raster (wrapped when periodic); 0 outside a non-periodic
+// raster.  Warp-uniform: y is the same in every lane.
+__device__ __forceinline__ uint32_t life_rowsum(const uint32_t *__restrict__ a, int64_t y,
+                                                int64_t qx, int64_t Wq, int64_t H,
+                                                int periodic, uint32_t &self) {
+  if (y < 0 || y >= H) {
+    if (!periodic) {
+      self = 0;
+      return 0;
+    }
+    y = y < 0 ? H - 1 : y - H;
+  }
+  const uint32_t *row = a + y * Wq;
+  const unsigned lane = threadIdx.x & 31;
+  const bool valid = qx < Wq;
+  const uint32_t c = valid ? row[qx] : 0u;
+  uint32_t lw = __shfl_up_sync(0xffffffffu, c, 1);
+  uint32_t rw = __shfl_down_sync(0xffffffffu, c, 1);
+  if (valid && lane == 0) lw = qx > 0 ? row[qx - 1] : (periodic ? row[Wq - 1] : 0u);
+  if (valid && (lane == 31 || qx + 1 >= Wq))
+    rw = qx + 1 < Wq ? row[qx + 1] : (periodic ? row[0] : 0u);
+  self = c;
   return ((c << 8) | (lw >> 24)) + c + ((c >> 8) | (rw << 24));
 }
 
-__global__ void k_life2d_x4(const uint32_t *__restrict__ a, uint32_t *__restrict__ o,
-                            int64_t Wq, int64_t H, int periodic) {
-  const int64_t qx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t y = (int64_t)blockIdx.y * blockDim.y + threadIdx.y;
-  if (qx >= Wq || y >= H) return;
-  const uint32_t self = a[y * Wq + qx];
-  uint32_t cnt = life_rowsum(a + y * Wq, qx, Wq, periodic) - self;
-  if (y > 0 || periodic) cnt += life_rowsum(a + ((y + H - 1) % H) * Wq, qx, Wq, periodic);
-  if (y + 1 < H || periodic) cnt += life_rowsum(a + ((y + 1) % H) * Wq, qx, Wq, periodic);
-  const uint32_t born = __vcmpeq4(cnt, 0x03030303u);
-  const uint32_t stay = __vcmpeq4(cnt, 0x02020202u) & __vcmpne4(self, 0u);
-  o[y * Wq + qx] = (born | stay) & 0x01010101u;
+// blocks of 32 x 8 threads; each thread LIFE_ROWS consecutive rows of one
+// word column, keeping the three row sums it needs in registers
+constexpr int LIFE_ROWS = 4;
+
+__global__ void __launch_bounds__(256) k_life2d_x4(const uint32_t *__restrict__ a,
+                                                   uint32_t *__restrict__ o, int64_t Wq,
+                                                   int64_t H, int periodic) {
+  const int64_t qx = (int64_t)blockIdx.x * 32 + (threadIdx.x & 31);
+  const int64_t y0 = ((int64_t)blockIdx.y * blockDim.y + threadIdx.y) * LIFE_ROWS;
+  if (y0 >= H) return;  // warp-uniform
+  const int64_t y1 = y0 + LIFE_ROWS < H ? y0 + LIFE_ROWS : H;
+  uint32_t selfp, selfc, selfn;
+  uint32_t sp = life_rowsum(a, y0 - 1, qx, Wq, H, periodic, selfp);
+  uint32_t sc = life_rowsum(a, y0, qx, Wq, H, periodic, selfc);
+  for (int64_t y = y0; y < y1; y++) {
+    const uint32_t sn = life_rowsum(a, y + 1, qx, Wq, H, periodic, selfn);
+    const uint32_t cnt = sp + sc + sn - selfc;
+    const uint32_t born = __vcmpeq4(cnt, 0x03030303u);
+    const uint32_t stay = __vcmpeq4(cnt, 0x02020202u) & __vcmpne4(selfc, 0u);
+    if (qx < Wq) o[y * Wq + qx] = (born | stay) & 0x01010101u;
+    sp = sc;
+    sc = sn;
+    selfc = selfn;
+  }
 }
 
 __global__ void k_life2d(const uint8_t *__restrict__ a, uint8_t *__restrict__ o,
@@ -994,7 +1028,8 @@ void tr_life(ApplyCtx &c) {
   if (moore2d && st.dims[0] % 4 == 0 && ((uintptr_t)in % 4) == 0 && ((uintptr_t)out % 4) == 0) {
     const int64_t Wq = st.dims[0] / 4;
     dim3 blk(32, 8);
-    dim3 grd((unsigned)((Wq + 31) / 32), (unsigned)((st.dims[1] + 7) / 8));
+    dim3 grd((unsigned)((Wq + 31) / 32),
+             (unsigned)((st.dims[1] + 8 * LIFE_ROWS - 1) / (8 * LIFE_ROWS)));
     k_life2d_x4<<<grd, blk, 0, s.stream>>>((const uint32_t *)in, (uint32_t *)out, Wq, st.dims[1],
                                           st.periodic);
   } else if (moore2d) {
