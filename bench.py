@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--plain-sample", type=int, default=24)
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=200)
+    ap.add_argument("--model-steps", type=int, default=0,
+                    help="sir/life workloads: timed steps (default: the model's 100 / 1000)")
     return ap.parse_args()
 
 
@@ -581,7 +583,7 @@ def run_model(args):
     for _ in range(args.warmup):
         run.step()
     vh.synchronize(run.sim)
-    K = steps
+    K = args.model_steps or steps
     total_ms, per, clocks = _timed_steps(run.step, stream, K, Clocks(0))
     vh.synchronize(run.sim)
     mean_ms = total_ms / K

@@ -348,6 +348,12 @@ int vg_selftest_fp64(uint64_t n, uint64_t seed, uint64_t *counts_out);
 int vg_selftest_sort(uint64_t n, int key_bits, int wide, int const_lo, int const_hi,
                      uint64_t seed, uint64_t *mismatch_out);
 
+/* Exclusive prefix sum of n generated values (32-bit, or 64-bit when
+ * wide != 0; in place when in_place != 0) with the library's single-pass
+ * device scan, compared with a host prefix sum; *mismatch_out = mismatching
+ * items.  The scan builds row pointers and compaction positions. */
+int vg_selftest_scan(uint64_t n, int wide, int in_place, uint64_t seed, uint64_t *mismatch_out);
+
 /* ---- allocation-free SIR step ---------------------------------------------
  * No counterpart in the reference.  One step of the "sir" transition on
  * device buffers the caller owns, for callers that cannot let a library

@@ -1,5 +1,6 @@
 """The device radix sort that rebuilds every CSR in insertion order (stable
-LSD sort, one launch per 8-bit digit with a chained look-back over tiles):
+LSD sort, one launch per 8-bit digit with a chained look-back over tiles)
+and the single-pass prefix scan behind row pointers and compactions:
 keys and carried indices equal a stable host sort for sizes around the
 2048-item tile, odd and even digit counts, 32- and 64-bit keys, and digits
 that every key shares."""
@@ -35,4 +36,16 @@ def test_radix_sort_matches_stable_host_sort(vh, n, bits, wide, lo, hi):
     from vahana_gb300._lib import check, lib
     bad = C.c_uint64(99)
     check(lib().vg_selftest_sort(n, bits, wide, lo, hi, 1234 + n, C.byref(bad)))
+    assert bad.value == 0
+
+
+@pytest.mark.parametrize("n", [0, 1, 4095, 4096, 4097, 100_003, 3_000_001, 16_777_217])
+@pytest.mark.parametrize("wide", [0, 1])
+@pytest.mark.parametrize("in_place", [0, 1])
+def test_scan_matches_host_prefix_sum(vh, n, wide, in_place):
+    from vahana_gb300._lib import check, lib
+    if wide and n > 4_000_000:
+        pytest.skip("the 64-bit case is covered at 3e6 items")
+    bad = C.c_uint64(99)
+    check(lib().vg_selftest_scan(n, wide, in_place, 4321 + n, C.byref(bad)))
     assert bad.value == 0

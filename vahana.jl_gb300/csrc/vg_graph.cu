@@ -342,23 +342,19 @@ __global__ void __launch_bounds__(TPB) k_rp_fill(const uint32_t *keys, uint64_t 
   for (uint32_t w2 = 0; w2 < wid; w2++) before = max(before, ws[w2]);
   const uint32_t excl_lane = __shfl_up_sync(0xffffffffu, incl, 1);
   uint32_t run = max(before, lane ? excl_lane : 0u);
-  // pass 2: rp of each row = the largest end before it; row lengths
+  // pass 2: rp of each row = the largest end before it; a row's length is
+  // its end minus that (0 for rows without an end: max(e, run) = run);
+  // rows at or beyond nrows hold no end
   unsigned dmax = 0;
-  const uint32_t row0 = tid * RP_PER_THREAD;
 #pragma unroll
   for (uint32_t q = 0; q < RP_PER_THREAD / 4; q++) {
-    uint32_t e[4] = {v[q].x, v[q].y, v[q].z, v[q].w}, o[4];
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-      o[j] = k0 + run;
-      if (e[j]) {
-        if (R0 + row0 + q * 4 + j < nrows) dmax = max(dmax, e[j] - run);
-        run = e[j];
-      }
-    }
-    v[q] = make_uint4(o[0], o[1], o[2], o[3]);
+    uint32_t o0, o1, o2, o3, t;
+    t = max(v[q].x, run); dmax = max(dmax, t - run); o0 = k0 + run; run = t;
+    t = max(v[q].y, run); dmax = max(dmax, t - run); o1 = k0 + run; run = t;
+    t = max(v[q].z, run); dmax = max(dmax, t - run); o2 = k0 + run; run = t;
+    t = max(v[q].w, run); dmax = max(dmax, t - run); o3 = k0 + run; run = t;
+    v[q] = make_uint4(o0, o1, o2, o3);
   }
-  __syncthreads();  // every thread has read its ends
 #pragma unroll
   for (uint32_t q = 0; q < RP_PER_THREAD / 4; q++) E4[(tid << 3) | (q ^ (tid & 7u))] = v[q];
   __syncthreads();

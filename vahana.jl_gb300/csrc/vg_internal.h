@@ -378,6 +378,10 @@ void radix_sort_pairs_u32(uint32_t *keys, uint32_t *vals, uint64_t n,
                           int bits, cudaStream_t st, Sim &s);
 void radix_sort_pairs_u64(uint64_t *keys, uint32_t *vals, uint64_t n,
                           int bits, cudaStream_t st, Sim &s);
+// caller-owned scratch of exclusive_scan_scratch_bytes(n) bytes: no allocation
+uint64_t exclusive_scan_scratch_bytes(uint64_t n);
+void exclusive_scan_u32_in(const uint32_t *in, uint32_t *out, uint64_t n, cudaStream_t st,
+                           int *err, void *scratch);
 // caller-owned scratch of radix_sort_scratch_bytes() bytes: no allocation
 uint64_t radix_sort_scratch_bytes(uint64_t n, int key_size, int bits);
 void radix_sort_pairs_u32_in(uint32_t *keys, uint32_t *vals, uint64_t n, int bits,

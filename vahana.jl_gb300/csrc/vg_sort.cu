@@ -53,20 +53,6 @@ __device__ T block_exclusive_scan(T v, T *warp_sums, T *block_total) {
   return r;
 }
 
-template <class T>
-__global__ void scan_partials(const T *in, uint64_t n, T *partials) {
-  __shared__ T ws[32];
-  __shared__ T tot;
-  uint64_t base = (uint64_t)blockIdx.x * SCAN_CHUNK;
-  T s = 0;
-  for (int k = 0; k < SCAN_IPT; k++) {
-    uint64_t i = base + (uint64_t)k * SCAN_TPB + threadIdx.x;
-    if (i < n) s += in[i];
-  }
-  block_exclusive_scan<T>(s, ws, &tot);
-  if (threadIdx.x == 0) partials[blockIdx.x] = tot;
-}
-
 // Each thread owns SCAN_IPT consecutive items; safe in place.
 template <class T>
 __global__ void scan_apply(const T *in, T *out, uint64_t n, const T *prefix) {
@@ -91,23 +77,151 @@ __global__ void scan_apply(const T *in, T *out, uint64_t n, const T *prefix) {
   }
 }
 
+// Single-pass exclusive scan over tiles of SCAN_CHUNK items with decoupled
+// look-back (D. Merrill and M. Garland, NVR-2016-002): a tile publishes its
+// total, then warp 0 reads the flags of the 32 preceding tiles at once and
+// adds totals back to the nearest tile whose inclusive prefix is known.
+// Tiles take their index from a ticket counter in start order (a tile only
+// waits for running tiles); every wait is bounded and records an error in
+// *err when it gives up.  In place is allowed (a tile reads all its items
+// before it writes).
+constexpr uint32_t SCAN_SPIN_LIMIT = 1u << 21;
+constexpr int SCAN_ERR_LOOKBACK = 0x5e02;
+
+__device__ __forceinline__ void st_release_u32(uint32_t *a, uint32_t v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(a), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t *a) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(a) : "memory");
+  return v;
+}
+__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t *a) {
+  uint32_t v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(a) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long *a) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(a) : "memory");
+  return v;
+}
+
 template <class T>
-void exclusive_scan_impl(const T *in, T *out, uint64_t n, cudaStream_t st) {
+struct ScanState {
+  uint32_t *flag;  // per tile: 0 nothing, 1 total in agg, 2 inclusive prefix in pre
+  T *agg, *pre;
+  uint32_t *ticket;
+};
+
+template <class T>
+__global__ void __launch_bounds__(SCAN_TPB) scan_lookback(const T *in, T *out, uint64_t n,
+                                                          ScanState<T> S, int *err) {
+  __shared__ T ws[32];
+  __shared__ T s_tot, s_excl;
+  __shared__ uint32_t s_tile;
+  if (threadIdx.x == 0) s_tile = atomicAdd(S.ticket, 1u);
+  __syncthreads();
+  const uint32_t tile = s_tile;
+  const uint64_t base = (uint64_t)tile * SCAN_CHUNK + (uint64_t)threadIdx.x * SCAN_IPT;
+  T v[SCAN_IPT];
+  T sum = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_IPT; k++) {
+    const uint64_t i = base + k;
+    v[k] = i < n ? in[i] : T(0);
+    sum += v[k];
+  }
+  T run = block_exclusive_scan<T>(sum, ws, &s_tot);
+  if (threadIdx.x < 32) {
+    const uint32_t lane = threadIdx.x;
+    const T total = s_tot;
+    T excl = 0;
+    if (tile == 0) {
+      if (lane == 0) {
+        S.pre[0] = total;
+        st_release_u32(S.flag, 2u);
+      }
+    } else {
+      if (lane == 0) {
+        S.agg[tile] = total;
+        st_release_u32(S.flag + tile, 1u);
+      }
+      int64_t t = (int64_t)tile - 1;
+      uint32_t spins = 0;
+      for (;;) {
+        const int64_t tt = t - (int64_t)lane;
+        const uint32_t f = tt >= 0 ? ld_acquire_u32(S.flag + tt) : 2u;
+        const unsigned pm = __ballot_sync(0xffffffffu, f == 2u);
+        const unsigned zm = __ballot_sync(0xffffffffu, f == 0u);
+        const int P = pm ? __ffs(pm) - 1 : 32;  // nearest predecessor with a prefix
+        const unsigned need = P == 32 ? 0xffffffffu : (2u << P) - 1u;
+        if (zm & need) {  // a tile in between has published nothing yet
+          if (++spins > SCAN_SPIN_LIMIT) {
+            if (lane == 0) atomicCAS(err, 0, SCAN_ERR_LOOKBACK);
+            break;
+          }
+          if (spins > 16) __nanosleep(64);
+          continue;
+        }
+        T x = 0;
+        if ((int)lane < P) x = ld_relaxed(S.agg + tt);
+        else if ((int)lane == P && tt >= 0) x = ld_relaxed(S.pre + tt);
+#pragma unroll
+        for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        excl += x;
+        if (P < 32) break;
+        t -= 32;
+        spins = 0;
+      }
+      if (lane == 0) {
+        S.pre[tile] = excl + total;
+        st_release_u32(S.flag + tile, 2u);
+      }
+    }
+    if (lane == 0) s_excl = excl;
+  }
+  __syncthreads();
+  run += s_excl;
+#pragma unroll
+  for (int k = 0; k < SCAN_IPT; k++) {
+    const uint64_t i = base + k;
+    if (i < n) out[i] = run;
+    run += v[k];
+  }
+}
+
+template <class T>
+uint64_t scan_scratch_bytes(uint64_t n) {
+  const uint64_t nt = (n + SCAN_CHUNK - 1) / SCAN_CHUNK;
+  return 64 + nt * 4 + 2 * nt * sizeof(T) + 64;
+}
+
+// scratch: null (allocated on the stream) or scan_scratch_bytes<T>(n) bytes
+template <class T>
+void exclusive_scan_impl(const T *in, T *out, uint64_t n, cudaStream_t st, int *err,
+                         void *scratch = nullptr) {
   if (n == 0) return;
-  uint64_t nb = (n + SCAN_CHUNK - 1) / SCAN_CHUNK;
-  if (nb == 1) {
+  const uint64_t nt = (n + SCAN_CHUNK - 1) / SCAN_CHUNK;
+  if (nt == 1) {
     scan_apply<T><<<1, SCAN_TPB, 0, st>>>(in, out, n, nullptr);
     VG_CUDA(cudaGetLastError());
     return;
   }
-  T *part = nullptr;
-  VG_CUDA(cudaMallocAsync((void **)&part, nb * sizeof(T), st));
-  scan_partials<T><<<(unsigned)nb, SCAN_TPB, 0, st>>>(in, n, part);
+  if (nt >= (1ull << 31)) fail(VG_ERR_NOMEM, "scan: too many items");
+  char *buf = (char *)scratch;
+  const uint64_t bytes = scan_scratch_bytes<T>(n);
+  if (!buf) VG_CUDA(cudaMallocAsync((void **)&buf, bytes, st));
+  ScanState<T> S;
+  S.ticket = (uint32_t *)buf;
+  S.flag = (uint32_t *)(buf + 64);
+  const uint64_t aoff = (64 + nt * 4 + 15) & ~15ull;
+  S.agg = (T *)(buf + aoff);
+  S.pre = S.agg + nt;
+  VG_CUDA(cudaMemsetAsync(buf, 0, 64 + nt * 4, st));
+  scan_lookback<T><<<(unsigned)nt, SCAN_TPB, 0, st>>>(in, out, n, S, err);
   VG_CUDA(cudaGetLastError());
-  exclusive_scan_impl<T>(part, part, nb, st);
-  scan_apply<T><<<(unsigned)nb, SCAN_TPB, 0, st>>>(in, out, n, part);
-  VG_CUDA(cudaGetLastError());
-  VG_CUDA(cudaFreeAsync(part, st));
+  if (!scratch) VG_CUDA(cudaFreeAsync(buf, st));
 }
 
 // ------------------------------------------------------------ radix sort
@@ -377,13 +491,21 @@ void radix_sort_impl(K *keys, uint32_t *vals, uint64_t n, int bits, cudaStream_t
 }  // namespace
 
 void exclusive_scan_u32(const uint32_t *in, uint32_t *out, uint64_t n,
-                        cudaStream_t st, Sim &) {
-  exclusive_scan_impl<uint32_t>(in, out, n, st);
+                        cudaStream_t st, Sim &s) {
+  exclusive_scan_impl<uint32_t>(in, out, n, st, s.d_status.as<int>());
 }
 void exclusive_scan_u64(const uint64_t *in, uint64_t *out, uint64_t n,
-                        cudaStream_t st, Sim &) {
+                        cudaStream_t st, Sim &s) {
   exclusive_scan_impl<unsigned long long>((const unsigned long long *)in,
-                                          (unsigned long long *)out, n, st);
+                                          (unsigned long long *)out, n, st,
+                                          s.d_status.as<int>());
+}
+uint64_t exclusive_scan_scratch_bytes(uint64_t n) {
+  return scan_scratch_bytes<uint32_t>(n);
+}
+void exclusive_scan_u32_in(const uint32_t *in, uint32_t *out, uint64_t n, cudaStream_t st,
+                           int *err, void *scratch) {
+  exclusive_scan_impl<uint32_t>(in, out, n, st, err, scratch);
 }
 void radix_sort_pairs_u32(uint32_t *keys, uint32_t *vals, uint64_t n, int bits,
                           cudaStream_t st, Sim &s) {
@@ -474,6 +596,68 @@ extern "C" int vg_selftest_sort(uint64_t n, int key_bits, int wide, int const_lo
     for (uint64_t i = 0; i < n; i++) {
       const unsigned long long kk = wide ? ok[i] : ok32[i];
       bad += (ov[i] != ref[i]) || (kk != k[ref[i]]);
+    }
+    *mismatch_out = bad;
+    return VG_OK;
+  } catch (const Error &e) {
+    set_last_error(e.msg);
+    return e.code;
+  }
+}
+
+// Exclusive scan of n generated values (32-bit, or 64-bit when wide != 0)
+// on the device, in place or out of place, against a host prefix sum
+// (wrapping arithmetic on both sides); *mismatch_out = mismatching items.
+extern "C" int vg_selftest_scan(uint64_t n, int wide, int in_place, uint64_t seed,
+                                uint64_t *mismatch_out) {
+  using namespace vg;
+  try {
+    std::vector<unsigned long long> h(n);
+    for (uint64_t i = 0; i < n; i++) {
+      uint64_t z = seed + (i + 1) * 0x9E3779B97F4A7C15ull;
+      z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+      z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+      z ^= z >> 31;
+      h[i] = (z & 7) == 0 ? 0 : (wide ? z >> 20 : (z >> 40) & 0xFFFFF);
+    }
+    const size_t es = wide ? 8 : 4;
+    std::vector<uint32_t> h32(wide ? 0 : n);
+    for (uint64_t i = 0; i < h32.size(); i++) h32[i] = (uint32_t)h[i];
+    void *din = nullptr, *dout = nullptr;
+    int *derr = nullptr;
+    VG_CUDA(cudaMalloc(&din, std::max<uint64_t>(n, 1) * es));
+    VG_CUDA(cudaMalloc(&dout, std::max<uint64_t>(n, 1) * es));
+    VG_CUDA(cudaMalloc(&derr, 4));
+    VG_CUDA(cudaMemset(derr, 0, 4));
+    VG_CUDA(cudaMemcpy(din, wide ? (const void *)h.data() : (const void *)h32.data(), n * es,
+                       cudaMemcpyHostToDevice));
+    cudaStream_t st;
+    VG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    void *o = in_place ? din : dout;
+    if (wide)
+      exclusive_scan_impl<unsigned long long>((const unsigned long long *)din,
+                                              (unsigned long long *)o, n, st, derr);
+    else
+      exclusive_scan_impl<uint32_t>((const uint32_t *)din, (uint32_t *)o, n, st, derr);
+    VG_CUDA(cudaStreamSynchronize(st));
+    std::vector<unsigned long long> r(n);
+    std::vector<uint32_t> r32(wide ? 0 : n);
+    int herr = 0;
+    VG_CUDA(cudaMemcpy(wide ? (void *)r.data() : (void *)r32.data(), o, n * es,
+                       cudaMemcpyDeviceToHost));
+    VG_CUDA(cudaMemcpy(&herr, derr, 4, cudaMemcpyDeviceToHost));
+    VG_CUDA(cudaStreamDestroy(st));
+    VG_CUDA(cudaFree(din));
+    VG_CUDA(cudaFree(dout));
+    VG_CUDA(cudaFree(derr));
+    if (herr) fail(VG_ERR_DEVICE, "vg_selftest_scan: device status " + std::to_string(herr));
+    uint64_t bad = 0;
+    unsigned long long acc = 0;
+    for (uint64_t i = 0; i < n; i++) {
+      const unsigned long long got = wide ? r[i] : r32[i];
+      const unsigned long long want = wide ? acc : (uint32_t)acc;
+      bad += got != want;
+      acc += h[i];
     }
     *mismatch_out = bad;
     return VG_OK;
