@@ -266,10 +266,20 @@ __global__ void __launch_bounds__(RS_TPB) rs_upfront(const K *keys, uint64_t n, 
   __shared__ uint32_t h[RS_MAXPASS][256];
   for (int i = threadIdx.x; i < RS_MAXPASS * 256; i += RS_TPB) (&h[0][0])[i] = 0;
   __syncthreads();
-  for (uint64_t i = (uint64_t)blockIdx.x * RS_TPB + threadIdx.x; i < n;
-       i += (uint64_t)gridDim.x * RS_TPB) {
-    const K k = keys[i];
-    for (int p = 0; p < passes; p++) atomicAdd(&h[p][(unsigned)(k >> (8 * p)) & 255u], 1u);
+  // a tile per round: its keys are requested before any is counted
+  for (uint64_t t0 = (uint64_t)blockIdx.x * RS_TILE; t0 < n;
+       t0 += (uint64_t)gridDim.x * RS_TILE) {
+    K k[RS_IPT];
+#pragma unroll
+    for (int i = 0; i < RS_IPT; i++) {
+      const uint64_t idx = t0 + (uint64_t)i * RS_TPB + threadIdx.x;
+      k[i] = idx < n ? keys[idx] : K(0);
+    }
+#pragma unroll
+    for (int i = 0; i < RS_IPT; i++) {
+      if (t0 + (uint64_t)i * RS_TPB + threadIdx.x >= n) break;
+      for (int p = 0; p < passes; p++) atomicAdd(&h[p][(unsigned)(k[i] >> (8 * p)) & 255u], 1u);
+    }
   }
   __syncthreads();
   for (int p = 0; p < passes; p++) {

@@ -490,54 +490,53 @@ __global__ void k_sir(const uint32_t *__restrict__ rp, const uint32_t *__restric
 // row for all four bytes at once (no byte exceeds 3, so no carries cross
 // bytes).  A warp holds 32 consecutive words of a row; the neighbouring
 // words come from the adjacent lanes, and only the warp's edge lanes load.
-// Row y of the raster (wrapped when periodic); 0 outside a non-periodic
-// raster.  Warp-uniform: y is the same in every lane.
-__device__ __forceinline__ uint32_t life_rowsum(const uint32_t *__restrict__ a, int64_t y,
-                                                int64_t qx, int64_t Wq, int64_t H,
-                                                int periodic, uint32_t &self) {
-  if (y < 0 || y >= H) {
-    if (!periodic) {
-      self = 0;
-      return 0;
-    }
-    y = y < 0 ? H - 1 : y - H;
-  }
-  const uint32_t *row = a + y * Wq;
-  const unsigned lane = threadIdx.x & 31;
-  const bool valid = qx < Wq;
-  const uint32_t c = valid ? row[qx] : 0u;
-  uint32_t lw = __shfl_up_sync(0xffffffffu, c, 1);
-  uint32_t rw = __shfl_down_sync(0xffffffffu, c, 1);
-  if (valid && lane == 0) lw = qx > 0 ? row[qx - 1] : (periodic ? row[Wq - 1] : 0u);
-  if (valid && (lane == 31 || qx + 1 >= Wq))
-    rw = qx + 1 < Wq ? row[qx + 1] : (periodic ? row[0] : 0u);
-  self = c;
+__device__ __forceinline__ uint32_t life_hsum(uint32_t c, uint32_t lw, uint32_t rw) {
   return ((c << 8) | (lw >> 24)) + c + ((c >> 8) | (rw << 24));
 }
 
 // blocks of 32 x 8 threads; each thread LIFE_ROWS consecutive rows of one
-// word column, keeping the three row sums it needs in registers
+// word column.  All LIFE_ROWS + 2 rows it reads are requested before any
+// is used (one memory latency per thread); rows outside a non-periodic
+// raster read as 0, a periodic raster wraps (a compare, no modulo).
 constexpr int LIFE_ROWS = 4;
 
 __global__ void __launch_bounds__(256) k_life2d_x4(const uint32_t *__restrict__ a,
                                                    uint32_t *__restrict__ o, int64_t Wq,
                                                    int64_t H, int periodic) {
-  const int64_t qx = (int64_t)blockIdx.x * 32 + (threadIdx.x & 31);
+  const unsigned lane = threadIdx.x & 31;
+  const int64_t qx = (int64_t)blockIdx.x * 32 + lane;
   const int64_t y0 = ((int64_t)blockIdx.y * blockDim.y + threadIdx.y) * LIFE_ROWS;
   if (y0 >= H) return;  // warp-uniform
-  const int64_t y1 = y0 + LIFE_ROWS < H ? y0 + LIFE_ROWS : H;
-  uint32_t selfp, selfc, selfn;
-  uint32_t sp = life_rowsum(a, y0 - 1, qx, Wq, H, periodic, selfp);
-  uint32_t sc = life_rowsum(a, y0, qx, Wq, H, periodic, selfc);
-  for (int64_t y = y0; y < y1; y++) {
-    const uint32_t sn = life_rowsum(a, y + 1, qx, Wq, H, periodic, selfn);
-    const uint32_t cnt = sp + sc + sn - selfc;
+  const int64_t y1 = y0 + LIFE_ROWS < H ? y0 + LIFE_ROWS : H;  // rows y0 .. y1-1 are written
+  const bool valid = qx < Wq;
+  const bool left_edge = valid && lane == 0;
+  const bool right_edge = valid && (lane == 31 || qx + 1 >= Wq);
+  uint32_t c[LIFE_ROWS + 2], lw[LIFE_ROWS + 2], rw[LIFE_ROWS + 2];
+#pragma unroll
+  for (int i = 0; i < LIFE_ROWS + 2; i++) {
+    const int64_t y = y0 - 1 + i;  // rows y0-1 .. y1 are read
+    int64_t yy = y < 0 ? H - 1 : (y >= H ? y - H : y);
+    const bool use = y <= y1 && ((y >= 0 && y < H) || periodic);
+    const uint32_t *row = a + yy * Wq;
+    c[i] = use && valid ? row[qx] : 0u;
+    lw[i] = use && left_edge ? (qx > 0 ? row[qx - 1] : (periodic ? row[Wq - 1] : 0u)) : 0u;
+    rw[i] = use && right_edge ? (qx + 1 < Wq ? row[qx + 1] : (periodic ? row[0] : 0u)) : 0u;
+  }
+  uint32_t hs[LIFE_ROWS + 2];
+#pragma unroll
+  for (int i = 0; i < LIFE_ROWS + 2; i++) {
+    const uint32_t l = __shfl_up_sync(0xffffffffu, c[i], 1);
+    const uint32_t r = __shfl_down_sync(0xffffffffu, c[i], 1);
+    hs[i] = life_hsum(c[i], left_edge ? lw[i] : l, right_edge ? rw[i] : r);
+  }
+#pragma unroll
+  for (int j = 0; j < LIFE_ROWS; j++) {
+    const int64_t y = y0 + j;
+    const uint32_t self = c[j + 1];
+    const uint32_t cnt = hs[j] + hs[j + 1] + hs[j + 2] - self;
     const uint32_t born = __vcmpeq4(cnt, 0x03030303u);
-    const uint32_t stay = __vcmpeq4(cnt, 0x02020202u) & __vcmpne4(selfc, 0u);
-    if (qx < Wq) o[y * Wq + qx] = (born | stay) & 0x01010101u;
-    sp = sc;
-    sc = sn;
-    selfc = selfn;
+    const uint32_t stay = __vcmpeq4(cnt, 0x02020202u) & __vcmpne4(self, 0u);
+    if (valid && y < y1) o[y * Wq + qx] = (born | stay) & 0x01010101u;
   }
 }
 
