@@ -963,11 +963,19 @@ uint64_t select_rows(Sim &s, const CSR &c, uint64_t n, uint32_t lo, uint32_t hi,
 }
 }  // namespace
 
+// in-degree of the row at each position of the slice order
+__global__ void k_order_deg(const uint32_t *rp, uint64_t nrows, const uint32_t *order,
+                            uint64_t m, uint32_t *deg) {
+  const uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < m) deg[k] = row_degree(rp, nrows, order[k]);
+}
+
 void ensure_schedule(Sim &s, CSR &c, uint32_t thr, uint64_t n) {
   if (c.schedule_valid && c.hub_threshold == thr && c.sched_n == n) return;
   cudaStream_t st = s.stream;
   c.hub_rows.release();
   c.order.release();
+  c.order_deg.release();
   c.slice_base.release();
   c.slice_deg.release();
   c.sell_src.release();
@@ -1013,6 +1021,9 @@ void ensure_schedule(Sim &s, CSR &c, uint32_t thr, uint64_t n) {
           rp, c.nrows, c.src.as<uint32_t>(), c.payload[0].as<double>(), c.order.as<uint32_t>(), m,
           c.slice_base.as<uint64_t>(), c.slice_deg.as<uint32_t>(), c.sell_src.as<uint32_t>(),
           c.sell_w.as<double>());
+      c.order_deg.alloc(std::max<uint64_t>(m, 1) * 4, &s.footprint);
+      k_order_deg<<<nblk(m), TPB, 0, st>>>(rp, c.nrows, c.order.as<uint32_t>(), m,
+                                           c.order_deg.as<uint32_t>());
     }
     VG_CUDA(cudaGetLastError());
     VG_CUDA(cudaStreamSynchronize(st));

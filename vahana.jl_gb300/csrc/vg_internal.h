@@ -171,6 +171,7 @@ struct CSR {
   DevBuf hub_rows;  // u32
   uint64_t nhub = 0;
   DevBuf order;     // u32 rows, position = 32 slice + lane
+  DevBuf order_deg; // u32 in-degree of the row at each position of `order`
   uint64_t norder = 0;
   DevBuf slice_base;  // u64 [nslices + 1]: first column-major slot of each slice
   DevBuf slice_deg;   // u32 [nslices]: the slice's largest degree

@@ -57,6 +57,7 @@ struct OpinionArgs {
   const uint32_t *__restrict__ hub_rows;  // degree > hub_thr, split over a warp
   uint64_t nhub;
   const uint32_t *__restrict__ order;  // the other rows, degree-sorted windows
+  const uint32_t *__restrict__ order_deg;  // their in-degrees, by position
   uint64_t norder;
   const uint64_t *__restrict__ slice_base;  // column-major slices of 32 rows
   const uint32_t *__restrict__ slice_deg;
@@ -257,12 +258,11 @@ template <bool GRID>
 __device__ __forceinline__ void sell_slice(const OpinionArgs &p, uint64_t sl) {
   const unsigned lane = threadIdx.x & 31;
   const uint64_t pos = sl * 32 + lane;
-  uint32_t r = 0, d = 0;
   const bool live = pos < p.norder;
-  if (live) {
-    r = p.order[pos];
-    if (r < p.nrows) d = p.rp[r + 1] - p.rp[r];
-  }
+  // the row and its degree are independent loads (the degree is stored by
+  // position, not read through the row pointers)
+  const uint32_t r = live ? p.order[pos] : 0u;
+  const uint32_t d = live ? p.order_deg[pos] : 0u;
   const double xi = live ? p.x[r] : 0.0;
   bool xi_ok;
   const float fxi = hi_float(xi, xi_ok);
@@ -357,7 +357,7 @@ __device__ __forceinline__ void opinion_block(const OpinionArgs &p, unsigned blk
 }
 
 template <bool GRID>
-__global__ void __launch_bounds__(TPB) k_opinion(OpinionArgs p) {
+__global__ void __launch_bounds__(TPB, 9) k_opinion(OpinionArgs p) {
   opinion_block<GRID>(p, blockIdx.x);
 }
 
@@ -487,6 +487,7 @@ static unsigned opinion_args(Sim &s, int e, int T, double eps, double a, double 
   p.hub_rows = cs.hub_rows.as<uint32_t>();
   p.nhub = cs.nhub;
   p.order = cs.order.as<uint32_t>();
+  p.order_deg = cs.order_deg.as<uint32_t>();
   p.norder = cs.norder;
   p.slice_base = cs.slice_base.as<uint64_t>();
   p.slice_deg = cs.slice_deg.as<uint32_t>();
