@@ -368,7 +368,7 @@ struct JobTile {
   uint32_t job, blk;
 };
 
-__global__ void __launch_bounds__(TPB) k_opinion_jobs(const OpinionArgs *jobs,
+__global__ void __launch_bounds__(TPB, 9) k_opinion_jobs(const OpinionArgs *jobs,
                                                       const JobTile *tiles) {
   __shared__ OpinionArgs sp;
   JobTile t = tiles[blockIdx.x];
