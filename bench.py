@@ -158,6 +158,24 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x, device="cpu"):
+    """The largest x over all ranks (a job's time is its slowest replica's);
+    x itself when no process group is running or it has one rank."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(world_size, units_per_rank, seconds):
+    """Whole-job units per second: every replica processes units_per_rank in
+    the job's time (the maximum over the ranks)."""
+    return world_size * units_per_rank / seconds
+
+
 # ------------------------------------------------------------- CPU legs
 def cpu_graph_from_device(vh, run):
     """CSR of the built graph (row_ptr, src, w) read back for the CPU step."""
@@ -280,11 +298,8 @@ def run_ours(args):
     total_ms = start.elapsed_time(end)
     kernel_ms = sorted(a.elapsed_time(b) for a, b in ev)
     mean_kernel_ms = sum(kernel_ms) / len(kernel_ms)
-    if ws > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = ws * E * K / (total_ms * 1e-3)
+    total_ms = max_over_ranks(total_ms, "cuda")
+    value = job_throughput(ws, E * K, total_ms * 1e-3)
 
     # ---- end to end through the C ABI with pinned host buffers
     Ke = args.e2e_steps
@@ -310,11 +325,8 @@ def run_ours(args):
         e2e_step()
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
-    if ws > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = {"value": ws * E * Ke / e2e_s, "unit": "edge-updates/s",
+    e2e_s = max_over_ranks(e2e_s, "cuda")
+    e2e = {"value": job_throughput(ws, E * Ke, e2e_s), "unit": "edge-updates/s",
            "h2d_bytes_per_step": 8 * N, "d2h_bytes_per_step": 8 * N}
 
     # ---- roofline of the gather kernel
