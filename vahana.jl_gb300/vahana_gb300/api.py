@@ -642,11 +642,9 @@ def _apply_args(sim, transition, call, read, write, add_existing, with_edge, par
 
 
 def _key(x):
-    if x is None or isinstance(x, (str, int, float)):
-        return x
-    if isinstance(x, TypeInfo):
-        return ("T", x.kind, x.name)
-    return tuple(_key(v) for v in x)
+    # lists become tuples; names, numbers and TypeInfo objects (hashed by
+    # identity, and unique per model) are their own keys
+    return tuple(x) if type(x) is list else x
 
 
 def apply_(sim, transition, call, read, write, add_existing=(), with_edge=None, params=()):
