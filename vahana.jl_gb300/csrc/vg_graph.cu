@@ -249,27 +249,23 @@ namespace {
 // row key of each record (target agent_nr - 1); a record of another type or
 // beyond the rows sets the status word (the records come from kernels that
 // declare their types)
-// vals: the record number k, or (src_vals) the source's agent_nr - 1, which
-// the stable sort then carries straight into the CSR's source column
+// key: the target row; value: the source's agent_nr - 1, which the stable
+// sort then carries straight into the CSR's source column
 __global__ void k_typed_keys(const uint64_t *to, const uint64_t *from, uint64_t n,
                              uint32_t target_type, uint32_t src_type, uint64_t nrows,
-                             uint32_t *keys, uint32_t *vals, int src_vals, int *status) {
+                             uint32_t *keys, uint32_t *src, int *status) {
   uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
-  const uint64_t t = to[k];
+  const uint64_t t = to[k], f = from[k];
   uint64_t r = (t & NR_MASK) - 1;
-  bool bad = (uint32_t)(t >> SHIFT_TYPE) != target_type || r >= nrows;
-  uint64_t f = 0;
-  if (from) {
-    f = from[k];
-    if ((uint32_t)(f >> SHIFT_TYPE) != src_type) bad = true;
-  }
+  const bool bad = (uint32_t)(t >> SHIFT_TYPE) != target_type || r >= nrows ||
+                   (uint32_t)(f >> SHIFT_TYPE) != src_type;
   if (bad) {
     atomicCAS(status, 0, 501);
     r = 0;
   }
   keys[k] = (uint32_t)r;
-  vals[k] = src_vals ? (uint32_t)((f & NR_MASK) - 1) : (uint32_t)k;
+  src[k] = (uint32_t)((f & NR_MASK) - 1);
 }
 
 // row_ptr of the rows 0..nrows from the sorted row keys: rp[r] = the
@@ -371,11 +367,6 @@ __global__ void __launch_bounds__(TPB) k_rp_fill(const uint32_t *keys, uint64_t 
   if (lane == 0 && dmax) atomicMax(maxdeg, dmax);
 }
 
-__global__ void k_gather_src(const uint64_t *from, const uint32_t *vals, uint64_t n,
-                             uint32_t *src) {
-  uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < n) src[k] = (uint32_t)((from[vals[k]] & NR_MASK) - 1);
-}
 }  // namespace
 
 uint32_t csr_max_degree(Sim &s, CSR &c) {
@@ -390,8 +381,10 @@ uint32_t csr_max_degree(Sim &s, CSR &c) {
 bool build_csr_typed(Sim &s, int e, const EdgeAppend &ap, uint64_t n) {
   const EdgeTypeDesc &ed = s.model->et(e);
   EdgeStore &es = s.edges[e];
-  if (!ap.ordered || ap.target_type <= 0 || (ed.stores_src() && ap.src_type <= 0) ||
-      ed.bool_only() || ed.singleedge() || es.add_existing || n >= (1ull << 31))
+  // the form the typed emitters produce: sources kept, no payload columns
+  if (!ap.ordered || ap.target_type <= 0 || !ed.stores_src() || ap.src_type <= 0 ||
+      ed.stores_payload() || ed.bool_only() || ed.singleedge() || es.add_existing ||
+      n >= (1ull << 31))
     return false;
   const int T = ap.target_type;
   if (T > (int)s.model->atypes.size() || (ed.singletype() && T != ed.target)) return false;
@@ -407,12 +400,9 @@ bool build_csr_typed(Sim &s, int e, const EdgeAppend &ap, uint64_t n) {
     if (b.bytes < bytes || !b.p) b.alloc(std::max<uint64_t>(bytes, 16), &s.footprint);
   };
   ensure(c.row_ptr, (nrows + 1) * 4);
-  if (ed.stores_src()) ensure(c.src, std::max<uint64_t>(n, 1) * 4);
-  else c.src.release();
+  ensure(c.src, std::max<uint64_t>(n, 1) * 4);
   c.src_type.release();
-  const int nf = ed.stores_payload() ? (int)ed.fields.size() : 0;
-  c.payload.resize(nf);
-  for (int f = 0; f < nf; f++) ensure(c.payload[f], std::max<uint64_t>(n, 1) * ed.fields[f].size);
+  c.payload.clear();
   ensure(c.d_max_degree, 4);
   if (!c.rebuild) c.rebuild.reset(new RebuildCache());
   RebuildCache &rc = *c.rebuild;
@@ -420,42 +410,30 @@ bool build_csr_typed(Sim &s, int e, const EdgeAppend &ap, uint64_t n) {
   const uint64_t nbr = (nrows + 1 + RP_ROWS - 1) / RP_ROWS;
   const uint64_t sort_bytes = radix_sort_scratch_bytes(n, 4, bits);
   ensure(rc.keys, std::max<uint64_t>(n, 1) * 4);
-  ensure(rc.vals, std::max<uint64_t>(n, 1) * 4);
   ensure(rc.bstart, (nbr + 1) * 4);
   if (sort_bytes) ensure(rc.sort, sort_bytes);
-  const uint64_t *from = ed.stores_src() ? ap.from.as<uint64_t>() : nullptr;
-  // without payload columns the sorted values are the source column itself
-  const bool src_vals = from && nf == 0;
-  uint32_t *keys = rc.keys.as<uint32_t>();
-  uint32_t *vals = src_vals ? c.src.as<uint32_t>() : rc.vals.as<uint32_t>();
+  const uint64_t *from = ap.from.as<uint64_t>();
+  // the sorted values are the source column itself
+  uint32_t *keys = rc.keys.as<uint32_t>(), *src = c.src.as<uint32_t>();
   // the launch sequence, a function of these arguments only
-  std::vector<uint64_t> args = {(uint64_t)ap.to.p, (uint64_t)from, n, nrows, (uint64_t)T,
-                                (uint64_t)ap.src_type, (uint64_t)c.row_ptr.p,
-                                (uint64_t)c.src.p, (uint64_t)c.d_max_degree.p,
-                                (uint64_t)keys, (uint64_t)vals, (uint64_t)rc.sort.p,
-                                (uint64_t)rc.bstart.p, (uint64_t)s.d_status.p, (uint64_t)nf};
-  for (int f = 0; f < nf; f++) {
-    args.push_back((uint64_t)ap.payload[f].p);
-    args.push_back((uint64_t)c.payload[f].p);
-  }
+  const std::vector<uint64_t> args = {
+      (uint64_t)ap.to.p,  (uint64_t)from,          n,
+      nrows,              (uint64_t)T,             (uint64_t)ap.src_type,
+      (uint64_t)c.row_ptr.p, (uint64_t)src,        (uint64_t)c.d_max_degree.p,
+      (uint64_t)keys,     (uint64_t)rc.sort.p,     (uint64_t)rc.bstart.p,
+      (uint64_t)s.d_status.p};
   auto enqueue = [&]() {
     VG_CUDA(cudaMemsetAsync(c.d_max_degree.p, 0, 4, st));
     if (n) {
       k_typed_keys<<<nblk(n), TPB, 0, st>>>(ap.to.as<uint64_t>(), from, n, (uint32_t)T,
-                                             (uint32_t)ap.src_type, nrows, keys, vals,
-                                             (int)src_vals, s.d_status.as<int>());
-      radix_sort_pairs_u32_in(keys, vals, n, bits, st, s.d_status.as<int>(), rc.sort.p);
+                                             (uint32_t)ap.src_type, nrows, keys, src,
+                                             s.d_status.as<int>());
+      radix_sort_pairs_u32_in(keys, src, n, bits, st, s.d_status.as<int>(), rc.sort.p);
     }
     k_rp_bounds<<<nblk(n + 1), TPB, 0, st>>>(keys, n, nbr, rc.bstart.as<uint32_t>());
     k_rp_fill<<<(unsigned)nbr, TPB, 0, st>>>(keys, nrows, rc.bstart.as<uint32_t>(),
                                              c.row_ptr.as<uint32_t>(),
                                              c.d_max_degree.as<unsigned>());
-    if (n) {
-      if (from && !src_vals)
-        k_gather_src<<<nblk(n), TPB, 0, st>>>(from, vals, n, c.src.as<uint32_t>());
-      for (int f = 0; f < nf; f++)
-        scatter_column(ed.fields[f].size, ap.payload[f].p, vals, nullptr, n, c.payload[f].p, st);
-    }
     VG_CUDA(cudaGetLastError());
   };
   const bool graphable = st != nullptr && st != cudaStreamLegacy && st != cudaStreamPerThread;

@@ -138,7 +138,7 @@ struct AgentStore {
 // launch sequence: recorded when the same arguments (sizes and buffers)
 // repeat on consecutive rebuilds, replayed while they stay the same.
 struct RebuildCache {
-  DevBuf keys, vals, sort, bstart;
+  DevBuf keys, sort, bstart;
   std::vector<uint64_t> last, graph_args;
   cudaGraphExec_t exec = nullptr;
   RebuildCache() = default;
