@@ -106,6 +106,53 @@ def test_opinion_hub_split(vh, hub):
     run.close()
 
 
+@pytest.mark.parametrize("weights", ["grid", "arbitrary"])
+def test_opinion_block_hubs(vh, weights):
+    """With a block threshold of 2048 (parameter 5), rows above it take a
+    whole block, their edges staged in shared memory by bulk copies in
+    chunks of 512 (unaligned row starts, a row of tens of chunks, tails of
+    1-3 edges): within 1e-12 relative of the sequential fold; rows below the
+    hub threshold stay bit-exact."""
+    from vahana_gb300 import models
+    rng = np.random.default_rng(17)
+    if weights == "grid":
+        run = models.build_opinion(n=60000, mean_degree=20, gamma=2.5, wmax=1e4, eps=0.3,
+                                   seed=21, hub_threshold=256)
+        sim, m, n = run.sim, run.model, run.n
+        frm, to, pl = models.staged_edges(sim, "Weight")
+        w = pl["w"]
+    else:
+        n, E = 8000, 120000
+        m = models.opinion_model()
+        sim = vh.create_simulation(m)
+        ids = vh.add_agents(sim, "Opinion", n, x=rng.random(n))
+        frm = ids[rng.integers(0, n, E)]
+        to = ids[np.minimum(rng.zipf(1.6, E) - 1, n - 1)]
+        w = rng.random(E) * 0.7 + 1e-3
+        vh.add_edges(sim, "Weight", frm, to, w=w)
+        run = None
+    x0 = vh.read_agents(sim, "Opinion")[0]["x"].copy()
+    deg = np.bincount((to & np.uint64((1 << 36) - 1)).astype(np.int64) - 1, minlength=n)
+    assert (deg > 2048).sum() >= 2 and deg.max() > 8 * 512
+    vh.finish_init(sim)
+    step = lambda: vh.apply_(sim, "bounded_confidence", ["Opinion"], ["Opinion", "Weight"],
+                             ["Opinion"], params=[m["Weight"].index, 0.3, 0.5, 0.5, 256, 2048])
+    step()
+    x1 = vh.read_agents(sim, "Opinion")[0]["x"].copy()
+    ref1 = om.run_opinion(n, frm, to, w, x0, 0.3, 1)
+    hubs = deg > 256
+    np.testing.assert_array_equal(x1[~hubs].view(np.uint64), ref1[~hubs].view(np.uint64))
+    np.testing.assert_allclose(x1[hubs], ref1[hubs], rtol=1e-12, atol=0)
+    for _ in range(4):
+        step()
+    x = vh.read_agents(sim, "Opinion")[0]["x"]
+    np.testing.assert_allclose(x, om.run_opinion(n, frm, to, w, x0, 0.3, 5), rtol=1e-12, atol=0)
+    if run is not None:
+        run.close()
+    else:
+        sim.close()
+
+
 def test_fp64_integer_arithmetic_matches_hardware(vh):
     """The integer-pipe binary64 add/mul/div used by the gather kernels
     equal the hardware instructions on 4M operand pairs (random, ties,

@@ -866,6 +866,12 @@ __global__ void k_compact_rows(const uint32_t *flag, const uint32_t *pos, uint64
 }
 
 // sort key of a hub row: descending degree
+__global__ void k_count_above(const uint32_t *rp, const uint32_t *rows, uint64_t m,
+                              uint32_t thr, unsigned *cnt) {
+  const uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < m && rp[rows[k] + 1] - rp[rows[k]] > thr) atomicAdd(cnt, 1u);
+}
+
 __global__ void k_hub_keys(const uint32_t *rp, const uint32_t *rows, uint64_t m, uint32_t *keys) {
   uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k < m) keys[k] = 0xFFFFFFFFu - (rp[rows[k] + 1] - rp[rows[k]]);
@@ -948,8 +954,10 @@ __global__ void k_order_deg(const uint32_t *rp, uint64_t nrows, const uint32_t *
   if (k < m) deg[k] = row_degree(rp, nrows, order[k]);
 }
 
-void ensure_schedule(Sim &s, CSR &c, uint32_t thr, uint64_t n) {
-  if (c.schedule_valid && c.hub_threshold == thr && c.sched_n == n) return;
+void ensure_schedule(Sim &s, CSR &c, uint32_t thr, uint32_t big_thr, uint64_t n) {
+  if (c.schedule_valid && c.hub_threshold == thr && c.block_threshold == big_thr &&
+      c.sched_n == n)
+    return;
   cudaStream_t st = s.stream;
   c.hub_rows.release();
   c.order.release();
@@ -958,7 +966,7 @@ void ensure_schedule(Sim &s, CSR &c, uint32_t thr, uint64_t n) {
   c.slice_deg.release();
   c.sell_src.release();
   c.sell_w.release();
-  c.nhub = c.norder = c.nslices = 0;
+  c.nhub = c.norder = c.nslices = c.nbig = 0;
   if (n > 0 && c.row_ptr.p) {
     const uint32_t *rp = c.row_ptr.as<uint32_t>();
     // hub rows by descending degree
@@ -967,6 +975,17 @@ void ensure_schedule(Sim &s, CSR &c, uint32_t thr, uint64_t n) {
       Tmp<uint32_t> keys(c.nhub, st);
       k_hub_keys<<<nblk(c.nhub), TPB, 0, st>>>(rp, c.hub_rows.as<uint32_t>(), c.nhub, keys.p);
       radix_sort_pairs_u32(keys.p, c.hub_rows.as<uint32_t>(), c.nhub, 32, st, s);
+    }
+    c.nbig = 0;
+    if (c.nhub && big_thr != 0xFFFFFFFFu) {  // the leading hubs above the block threshold
+      Tmp<unsigned> cnt(1, st);
+      VG_CUDA(cudaMemsetAsync(cnt.p, 0, 4, st));
+      k_count_above<<<nblk(c.nhub), TPB, 0, st>>>(rp, c.hub_rows.as<uint32_t>(), c.nhub,
+                                                  big_thr, cnt.p);
+      unsigned h = 0;
+      VG_CUDA(cudaMemcpyAsync(&h, cnt.p, 4, cudaMemcpyDeviceToHost, st));
+      VG_CUDA(cudaStreamSynchronize(st));
+      c.nbig = h;
     }
     // the other rows by descending degree in windows of 2^16 rows (or
     // more, so that the window number stays below the sentinel)
@@ -1008,6 +1027,7 @@ void ensure_schedule(Sim &s, CSR &c, uint32_t thr, uint64_t n) {
   }
   c.sched_n = n;
   c.hub_threshold = thr;
+  c.block_threshold = big_thr;
   c.schedule_valid = true;
 }
 

@@ -170,6 +170,10 @@ struct CSR {
   // degree (padding: source 0, weight 0)
   DevBuf hub_rows;  // u32
   uint64_t nhub = 0;
+  // the first nbig hub rows have more than block_threshold in-edges: one
+  // block each, staged through shared memory by bulk copies
+  uint64_t nbig = 0;
+  uint32_t block_threshold = 0xFFFFFFFFu;
   DevBuf order;     // u32 rows, position = 32 slice + lane
   DevBuf order_deg; // u32 in-degree of the row at each position of `order`
   uint64_t norder = 0;
@@ -362,6 +366,7 @@ struct OpinionJob {
   int edge_type, type_nr;
   double eps, a, b;
   uint32_t hub_thr;
+  uint32_t block_thr = 0xFFFFFFFFu;
 };
 void launch_opinion_jobs(const std::vector<OpinionJob> &jobs, cudaStream_t st, DevBuf &args_buf,
                          DevBuf &tiles_buf, uint64_t *footprint);
@@ -398,7 +403,9 @@ void build_csr_from_records(Sim &s, int edge_type, const uint64_t *d_from,
 void remove_died_edges(Sim &s, int died_type, const uint8_t *died_now,
                        uint64_t n_died);
 // hub list and degree-sorted row order over n agent slots (n >= nrows)
-void ensure_schedule(Sim &s, CSR &c, uint32_t hub_threshold, uint64_t n);
+// block_threshold: hub rows above it take a whole block (UINT32_MAX: none)
+void ensure_schedule(Sim &s, CSR &c, uint32_t hub_threshold, uint32_t block_threshold,
+                     uint64_t n);
 // largest row length (synchronises when the value is still on the device)
 uint32_t csr_max_degree(Sim &s, CSR &c);
 // rebuild of an edge type's container from typed, ordered records without

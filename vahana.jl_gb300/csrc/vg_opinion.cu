@@ -15,6 +15,8 @@
 //     ensure_schedule): lane l of a warp folds its row's edges in insertion
 //     order while every load of the warp is one coalesced access --
 //     bit-identical to the sequential binary64 computation.
+//   rows above block_thr (an optional parameter): one block per row, the
+//     row's edges staged through shared memory by bulk copies (hub_block).
 //   rows above hub_thr ("hubs"): one warp per row, lane l folds the edges
 //     l, l + 32, ... in order and the 32 lane sums are combined in a fixed
 //     tree.  The additions are regrouped, so these rows agree with the
@@ -56,6 +58,8 @@ struct OpinionArgs {
   uint64_t n, nrows;
   const uint32_t *__restrict__ hub_rows;  // degree > hub_thr, split over a warp
   uint64_t nhub;
+  uint64_t nbig;         // the first nbig hub rows take a whole block each
+  int *status;           // the simulation's device error word
   const uint32_t *__restrict__ order;  // the other rows, degree-sorted windows
   const uint32_t *__restrict__ order_deg;  // their in-degrees, by position
   uint64_t norder;
@@ -65,7 +69,7 @@ struct OpinionArgs {
   const double *__restrict__ sell_w;
   uint64_t nslices;
   uint32_t hub_thr;
-  unsigned hub_blocks;
+  unsigned hub_blocks;   // blocks of the other hub rows, 4 per block
   double eps, a, b;
   int a_pow2, b_pow2, a_k, b_k;  // a = 2^a_k, b = 2^b_k (positive normal powers of two)
   float eps_lo, eps_hi;  // float filter: certainly inside / certainly outside
@@ -342,14 +346,230 @@ __device__ __forceinline__ void hub_warp(const OpinionArgs &p, uint32_t r) {
   if (lane == 0) p.xo[r] = cnt ? finish(p, xi, sw, swx) : xi;
 }
 
+// One block per hub row above HUB_BLOCK_DEGREE in-edges.  The row's source
+// indices and weights are staged through shared memory in chunks of
+// HB_CHUNK edges by 1-D bulk copies (cp.async.bulk, completion counted in
+// bytes on an mbarrier), two chunks in flight; thread t folds the chunk
+// positions t, t + 128, ... and the 128 partial sums are combined in a
+// fixed tree (warps as in hub_warp, then warps 0+1, 2+3, and the two
+// halves), so the result is the same on every run and within 1e-12 of the
+// sequential fold.  Bulk copies need 16-byte aligned starts and sizes: the
+// chunks start at the row's first edge rounded down to a multiple of 4
+// (edges of the previous row are skipped) and end at its last edge rounded
+// down; the at most 3 edges after that are read directly.  Every wait is
+// bounded: on a timeout the block records an error in the status word,
+// waits (bounded) for its copies in flight and leaves the row unwritten.
+constexpr uint32_t HB_CHUNK = 512;  // edges per stage, a multiple of 4
+constexpr uint32_t HB_SPIN_LIMIT = 1u << 20;
+constexpr int HB_ERR_WAIT = 0x5e03;
+
+struct HubStage {
+  uint32_t src[HB_CHUNK];
+  double w[HB_CHUNK];
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *q) {
+  return (uint32_t)__cvta_generic_to_shared(q);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_inval(uint64_t *bar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(done)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+// bounded wait for the phase with the given parity; false on a timeout
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+  for (uint32_t i = 0; i < HB_SPIN_LIMIT; i++)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void bulk_copy(void *dst, const void *src, uint32_t bytes,
+                                          uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+      ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+struct HubShared {
+  HubStage stage[2];
+  uint64_t bar[2];
+  uint64_t part_sw[TPB / 32], part_swx[TPB / 32];
+  uint32_t part_cnt[TPB / 32];
+  int failed;
+};
+// one copy per kernel, whichever weight form its blocks instantiate
+__device__ __forceinline__ HubShared &hub_shared() {
+  __shared__ __align__(16) HubShared h;
+  return h;
+}
+
+template <bool GRID>
+__device__ __noinline__ void hub_block(const OpinionArgs &p, uint32_t r) {
+  HubShared &H = hub_shared();
+  HubStage *stage = H.stage;
+  uint64_t *bar = H.bar;
+  uint64_t *part_sw = H.part_sw, *part_swx = H.part_swx;
+  uint32_t *part_cnt = H.part_cnt;
+  int &failed = H.failed;
+  const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const double xi = p.x[r];
+  bool xi_ok;
+  const float fxi = hi_float(xi, xi_ok);
+  const uint32_t b = p.rp[r], e = p.rp[r + 1];
+  const uint32_t a0 = b & ~3u, e_al = e & ~3u;
+  const uint32_t nch = e_al > a0 ? (e_al - a0 + HB_CHUNK - 1) / HB_CHUNK : 0;
+  const uint64_t pol_keep = policy_evict_last();
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    failed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  auto issue = [&](uint32_t k) {  // chunk k into stage k & 1 (thread 0)
+    const uint32_t c0 = a0 + k * HB_CHUNK;
+    const uint32_t c1 = c0 + HB_CHUNK < e_al ? c0 + HB_CHUNK : e_al;
+    const uint32_t m = c1 - c0;  // a multiple of 4
+    HubStage &S = stage[k & 1];
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect_tx(&bar[k & 1], m * 12u);
+    bulk_copy(S.src, p.src + c0, m * 4u, &bar[k & 1]);
+    bulk_copy(S.w, p.w + c0, m * 8u, &bar[k & 1]);
+  };
+  if (tid == 0) {
+    if (nch > 0) issue(0);
+    if (nch > 1) issue(1);
+  }
+  double dsw = 0.0, dswx = 0.0;
+  uint32_t cnt = 0;
+  auto fold_x = [&](double xj, double wv) {
+    if (within(xj, xi, fxi, xi_ok, p)) {
+      bool ok;
+      const uint64_t pk = GRID ? emu_mul_grid(bits(wv), bits(xj), ok)
+                               : emu_mul_fast(bits(wv), bits(xj), ok);
+      dswx = __dadd_rn(dswx, ok ? dbl(pk) : mul_hw(wv, xj));
+      dsw = __dadd_rn(dsw, wv);
+      cnt++;
+    }
+  };
+  uint32_t k = 0;
+  for (; k < nch; k++) {
+    if (!mbar_wait(&bar[k & 1], (k >> 1) & 1u)) {
+      atomicCAS(p.status, 0, HB_ERR_WAIT);
+      failed = 1;
+    }
+    __syncthreads();
+    if (failed) break;
+    const uint32_t c0 = a0 + k * HB_CHUNK;
+    const uint32_t c1 = c0 + HB_CHUNK < e_al ? c0 + HB_CHUNK : e_al;
+    const HubStage &S = stage[k & 1];
+    // the thread's HB_CHUNK / TPB positions: opinions requested together
+    constexpr uint32_t PER = HB_CHUNK / TPB;
+    uint32_t jv[PER];
+    double wv[PER], xv[PER];
+    bool use[PER];
+#pragma unroll
+    for (uint32_t u = 0; u < PER; u++) {
+      const uint32_t i = tid + u * TPB;
+      use[u] = i < c1 - c0 && c0 + i >= b;
+      jv[u] = use[u] ? S.src[i] : 0u;
+      wv[u] = use[u] ? S.w[i] : 0.0;
+    }
+#pragma unroll
+    for (uint32_t u = 0; u < PER; u++) xv[u] = use[u] ? ld_keep(p.x + jv[u], pol_keep) : 0.0;
+#pragma unroll
+    for (uint32_t u = 0; u < PER; u++)
+      if (use[u]) fold_x(xv[u], wv[u]);
+    __syncthreads();  // stage k & 1 is read
+    if (tid == 0 && k + 2 < nch) issue(k + 2);
+  }
+  if (failed) {  // let the copies still in flight (chunks k, k + 1) land before leaving
+    for (uint32_t j = k; j < nch && j < k + 2; j++) mbar_wait(&bar[j & 1], (j >> 1) & 1u);
+    return;
+  }
+  // the edges after the last bulk copy (fewer than 4)
+  const uint32_t t0 = e_al > b ? e_al : b;
+  if (t0 + tid < e) fold_x(ld_keep(p.x + p.src[t0 + tid], pol_keep), p.w[t0 + tid]);
+  // fixed tree: within each warp (lane l receives lane l + off), then warps
+  uint64_t sw = bits(dsw), swx = bits(dswx);
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const uint64_t osw = __shfl_down_sync(0xffffffffu, sw, off);
+    const uint64_t oswx = __shfl_down_sync(0xffffffffu, swx, off);
+    const uint32_t ocnt = __shfl_down_sync(0xffffffffu, cnt, off);
+    if ((lane & (2 * off - 1)) == 0 && ocnt) {
+      sw = add_rn(sw, osw);
+      swx = add_rn(swx, oswx);
+      cnt += ocnt;
+    }
+  }
+  if (lane == 0) {
+    part_sw[wid] = sw;
+    part_swx[wid] = swx;
+    part_cnt[wid] = cnt;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    uint64_t s2[2], x2[2];
+    uint32_t c2[2];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      s2[h] = part_sw[2 * h];
+      x2[h] = part_swx[2 * h];
+      c2[h] = part_cnt[2 * h];
+      if (part_cnt[2 * h + 1]) {
+        s2[h] = add_rn(s2[h], part_sw[2 * h + 1]);
+        x2[h] = add_rn(x2[h], part_swx[2 * h + 1]);
+        c2[h] += part_cnt[2 * h + 1];
+      }
+    }
+    if (c2[1]) {
+      s2[0] = add_rn(s2[0], s2[1]);
+      x2[0] = add_rn(x2[0], x2[1]);
+      c2[0] += c2[1];
+    }
+    p.xo[r] = c2[0] ? finish(p, xi, s2[0], x2[0]) : xi;
+    mbar_inval(&bar[0]);
+    mbar_inval(&bar[1]);
+  }
+}
+
 // The work of one block of the gather grid: hub warps, then slices (one
 // per warp).  Shared by the single-simulation kernel and the multi-job
 // kernel of the serving loop.
-template <bool GRID>
+// BIG: the block range starts with the block-wide hub rows; otherwise they
+// are run by their own launch (k_opinion_big) and the range starts at the
+// warp hubs, so that this kernel needs no shared memory (its L1 keeps the
+// whole unified array).
+template <bool GRID, bool BIG>
 __device__ __forceinline__ void opinion_block(const OpinionArgs &p, unsigned blk) {
+  if (BIG) {
+    if (blk < p.nbig) {  // block-wide hub rows (whole blocks: the test is uniform)
+      hub_block<GRID>(p, p.hub_rows[blk]);
+      return;
+    }
+    blk -= (unsigned)p.nbig;
+  }
   const uint64_t warp = (uint64_t)blk * (TPB / 32) + (threadIdx.x >> 5);
   if (blk < p.hub_blocks) {
-    if (warp < p.nhub) hub_warp<GRID>(p, p.hub_rows[warp]);
+    if (p.nbig + warp < p.nhub) hub_warp<GRID>(p, p.hub_rows[p.nbig + warp]);
     return;
   }
   const uint64_t sl = warp - (uint64_t)p.hub_blocks * (TPB / 32);
@@ -358,7 +578,13 @@ __device__ __forceinline__ void opinion_block(const OpinionArgs &p, unsigned blk
 
 template <bool GRID>
 __global__ void __launch_bounds__(TPB, 9) k_opinion(OpinionArgs p) {
-  opinion_block<GRID>(p, blockIdx.x);
+  opinion_block<GRID, false>(p, blockIdx.x);
+}
+
+// the block-wide hub rows of one simulation, one block each
+template <bool GRID>
+__global__ void __launch_bounds__(TPB) k_opinion_big(OpinionArgs p) {
+  hub_block<GRID>(p, p.hub_rows[blockIdx.x]);
 }
 
 // Many simulations in one launch: block i runs virtual block tiles[i].blk of
@@ -374,8 +600,8 @@ __global__ void __launch_bounds__(TPB, 9) k_opinion_jobs(const OpinionArgs *jobs
   JobTile t = tiles[blockIdx.x];
   if (threadIdx.x == 0) sp = jobs[t.job];
   __syncthreads();
-  if (sp.grid) opinion_block<true>(sp, t.blk);
-  else opinion_block<false>(sp, t.blk);
+  if (sp.grid) opinion_block<true, true>(sp, t.blk);
+  else opinion_block<false, true>(sp, t.blk);
 }
 
 
@@ -397,10 +623,12 @@ __global__ void k_check_grid(const double *w, uint64_t n, int *bad) {
 }  // namespace
 
 static unsigned opinion_args(Sim &s, int e, int T, double eps, double a, double b,
-                             uint32_t thr, OpinionArgs &p, cudaStream_t launch_stream);
+                             uint32_t thr, uint32_t big_thr, OpinionArgs &p,
+                             cudaStream_t launch_stream);
 
 // apply!(sim, bounded_confidence, [T], [T, E], [T]; params = [E, eps, a, b,
-// hub_thr]); defaults eps 0.3, a 0.5, b 1 - a, hub_thr 256.
+// hub_thr, block_thr]); defaults eps 0.3, a 0.5, b 1 - a, hub_thr 256,
+// block_thr none (hub rows above block_thr take a whole block each).
 void tr_bounded_confidence(ApplyCtx &c) {
   Sim &s = *c.sim;
   const AgentTypeDesc &ad = s.model->at(c.call_type);
@@ -424,11 +652,23 @@ void tr_bounded_confidence(ApplyCtx &c) {
   double b = c.nparams > 3 ? c.params[3] : 1.0 - a;
   double thr_d = c.param(4, 256);
   uint32_t thr = thr_d >= 4294967295.0 ? 0xffffffffu : (uint32_t)thr_d;
+  // rows above this many in-edges take a whole block (default: none)
+  double big_d = c.param(5, 4294967295.0);
+  uint32_t big_thr = big_d >= 4294967295.0 ? 0xffffffffu : (uint32_t)big_d;
   OpinionArgs p{};
-  unsigned grid = opinion_args(s, e, c.call_type, eps, a, b, thr, p, s.stream);
+  unsigned grid = opinion_args(s, e, c.call_type, eps, a, b, thr, big_thr, p, s.stream);
   if (!grid) return;
-  if (p.grid) k_opinion<true><<<grid, TPB, 0, s.stream>>>(p);
-  else k_opinion<false><<<grid, TPB, 0, s.stream>>>(p);
+  // block-wide hubs (only with a block threshold) by their own launch, then
+  // the rest: the two write disjoint rows and read only the old opinions
+  const unsigned nbig = (unsigned)p.nbig;
+  if (nbig) {
+    if (p.grid) k_opinion_big<true><<<nbig, TPB, 0, s.stream>>>(p);
+    else k_opinion_big<false><<<nbig, TPB, 0, s.stream>>>(p);
+  }
+  if (grid > nbig) {
+    if (p.grid) k_opinion<true><<<grid - nbig, TPB, 0, s.stream>>>(p);
+    else k_opinion<false><<<grid - nbig, TPB, 0, s.stream>>>(p);
+  }
   VG_CUDA(cudaGetLastError());
 }
 
@@ -436,7 +676,8 @@ void tr_bounded_confidence(ApplyCtx &c) {
 // is nothing to launch (no agents, or no edges: then x' = x, copied here on
 // the stream the launch would use)
 static unsigned opinion_args(Sim &s, int e, int T, double eps, double a, double b,
-                             uint32_t thr, OpinionArgs &p, cudaStream_t launch_stream) {
+                             uint32_t thr, uint32_t big_thr, OpinionArgs &p,
+                             cudaStream_t launch_stream) {
   EdgeStore &es = s.edges[e];
   DevCSRView v = csr_view(s, e, T);
   if (v.nedges && v.src_type_const != T)
@@ -483,9 +724,11 @@ static unsigned opinion_args(Sim &s, int e, int T, double eps, double a, double 
     cs.unit_grid_weights = h ? 0 : 1;
   }
   p.grid = cs.unit_grid_weights;
-  ensure_schedule(s, cs, thr, av.n);
+  ensure_schedule(s, cs, thr, big_thr, av.n);
   p.hub_rows = cs.hub_rows.as<uint32_t>();
   p.nhub = cs.nhub;
+  p.nbig = cs.nbig;
+  p.status = s.d_status.as<int>();
   p.order = cs.order.as<uint32_t>();
   p.order_deg = cs.order_deg.as<uint32_t>();
   p.norder = cs.norder;
@@ -494,8 +737,8 @@ static unsigned opinion_args(Sim &s, int e, int T, double eps, double a, double 
   p.sell_src = cs.sell_src.as<uint32_t>();
   p.sell_w = cs.sell_w.as<double>();
   p.nslices = cs.nslices;
-  p.hub_blocks = (unsigned)((cs.nhub + (TPB / 32) - 1) / (TPB / 32));
-  return p.hub_blocks + (unsigned)((cs.nslices + (TPB / 32) - 1) / (TPB / 32));
+  p.hub_blocks = (unsigned)((cs.nhub - cs.nbig + (TPB / 32) - 1) / (TPB / 32));
+  return (unsigned)cs.nbig + p.hub_blocks + (unsigned)((cs.nslices + (TPB / 32) - 1) / (TPB / 32));
 }
 
 // Builds what a job's launches need ahead of its first step (the weight
@@ -504,7 +747,8 @@ void prepare_opinion_job(const OpinionJob &j) {
   OpinionArgs p{};
   DevCSRView v = csr_view(*j.sim, j.edge_type, j.type_nr);
   if (v.nedges == 0) return;  // nothing to prepare (and no copy to queue)
-  opinion_args(*j.sim, j.edge_type, j.type_nr, j.eps, j.a, j.b, j.hub_thr, p, j.sim->stream);
+  opinion_args(*j.sim, j.edge_type, j.type_nr, j.eps, j.a, j.b, j.hub_thr, j.block_thr, p,
+               j.sim->stream);
   VG_CUDA(cudaStreamSynchronize(j.sim->stream));
 }
 
@@ -518,7 +762,7 @@ void launch_opinion_jobs(const std::vector<OpinionJob> &jobs, cudaStream_t st, D
   for (size_t j = 0; j < jobs.size(); j++) {
     OpinionArgs p{};
     unsigned g = opinion_args(*jobs[j].sim, jobs[j].edge_type, jobs[j].type_nr, jobs[j].eps,
-                              jobs[j].a, jobs[j].b, jobs[j].hub_thr, p, st);
+                              jobs[j].a, jobs[j].b, jobs[j].hub_thr, jobs[j].block_thr, p, st);
     args.push_back(p);
     for (unsigned k = 0; k < g; k++) tiles.push_back({(uint32_t)j, k});
   }
