@@ -171,15 +171,7 @@ __device__ __forceinline__ double finish(const OpinionArgs &p, double xi, uint64
 }
 
 
-// One slice of 32 rows of similar degree, lane l owning row order[32 s +
-// l]: the lanes walk their rows' edges in insertion order in lock-step; the
-// column-major slice layout makes every load of a source index or weight
-// one coalesced 128 or 256-byte access.  Slots are taken in groups of
-// SELL_U with a two-stage software pipeline (while group g is folded, the
-// opinions of group g + 1 and the sources and weights of group g + 2 are in
-// flight), so that each warp keeps 2 SELL_U slots per lane outstanding.
-// Branch-free fold: a rejected edge adds +0 to swx and 0 K units to sw,
-// which leaves both sums unchanged, so no lane is masked off.
+// slots of a slice folded per pipeline step (see sell_slice)
 constexpr uint32_t SELL_U = 2;
 
 struct SellGroup {
