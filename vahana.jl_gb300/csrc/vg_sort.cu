@@ -53,7 +53,9 @@ __device__ T block_exclusive_scan(T v, T *warp_sums, T *block_total) {
   return r;
 }
 
-// Each thread owns SCAN_IPT consecutive items; safe in place.
+// The scan of at most one tile (SCAN_CHUNK items) in a single block, plus
+// an optional per-block prefix.  Each thread owns SCAN_IPT consecutive
+// items; safe in place.
 template <class T>
 __global__ void scan_apply(const T *in, T *out, uint64_t n, const T *prefix) {
   __shared__ T ws[32];
