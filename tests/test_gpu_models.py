@@ -32,6 +32,29 @@ def test_sir_bit_exact(vh):
     run.close()
 
 
+def test_sir_changing_beta_between_steps(vh):
+    """The infection table (1 - (1 - beta)^k per infected-neighbour count)
+    is uploaded once per content: a beta that changes between apply! calls
+    is picked up at the next call, and going back reuses nothing stale."""
+    from vahana_gb300 import models
+    run = models.build_sir(n=3000, degree=10, beta=0.05, recovery=7, seed=9, n_infected=30)
+    sim, m = run.sim, run.model
+    frm, to, _ = models.staged_edges(sim, "Contact")
+    st0, d0 = vh.read_agents(sim, "Person")[0].values()
+    vh.finish_init(sim)
+    g = om.build_inedges(run.n, frm, to)
+    s_ref, d_ref = np.ascontiguousarray(st0, np.uint8), np.ascontiguousarray(d0, np.int32)
+    betas = [0.05, 0.05, 0.2, 0.2, 0.05, 0.11, 0.2, 0.05] * 3
+    for t, beta in enumerate(betas):
+        vh.apply_(sim, "sir", ["Person"], ["Person", "Contact"], ["Person"],
+                  params=[m["Contact"].index, beta, 7, 9])
+        s_ref, d_ref = om.sir_step(g, s_ref, d_ref, beta, 7, 9, t + 1)
+    cols = vh.read_agents(sim, "Person")[0]
+    np.testing.assert_array_equal(cols["state"], s_ref)
+    np.testing.assert_array_equal(cols["days"], d_ref)
+    run.close()
+
+
 NO_SPLIT = 4294967295  # hub threshold that keeps every row on the ordered path
 
 

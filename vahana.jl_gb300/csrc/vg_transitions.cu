@@ -498,7 +498,7 @@ __device__ __forceinline__ uint32_t life_hsum(uint32_t c, uint32_t lw, uint32_t 
 // word column.  All LIFE_ROWS + 2 rows it reads are requested before any
 // is used (one memory latency per thread); rows outside a non-periodic
 // raster read as 0, a periodic raster wraps (a compare, no modulo).
-constexpr int LIFE_ROWS = 4;
+constexpr int LIFE_ROWS = 8;
 
 __global__ void __launch_bounds__(256) k_life2d_x4(const uint32_t *__restrict__ a,
                                                    uint32_t *__restrict__ o, int64_t Wq,
