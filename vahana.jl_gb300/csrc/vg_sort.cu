@@ -237,11 +237,13 @@ void exclusive_scan_impl(const T *in, T *out, uint64_t n, cudaStream_t st, int *
 // arXiv:2206.01784, 2022).  Tiles take their index from a counter in the
 // order the blocks start, so a tile only waits for tiles that are already
 // running.
-constexpr int RS_TPB = 256;
+constexpr int RS_TPB = 512;                        // threads of a pass tile
 constexpr int RS_WARPS = RS_TPB / 32;
 constexpr int RS_IPT = 8;                          // items per lane
 constexpr int RS_WARP_ITEMS = 32 * RS_IPT;         // 256
-constexpr int RS_TILE = RS_WARPS * RS_WARP_ITEMS;  // 2048
+constexpr int RS_TILE = RS_WARPS * RS_WARP_ITEMS;  // 4096
+constexpr int RS_UP_TPB = 256;                     // the upfront count's blocks
+constexpr int RS_UP_ROUND = RS_UP_TPB * RS_IPT;    // keys per block and round
 constexpr int RS_MAXPASS = 8;
 // look-back polls of one tile's status before the pass gives up, records an
 // error in the simulation's status word and treats the count as zero
@@ -263,23 +265,23 @@ __device__ __forceinline__ unsigned long long ld_status(const unsigned long long
 }
 
 template <class K>
-__global__ void __launch_bounds__(RS_TPB) rs_upfront(const K *keys, uint64_t n, int passes,
-                                                      uint32_t *ghist) {
+__global__ void __launch_bounds__(RS_UP_TPB) rs_upfront(const K *keys, uint64_t n, int passes,
+                                                         uint32_t *ghist) {
   __shared__ uint32_t h[RS_MAXPASS][256];
-  for (int i = threadIdx.x; i < RS_MAXPASS * 256; i += RS_TPB) (&h[0][0])[i] = 0;
+  for (int i = threadIdx.x; i < RS_MAXPASS * 256; i += RS_UP_TPB) (&h[0][0])[i] = 0;
   __syncthreads();
-  // a tile per round: its keys are requested before any is counted
-  for (uint64_t t0 = (uint64_t)blockIdx.x * RS_TILE; t0 < n;
-       t0 += (uint64_t)gridDim.x * RS_TILE) {
+  // a round of RS_UP_ROUND keys: requested before any is counted
+  for (uint64_t t0 = (uint64_t)blockIdx.x * RS_UP_ROUND; t0 < n;
+       t0 += (uint64_t)gridDim.x * RS_UP_ROUND) {
     K k[RS_IPT];
 #pragma unroll
     for (int i = 0; i < RS_IPT; i++) {
-      const uint64_t idx = t0 + (uint64_t)i * RS_TPB + threadIdx.x;
+      const uint64_t idx = t0 + (uint64_t)i * RS_UP_TPB + threadIdx.x;
       k[i] = idx < n ? keys[idx] : K(0);
     }
 #pragma unroll
     for (int i = 0; i < RS_IPT; i++) {
-      if (t0 + (uint64_t)i * RS_TPB + threadIdx.x >= n) break;
+      if (t0 + (uint64_t)i * RS_UP_TPB + threadIdx.x >= n) break;
       for (int p = 0; p < passes; p++) atomicAdd(&h[p][(unsigned)(k[i] >> (8 * p)) & 255u], 1u);
     }
   }
@@ -307,22 +309,24 @@ struct RsShared {
 // look-back, staged in shared memory in digit order and written out in
 // runs of consecutive positions.
 template <class K>
-__global__ void __launch_bounds__(RS_TPB, 4) rs_pass(const K *kin, const uint32_t *vin, K *kout,
+__global__ void __launch_bounds__(RS_TPB, 2) rs_pass(const K *kin, const uint32_t *vin, K *kout,
                                                    uint32_t *vout, uint64_t n, int pass,
                                                    const uint32_t *ghist,
                                                    unsigned long long *status,
                                                    uint32_t *ticket, int *err) {
-  __shared__ RsShared<K> S;
+  extern __shared__ __align__(16) unsigned char rs_smem[];
+  RsShared<K> &S = *reinterpret_cast<RsShared<K> *>(rs_smem);
+  const bool digit_thread = threadIdx.x < 256;  // thread d owns digit d
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int shift = 8 * pass;
-  const uint32_t gcount = ghist[pass * 256 + threadIdx.x];
+  const uint32_t gcount = digit_thread ? ghist[pass * 256 + threadIdx.x] : 0u;
   if (threadIdx.x == 0) {
     S.tile = atomicAdd(ticket, 1u);
     S.trivial = 0;
   }
   for (int d = threadIdx.x; d < RS_WARPS * 256; d += RS_TPB) (&S.wcnt[0][0])[d] = 0;
   __syncthreads();
-  if (gcount == n) S.trivial = 1;  // every key has this digit: the pass keeps the order
+  if (digit_thread && gcount == n) S.trivial = 1;  // every key has this digit: order kept
   const uint32_t tile = S.tile;
   const uint64_t t0 = (uint64_t)tile * RS_TILE;
   const uint32_t m = (uint32_t)(n - t0 < (uint64_t)RS_TILE ? n - t0 : (uint64_t)RS_TILE);
@@ -355,22 +359,25 @@ __global__ void __launch_bounds__(RS_TPB, 4) rs_pass(const K *kin, const uint32_
     __syncwarp();
   }
   __syncthreads();
-  // thread d: exclusive counts of digit d over the warps, the tile's count
-  const int d = threadIdx.x;
+  // thread d < 256: exclusive counts of digit d over the warps, the tile's count
+  const int d = digit_thread ? threadIdx.x : 0;
   uint32_t c = 0;
+  if (digit_thread) {
 #pragma unroll
-  for (int w2 = 0; w2 < RS_WARPS; w2++) {
-    const uint32_t t = S.wcnt[w2][d];
-    S.wcnt[w2][d] = c;
-    c += t;
+    for (int w2 = 0; w2 < RS_WARPS; w2++) {
+      const uint32_t t = S.wcnt[w2][d];
+      S.wcnt[w2][d] = c;
+      c += t;
+    }
   }
   const unsigned long long tag = (unsigned long long)(pass + 1) << 34;
   unsigned long long *my = status + (uint64_t)tile * 256 + d;
-  st_status(my, tag | ((tile ? 1ull : 2ull) << 32) | c);
+  if (digit_thread) st_status(my, tag | ((tile ? 1ull : 2ull) << 32) | c);
+  // all threads take part in the block scans (the others add 0)
   const uint32_t ds = block_exclusive_scan<uint32_t>(c, S.ws, (uint32_t *)nullptr);
   const uint32_t gex = block_exclusive_scan<uint32_t>(gcount, S.ws, (uint32_t *)nullptr);
   uint32_t excl = 0;
-  if (tile) {
+  if (digit_thread && tile) {
     // RS_LOOK predecessors per round trip: their words are loaded together
     // and consumed in order until a prefix, or a word not yet published
     int64_t t = (int64_t)tile - 1;
@@ -409,8 +416,10 @@ __global__ void __launch_bounds__(RS_TPB, 4) rs_pass(const K *kin, const uint32_
     }
     st_status(my, tag | (2ull << 32) | (excl + c));
   }
-  S.dstart[d] = ds;
-  S.gbase[d] = gex + excl;
+  if (digit_thread) {
+    S.dstart[d] = ds;
+    S.gbase[d] = gex + excl;
+  }
   __syncthreads();
 #pragma unroll
   for (int k = 0; k < RS_IPT; k++) {
@@ -474,8 +483,15 @@ void radix_sort_impl(K *keys, uint32_t *vals, uint64_t n, int bits, cudaStream_t
   uint32_t *va = (uint32_t *)(buf + head + stat + kb);
   K *kb2 = nalt == 2 ? (K *)(buf + head + stat + kb + vb) : nullptr;
   uint32_t *vb2 = nalt == 2 ? (uint32_t *)(buf + head + stat + 2 * kb + vb) : nullptr;
-  const unsigned hblocks = (unsigned)std::min<uint64_t>(ntiles, 152 * 4);
-  rs_upfront<K><<<hblocks, RS_TPB, 0, st>>>(keys, n, passes, ghist);
+  const unsigned hblocks =
+      (unsigned)std::min<uint64_t>((n + RS_UP_ROUND - 1) / RS_UP_ROUND, 152 * 4);
+  rs_upfront<K><<<hblocks, RS_UP_TPB, 0, st>>>(keys, n, passes, ghist);
+  // the pass's shared memory exceeds the 48 KB of a static allocation
+  static const bool smem_ok = [] {
+    return cudaFuncSetAttribute(rs_pass<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)sizeof(RsShared<K>)) == cudaSuccess;
+  }();
+  if (!smem_ok) fail(VG_ERR_CUDA, "radix sort: cannot reserve the pass's shared memory");
   VG_CUDA(cudaGetLastError());
   // buffer sequence: keys -> a -> keys ... for an even number of passes;
   // keys -> a -> b -> keys -> ... with three buffers for an odd number
@@ -487,7 +503,8 @@ void radix_sort_impl(K *keys, uint32_t *vals, uint64_t n, int bits, cudaStream_t
     if (nalt == 1) nxt = cur == 0 ? 1 : 0;
     else if (p == passes - 1) nxt = 0;
     else nxt = cur == 0 ? 1 : (cur == 1 ? 2 : 1);
-    rs_pass<K><<<(unsigned)ntiles, RS_TPB, 0, st>>>(kbufs[cur], vbufs[cur], kbufs[nxt],
+    rs_pass<K><<<(unsigned)ntiles, RS_TPB, sizeof(RsShared<K>), st>>>(kbufs[cur], vbufs[cur],
+                                                                      kbufs[nxt],
                                                     vbufs[nxt], n, p, ghist, status,
                                                     tickets + p, err);
     VG_CUDA(cudaGetLastError());
