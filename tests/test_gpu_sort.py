@@ -1,6 +1,6 @@
 """The device radix sort that rebuilds every CSR in insertion order (stable
 LSD sort, one launch per 8-bit digit with a chained look-back over
-4096-item tiles)
+8192-item tiles)
 and the single-pass prefix scan behind row pointers and compactions:
 keys and carried indices equal a stable host sort for sizes around the
 2048-item tile, odd and even digit counts, 32- and 64-bit keys, and digits
@@ -24,6 +24,8 @@ CASES = [
     (4096, 12, 0, 0, 0),
     (4097, 13, 0, 0, 0),
     (8193, 24, 0, 0, 0),
+    (8191, 14, 0, 0, 0),
+    (16385, 24, 0, 0, 0),
     (100_003, 17, 0, 0, 0),
     (1_000_000, 24, 0, 0, 0),
     (1_000_000, 32, 0, 0, 0),

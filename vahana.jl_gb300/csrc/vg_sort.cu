@@ -237,11 +237,11 @@ void exclusive_scan_impl(const T *in, T *out, uint64_t n, cudaStream_t st, int *
 // arXiv:2206.01784, 2022).  Tiles take their index from a counter in the
 // order the blocks start, so a tile only waits for tiles that are already
 // running.
-constexpr int RS_TPB = 512;                        // threads of a pass tile
+constexpr int RS_TPB = 1024;                       // threads of a pass tile
 constexpr int RS_WARPS = RS_TPB / 32;
 constexpr int RS_IPT = 8;                          // items per lane
 constexpr int RS_WARP_ITEMS = 32 * RS_IPT;         // 256
-constexpr int RS_TILE = RS_WARPS * RS_WARP_ITEMS;  // 4096
+constexpr int RS_TILE = RS_WARPS * RS_WARP_ITEMS;  // 8192
 constexpr int RS_UP_TPB = 256;                     // the upfront count's blocks
 constexpr int RS_UP_ROUND = RS_UP_TPB * RS_IPT;    // keys per block and round
 constexpr int RS_MAXPASS = 8;
@@ -309,7 +309,7 @@ struct RsShared {
 // look-back, staged in shared memory in digit order and written out in
 // runs of consecutive positions.
 template <class K>
-__global__ void __launch_bounds__(RS_TPB, 2) rs_pass(const K *kin, const uint32_t *vin, K *kout,
+__global__ void __launch_bounds__(RS_TPB, 1) rs_pass(const K *kin, const uint32_t *vin, K *kout,
                                                    uint32_t *vout, uint64_t n, int pass,
                                                    const uint32_t *ghist,
                                                    unsigned long long *status,
