@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--mean-degree", type=float, default=20.0)
     ap.add_argument("--wmax", type=float, default=1e4)
     ap.add_argument("--seed", type=int, default=1)
-    ap.add_argument("--hub-threshold", type=int, default=256)
+    ap.add_argument("--hub-threshold", type=int, default=1024)
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -456,7 +456,8 @@ def run_serve(args):
             T = "Person"
         else:
             run = models.build_opinion(n=s.n, mean_degree=s.mean_degree, gamma=2.5, wmax=s.wmax,
-                                       eps=s.eps, seed=s.seed, hub_threshold=256)
+                                       eps=s.eps, seed=s.seed,
+                                       hub_threshold=models.OPINION_HUB_THRESHOLD)
             T = "Opinion"
         vh.finish_init(run.sim)
         for _ in range(s.steps):

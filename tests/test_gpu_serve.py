@@ -16,7 +16,7 @@ def _alone(spec):
     else:
         run = models.build_opinion(n=spec.n, mean_degree=spec.mean_degree, gamma=2.5,
                                    wmax=spec.wmax, eps=spec.eps, seed=spec.seed,
-                                   hub_threshold=256)
+                                   hub_threshold=models.OPINION_HUB_THRESHOLD)
         T = "Opinion"
     import vahana_gb300 as vh
     vh.finish_init(run.sim)

@@ -32,7 +32,7 @@ def test_opinion_checkpoint_continues_bit_identically(vh, tmp_path):
     for _ in range(4):
         run.step()
         vh.apply_(loaded, "bounded_confidence", ["Opinion"], ["Opinion", "Weight"], ["Opinion"],
-                  params=[E, 0.3, 0.5, 0.5, 256])
+                  params=[E, 0.3, 0.5, 0.5, models.OPINION_HUB_THRESHOLD])
     _same_x(vh, run.sim, loaded, "Opinion", "x")
     loaded.close()
     run.close()

@@ -619,7 +619,7 @@ static unsigned opinion_args(Sim &s, int e, int T, double eps, double a, double 
                              cudaStream_t launch_stream);
 
 // apply!(sim, bounded_confidence, [T], [T, E], [T]; params = [E, eps, a, b,
-// hub_thr, block_thr]); defaults eps 0.3, a 0.5, b 1 - a, hub_thr 256,
+// hub_thr, block_thr]); defaults eps 0.3, a 0.5, b 1 - a, hub_thr 1024,
 // block_thr none (hub rows above block_thr take a whole block each).
 void tr_bounded_confidence(ApplyCtx &c) {
   Sim &s = *c.sim;
@@ -642,7 +642,7 @@ void tr_bounded_confidence(ApplyCtx &c) {
   double eps = c.param(1, 0.3);
   double a = c.param(2, 0.5);
   double b = c.nparams > 3 ? c.params[3] : 1.0 - a;
-  double thr_d = c.param(4, 256);
+  double thr_d = c.param(4, OPINION_HUB_DEFAULT);
   uint32_t thr = thr_d >= 4294967295.0 ? 0xffffffffu : (uint32_t)thr_d;
   // rows above this many in-edges take a whole block (default: none)
   double big_d = c.param(5, 4294967295.0);

@@ -197,7 +197,8 @@ void build_job(vg_server *S, Job *J, cudaStream_t bst) {
                                     sp.wmax, sp.seed, 0)))
       fail(rc, vg_last_error());
     if ((rc = vg_finish_init(J->sim))) fail(rc, vg_last_error());
-    prepare_opinion_job({J->sim->s.get(), S->op_edge, S->op_agent, J->spec.eps, 0.5, 0.5, 256});
+    prepare_opinion_job({J->sim->s.get(), S->op_edge, S->op_agent, J->spec.eps, 0.5, 0.5,
+                         OPINION_HUB_DEFAULT});
   }
 }
 
@@ -276,7 +277,7 @@ void tick(vg_server *S) {
       for (uint64_t a = 0; a < A.n; a += 256) stiles.push_back({ji, (uint32_t)a});
       sir_jobs.push_back(J);
     } else {
-      oj.push_back({&s, S->op_edge, S->op_agent, J->spec.eps, 0.5, 0.5, 256});
+      oj.push_back({&s, S->op_edge, S->op_agent, J->spec.eps, 0.5, 0.5, OPINION_HUB_DEFAULT});
       op_jobs.push_back(J);
     }
   }

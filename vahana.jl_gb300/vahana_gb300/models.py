@@ -85,8 +85,13 @@ def opinion_initial_state(n, seed):
                                                  philox.TAG_INIT)))
 
 
+# rows above this in-degree are split across a warp (1e-12 relative), the
+# others fold in order (bit-exact); the library's default as well
+OPINION_HUB_THRESHOLD = 1024
+
+
 def build_opinion(n=10_000_000, mean_degree=20, gamma=2.5, wmax=1e4, eps=0.3, seed=1,
-                  stream=None, hub_threshold=256):
+                  stream=None, hub_threshold=OPINION_HUB_THRESHOLD):
     model = opinion_model()
     sim = api.create_simulation(model, stream=stream)
     x = opinion_initial_state(n, seed)
