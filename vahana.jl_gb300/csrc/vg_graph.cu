@@ -987,9 +987,9 @@ void ensure_schedule(Sim &s, CSR &c, uint32_t thr, uint32_t big_thr, uint64_t n)
       VG_CUDA(cudaStreamSynchronize(st));
       c.nbig = h;
     }
-    // the other rows by descending degree in windows of 2^16 rows (or
+    // the other rows by descending degree in windows of 2^13 rows (or
     // more, so that the window number stays below the sentinel)
-    uint32_t wshift = 16;
+    uint32_t wshift = 13;
     while ((n >> wshift) >= 0xFFFFull) wshift++;
     Tmp<uint32_t> keys(n, st);
     c.order.alloc(n * 4, &s.footprint);

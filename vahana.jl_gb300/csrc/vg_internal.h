@@ -164,7 +164,7 @@ struct CSR {
   // use by the gather kernels, cached until the CSR changes):
   // hub rows (degree > hub threshold) by descending degree; the other rows
   // (agents beyond the CSR's rows included) in `order`, by descending
-  // degree inside windows of 2^16 consecutive rows, cut into slices of 32;
+  // degree inside windows of 2^13 consecutive rows, cut into slices of 32;
   // the edges of a slice stored column-major (SELL-C-sigma): edge k of the
   // slice's lane l at slice_base + 32 k + l, padded to the slice's largest
   // degree (padding: source 0, weight 0)
