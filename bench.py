@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--mean-degree", type=float, default=20.0)
     ap.add_argument("--wmax", type=float, default=1e4)
     ap.add_argument("--seed", type=int, default=1)
-    ap.add_argument("--hub-threshold", type=int, default=1024)
+    ap.add_argument("--hub-threshold", type=int, default=1536)
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")

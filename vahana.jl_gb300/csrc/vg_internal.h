@@ -363,8 +363,8 @@ void tr_bounded_confidence(ApplyCtx &ctx);  // vg_opinion.cu
 // one bounded-confidence launch over many simulations (vg_opinion.cu)
 // default hub threshold of the bounded-confidence gather: rows above it are
 // split across a warp (1e-12 relative), rows at or below it fold in order
-// (bit-exact); 1024 measured fastest on the benchmark graph
-constexpr uint32_t OPINION_HUB_DEFAULT = 1024;
+// (bit-exact); 1536 measured fastest on the benchmark graph
+constexpr uint32_t OPINION_HUB_DEFAULT = 1536;
 
 struct OpinionJob {
   Sim *sim;

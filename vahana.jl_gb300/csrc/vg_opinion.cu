@@ -619,7 +619,7 @@ static unsigned opinion_args(Sim &s, int e, int T, double eps, double a, double 
                              cudaStream_t launch_stream);
 
 // apply!(sim, bounded_confidence, [T], [T, E], [T]; params = [E, eps, a, b,
-// hub_thr, block_thr]); defaults eps 0.3, a 0.5, b 1 - a, hub_thr 1024,
+// hub_thr, block_thr]); defaults eps 0.3, a 0.5, b 1 - a, hub_thr 1536,
 // block_thr none (hub rows above block_thr take a whole block each).
 void tr_bounded_confidence(ApplyCtx &c) {
   Sim &s = *c.sim;

@@ -87,7 +87,7 @@ def opinion_initial_state(n, seed):
 
 # rows above this in-degree are split across a warp (1e-12 relative), the
 # others fold in order (bit-exact); the library's default as well
-OPINION_HUB_THRESHOLD = 1024
+OPINION_HUB_THRESHOLD = 1536
 
 
 def build_opinion(n=10_000_000, mean_degree=20, gamma=2.5, wmax=1e4, eps=0.3, seed=1,
