@@ -154,3 +154,28 @@ def test_life_walkers_generic_vs_c():
         pos = (c % W + 1, c // W + 1)
         ids = V.neighborids(sim, grid[pos], "OnCell") or []
         assert [V.agent_nr(i) for i in ids] == list(src_c[int(rp_c[c]):int(rp_c[c + 1])])
+
+
+def test_life_bounded_generic_vs_c():
+    """The C restatement's Life on a bounded raster (positions outside are
+    dropped, src/Raster.jl:479-499) equals Life written as a transition on
+    the generic oracle with connect_raster_neighbors!(periodic = false)."""
+    W, H, steps = 8, 6, 5
+    rng = np.random.default_rng(4)
+    alive = rng.random(W * H) < 0.4
+    m = (V.ModelTypes().register_agenttype("Cell", [("alive", "bool")], ":Immortal")
+         .register_edgetype("Neighbor", [], ":Stateless", target="Cell").create_model("LifeB"))
+    sim = V.create_simulation(m)
+    flat = alive.reshape((H, W)).T
+    V.add_raster(sim, "raster", (W, H), "Cell", lambda p: {"alive": bool(flat[p[0] - 1, p[1] - 1])})
+    V.connect_raster_neighbors(sim, "raster", "Neighbor", lambda a, b: None, periodic=False)
+    V.finish_init(sim)
+
+    def life(a, id, s):
+        c = sum(1 for x in (V.neighborstates(s, id, "Neighbor", "Cell") or []) if x["alive"])
+        return {"alive": c == 3 or (a["alive"] and c == 2)}
+    ref = alive.astype(np.uint8)
+    for _ in range(steps):
+        V.apply_(sim, life, "Cell", ["Cell", "Neighbor"], "Cell")
+        ref = om.life_step(ref, W, H, periodic=False)
+    assert [bool(c["alive"]) for c in V.all_agents(sim, "Cell")] == [bool(v) for v in ref]
