@@ -116,6 +116,8 @@ def test_raster_staging_counts(vh):
 
 
 def test_params_and_globals(vh):
+    """test/globals.jl:1-17 (set_global! of a scalar, push_global! twice onto
+    a series) and register_param!/param/set_param! (src/Simulation.jl:587-630)"""
     m = (vh.ModelTypes().register_agenttype("A", [("foo", "i64")])
          .register_param("beta", 0.1).register_global("count", 0.0).create_model("pg"))
     sim = vh.create_simulation(m)
@@ -127,4 +129,24 @@ def test_params_and_globals(vh):
     vh.push_global(sim, "series", 2.0)
     assert vh.get_global(sim, "count") == 3.0
     assert list(vh.global_series(sim, "series")) == [1.0, 2.0]
+    sim.close()
+
+
+def test_parametric_type_names(vh):
+    """test/parametric_types.jl:1-38: a parametric Julia type is registered
+    under its full name; agents of it, a plain agent type and a parametric
+    edge type are read back through edges, edgestates and neighborstates
+    (here on the staged init-phase edges)."""
+    m = (vh.ModelTypes().register_agenttype("PAgent{Float64}", [("t", "f64")])
+         .register_agenttype("PAgent2", [("t", "f64")])
+         .register_edgetype("PEdge{Float64}", [("t", "f64")]).create_model("parametric types"))
+    sim = vh.create_simulation(m)
+    id1 = vh.add_agent(sim, "PAgent{Float64}", t=1.0)
+    id2 = vh.add_agent(sim, "PAgent2", t=2.0)
+    vh.add_edge(sim, id1, id2, "PEdge{Float64}", t=3.0)
+    assert vh.edges(sim, id2, "PEdge{Float64}")[0].state == {"t": 3.0}
+    assert vh.edgestates(sim, id2, "PEdge{Float64}") == [{"t": 3.0}]
+    assert vh.neighborstates(sim, id2, "PEdge{Float64}", "PAgent{Float64}") == [{"t": 1.0}]
+    assert vh.type_nr(id1) == m["PAgent{Float64}"].index
+    assert vh.type_nr(id2) == m["PAgent2"].index
     sim.close()

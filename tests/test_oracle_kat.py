@@ -516,6 +516,32 @@ def test_complete_graph_sum():
     assert V.mapreduce(sim, lambda a: a["sum"], "+", "GraphA") == sum(range(1, n + 1)) * (n - 1)
 
 
+# ------------------------------------------------- test/parametric_types.jl
+def test_parametric_types():
+    """test/parametric_types.jl:1-38: a parametric type is one more type
+    name; an agent type, a non-parametric agent type and a parametric edge
+    type are read back through edges, edgestates and neighborstates"""
+    m = (V.ModelTypes().register_agenttype("PAgent{Float64}", [("t", "f64")])
+         .register_agenttype("PAgent2", [("t", "f64")])
+         .register_edgetype("PEdge{Float64}", [("t", "f64")]).create_model("parametric types"))
+    sim = V.create_simulation(m)
+    id1 = V.add_agent(sim, "PAgent{Float64}", {"t": 1.0})
+    id2 = V.add_agent(sim, "PAgent2", {"t": 2.0})
+    V.add_edge(sim, id1, id2, "PEdge{Float64}", {"t": 3.0})
+    V.finish_init(sim)
+    seen = []
+
+    def f(state, id, sim_):
+        assert V.edges(sim_, id, "PEdge{Float64}")[0].state["t"] == 3.0
+        assert V.edgestates(sim_, id, "PEdge{Float64}") == [{"t": 3.0}]
+        assert V.neighborstates(sim_, id, "PEdge{Float64}", "PAgent{Float64}") == [{"t": 1.0}]
+        seen.append(id)
+        return state
+    V.apply_(sim, f, "PAgent2", ["PAgent{Float64}", "PAgent2", "PEdge{Float64}"], "PAgent2")
+    assert seen == [id2]
+    assert V.type_nr(id1) != V.type_nr(id2)
+
+
 # ------------------------------------------------------ test/addexisting.jl
 def test_add_existing_reset():
     """test/addexisting.jl:127-184 (the parts without add_agent! in a transition)"""
