@@ -516,6 +516,43 @@ def test_complete_graph_sum():
     assert V.mapreduce(sim, lambda a: a["sum"], "+", "GraphA") == sum(range(1, n + 1)) * (n - 1)
 
 
+# ------------------------------------------------------ test/independent.jl
+def test_independent_equivalence():
+    """test/independent.jl:31-216: the same model under :Independent, without
+    it, and the second :Independent type (named Immortal in the reference)
+    gives equal agent and edge counts after each of the three transitions:
+    agents with foo == 1 die while the others link to and from their
+    neighbours, then foo == 2, then every agent adds two agents (foo + 10,
+    foo + 20) linked both ways with add_existing."""
+    counts = {}
+    for T, hints in (("AIndependent", [":Independent"]), ("ANotIndependent", []),
+                     ("AIndependentImmortal", [":Independent"])):
+        m = (V.ModelTypes().register_agenttype(T, [("foo", "i64")], *hints)
+             .register_edgetype("AFooEdge", [("foo", "i64")]).register_edgetype("AEdge", [])
+             .create_model("Test Independent"))
+        sim = V.create_simulation(m)
+        ids = [V.add_agent(sim, T, {"foo": i}) for i in range(1, 11)]
+        for a in ids:
+            for b in ids:
+                V.add_edge(sim, a, b, "AEdge")
+        V.finish_init(sim)
+        assert V.num_agents(sim, T) == 10
+        assert V.num_edges_total(sim, "AEdge") == 100
+        c = []
+        for foo in (1, 2):
+            V.apply_(sim, V.tr_link_neighbors("AEdge", "AFooEdge", foo), T, [T, "AEdge"],
+                     [T, "AFooEdge"])
+            c.append((V.num_agents(sim, T), V.num_edges_total(sim, "AEdge"),
+                      V.num_edges_total(sim, "AFooEdge")))
+        V.apply_(sim, V.tr_spawn([10, 20], "AFooEdge"), T, [T, "AEdge"], [T, "AFooEdge"],
+                 add_existing="AFooEdge")
+        c.append((V.num_agents(sim, T), V.num_edges_total(sim, "AEdge"),
+                  V.num_edges_total(sim, "AFooEdge")))
+        counts[T] = c
+    assert counts["AIndependent"] == counts["ANotIndependent"] == counts["AIndependentImmortal"]
+    assert counts["ANotIndependent"] == [(9, 81, 162), (8, 64, 128), (24, 64, 160)]
+
+
 # ------------------------------------------------- test/parametric_types.jl
 def test_parametric_types():
     """test/parametric_types.jl:1-38: a parametric type is one more type
