@@ -337,6 +337,10 @@ def run_ours(args):
             "frac": achieved / peak, "peak_kind": kind, "traffic": traffic_per_launch(),
             "algorithmic_bytes_per_launch": alg_bytes, "kernel": "k_opinion",
             "kernel_ms_mean": mean_kernel_ms, "kernel_ms_median": kernel_ms[len(kernel_ms) // 2]}
+    # every gathered opinion counted (8 B per edge more): reported beside, not the target
+    touch_bytes = 20 * E + 20 * N
+    roof["element_touch_bytes_per_launch"] = touch_bytes
+    roof["element_touch_gbs"] = touch_bytes / (mean_kernel_ms * 1e-3) / 1e9
 
     out = {"metric": METRIC, "value": value, "unit": "edge-updates/s", "n_gpus": ws,
            "steps": K, "warmup": args.warmup, "ms_per_step": total_ms / K,
