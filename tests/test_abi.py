@@ -150,3 +150,30 @@ def test_parametric_type_names(vh):
     assert vh.type_nr(id1) == m["PAgent{Float64}"].index
     assert vh.type_nr(id2) == m["PAgent2"].index
     sim.close()
+
+
+def test_neighborstates_iterators(vh):
+    """neighborstates_iter (src/EdgeMethods.jl:783-803) and
+    neighborstates_flexible_iter (src/Edge.jl:328-335) on staged edges:
+    states in insertion order; the :SingleEdge / :IgnoreFrom rules."""
+    m = (vh.ModelTypes().register_agenttype("A", [("foo", "i64")])
+         .register_edgetype("D", [("foo", "i64")])
+         .register_edgetype("SE", [("foo", "i64")], ":SingleEdge")
+         .register_edgetype("IF", [("foo", "i64")], ":IgnoreFrom")
+         .create_model("iter"))
+    sim = vh.create_simulation(m)
+    a1, a2, a3 = vh.add_agents(sim, "A", 3, foo=[1, 2, 3])
+    vh.add_edge(sim, a2, a3, "D", foo=1)
+    vh.add_edge(sim, a1, a3, "D", foo=2)
+    vh.add_edge(sim, a2, a3, "SE", foo=1)
+    vh.add_edge(sim, a1, a3, "IF", foo=1)
+    assert list(vh.neighborstates_iter(sim, a3, "D", "A")) == [{"foo": 2}, {"foo": 1}]
+    assert vh.neighborstates_iter(sim, a1, "D", "A") is None
+    assert list(vh.neighborstates_flexible_iter(sim, a3, "D")) == [{"foo": 2}, {"foo": 1}]
+    assert list(vh.neighborstates_flexible_iter(sim, a3, "SE")) == [{"foo": 2}]
+    for T in ("SE", "IF"):
+        with pytest.raises(AssertionError):
+            vh.neighborstates_iter(sim, a3, T, "A")
+    with pytest.raises(AssertionError):
+        vh.neighborstates_flexible_iter(sim, a3, "IF")
+    sim.close()

@@ -17,7 +17,8 @@ export ModelTypes, register_agenttype!, register_edgetype!, register_param!,
        register_global!, create_model, create_simulation, finish_simulation!,
        copy_simulation, finish_init!, add_agent!, add_agents!, add_edge!, add_edges!,
        apply!, apply, mapreduce, agentstate, agentstate_flexible, edges, neighborids,
-       neighborstates, edgestates, num_edges, has_edge, num_agents, all_agents,
+       neighborids_iter, neighborstates, neighborstates_iter, neighborstates_flexible,
+       neighborstates_flexible_iter, edgestates, edgestates_iter, num_edges, has_edge, num_agents, all_agents,
        all_agentids, add_raster!, connect_raster_neighbors!, move_to!, cellid,
        rastervalues, calc_rasterstate, param, set_param!, get_global, set_global!,
        push_global!, disable_transition_checks, transition_names, Edge, AgentID,
@@ -298,6 +299,44 @@ end
 
 neighborstates(sim::Simulation, id::AgentID, ::Type{E}, ::Type{A}) where {E, A} =
     (ids = neighborids(sim, id, E); ids === nothing ? nothing : [agentstate(sim, i, A) for i in ids])
+
+"the normalised hint bits of edge type T (vg_model_edge_hints)"
+function edgehints(model::ModelTypes, ::Type{T}) where T
+    h = Ref{Cuint}(0)
+    check(ccall((:vg_model_edge_hints, LIB), Cint, (Ptr{Cvoid}, Cint, Ptr{Cuint}),
+                model.h, model.edges[T], h))
+    h[]
+end
+
+function notdefined(sim, ::Type{T}, fn, hints...) where T
+    h = edgehints(sim.model, T)
+    any(x -> h & HINTS[x] != 0, hints) &&
+        throw(AssertionError("$fn is not defined for edgetypes with the " *
+                             join(string.(":", hints), " or ") * " hint"))
+end
+
+"neighborstates_flexible(sim, id, T) -- src/Edge.jl:303-306"
+neighborstates_flexible(sim::Simulation, id::AgentID, ::Type{E}) where E =
+    (ids = neighborids(sim, id, E); ids === nothing ? nothing : [agentstate_flexible(sim, i) for i in ids])
+
+"neighborids_iter(sim, id, T) -- src/EdgeMethods.jl:744-760"
+neighborids_iter(sim::Simulation, id::AgentID, ::Type{E}) where E =
+    (notdefined(sim, E, "neighborids_iter", :SingleEdge, :IgnoreFrom);
+     ids = neighborids(sim, id, E); ids === nothing ? nothing : (i for i in ids))
+
+"edgestates_iter(sim, id, T) -- src/Edge.jl:208-224"
+edgestates_iter(sim::Simulation, id::AgentID, ::Type{E}) where E =
+    (notdefined(sim, E, "edgestates_iter", :SingleEdge, :Stateless);
+     es = edgestates(sim, id, E); es === nothing ? nothing : (e for e in es))
+
+"neighborstates_iter(sim, id, T, A) -- src/EdgeMethods.jl:783-803"
+neighborstates_iter(sim::Simulation, id::AgentID, ::Type{E}, ::Type{A}) where {E, A} =
+    (notdefined(sim, E, "neighborstates_iter", :SingleEdge, :IgnoreFrom);
+     ids = neighborids(sim, id, E); ids === nothing ? nothing : (agentstate(sim, i, A) for i in ids))
+
+"neighborstates_flexible_iter(sim, id, T) -- src/Edge.jl:328-335"
+neighborstates_flexible_iter(sim::Simulation, id::AgentID, ::Type{E}) where E =
+    (ids = neighborids(sim, id, E); ids === nothing ? nothing : (agentstate_flexible(sim, i) for i in ids))
 
 "edgestates(sim, id, T) -- src/EdgeMethods.jl:805-829"
 function edgestates(sim::Simulation, id::AgentID, ::Type{T}) where T

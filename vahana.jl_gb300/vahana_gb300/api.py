@@ -577,6 +577,28 @@ def neighborstates_flexible(sim, id, T):
     return [agentstate_flexible(sim, i) for i in ids]
 
 
+def neighborstates_iter(sim, id, T, AT):
+    """neighborstates_iter(sim, id, T, AT) -- src/EdgeMethods.jl:783-803"""
+    t = sim.T(T)
+    if sim.model.has_hint(t.name, ":SingleEdge") or sim.model.has_hint(t.name, ":IgnoreFrom"):
+        raise AssertionError("neighborstates_iter is not defined for edgetypes with the "
+                             ":SingleEdge or :IgnoreFrom hint")
+    ids = neighborids(sim, id, T)
+    return None if ids is None else (agentstate(sim, i, AT) for i in ids)
+
+
+def neighborstates_flexible_iter(sim, id, T):
+    """neighborstates_flexible_iter -- src/Edge.jl:328-335: no check of its
+    own; :IgnoreFrom fails in neighborids, and the single id of a
+    :SingleEdge row is iterated as one element, as a Julia number is."""
+    ids = neighborids(sim, id, T)
+    if ids is None:
+        return None
+    if sim.model.has_hint(sim.T(T).name, ":SingleEdge"):
+        ids = [ids]
+    return (agentstate_flexible(sim, i) for i in ids)
+
+
 def num_edges(sim, id_or_T, T=None, write=None):
     """num_edges(sim, id, T) -- src/EdgeMethods.jl:851-869 and
     num_edges(sim, T; write) -- src/Edge.jl:373-389"""
