@@ -75,6 +75,10 @@ def test_init_phase_staging_and_accessors(vh):
     with pytest.raises(AssertionError):
         vh.add_edge(sim, a1, a3, "SE", foo=2)
     vh.add_edge(sim, a1, a3, "S")
+    vh.add_edge(sim, a2, vh.Edge(a3, {"foo": 7}), "D")  # add_edge!(sim, to, Edge(from, state))
+    assert vh.edges(sim, a2, "D") == [vh.Edge(a3, {"foo": 7})]
+    assert vh.num_edges(sim, "D", write=True) == 3
+    vh.remove_edges(sim, a2, "D")
     assert vh.num_edges(sim, "D", write=True) == 2
     assert vh.num_edges(sim, "D", write=False) == 0
     assert vh.num_edges(sim, "SE", write=True) == 1

@@ -424,7 +424,10 @@ def add_edges(sim, T, frm, to, **payload):
 
 
 def add_edge(sim, frm, to, T, **payload):
-    """add_edge!(sim, from, to, state)"""
+    """add_edge!(sim, from, to, state); add_edge(sim, to, Edge(from, state), T)
+    is the form add_edge!(sim, to, edge) (src/EdgeMethods.jl:388-523)."""
+    if isinstance(to, Edge):
+        frm, to, payload = to.frm, frm, dict(to.state or {}, **payload)
     add_edges(sim, T, [frm], [to], **payload)
 
 
