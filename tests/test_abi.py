@@ -181,3 +181,37 @@ def test_neighborstates_iterators(vh):
     with pytest.raises(AssertionError):
         vh.neighborstates_flexible_iter(sim, a3, "IF")
     sim.close()
+
+
+def test_null_and_bad_arguments_return_errors(vh):
+    """Misuse at the C ABI returns VG_ERR_ARG (2) with a message instead of
+    crashing: null handles, names, field arrays and output pointers, and
+    unknown type numbers or names."""
+    import ctypes as C
+    L = vh.lib()
+    m = C.c_void_p()
+    sim = C.c_void_p()
+    nr = C.c_int()
+    hints = C.c_uint()
+    d = C.c_double()
+    assert L.vg_model_create(None) == 2
+    assert L.vg_sim_create(None, b"x", None, C.byref(sim)) == 2
+    assert b"null model handle" in L.vg_last_error()
+    assert L.vg_model_create(C.byref(m)) == 0
+    assert L.vg_model_register_agenttype(m, None, 0, None, None, 0, C.byref(nr)) == 2
+    assert L.vg_model_register_agenttype(m, b"A", 1, None, None, 0, C.byref(nr)) == 2
+    assert L.vg_model_register_agenttype(m, b"A", -1, None, None, 0, C.byref(nr)) == 2
+    assert L.vg_model_register_edgetype(m, None, 0, None, None, 0, 0, 0, C.byref(nr)) == 2
+    assert L.vg_model_register_param(m, None, 1.0) == 2
+    assert L.vg_model_register_global(None, b"g", 1.0) == 2
+    assert L.vg_model_edge_hints(m, 99, C.byref(hints)) == 2
+    assert L.vg_model_edge_hints(m, 0, None) == 2
+    assert L.vg_model_type_by_name(m, b"nope", C.byref(nr)) == 2
+    assert L.vg_model_type_by_name(m, None, C.byref(nr)) == 2
+    assert L.vg_model_finalize(m, b"bad args") == 0
+    assert L.vg_sim_create(m, b"x", None, None) == 2
+    assert L.vg_sim_load(m, None, None, C.byref(sim)) == 2
+    assert L.vg_num_agents(None, 1, C.byref(C.c_uint64())) == 2
+    assert L.vg_get_global(None, b"g", C.byref(d)) == 2
+    assert L.vg_finish_init(None) == 2
+    L.vg_model_destroy(m)

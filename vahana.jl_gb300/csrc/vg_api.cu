@@ -213,6 +213,23 @@ static Sim &S(vg_sim *s) {
   return *s->s;
 }
 
+static Model &MD(const vg_model *m) {
+  if (!m || !m->m) fail(VG_ERR_ARG, "null model handle");
+  return *m->m;
+}
+
+static const char *NM(const char *name) {
+  if (!name) fail(VG_ERR_ARG, "null name");
+  return name;
+}
+
+static void check_field_args(int nfields, const char *const *names, const int *dtypes) {
+  if (nfields < 0) fail(VG_ERR_ARG, "negative field count");
+  if (nfields > 0 && (!names || !dtypes)) fail(VG_ERR_ARG, "null field arrays");
+  for (int i = 0; i < nfields; i++)
+    if (!names[i]) fail(VG_ERR_ARG, "null field name");
+}
+
 static void check_fields(const std::vector<FieldDesc> &fs) {
   if (fs.size() > (size_t)MAX_FIELDS)
     fail(VG_ERR_ARG, "at most " + std::to_string(MAX_FIELDS) + " fields per type");
@@ -237,6 +254,7 @@ int vg_device_count(int *out) {
 // ------------------------------------------------------------------ model
 int vg_model_create(vg_model **out) {
   API_BEGIN
+  if (!out) fail(VG_ERR_ARG, "null output pointer");
   *out = new vg_model{std::make_shared<Model>()};
   API_END
 }
@@ -247,7 +265,9 @@ int vg_model_register_agenttype(vg_model *m, const char *name, int nfields,
                                 const char *const *names, const int *dtypes,
                                 unsigned hints, int *type_nr_out) {
   API_BEGIN
-  Model &M = *m->m;
+  Model &M = MD(m);
+  NM(name);
+  check_field_args(nfields, names, dtypes);
   if (M.finalized) fail(VG_ERR_STATE, "model already created");
   for (auto &a : M.atypes)
     if (a.name == name) fail(VG_ERR_ASSERT, std::string("Type ") + name + " is already registered");
@@ -275,7 +295,9 @@ int vg_model_register_edgetype(vg_model *m, const char *name, int nfields,
                                unsigned hints, int target, int64_t size,
                                int *edge_type_out) {
   API_BEGIN
-  Model &M = *m->m;
+  Model &M = MD(m);
+  NM(name);
+  check_field_args(nfields, names, dtypes);
   if (M.finalized) fail(VG_ERR_STATE, "model already created");
   for (auto &e : M.etypes)
     if (e.name == name) fail(VG_ERR_ASSERT, std::string("Type ") + name + " is already registered");
@@ -315,33 +337,37 @@ int vg_model_register_edgetype(vg_model *m, const char *name, int nfields,
 
 int vg_model_register_param(vg_model *m, const char *name, double d) {
   API_BEGIN
-  m->m->params.push_back({name, d});
+  MD(m).params.push_back({NM(name), d});
   API_END
 }
 int vg_model_register_global(vg_model *m, const char *name, double d) {
   API_BEGIN
-  m->m->globals.push_back({name, d});
+  MD(m).globals.push_back({NM(name), d});
   API_END
 }
 
 int vg_model_finalize(vg_model *m, const char *name) {
   API_BEGIN
-  m->m->name = name ? name : "";
-  m->m->finalized = true;
+  Model &M = MD(m);
+  M.name = name ? name : "";
+  M.finalized = true;
   API_END
 }
 
 int vg_model_edge_hints(const vg_model *m, int e, unsigned *out) {
   API_BEGIN
-  *out = m->m->et(e).hints;
+  if (!out) fail(VG_ERR_ARG, "null output pointer");
+  *out = MD(m).et(e).hints;
   API_END
 }
 
 int vg_model_type_by_name(const vg_model *m, const char *name, int *out) {
   API_BEGIN
-  for (auto &a : m->m->atypes)
+  NM(name);
+  if (!out) fail(VG_ERR_ARG, "null output pointer");
+  for (auto &a : MD(m).atypes)
     if (a.name == name) { *out = a.nr; return VG_OK; }
-  for (auto &e : m->m->etypes)
+  for (auto &e : MD(m).etypes)
     if (e.name == name) { *out = VG_EDGE(e.idx); return VG_OK; }
   fail(VG_ERR_ARG, std::string("unknown type ") + name);
   API_END
@@ -350,7 +376,8 @@ int vg_model_type_by_name(const vg_model *m, const char *name, int *out) {
 // ------------------------------------------------------------- lifecycle
 int vg_sim_create(vg_model *m, const char *name, void *stream, vg_sim **out) {
   API_BEGIN
-  if (!m->m->finalized) fail(VG_ERR_STATE, "call create_model (vg_model_finalize) first");
+  if (!out) fail(VG_ERR_ARG, "null output pointer");
+  if (!MD(m).finalized) fail(VG_ERR_STATE, "call create_model (vg_model_finalize) first");
   auto s = std::make_unique<Sim>();
   s->model = m->m;
   s->name = name ? name : m->m->name;

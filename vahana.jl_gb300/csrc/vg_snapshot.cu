@@ -218,7 +218,8 @@ int vg_sim_save(vg_sim *h, const char *path) {
 
 int vg_sim_load(vg_model *m, const char *path, void *stream, vg_sim **out) {
   API_BEGIN
-  if (!m || !m->m->finalized) fail(VG_ERR_ARG, "load: finalized model required");
+  if (!m || !m->m || !m->m->finalized) fail(VG_ERR_ARG, "load: finalized model required");
+  if (!path || !out) fail(VG_ERR_ARG, "load: null path or output pointer");
   File F(path, "rb");
   char magic[8];
   F.get(magic, 8);
