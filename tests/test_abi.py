@@ -214,4 +214,33 @@ def test_null_and_bad_arguments_return_errors(vh):
     assert L.vg_num_agents(None, 1, C.byref(C.c_uint64())) == 2
     assert L.vg_get_global(None, b"g", C.byref(d)) == 2
     assert L.vg_finish_init(None) == 2
+    assert L.vg_model_finalize(None, b"x") == 2
     L.vg_model_destroy(m)
+    # a staged simulation: required output pointers and argument arrays
+    mm = (vh.ModelTypes().register_agenttype("A", [("foo", "i64")])
+          .register_agenttype("Cell", [("v", "i64")])
+          .register_edgetype("D", [("foo", "i64")]).create_model("bad args 2"))
+    s = vh.create_simulation(mm)
+    vh.add_agents(s, "A", 3, foo=[1, 2, 3])
+    vh.add_raster(s, "r", (4, 4), "Cell", v=0)
+    h, a, e = s._h, mm["A"].index, mm["D"].index
+    u = C.c_uint64()
+    nd = C.c_int()
+    assert L.vg_num_agents(h, a, None) == 2
+    assert L.vg_agent_slots(h, a, None) == 2
+    assert L.vg_read_agents(h, a, None, None, 2, None) == 2
+    assert L.vg_sim_num_transitions(h, None) == 2
+    assert L.vg_sim_device_bytes(h, None) == 2
+    assert L.vg_num_edges_total(h, e, 1, None) == 2
+    assert L.vg_global_series(h, b"g", None, 0, None) == 2
+    assert L.vg_add_edges(h, e, 2, None, None, None) == 2
+    assert L.vg_remove_edges(h, e, 2, None, None) == 2
+    assert L.vg_cellid(h, b"r", None, C.byref(u)) == 2
+    assert L.vg_raster_dims(h, b"r", None, None) == 2
+    assert L.vg_raster_dims(h, b"r", None, C.byref(nd)) == 0 and nd.value == 2
+    assert L.vg_raster_dims(h, None, None, C.byref(nd)) == 2
+    assert L.vg_move_to(h, b"r", 1, None, -1, None, -1, None, 0.0, 0, 1, 0) == 2
+    assert L.vg_add_graph(h, a, 2, None, e, 2, None, None, 1, None, None) == 2
+    assert L.vg_read_staged_edges(h, e, None, None, None, 0, None) == 2
+    assert vh.num_agents(s, "A") == 3  # the simulation is still usable
+    s.close()

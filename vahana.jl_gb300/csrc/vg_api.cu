@@ -452,13 +452,13 @@ int vg_write_agents(vg_sim *h, int nr, const void *const *fields, uint64_t n) {
 
 int vg_sim_num_transitions(vg_sim *h, int64_t *out) {
   API_BEGIN
-  *out = S(h).num_transitions;
+  *need(out, "output pointer") = S(h).num_transitions;
   API_END
 }
 
 int vg_sim_device_bytes(vg_sim *h, uint64_t *out) {
   API_BEGIN
-  *out = S(h).footprint;
+  *need(out, "output pointer") = S(h).footprint;
   API_END
 }
 
@@ -581,7 +581,8 @@ int vg_push_global(vg_sim *h, const char *name, double v) {
 int vg_global_series(vg_sim *h, const char *name, double *out, uint64_t cap,
                      uint64_t *n_out) {
   API_BEGIN
-  auto &v = S(h).global_series[name];
+  need(n_out, "count pointer");
+  auto &v = S(h).global_series[need(name, "name")];
   *n_out = v.size();
   if (out) std::memcpy(out, v.data(), std::min<uint64_t>(cap, v.size()) * 8);
   API_END
@@ -695,6 +696,7 @@ int vg_agentstate(vg_sim *h, uint64_t id, int nr, void *const *out) {
 
 int vg_agent_slots(vg_sim *h, int nr, uint64_t *out) {
   API_BEGIN
+  need(out, "output pointer");
   Sim &s = S(h);
   s.model->at(nr);
   AgentStore &a = s.agents[nr - 1];
@@ -714,6 +716,7 @@ static std::vector<uint8_t> read_died(Sim &s, int nr) {
 
 int vg_num_agents(vg_sim *h, int nr, uint64_t *out) {
   API_BEGIN
+  need(out, "output pointer");
   Sim &s = S(h);
   s.model->at(nr);
   AgentStore &a = s.agents[nr - 1];
@@ -731,6 +734,7 @@ int vg_num_agents(vg_sim *h, int nr, uint64_t *out) {
 int vg_read_agents(vg_sim *h, int nr, void *const *fields_out, uint8_t *died_out,
                    uint64_t cap, uint64_t *n_out) {
   API_BEGIN
+  need(n_out, "count pointer");
   Sim &s = S(h);
   const AgentTypeDesc &ad = s.model->at(nr);
   AgentStore &a = s.agents[nr - 1];
@@ -921,6 +925,7 @@ extern "C" {
 int vg_add_edges(vg_sim *h, int e, uint64_t n, const uint64_t *from,
                  const uint64_t *to, const void *const *payload) {
   API_BEGIN
+  if (n) need(to, "target ids");
   Sim &s = S(h);
   const EdgeTypeDesc &ed = s.model->et(e);
   if (s.initialized && !s.intransition)
@@ -944,6 +949,13 @@ int vg_add_graph(vg_sim *h, int type_nr, uint64_t nv, const void *const *fields,
   if (s.initialized)
     fail(VG_ERR_ASSERT, "add_graph! adds agents: only in the initialization phase (until "
                         "`finish_init!` is called).");
+  if (ne) {
+    need(src, "source vertices");
+    need(dst, "target vertices");
+    if (ed.stores_payload())
+      for (size_t f = 0; f < ed.fields.size(); f++)
+        if (!payload || !payload[f]) fail(VG_ERR_ARG, "null edge field values");
+  }
   for (uint64_t k = 0; k < ne; k++)
     if (src[k] < 1 || src[k] > nv || dst[k] < 1 || dst[k] > nv)
       fail(VG_ERR_ARG, "graph edge " + std::to_string(k + 1) + " names a vertex outside 1.." +
@@ -1001,6 +1013,7 @@ int vg_remove_edges(vg_sim *h, int e, uint64_t n, const uint64_t *from,
     fail(VG_ERR_ASSERT, "You can call remove_edges! only in the initialization phase (until "
                         "`finish_init!` is called) or within a transition function called "
                         "by `apply`.");
+  if (n) need(to, "target ids");
   if (from && ed.ignorefrom())
     fail(VG_ERR_ASSERT, "remove_edges! with a source agent is not defined for edgetypes "
                         "with the :IgnoreFrom hint.");
@@ -1259,6 +1272,7 @@ int vg_has_edge(vg_sim *h, uint64_t to, int e, int *out) {
 
 int vg_num_edges_total(vg_sim *h, int e, int write, uint64_t *out) {
   API_BEGIN
+  need(out, "output pointer");
   Sim &s = S(h);
   const EdgeTypeDesc &ed = s.model->et(e);
   EdgeStore &es = s.edges[e];
@@ -1553,6 +1567,7 @@ int vg_move_to(vg_sim *h, const char *name, uint64_t id, const int64_t *pos, int
   if (ri < 0) fail(VG_ERR_ARG, std::string("unknown raster ") + name);
   const Raster &R = s.rasters[ri];
   int n = R.ndims;
+  need(pos, "position");
   auto cell = [&](const int64_t *p) { return make_id(R.type_nr, R.first_nr + lin_of(p, R.dims, n)); };
   auto add = [&](int e, uint64_t f, uint64_t t, const void *const *pl) {
     int rc = vg_add_edges(h, e, 1, &f, &t, pl);
@@ -1582,9 +1597,10 @@ int vg_cellid(vg_sim *h, const char *name, const int64_t *pos, uint64_t *out) {
   int ri = s.raster_index(name);
   if (ri < 0) fail(VG_ERR_ARG, std::string("unknown raster ") + name);
   const Raster &R = s.rasters[ri];
+  need(pos, "position");
   for (int i = 0; i < R.ndims; i++)
     if (pos[i] < 1 || pos[i] > R.dims[i]) fail(VG_ERR_ARG, "position outside the raster");
-  *out = make_id(R.type_nr, R.first_nr + lin_of(pos, R.dims, R.ndims));
+  *need(out, "output pointer") = make_id(R.type_nr, R.first_nr + lin_of(pos, R.dims, R.ndims));
   API_END
 }
 
@@ -1594,8 +1610,9 @@ int vg_raster_dims(vg_sim *h, const char *name, int64_t *dims_out, int *ndims_ou
   int ri = s.raster_index(name);
   if (ri < 0) fail(VG_ERR_ARG, std::string("unknown raster ") + name);
   const Raster &R = s.rasters[ri];
-  *ndims_out = R.ndims;
-  for (int i = 0; i < R.ndims; i++) dims_out[i] = R.dims[i];
+  *need(ndims_out, "dimension count pointer") = R.ndims;
+  if (dims_out)
+    for (int i = 0; i < R.ndims; i++) dims_out[i] = R.dims[i];
   API_END
 }
 

@@ -224,6 +224,7 @@ int vg_gen_chung_lu_edges(vg_sim *h, int e, int type_nr, uint64_t nedges, double
 int vg_read_staged_edges(vg_sim *h, int e, uint64_t *from_out, uint64_t *to_out,
                          void *const *payload_out, uint64_t cap, uint64_t *n_out) {
   API_BEGIN
+  need(n_out, "count pointer");
   Sim &s = S(h);
   const EdgeTypeDesc &ed = s.model->et(e);
   EdgeStore &es = s.edges[e];

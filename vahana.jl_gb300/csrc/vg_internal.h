@@ -45,6 +45,14 @@ struct Error {
   std::string msg;
 };
 [[noreturn]] void fail(int code, const std::string &msg);
+
+// A pointer argument a C-ABI entry cannot do without: null fails with
+// VG_ERR_ARG instead of being dereferenced.
+template <class T>
+inline T *need(T *p, const char *what) {
+  if (!p) fail(VG_ERR_ARG, std::string("null ") + what);
+  return p;
+}
 void cuda_check(cudaError_t e, const char *what);
 #define VG_CUDA(x) ::vg::cuda_check((x), #x)
 #define VG_REQUIRE(cond, msg) \
