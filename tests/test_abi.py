@@ -244,3 +244,14 @@ def test_null_and_bad_arguments_return_errors(vh):
     assert L.vg_read_staged_edges(h, e, None, None, None, 0, None) == 2
     assert vh.num_agents(s, "A") == 3  # the simulation is still usable
     s.close()
+    # serving and batch handles (checked before any device work)
+    assert L.vg_serve_create(1 << 20, 1, None) == 2
+    assert L.vg_serve_submit(None, None, None) == 2
+    assert L.vg_serve_poll(None, None, 0, C.byref(u)) == 2
+    assert L.vg_serve_job_state(None, 1, None, 0, C.byref(u)) == 2
+    assert L.vg_serve_stats(None, None, None, None, None, None, None) == 2
+    assert L.vg_serve_drain(None) == 2
+    assert L.vg_serve_destroy(None) == 0
+    assert L.vg_batch_create_sir(2, None, None, None, None, None, 10, None, None) == 2
+    assert L.vg_batch_step(None, 1, 0) == 2
+    assert L.vg_batch_destroy(None) == 0

@@ -261,6 +261,12 @@ int vg_batch_create_sir(int n, const int64_t *N, const int32_t *deg, const doubl
                         int64_t n_init_infected_per_1000, void *stream, vg_batch **out) {
   API_BEGIN
   if (n <= 0 || n > 65535) fail(VG_ERR_ARG, "batch: 1..65535 instances");
+  need(N, "instance sizes");
+  need(deg, "instance degrees");
+  need(beta, "instance infection rates");
+  need(rec, "instance recovery days");
+  need(seeds, "instance seeds");
+  need(out, "output pointer");
   auto b = std::make_unique<vg_batch>();
   b->n = n;
   b->N.assign(N, N + n);

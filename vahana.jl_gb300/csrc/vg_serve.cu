@@ -417,6 +417,7 @@ extern "C" {
 
 int vg_serve_create(uint64_t budget_bytes, int max_active, vg_server **out) {
   API_BEGIN
+  need(out, "output pointer");
   auto S = std::make_unique<vg_server>();
   S->budget = budget_bytes;
   S->max_active = max_active > 0 ? max_active : 1 << 20;
@@ -455,6 +456,7 @@ int vg_serve_create(uint64_t budget_bytes, int max_active, vg_server **out) {
 int vg_serve_submit(vg_server *S, const vg_job_spec *spec, int64_t *id_out) {
   API_BEGIN
   if (!S) fail(VG_ERR_ARG, "null server");
+  need(spec, "job spec");
   if (spec->model != 0 && spec->model != 1) fail(VG_ERR_ARG, "job model 0 (SIR) or 1 (opinion)");
   if (spec->n < 2 || spec->steps < 0) fail(VG_ERR_ARG, "job size");
   Job *J = new Job();
@@ -479,6 +481,9 @@ int vg_serve_submit(vg_server *S, const vg_job_spec *spec, int64_t *id_out) {
 // finished jobs since the last poll (at most cap); *n_out = number written
 int vg_serve_poll(vg_server *S, vg_job_result *out, uint64_t cap, uint64_t *n_out) {
   API_BEGIN
+  if (!S) fail(VG_ERR_ARG, "null server");
+  need(n_out, "count pointer");
+  if (cap) need(out, "result array");
   std::lock_guard<std::mutex> lk(S->mu);
   if (!S->error.empty()) fail(VG_ERR_DEVICE, "server stopped: " + S->error);
   uint64_t k = 0;
@@ -495,6 +500,8 @@ int vg_serve_poll(vg_server *S, vg_job_result *out, uint64_t cap, uint64_t *n_ou
 // the final state bytes of a finished job submitted with keep_state
 int vg_serve_job_state(vg_server *S, int64_t id, void *out, uint64_t cap, uint64_t *n_out) {
   API_BEGIN
+  if (!S) fail(VG_ERR_ARG, "null server");
+  need(n_out, "count pointer");
   std::lock_guard<std::mutex> lk(S->mu);
   for (Job *J : S->done)
     if (J->id == id) {
@@ -509,6 +516,7 @@ int vg_serve_job_state(vg_server *S, int64_t id, void *out, uint64_t cap, uint64
 int vg_serve_stats(vg_server *S, uint64_t *queued, uint64_t *active, uint64_t *done,
                    uint64_t *ticks, uint64_t *sim_steps, uint64_t *bytes_in_use) {
   API_BEGIN
+  if (!S) fail(VG_ERR_ARG, "null server");
   std::lock_guard<std::mutex> lk(S->mu);
   if (queued) *queued = S->queue.size();
   if (active) *active = S->active.size();
@@ -538,6 +546,7 @@ static void stop_threads(vg_server *S) {
 
 int vg_serve_drain(vg_server *S) {
   API_BEGIN
+  if (!S) fail(VG_ERR_ARG, "null server");
   stop_threads(S);
   if (!S->error.empty()) fail(VG_ERR_DEVICE, "server stopped: " + S->error);
   API_END
