@@ -255,3 +255,42 @@ def test_null_and_bad_arguments_return_errors(vh):
     assert L.vg_batch_create_sir(2, None, None, None, None, None, 10, None, None) == 2
     assert L.vg_batch_step(None, 1, 0) == 2
     assert L.vg_batch_destroy(None) == 0
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_init_phase_remove_edges_matches_sequential_removal(vh, seed):
+    """remove_edges!(sim, to, T) and remove_edges!(sim, from, to, T) in the
+    initialization phase (src/EdgeMethods.jl:527-599), many removals in one
+    call and calls interleaved with add_edge!: the staged edges equal those
+    left by removing one key at a time from the insertion-ordered list."""
+    rng = np.random.default_rng(seed)
+    m = (vh.ModelTypes().register_agenttype("A", [("foo", "i64")])
+         .register_edgetype("D", [("w", "i64")]).create_model("rm"))
+    sim = vh.create_simulation(m)
+    ids = [int(x) for x in vh.add_agents(sim, "A", 40, foo=np.arange(40))]
+    ref = []  # (from, to, w) in insertion order
+    w = 0
+    for _ in range(6):
+        k = int(rng.integers(50, 200))
+        frm = [ids[i] for i in rng.integers(0, 40, k)]
+        to = [ids[i] for i in rng.integers(0, 40, k)]
+        ws = np.arange(w, w + k)
+        w += k
+        vh.add_edges(sim, "D", frm, to, w=ws)
+        ref += list(zip(frm, to, ws.tolist()))
+        r = int(rng.integers(1, 15))
+        rto = [ids[i] for i in rng.integers(0, 40, r)]
+        if rng.integers(0, 2):
+            rfrom = [ids[i] for i in rng.integers(0, 40, r)]
+            vh.remove_edges(sim, rto, "D", frm=rfrom)
+            for a, b in zip(rfrom, rto):
+                ref = [x for x in ref if not (x[1] == b and x[0] == a)]
+        else:
+            vh.remove_edges(sim, rto, "D")
+            for b in rto:
+                ref = [x for x in ref if x[1] != b]
+    from vahana_gb300 import models
+    frm, to, pl = models.staged_edges(sim, "D")
+    assert list(zip(frm.tolist(), to.tolist(), pl["w"].tolist())) == ref
+    assert vh.num_edges(sim, "D", write=True) == len(ref)
+    sim.close()

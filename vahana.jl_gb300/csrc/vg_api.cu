@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstring>
 #include <numeric>
+#include <unordered_set>
 
 #include "vg_internal.h"
 
@@ -1022,12 +1023,29 @@ int vg_remove_edges(vg_sim *h, int e, uint64_t n, const uint64_t *from,
     EdgeStore &es = s.edges[e];
     for (auto &sg : es.staged)
       if (sg.device) fail(VG_ERR_STATE, "remove_edges! on device-staged edges before finish_init!");
+    // One filtering pass for all n removals: dropping the edges that match
+    // any of the keys equals dropping them key by key, and keeps the
+    // insertion order of the rest.
+    struct PairHash {
+      size_t operator()(const std::pair<uint64_t, uint64_t> &p) const {
+        return std::hash<uint64_t>()(p.first * 0x9e3779b97f4a7c15ull ^ p.second);
+      }
+    };
+    std::unordered_set<uint64_t> drop_to;
+    std::unordered_set<std::pair<uint64_t, uint64_t>, PairHash> drop_pair;
     for (uint64_t i = 0; i < n; i++) {
+      if (from)
+        drop_pair.insert({to[i], from[i]});
+      else
+        drop_to.insert(to[i]);
+    }
+    if (n) {
       for (auto &sg : es.staged) {
         EdgeSegment ns;
         ns.h_payload.resize(sg.h_payload.size());
         for (uint64_t j = 0; j < sg.n; j++) {
-          bool drop = sg.h_to[j] == to[i] && (!from || sg.h_from[j] == from[i]);
+          bool drop = from ? drop_pair.count({sg.h_to[j], sg.h_from[j]}) != 0
+                           : drop_to.count(sg.h_to[j]) != 0;
           if (drop) continue;
           ns.h_from.push_back(sg.h_from[j]);
           ns.h_to.push_back(sg.h_to[j]);
