@@ -242,6 +242,22 @@ def test_null_and_bad_arguments_return_errors(vh):
     assert L.vg_move_to(h, b"r", 1, None, -1, None, -1, None, 0.0, 0, 1, 0) == 2
     assert L.vg_add_graph(h, a, 2, None, e, 2, None, None, 1, None, None) == 2
     assert L.vg_read_staged_edges(h, e, None, None, None, 0, None) == 2
+    # :SingleEdge duplicate check against a staged edge, payload omitted
+    mse = (vh.ModelTypes().register_agenttype("A", [("foo", "i64")])
+           .register_edgetype("SE", [("foo", "i64")], ":SingleEdge").create_model("se"))
+    s2 = vh.create_simulation(mse)
+    x = [int(i) for i in vh.add_agents(s2, "A", 2, foo=[1, 2])]
+    one = np.array([x[0]], dtype=np.uint64)
+    two = np.array([x[1]], dtype=np.uint64)
+    P64 = C.POINTER(C.c_uint64)
+    se = mse["SE"].index
+    assert L.vg_add_edges(s2._h, se, 1, one.ctypes.data_as(P64), two.ctypes.data_as(P64), None) == 0
+    assert L.vg_add_edges(s2._h, se, 1, one.ctypes.data_as(P64), two.ctypes.data_as(P64), None) == 0
+    vh.add_edge(s2, x[0], x[1], "SE", foo=0)  # identical (zero) value: allowed
+    with pytest.raises(AssertionError):
+        vh.add_edge(s2, x[0], x[1], "SE", foo=3)
+    assert vh.num_edges(s2, "SE", write=True) == 1
+    s2.close()
     assert vh.num_agents(s, "A") == 3  # the simulation is still usable
     s.close()
     # serving and batch handles (checked before any device work)

@@ -844,9 +844,13 @@ static void stage_host_edges(Sim &s, int e, uint64_t n, const uint64_t *from,
               if (ed.stores_src() && sg.h_from[j] != (from ? from[i] : 0)) same = false;
               for (size_t f = 0; f < sg.h_payload.size(); f++) {
                 size_t sz = ed.fields[f].size;
-                if (std::memcmp(sg.h_payload[f].data() + j * sz,
-                                (const uint8_t *)payload[f] + i * sz, sz))
-                  same = false;
+                const uint8_t *old_v = sg.h_payload[f].data() + j * sz;
+                if (payload && payload[f]) {
+                  if (std::memcmp(old_v, (const uint8_t *)payload[f] + i * sz, sz)) same = false;
+                } else {  // a missing payload is staged as zeros
+                  for (size_t b = 0; b < sz; b++)
+                    if (old_v[b]) same = false;
+                }
               }
             }
             break;
