@@ -50,3 +50,23 @@ def test_single_process_needs_no_group():
     import bench
     assert bench.max_over_ranks(3.0) == 3.0
     assert bench.job_throughput(1, 10.0, 2.0) == 5.0
+
+
+def test_traffic_summary_matches_the_profile():
+    """roofline.traffic is the committed one-pass ncu capture of the gather
+    kernel: the mean of its launches' DRAM read + write bytes, above the
+    algorithmic 12 E + 20 N + 4 bytes (opinion gathers that miss L2) and
+    below the element-touch 20 E + 20 N plus a second read of the 12 E
+    bytes of the edge stream."""
+    import json
+    import bench
+    d = json.load(open(os.path.join(os.path.dirname(bench.__file__), "profiles",
+                                    "k_opinion_traffic.json")))
+    t = bench.traffic_per_launch()
+    per = [r + w for r, w in zip(d["dram_bytes_read_per_launch"],
+                                 d["dram_bytes_write_per_launch"])]
+    assert t == d["bytes_per_launch_full_size"]
+    assert abs(t - sum(per) / len(per)) <= 1
+    E, N = 200_000_000, 10_000_000
+    assert d["algorithmic_bytes_per_launch"] == 12 * E + 20 * N + 4
+    assert 12 * E + 20 * N + 4 < t < 20 * E + 20 * N + 12 * E
