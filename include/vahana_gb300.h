@@ -354,6 +354,12 @@ int vg_selftest_sort(uint64_t n, int key_bits, int wide, int const_lo, int const
  * items.  The scan builds row pointers and compaction positions. */
 int vg_selftest_scan(uint64_t n, int wide, int in_place, uint64_t seed, uint64_t *mismatch_out);
 
+/* Failure detection without a GPU fault: a look-back scan whose first tile
+ * never publishes.  Its successor's bounded wait gives up, records 0x5e02 in
+ * the status word and the kernel ends; *status_out = that word, *ms_out =
+ * the kernel's duration.  The context stays usable afterwards. */
+int vg_selftest_scan_timeout(int *status_out, double *ms_out);
+
 /* ---- allocation-free SIR step ---------------------------------------------
  * No counterpart in the reference.  One step of the "sir" transition on
  * device buffers the caller owns, for callers that cannot let a library

@@ -56,3 +56,19 @@ def test_scan_matches_host_prefix_sum(vh, n, wide, in_place):
     bad = C.c_uint64(99)
     check(lib().vg_selftest_scan(n, wide, in_place, 4321 + n, C.byref(bad)))
     assert bad.value == 0
+
+
+def test_lookback_wait_gives_up_with_a_status(vh):
+    """Failure detection without a GPU fault: a look-back scan whose first
+    tile never publishes ends with status 0x5e02 instead of waiting forever
+    (the bounded wait of every chained scan and sort pass), and the context
+    stays usable for the next scan."""
+    from vahana_gb300._lib import check, lib
+    status = C.c_int(0)
+    ms = C.c_double(-1.0)
+    check(lib().vg_selftest_scan_timeout(C.byref(status), C.byref(ms)))
+    assert status.value == 0x5e02
+    assert 0.0 < ms.value < 120_000.0
+    bad = C.c_uint64(99)
+    check(lib().vg_selftest_scan(3_000_001, 0, 0, 77, C.byref(bad)))
+    assert bad.value == 0

@@ -637,6 +637,67 @@ extern "C" int vg_selftest_sort(uint64_t n, int key_bits, int wide, int const_lo
 // Exclusive scan of n generated values (32-bit, or 64-bit when wide != 0)
 // on the device, in place or out of place, against a host prefix sum
 // (wrapping arithmetic on both sides); *mismatch_out = mismatching items.
+// Failure detection without a GPU fault: a three-tile look-back scan is
+// launched with two blocks and its tile counter starting at 1, so tile 0
+// never runs and never publishes.  Tile 1 (and possibly tile 2) waits for
+// it until the spin limit, records SCAN_ERR_LOOKBACK in the status word and
+// finishes; every index stays inside the three tiles' buffers.  Reports the
+// status word and the kernel's duration.
+extern "C" int vg_selftest_scan_timeout(int *status_out, double *ms_out) {
+  using namespace vg;
+  try {
+    need(status_out, "status pointer");
+    const uint64_t nt = 3, n = nt * SCAN_CHUNK;
+    uint32_t *din = nullptr, *dout = nullptr;
+    int *derr = nullptr;
+    char *buf = nullptr;
+    const uint64_t bytes = scan_scratch_bytes<uint32_t>(n);
+    VG_CUDA(cudaMalloc(&din, n * 4));
+    VG_CUDA(cudaMalloc(&dout, n * 4));
+    VG_CUDA(cudaMalloc(&derr, 4));
+    VG_CUDA(cudaMalloc(&buf, bytes));
+    VG_CUDA(cudaMemset(din, 0, n * 4));
+    VG_CUDA(cudaMemset(dout, 0, n * 4));
+    VG_CUDA(cudaMemset(derr, 0, 4));
+    VG_CUDA(cudaMemset(buf, 0, bytes));
+    const uint32_t first_ticket = 1;
+    VG_CUDA(cudaMemcpy(buf, &first_ticket, 4, cudaMemcpyHostToDevice));
+    ScanState<uint32_t> S;
+    S.ticket = (uint32_t *)buf;
+    S.flag = (uint32_t *)(buf + 64);
+    const uint64_t aoff = (64 + nt * 4 + 15) & ~15ull;
+    S.agg = (uint32_t *)(buf + aoff);
+    S.pre = S.agg + nt;
+    cudaStream_t st;
+    cudaEvent_t e0, e1;
+    VG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    VG_CUDA(cudaEventCreate(&e0));
+    VG_CUDA(cudaEventCreate(&e1));
+    VG_CUDA(cudaEventRecord(e0, st));
+    scan_lookback<uint32_t><<<(unsigned)(nt - 1), SCAN_TPB, 0, st>>>(din, dout, n, S, derr);
+    VG_CUDA(cudaGetLastError());
+    VG_CUDA(cudaEventRecord(e1, st));
+    VG_CUDA(cudaStreamSynchronize(st));
+    float ms = 0.f;
+    VG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    int herr = 0;
+    VG_CUDA(cudaMemcpy(&herr, derr, 4, cudaMemcpyDeviceToHost));
+    VG_CUDA(cudaEventDestroy(e0));
+    VG_CUDA(cudaEventDestroy(e1));
+    VG_CUDA(cudaStreamDestroy(st));
+    VG_CUDA(cudaFree(din));
+    VG_CUDA(cudaFree(dout));
+    VG_CUDA(cudaFree(derr));
+    VG_CUDA(cudaFree(buf));
+    *status_out = herr;
+    if (ms_out) *ms_out = ms;
+    return VG_OK;
+  } catch (const Error &e) {
+    set_last_error(e.msg);
+    return e.code;
+  }
+}
+
 extern "C" int vg_selftest_scan(uint64_t n, int wide, int in_place, uint64_t seed,
                                 uint64_t *mismatch_out) {
   using namespace vg;
