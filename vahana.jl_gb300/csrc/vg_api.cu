@@ -1123,7 +1123,7 @@ struct HostRow {
   uint64_t count = 0;
 };
 
-void stencil_sources(const Sim &s, const StencilDesc &st, uint64_t cell,
+void stencil_sources(const Sim &, const StencilDesc &st, uint64_t cell,
                      std::vector<uint64_t> &out_lin);
 
 HostRow host_row(Sim &s, int e, uint64_t to, bool want_data) {
@@ -1449,7 +1449,7 @@ static uint64_t lin_of(const int64_t *pos, const int64_t *dims, int n) {
 // in insertion order: connect_raster_neighbors! iterates the source cells
 // in column-major order and, for each, the stencil offsets in order.  The
 // sources of one target are therefore ordered by (source index, offset).
-void stencil_sources(const Sim &s, const StencilDesc &st, uint64_t cell,
+void stencil_sources(const Sim &, const StencilDesc &st, uint64_t cell,
                      std::vector<uint64_t> &out) {
   out.clear();
   int n = st.ndims;

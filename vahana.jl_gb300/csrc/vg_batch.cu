@@ -169,7 +169,7 @@ BatchArgs batch_args(vg_batch *b, int cur, uint32_t step, const int64_t *step_ba
   return a;
 }
 
-void launch_step(vg_batch *b, const BatchArgs &a, int tpb, int apt, cudaStream_t st) {
+void launch_step(vg_batch *, const BatchArgs &a, int tpb, int apt, cudaStream_t st) {
   uint64_t threads = (a.n + apt - 1) / apt;
   unsigned g = blocks(threads, tpb);
   switch (apt) {
