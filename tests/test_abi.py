@@ -310,3 +310,24 @@ def test_init_phase_remove_edges_matches_sequential_removal(vh, seed):
     assert list(zip(frm.tolist(), to.tolist(), pl["w"].tolist())) == ref
     assert vh.num_edges(sim, "D", write=True) == len(ref)
     sim.close()
+
+
+def test_transition_registry_lists_every_named_kernel(vh):
+    """apply! binds a transition by name (the reference passes a Julia
+    callable, src/Simulation.jl:720-726): the registry names the three test
+    models' rules and the generic rules the ported tests use, each once.
+    Before finish_init! apply! is refused with the reference's message
+    whatever the name (src/Simulation.jl:727)."""
+    names = vh.transition_names()
+    for n in ("bounded_confidence", "sir", "life", "random_walk", "neighbor_sum",
+              "neighbor_or", "count_edges", "die_if", "set_field", "keep", "self_edge",
+              "readd_edges", "spawn", "link_neighbors", "remove_edges"):
+        assert n in names
+    assert len(set(names)) == len(names)
+    m = vh.ModelTypes().register_agenttype("A", [("foo", "i64")]).create_model("names")
+    sim = vh.create_simulation(m)
+    vh.add_agents(sim, "A", 2, foo=[1, 2])
+    for rule in ("no_such_rule", "keep"):
+        with pytest.raises(AssertionError, match="finish_init"):
+            vh.apply_(sim, rule, "A", ["A"], ["A"])
+    sim.close()
