@@ -1,11 +1,11 @@
 #!/usr/bin/env python
 """Benchmark of the GB300 transition step (apply! of Vahana.jl).
 
-Workload: bounded-confidence opinion dynamics, Opinion{x::Float64} with
-N = 10^7 agents on a directed Chung-Lu graph (exponent 2.5, mean in-degree
-20, expected degree capped at 10^4, E = 2*10^8 edges with Float64 weights),
-all inputs synthetic and seeded (Philox4x32-10).  One bench step is one
-apply!(sim, bounded_confidence, Opinion, [Opinion, Weight], Opinion).
+Headline workload: bounded-confidence opinion dynamics, Opinion{x::Float64}
+with N = 10^7 agents on a directed Chung-Lu graph (exponent 2.5, mean
+in-degree 20, expected degree capped at 10^4, E = 2*10^8 edges with Float64
+weights), all inputs synthetic and seeded (Philox4x32-10).  One bench step is
+one apply!(sim, bounded_confidence, Opinion, [Opinion, Weight], Opinion).
 
   value  edge-updates/s with the state resident in HBM (CUDA events on the
          simulation's stream around K steps; inputs are larger than L2).
@@ -16,11 +16,20 @@ apply!(sim, bounded_confidence, Opinion, [Opinion, Weight], Opinion).
          12 E + 20 N + 4 (4 B source index + 8 B weight per edge, row
          pointers, opinion read and write), over its CUDA-event duration,
          against the measured HBM copy bandwidth.
-  cpu_baseline  the oracle's C restatement of the same step (OpenMP over
-         all host cores) on the same graph.
+  parity the model's 50 steps from the initial state on the GPU against the
+         oracle's C restatement on the same graph: rows up to the hub
+         threshold bit-exact after one step, every row within 1e-12 relative
+         after 50 steps, and the ordered path (no hub split) bit-exact after
+         50 steps.
+  cpu_baseline  the oracle's 50 steps of that comparison (OpenMP over all
+         host cores), timed.
+  secondary  the other workloads, each in its own process, each with its own
+         parity check: SIR (N = 10^5, 100 steps), Life B3/S23 on 4096^2 cells
+         with 10^6 walkers (1000 steps), the batched ensemble of 512 SIR
+         instances and the serving stream (1024 jobs at 10 and 1000 jobs/s).
 
 --impl reference times that CPU restatement alone on this workload (the
-reference itself is Julia and cannot run here).
+reference itself is Julia, which neither machine has).
 Multi-GPU: replicas only (one independent simulation per rank).
 """
 import argparse
@@ -56,7 +65,12 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="opinion",
-                    choices=["opinion", "batch", "serve", "sir", "life"])
+                    choices=["opinion", "batch", "serve", "sir", "life", "fp64"])
+    ap.add_argument("--secondary", default="sir,life,batch,serve",
+                    help="opinion workload: the other workloads run afterwards, each in "
+                         "its own process (empty: none)")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="opinion workload: skip the 50-step oracle comparison")
     ap.add_argument("--jobs", type=int, default=512)
     ap.add_argument("--rates", default="100,1000")
     ap.add_argument("--serve-budget-gb", type=float, default=64.0)
@@ -177,11 +191,87 @@ def job_throughput(world_size, units_per_rank, seconds):
 
 
 # ------------------------------------------------------------- CPU legs
-def cpu_graph_from_device(vh, run):
-    """CSR of the built graph (row_ptr, src, w) read back for the CPU step."""
-    rp, frm, pl = vh.read_edges(run.sim, "Weight", "Opinion")
-    src = ((frm & ((1 << 36) - 1)) - 1).astype("uint32")
-    return rp.astype("uint64"), src, pl["w"].astype("float64")
+NO_SPLIT = 4294967295  # hub threshold that keeps every row on the ordered path
+PARITY_STEPS = 50       # the model's step count for the opinion workload
+PARITY_RTOL = 1e-12     # stated tolerance where hub rows regroup their sums
+
+
+def oracle_graph(vh, models, run):
+    """The oracle's own per-target containers, built from the edge records
+    staged before finish_init! (in add_edge! call order): (row_ptr, src, w)
+    with w in container order."""
+    from oracle import models as om
+    frm, to, pl = models.staged_edges(run.sim, "Weight")
+    g = om.build_inedges(run.n, frm, to)
+    del frm, to
+    w_in = np.ascontiguousarray(pl["w"][g[2]])
+    return g[0], g[1], w_in
+
+
+def max_rel_err(got, ref):
+    """Largest |got - ref| / |ref| over the entries whose bits differ."""
+    diff = got.view(np.uint64) != ref.view(np.uint64)
+    if not diff.any():
+        return 0.0
+    g, r = got[diff], ref[diff]
+    with np.errstate(divide="ignore", invalid="ignore"):
+        rel = np.abs(g - r) / np.abs(r)
+    rel[~np.isfinite(rel)] = np.inf
+    return float(rel.max())
+
+
+def opinion_parity(vh, run, g, x_init, hub_thr, steps=PARITY_STEPS):
+    """The model's `steps` steps from the initial state on the GPU, once with
+    the hub split at hub_thr (the timed configuration) and once on the
+    ordered path, against the oracle's C restatement on its own containers
+    of the same edges.  Returns (parity record, oracle steps, oracle seconds,
+    oracle threads)."""
+    from oracle import models as om
+    rp, src, w = g
+    threads = om.threads()
+    x = x_init.copy()
+    t0 = time.perf_counter()
+    for k in range(steps):
+        x = om.opinion_step((rp, src, None), w, x, 0.3, 0.5, 0.5, nthreads=threads)
+        if k == 0:
+            ref1 = x.copy()
+    t_cpu = time.perf_counter() - t0
+    ref = x
+    m = run.model
+
+    def gpu_steps(thr, k):
+        for _ in range(k):
+            vh.apply_(run.sim, "bounded_confidence", ["Opinion"], ["Opinion", "Weight"],
+                      ["Opinion"], params=[m["Weight"].index, 0.3, 0.5, 0.5, thr])
+        vh.synchronize(run.sim)
+        return vh.read_agents(run.sim, "Opinion")[0]["x"].copy()
+
+    vh.write_agents(run.sim, "Opinion", x=x_init)
+    g1 = gpu_steps(hub_thr, 1)
+    gk = gpu_steps(hub_thr, steps - 1)
+    vh.write_agents(run.sim, "Opinion", x=x_init)
+    ok = gpu_steps(NO_SPLIT, steps)
+    deg = np.diff(rp.astype(np.int64))
+    hub = deg > hub_thr
+    b = lambda a: a.view(np.uint64)
+    low_exact = int((b(g1)[~hub] == b(ref1)[~hub]).sum())
+    split = {"hub_threshold": int(hub_thr), "hub_rows": int(hub.sum()),
+             "step1_rows_at_or_below_threshold": int((~hub).sum()),
+             "step1_rows_at_or_below_threshold_bit_exact": low_exact,
+             "step1_hub_rows_max_rel_err": max_rel_err(g1[hub], ref1[hub]),
+             "final_rows_bit_exact": int((b(gk) == b(ref)).sum()),
+             "final_max_rel_err": max_rel_err(gk, ref)}
+    ordered = {"final_rows_bit_exact": int((b(ok) == b(ref)).sum()),
+               "final_max_rel_err": max_rel_err(ok, ref)}
+    n = int(x_init.size)
+    passed = (low_exact == split["step1_rows_at_or_below_threshold"]
+              and split["step1_hub_rows_max_rel_err"] <= PARITY_RTOL
+              and split["final_max_rel_err"] <= PARITY_RTOL
+              and ordered["final_rows_bit_exact"] == n)
+    rec = {"steps": steps, "rows": n, "from": "initial state", "rtol": PARITY_RTOL,
+           "oracle": "oracle/models.c on containers built from the staged edge records",
+           "split": split, "ordered": ordered, "pass": bool(passed)}
+    return rec, steps, t_cpu, threads
 
 
 def cpu_graph_host(args):
@@ -264,6 +354,9 @@ def run_ours(args):
     run = models.build_opinion(n=args.n, mean_degree=args.mean_degree, wmax=args.wmax,
                                seed=args.seed, stream=stream.cuda_stream,
                                hub_threshold=args.hub_threshold)
+    check_parity = rank == 0 and ws == 1 and not args.no_parity
+    x_init = vh.read_agents(run.sim, "Opinion")[0]["x"].copy()
+    g_oracle = oracle_graph(vh, models, run) if check_parity else None
     vh.finish_init(run.sim)
     vh.set_async(run.sim, True)
     E, N = run.nedges, run.n
@@ -348,28 +441,65 @@ def run_ours(args):
            "data": "synthetic", "config": config(args), "e2e": e2e, "roofline": roof,
            "clocks": clocks, "gpu_launches": K}
 
-    # ---- CPU baseline (rank 0, N = 1 only)
-    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        g = cpu_graph_from_device(vh, run)
-        x0 = vh.read_agents(run.sim, "Opinion")[0]["x"].copy()
-        steps, el, threads = time_cpu(g, x0, args.cpu_seconds)
-        cv = E * steps / el
-        out["cpu_baseline"] = {"value": cv, "unit": "edge-updates/s", "cores": threads,
-                               "kind": "port",
-                               "sample": "%d full steps (%.1f s) of the oracle's C restatement "
-                                         "on the same graph" % (steps, el)}
+    # ---- parity at the model's size and step count, and the CPU baseline
+    # (rank 0, N = 1 only): the oracle's 50 steps of the comparison, timed
+    if check_parity:
+        par, steps, el, threads = opinion_parity(vh, run, g_oracle, x_init, args.hub_threshold)
+        out["parity"] = par
+        if not args.no_cpu_baseline:
+            out["cpu_baseline"] = {
+                "value": E * steps / el, "unit": "edge-updates/s", "cores": threads,
+                "kind": "port",
+                "sample": "%d full steps (%.1f s) of the oracle's C restatement on the same "
+                          "edges (the parity comparison's oracle run)" % (steps, el)}
+        del g_oracle
     run.close()
+    if rank == 0 and ws == 1 and args.secondary:
+        out["secondary"] = run_secondaries(args)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
 
 
+def run_secondaries(args):
+    """The other workloads, one process each (a failure of one leaves the
+    headline line intact); each returns its own JSON line."""
+    res = {}
+    for name in [s.strip() for s in args.secondary.split(",") if s.strip()]:
+        cmd = [sys.executable, os.path.abspath(__file__), "--workload", name, "--warmup", "3",
+               "--seed", str(args.seed), "--cpu-seconds", str(args.cpu_seconds)]
+        if name == "serve":
+            cmd += ["--jobs", "1024", "--rates", "10,1000"]
+        t0 = time.perf_counter()
+        try:
+            r = subprocess.run(cmd, capture_output=True, text=True, timeout=900)
+            line = None
+            for ln in reversed(r.stdout.splitlines()):
+                if ln.strip().startswith("{"):
+                    try:
+                        line = json.loads(ln)
+                        break
+                    except ValueError:
+                        pass
+            if r.returncode != 0 or line is None:
+                line = {"error": "rc %d: %s" % (r.returncode, (r.stderr or r.stdout)[-800:])}
+        except subprocess.TimeoutExpired:
+            line = {"error": "did not finish within 900 s"}
+        line["wall_s"] = round(time.perf_counter() - t0, 1)
+        res[name] = line
+    return res
+
+
 def run_batch(args):
     """Batched ensemble: 512 SIR instances (N log-uniform 1e3..1e5, out-degree
     5..30, beta 0.01..0.1, recovery 5..10, seed = instance index), 200 steps
     as one CUDA graph, against the same instances stepped one at a time with
-    the plain kernels (apply! per instance and step)."""
+    the plain kernels (apply! per instance and step).  Two batched calls of
+    `steps` steps each: the first includes the autotuner and the graph
+    capture, the second replays the captured graph (steady state); the plain
+    path steps every instance over the same 2 * steps steps, and every
+    instance's final state must be bit-identical on both paths."""
     import torch
     import vahana_gb300 as vh
     from vahana_gb300 import models
@@ -382,14 +512,17 @@ def run_batch(args):
     w.close()
     b = models.Batch(N, deg, beta, rec, seeds)
     torch.cuda.synchronize()
-    # both paths step the same fresh instances over the same steps 1..steps
     t0 = time.perf_counter()
-    b.step(steps, mode=1)  # autotune + capture + replay, all inside the timed region
+    b.step(steps, mode=1)  # autotune + capture + replay
     torch.cuda.synchronize()
-    t_batch = time.perf_counter() - t0
+    t_first = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    b.step(steps, mode=1)  # replay of the captured step loop
+    torch.cuda.synchronize()
+    t_steady = time.perf_counter() - t0
     t0 = time.perf_counter()
     for i in range(n_inst):
-        b.step_one(i, steps)
+        b.step_one(i, 2 * steps)
     torch.cuda.synchronize()
     t_plain = time.perf_counter() - t0
     bad = 0
@@ -399,17 +532,22 @@ def run_batch(args):
         bad += int(not (np.array_equal(sb, sp) and np.array_equal(db, dp)))
     info = b.info()
     b.close()
-    v = n_inst * steps / t_batch
+    plain_rate = n_inst * 2 * steps / t_plain
+    v = n_inst * steps / t_steady
     out = {"metric": "sim-steps/s", "value": v, "unit": "instance-steps/s", "n_gpus": 1,
-           "steps": steps, "warmup": 1, "ms_per_step": 1e3 * t_batch / steps,
+           "steps": steps, "warmup": 1, "ms_per_step": 1e3 * t_steady / steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/i32",
            "data": "synthetic",
            "config": {"workload": "batched_sir_ensemble", "instances": n_inst,
                       "agents": info["agents"], "edges": info["edges"],
                       "launch": {"tpb": info["tpb"], "agents_per_thread": info["apt"]}},
-           "plain_one_at_a_time": n_inst * steps / t_plain,
-           "speedup_vs_plain": t_plain / t_batch,
-           "instances_differing_batched_vs_alone": bad}
+           "first_call": {"value": n_inst * steps / t_first, "seconds": t_first,
+                          "includes": "autotuner, graph capture, replay"},
+           "plain_one_at_a_time": plain_rate,
+           "speedup_vs_plain": v / plain_rate,
+           "speedup_vs_plain_first_call": n_inst * steps / t_first / plain_rate,
+           "parity": {"instances": n_inst, "steps": 2 * steps,
+                      "instances_differing_batched_vs_alone": bad, "pass": bad == 0}}
     print(json.dumps(out), flush=True)
 
 
@@ -525,7 +663,10 @@ def run_serve(args):
            "per_rate": per_rate,
            "plain_one_by_one": {"sim_steps_per_s": plain_rate, "sample_jobs": len(sample)},
            "speedup_vs_plain": best["sim_steps_per_s"] / plain_rate,
-           "sample_jobs_differing_served_vs_alone": mismatched}
+           "sample_jobs_differing_served_vs_alone": mismatched,
+           "parity": {"sample_jobs": len(sample), "rates": len(per_rate),
+                      "served_results_differing_from_alone": mismatched,
+                      "pass": mismatched == 0}}
     print(json.dumps(out), flush=True)
 
 
@@ -561,7 +702,10 @@ def run_model(args):
     B3/S23 on a 4096 x 4096 periodic raster with 10^6 random walkers whose
     walker -> cell edges are rebuilt every step, 1000 steps): the same
     metric, edge-updates/s, for these parity workloads (the per-agent loop
-    of apply! on each), with the oracle's C restatement timed beside."""
+    of apply! on each).  The oracle's C restatement runs every step the GPU
+    ran, from the same initial state, and the final states (and, for Life,
+    the rebuilt walker -> cell containers) must be bit-identical; that run,
+    timed, is the CPU baseline."""
     import torch
     import vahana_gb300 as vh
     from vahana_gb300 import models
@@ -569,8 +713,9 @@ def run_model(args):
     vh.build()
     stream = torch.cuda.Stream()
     peak, kind = peaks()
+    K = args.model_steps or (100 if args.workload == "sir" else 1000)
     if args.workload == "sir":
-        N, deg, steps = 100_000, 10, 100
+        N, deg = 100_000, 10
         run = models.build_sir(n=N, degree=deg, beta=0.05, recovery=7, seed=args.seed,
                                stream=stream.cuda_stream)
         frm, to, _ = models.staged_edges(run.sim, "Contact")
@@ -579,12 +724,12 @@ def run_model(args):
         E = N * deg
         alg = 4 * E + 14 * N + 4
         cfg = {"workload": "sir_uniform_out_degree", "agents": N, "edges": E,
-               "out_degree": deg, "beta": 0.05, "recovery": 7, "model_steps_reference": steps,
+               "out_degree": deg, "beta": 0.05, "recovery": 7, "model_steps_reference": 100,
                "l2": "L2-resident (5.4 MB per step): latency bound"}
         kern = "k_sir"
     else:
         W = H = 4096
-        nw, steps = 1_000_000, 1000
+        nw = 1_000_000
         run = models.build_life(W, H, nw, 0.3, args.seed, stream=stream.cuda_stream)
         a0 = vh.read_agents(run.sim, "Cell")[0]["alive"].copy()
         wc = vh.read_agents(run.sim, "Walker")[0]
@@ -592,7 +737,7 @@ def run_model(args):
         E = 8 * W * H + nw
         alg = 2 * W * H + 16 * nw + 4 * (W * H + 1) + 4 * nw
         cfg = {"workload": "life_b3s23_raster_walkers", "raster": [W, H], "cells": W * H,
-               "walkers": nw, "edges_per_step": E, "model_steps_reference": steps,
+               "walkers": nw, "edges_per_step": E, "model_steps_reference": 1000,
                "l2": "inputs larger than L2 (121 MB per step)"}
         kern = "k_life2d + k_random_walk + walker edge rebuild"
     vh.finish_init(run.sim)
@@ -600,9 +745,9 @@ def run_model(args):
     for _ in range(args.warmup):
         run.step()
     vh.synchronize(run.sim)
-    K = args.model_steps or steps
     total_ms, per, clocks = _timed_steps(run.step, stream, K, Clocks(0))
     vh.synchronize(run.sim)
+    done = args.warmup + K + len(per)  # model steps the GPU ran from the initial state
     mean_ms = total_ms / K
     out = {"metric": METRIC, "value": E * K / (total_ms * 1e-3), "unit": "edge-updates/s",
            "n_gpus": 1, "steps": K, "warmup": args.warmup, "ms_per_step": total_ms / K,
@@ -614,32 +759,93 @@ def run_model(args):
                         "peak_kind": kind, "traffic": None, "algorithmic_bytes_per_step": alg,
                         "kernel": kern, "step_ms_mean": mean_ms,
                         "single_step_ms_median": per[len(per) // 2]},
-           "clocks": clocks}
-    if not args.no_cpu_baseline:
-        t0 = time.perf_counter()
-        done = 0
-        if args.workload == "sir":
-            g = om.build_inedges(N, frm, to)
-            s_, d_ = st0, d0
-            while done < K and time.perf_counter() - t0 < args.cpu_seconds:
-                s_, d_ = om.sir_step(g, s_, d_, 0.05, 7, args.seed, 1 + done)
-                done += 1
-        else:
-            a_, x_, y_ = a0, x0, y0
-            while done < K and time.perf_counter() - t0 < args.cpu_seconds:
-                a_ = om.life_step(a_, W, H)
-                x_, y_, _ = om.walk_step(x_, y_, W, H, args.seed, 2 + 2 * done)
-                done += 1
+           "clocks": clocks, "gpu_launches_per_step": 1 if args.workload == "sir" else None}
+    # oracle over the same `done` steps from the initial state (timed: the CPU baseline)
+    t0 = time.perf_counter()
+    if args.workload == "sir":
+        s_ref, d_ref = om.run_sir(N, frm, to, st0, d0, 0.05, 7, args.seed, done, first_step=1)
         el = time.perf_counter() - t0
+        cols = vh.read_agents(run.sim, "Person")[0]
+        same = {"state": int((cols["state"] == s_ref).sum()),
+                "days": int((cols["days"] == d_ref).sum())}
+        passed = same["state"] == N and same["days"] == N
+        out["parity"] = {"steps": done, "from": "initial state", "agents": N,
+                         "agents_equal": same, "recovered": int((s_ref == 2).sum()),
+                         "pass": bool(passed)}
+    else:
+        a_ref, x_ref, y_ref, rp_ref, src_ref = om.run_life_walkers(a0, x0, y0, W, H, args.seed,
+                                                                  done)
+        el = time.perf_counter() - t0
+        a = vh.read_agents(run.sim, "Cell")[0]["alive"].astype(np.uint8)
+        wk = vh.read_agents(run.sim, "Walker")[0]
+        rp, frm_c, _ = vh.read_edges(run.sim, "OnCell", "Cell")
+        src_c = frm_c & np.uint64((1 << 36) - 1)
+        same = {"cells": int((a == a_ref).sum()),
+                "walkers": int(((wk["x"] == x_ref) & (wk["y"] == y_ref)).sum()),
+                "oncell_row_ptr_equal": bool(np.array_equal(rp, rp_ref)),
+                "oncell_sources_equal": bool(np.array_equal(src_c, src_ref))}
+        passed = (same["cells"] == W * H and same["walkers"] == nw
+                  and same["oncell_row_ptr_equal"] and same["oncell_sources_equal"])
+        out["parity"] = {"steps": done, "from": "initial state", "cells_and_walkers_equal": same,
+                         "alive_cells": int(a_ref.sum()), "pass": bool(passed)}
+    if not args.no_cpu_baseline:
         out["cpu_baseline"] = {"value": E * done / el, "unit": "edge-updates/s",
                                "cores": om.threads(), "kind": "port",
-                               "sample": "%d steps (%.1f s) of the oracle's C restatement" % (done, el)}
+                               "sample": "%d steps (%.1f s) of the oracle's C restatement "
+                                         "(the parity run)" % (done, el)}
     run.close()
+    print(json.dumps(out), flush=True)
+
+
+def run_rates(args):
+    """Arithmetic throughput of this GPU (vg_selftest_rate): binary64 add,
+    multiply and fused multiply-add, the gather kernel's integer-pipe
+    product and a 32-bit integer multiply-add, with every lane of a warp
+    active, and the binary64 add with part of each warp's lanes active.  The
+    last figure bounds the gather kernel of the opinion workload, which
+    issues two binary64 additions per edge: 2 E / (add rate) per step."""
+    import ctypes as C
+    import torch  # noqa: F401  (CUDA context in the same process as the sampler)
+    import vahana_gb300 as vh
+    from vahana_gb300._lib import check, lib
+    vh.build()
+    names = {0: "dadd", 1: "dmul", 2: "dfma", 3: "emu_mul_grid", 4: "imad32"}
+    blocks = 152 * 8
+    ms, ops = C.c_double(), C.c_double()
+    runs = [(m, 32) for m in range(5)] + [(0, 16), (0, 8), (0, 1)]
+    clk = Clocks(0)
+    clk.start()
+    time.sleep(0.3)
+    res = []
+    for mode, lanes in runs:
+        iters = 1 << 14 if mode in (0, 1, 2) else 1 << 12
+        check(lib().vg_selftest_rate(mode, blocks, iters, lanes, C.byref(ms), C.byref(ops)))
+        res.append({"op": names[mode], "active_lanes": lanes, "ms": ms.value,
+                    "lane_ops_per_s": ops.value / (ms.value * 1e-3),
+                    "warp_instr_per_s": ops.value / lanes / (ms.value * 1e-3)})
+    clocks = clk.stop()
+    mhz = clocks.get("sm_mhz") or 2070.0
+    for r in res:
+        r["lane_ops_per_sm_per_clock"] = r["lane_ops_per_s"] / (152 * mhz * 1e6)
+    dadd = res[0]["lane_ops_per_s"]
+    E = 200_000_000
+    out = {"metric": "binary64 add/s", "value": dadd, "unit": "lane-ops/s", "n_gpus": 1,
+           "steps": len(runs), "warmup": 1, "ms_per_step": res[0]["ms"],
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic", "config": {"workload": "arithmetic_throughput",
+                                           "blocks": blocks, "threads_per_block": 256,
+                                           "chains_per_thread": 8},
+           "rates": res, "clocks": clocks,
+           "opinion_step_fp64_floor_ms": 2 * E / dadd * 1e3,
+           "opinion_step_fp64_floor_note": "two binary64 additions per edge, E = 2e8"}
     print(json.dumps(out), flush=True)
 
 
 def main():
     args = parse()
+    if args.workload == "fp64":
+        run_rates(args)
+        return
     if args.workload == "batch":
         run_batch(args)
     elif args.workload == "serve":

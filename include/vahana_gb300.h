@@ -339,6 +339,17 @@ int vg_read_staged_edges(vg_sim *s, int edge_type, uint64_t *from_out,
  * the general add, mul and div. */
 int vg_selftest_fp64(uint64_t n, uint64_t seed, uint64_t *counts_out);
 
+/* Arithmetic throughput on this GPU (no reference counterpart; it measures
+ * the pipe the gather kernels' binary64 work runs on).  One launch of
+ * `blocks` blocks of 256 threads; in each warp the first active_lanes lanes
+ * run iters rounds of 8 independent chains of one operation (mode 0
+ * binary64 add, 1 binary64 multiply, 2 binary64 fused multiply-add, 3 the
+ * gather kernels' integer-pipe product, 4 32-bit integer multiply-add), the
+ * other lanes branch around.  *ms_out = the launch's CUDA-event duration,
+ * *lane_ops_out = operations performed (lanes x rounds x 8). */
+int vg_selftest_rate(int mode, uint32_t blocks, uint32_t iters, uint32_t active_lanes,
+                     double *ms_out, double *lane_ops_out);
+
 /* Sorts n generated (key, index) pairs with the library's device radix sort
  * (32-bit keys, or 64-bit keys when wide != 0, key_bits significant bits,
  * bits [const_lo, const_hi) equal in every key) and compares keys and
@@ -370,10 +381,15 @@ int vg_selftest_scan_timeout(int *status_out, double *ms_out);
  * file-scope device array of max_in_degree + 1 <= 4096 entries; larger
  * max_in_degree is rejected with VG_ERR_ARG.  Calls share that array, so
  * calls that overlap on the GPU race and must be serialised by the caller.
- * The first call on a device looks the array's address up and caches it:
- * make it before any stream capture.  row_ptr u32[n+1] and src u32 (0-based
- * sources) form the in-edge CSR; state/days are read from the *_in buffers
- * and written to the *_out buffers; step is the transition number
+ * The first call in a CUDA context (the device's primary context, or the
+ * context the caller made current) looks the array's address up in that
+ * context and caches it under the context's id: make that call before any
+ * stream capture.  row_ptr u32[n+1] and src u32 (0-based sources) form the
+ * in-edge CSR; state/days are read from the *_in buffers and written to the
+ * *_out buffers, which must not overlap the inputs or each other (no
+ * in-place step: VG_ERR_ARG); max_in_degree may understate the largest
+ * in-degree, in which case the rows beyond the table form the product on
+ * the device (same roundings); step is the transition number
  * (num_transitions) that apply! would use; stream is a cudaStream_t. */
 int vg_sir_step_noalloc(const uint32_t *row_ptr, const uint32_t *src,
                         const uint8_t *state_in, const int32_t *days_in,

@@ -7,7 +7,10 @@ running while another framework captures a CUDA graph.  For them the
 library offers one SIR step on caller-owned buffers whose only scratch is a
 fixed file-scope device table.  This test runs two such steps in a row
 (ping-pong buffers) next to two apply! steps on the same graph and state,
-and requires bit-identical results (tolerance 0, as every SIR test).
+and requires bit-identical results (tolerance 0, as every SIR test); then
+two more with the largest in-degree understated (the rows beyond the table),
+and checks that an in-place call and a table beyond its fixed size are
+refused.
 It is collected last and runs alone or after the other tests.
 """
 import ctypes as C
@@ -54,6 +57,31 @@ def test_sir_step_noalloc_matches_apply(vh):
         np.testing.assert_array_equal(got_s, ref["state"])
         np.testing.assert_array_equal(got_d, ref["days"])
     assert (got_s == 1).sum() > 0
+    # a caller that understates the largest in-degree (1, then 0): rows with
+    # more infected neighbours than the table covers form the same product
+    # on the device; still bit-identical to apply!
+    for call, kmax in ((2, 1), (3, 0)):
+        step = vh.num_transitions(run.sim)
+        a, b = call % 2, (call + 1) % 2
+        check(lib().vg_sir_step_noalloc(
+            C.c_void_p(row_ptr.data_ptr()), C.c_void_p(src.data_ptr()),
+            C.c_void_p(st[a].data_ptr()), C.c_void_p(dy[a].data_ptr()),
+            C.c_void_p(st[b].data_ptr()), C.c_void_p(dy[b].data_ptr()),
+            C.c_uint64(n), C.c_uint32(kmax), C.c_double(beta), C.c_int32(rec),
+            C.c_uint64(seed), C.c_uint32(step), C.c_void_p(stream)))
+        run.step()
+        torch.cuda.synchronize()
+        ref, _ = vh.read_agents(run.sim, "Person")
+        np.testing.assert_array_equal(st[b].cpu().numpy().view(np.uint8), ref["state"])
+        np.testing.assert_array_equal(dy[b].cpu().numpy(), ref["days"])
+    # an in-place step (output = input) is refused, not run half-updated
+    rc = lib().vg_sir_step_noalloc(
+        C.c_void_p(row_ptr.data_ptr()), C.c_void_p(src.data_ptr()),
+        C.c_void_p(st[0].data_ptr()), C.c_void_p(dy[0].data_ptr()),
+        C.c_void_p(st[0].data_ptr()), C.c_void_p(dy[1].data_ptr()),
+        C.c_uint64(n), C.c_uint32(int(deg.max())), C.c_double(beta), C.c_int32(rec),
+        C.c_uint64(seed), C.c_uint32(1), C.c_void_p(stream))
+    assert rc != 0 and b"overlap" in lib().vg_last_error()
     # sizes beyond the fixed table are rejected with a clear error
     rc = lib().vg_sir_step_noalloc(
         C.c_void_p(row_ptr.data_ptr()), C.c_void_p(src.data_ptr()),

@@ -12,10 +12,16 @@
 // 0..max_in_degree before its step kernel reads them (stream order), so
 // nothing has to start at zero.
 //
-// Set-up: the first call on a device, with that device current, looks up
-// the array's device address (cudaGetSymbolAddress) once and caches it per
-// device; make that first call before any stream capture.
+// Set-up: the first call in a CUDA context (the device's primary context,
+// or whichever context the caller made current) looks up the array's device
+// address in that context (cudaGetSymbolAddress) once and caches it under
+// the context's unique id; a context that is destroyed and created again
+// gets a new id and a new look-up.  Make the first call in a context before
+// any stream capture.
+#include <cuda.h>
+
 #include <mutex>
+#include <unordered_map>
 
 #include "vg_internal.h"
 #include "vg_philox.cuh"
@@ -24,11 +30,10 @@ namespace vg {
 namespace {
 
 constexpr int NOALLOC_MAX_DEGREE = 4095;  // largest in-degree the table covers
-constexpr int MAX_DEVICES = 64;
 
 static __device__ __align__(256) double g_sir_ptab[NOALLOC_MAX_DEGREE + 1];
 
-double *g_ptab_addr[MAX_DEVICES] = {nullptr};
+std::unordered_map<unsigned long long, double *> g_ptab_addr;  // context id -> address
 std::mutex g_setup_mutex;
 
 // p_k = 1 - q_k with q_k = q_{k-1} * (1 - beta), k = 0..kmax, computed by
@@ -80,20 +85,61 @@ __global__ void k_sir_noalloc(const uint32_t *__restrict__ rp, const uint32_t *_
   d_wr[i] = d;
 }
 
-double *ptab_address() {
-  int dev = 0;
-  VG_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= MAX_DEVICES) fail(VG_ERR_ARG, "device ordinal out of range");
-  std::lock_guard<std::mutex> lk(g_setup_mutex);
-  if (!g_ptab_addr[dev]) {
-    void *p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_sir_ptab);
-    if (e != cudaSuccess || !p)
-      fail(VG_ERR_CUDA, std::string("cudaGetSymbolAddress of the SIR table failed: ") +
-                            cudaGetErrorString(e));
-    g_ptab_addr[dev] = (double *)p;
+// the unique id of the calling thread's current context (0 when none is
+// current yet), through the driver's entry points: the library links the
+// CUDA runtime only
+unsigned long long current_context_id() {
+  using GetCurrent = CUresult (*)(CUcontext *);
+  using GetId = CUresult (*)(CUcontext, unsigned long long *);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  if (!get_current || !get_id) {
+    void *f1 = nullptr, *f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    VG_CUDA(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault,
+                                             &q1));
+    VG_CUDA(cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2));
+    if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+      fail(VG_ERR_CUDA, "cuCtxGetCurrent / cuCtxGetId are not available from the driver");
+    get_current = (GetCurrent)f1;
+    get_id = (GetId)f2;
   }
-  return g_ptab_addr[dev];
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&ctx) != CUDA_SUCCESS || !ctx) return 0;
+  if (get_id(ctx, &id) != CUDA_SUCCESS) fail(VG_ERR_CUDA, "cuCtxGetId failed");
+  return id;
+}
+
+double *symbol_address() {
+  void *p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_sir_ptab);
+  if (e != cudaSuccess || !p)
+    fail(VG_ERR_CUDA, std::string("cudaGetSymbolAddress of the SIR table failed: ") +
+                          cudaGetErrorString(e));
+  return (double *)p;
+}
+
+double *ptab_address() {
+  std::lock_guard<std::mutex> lk(g_setup_mutex);
+  unsigned long long ctx = current_context_id();
+  if (ctx) {
+    auto it = g_ptab_addr.find(ctx);
+    if (it != g_ptab_addr.end()) return it->second;
+  }
+  // the look-up also makes the device's primary context current when the
+  // thread has no context yet
+  double *p = symbol_address();
+  if (!ctx) ctx = current_context_id();
+  if (!ctx) fail(VG_ERR_CUDA, "no current CUDA context after the symbol look-up");
+  g_ptab_addr[ctx] = p;
+  return p;
+}
+
+// [a, a + na) and [b, b + nb) share a byte
+bool overlap(const void *a, uint64_t na, const void *b, uint64_t nb) {
+  const uintptr_t x = (uintptr_t)a, y = (uintptr_t)b;
+  return x < y + nb && y < x + na;
 }
 
 }  // namespace
@@ -117,6 +163,13 @@ extern "C" int vg_sir_step_noalloc(const uint32_t *row_ptr, const uint32_t *src,
     if (n == 0) return VG_OK;
     if (!row_ptr || !state_in || !days_in || !state_out || !days_out || (!src && max_in_degree))
       fail(VG_ERR_ARG, "vg_sir_step_noalloc: null buffer");
+    // the step reads every agent's old state while it writes the new ones:
+    // an output that shares memory with an input would be read half-updated
+    if (overlap(state_out, n, state_in, n) || overlap(state_out, n, days_in, 4 * n) ||
+        overlap(days_out, 4 * n, state_in, n) || overlap(days_out, 4 * n, days_in, 4 * n) ||
+        overlap(state_out, n, days_out, 4 * n))
+      fail(VG_ERR_ARG, "vg_sir_step_noalloc: the output buffers must not overlap the input "
+                       "buffers or each other (no in-place step)");
     cudaStream_t st = (cudaStream_t)stream;
     double *tab = ptab_address();
     k_fill_ptab<<<1, 1, 0, st>>>(tab, max_in_degree, beta);

@@ -107,6 +107,70 @@ __global__ void k_selftest(uint64_t n, uint64_t seed, unsigned long long *counts
   }
 }
 
+// Throughput of one arithmetic form: every thread of the first `active`
+// lanes of each warp runs `iters` rounds of 8 independent dependency chains
+// (the other lanes branch around the loop, so the warp issues with a
+// partial mask).  mode 0: binary64 add, 1: binary64 multiply, 2: fused
+// multiply-add, 3: the gather kernels' integer-pipe product of a 2^-53-grid
+// weight (emu_mul_grid), 4: 32-bit integer multiply-add (the integer pipe).
+// The chains' results are stored so that nothing is optimised away.
+__global__ void k_rate(int mode, uint32_t iters, uint32_t active, double *sink) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (lane >= active) return;
+  double v[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) v[k] = 1.0 + 1e-3 * (double)(k + (gid & 7));
+  if (mode == 0) {
+    const double c = 1e-12;
+    for (uint32_t i = 0; i < iters; i++) {
+#pragma unroll
+      for (int k = 0; k < 8; k++) v[k] = __dadd_rn(v[k], c);
+    }
+  } else if (mode == 1) {
+    const double c = 1.0 + 1e-12;
+    for (uint32_t i = 0; i < iters; i++) {
+#pragma unroll
+      for (int k = 0; k < 8; k++) v[k] = __dmul_rn(v[k], c);
+    }
+  } else if (mode == 2) {
+    const double c = 1.0 + 1e-12, d = 1e-12;
+    for (uint32_t i = 0; i < iters; i++) {
+#pragma unroll
+      for (int k = 0; k < 8; k++) v[k] = __fma_rn(v[k], c, d);
+    }
+  } else if (mode == 3) {
+    const uint64_t w = dbits(0.75);  // 3 * 2^-2: on the 2^-53 grid
+    uint64_t u[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) u[k] = dbits(v[k]);
+    for (uint32_t i = 0; i < iters; i++) {
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        bool ok;
+        const uint64_t r = emu_mul_grid(w, u[k], ok);
+        u[k] = ok ? (r | (1ull << 62)) & ~(1ull << 61) : u[k] + 1;  // stay in [1, 2)
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 8; k++) v[k] = bdbl(u[k]);
+  } else {
+    uint32_t u[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) u[k] = (uint32_t)gid + k;
+    for (uint32_t i = 0; i < iters; i++) {
+#pragma unroll
+      for (int k = 0; k < 8; k++) u[k] = u[k] * 1664525u + 1013904223u;
+    }
+#pragma unroll
+    for (int k = 0; k < 8; k++) v[k] = (double)u[k];
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) s += v[k];
+  if (s == 12345.678) sink[gid & 1023] = s;  // practically never: keeps the chains live
+}
+
 }  // namespace
 }  // namespace vg
 
@@ -124,6 +188,37 @@ extern "C" int vg_selftest_fp64(uint64_t n, uint64_t seed, uint64_t *counts_out)
     VG_CUDA(cudaGetLastError());
     VG_CUDA(cudaMemcpy(counts_out, d, 6 * 8, cudaMemcpyDeviceToHost));
     VG_CUDA(cudaFree(d));
+    return VG_OK;
+  } catch (const Error &e) {
+    set_last_error(e.msg);
+    return e.code;
+  }
+}
+
+extern "C" int vg_selftest_rate(int mode, uint32_t blocks, uint32_t iters, uint32_t active_lanes,
+                                double *ms_out, double *lane_ops_out) {
+  try {
+    if (mode < 0 || mode > 4 || blocks == 0 || iters == 0 || active_lanes == 0 ||
+        active_lanes > 32 || !ms_out || !lane_ops_out)
+      fail(VG_ERR_ARG, "vg_selftest_rate: mode 0..4, blocks, iters > 0, 1..32 active lanes");
+    double *sink = nullptr;
+    VG_CUDA(cudaMalloc(&sink, 1024 * 8));
+    cudaEvent_t a, b;
+    VG_CUDA(cudaEventCreate(&a));
+    VG_CUDA(cudaEventCreate(&b));
+    k_rate<<<blocks, 256>>>(mode, iters / 8 + 1, active_lanes, sink);  // warm-up
+    VG_CUDA(cudaEventRecord(a));
+    k_rate<<<blocks, 256>>>(mode, iters, active_lanes, sink);
+    VG_CUDA(cudaEventRecord(b));
+    VG_CUDA(cudaEventSynchronize(b));
+    VG_CUDA(cudaGetLastError());
+    float ms = 0.f;
+    VG_CUDA(cudaEventElapsedTime(&ms, a, b));
+    VG_CUDA(cudaEventDestroy(a));
+    VG_CUDA(cudaEventDestroy(b));
+    VG_CUDA(cudaFree(sink));
+    *ms_out = ms;
+    *lane_ops_out = (double)blocks * (256.0 / 32.0) * active_lanes * (double)iters * 8.0;
     return VG_OK;
   } catch (const Error &e) {
     set_last_error(e.msg);
