@@ -79,6 +79,14 @@ extern "C" {
 #define VG_OP_MIN 4
 #define VG_OP_AND 5
 #define VG_OP_OR 6
+/* or-ed into op: the fold order.  By default Float + and * fold
+ * sequentially in the reference's order (bit-identical results) and every
+ * other reduction, whose result does not depend on the order, takes a
+ * parallel tree.  VG_REDUCE_ORDERED forces the sequential fold,
+ * VG_REDUCE_TREE the tree (Float + and *: within 2 (n - 1) 2^-53 sum|f(x)|
+ * of the sequential result). */
+#define VG_REDUCE_ORDERED 0x100
+#define VG_REDUCE_TREE 0x200
 
 /* map function applied to each element before the reduction (mapreduce's
  * `f`): the field itself, or the field compared with a constant. */
@@ -265,6 +273,21 @@ int vg_apply(vg_sim *s, const char *transition, const int *call, int ncall,
              const int *read, int nread, const int *write, int nwrite,
              const int *add_existing, int nadd, int with_edge,
              const double *params, int nparams);
+/* apply! for a host that keeps the called type's state in its own memory:
+ * the n agents' fields of type_nr are uploaded from in_fields (host SoA
+ * columns; NULL entries keep the device column), apply!(sim, transition,
+ * ...) runs exactly as vg_apply, and the new state of those agents is
+ * written to out_fields before the call returns -- the same result as
+ * vg_write_agents, vg_apply and vg_read_agents (src/Simulation.jl:720-821
+ * with the state round-tripped through the host, as a Julia caller whose
+ * agent vectors live in host memory does).  For "bounded_confidence" the
+ * gather runs in row-range chunks and each finished range is downloaded
+ * while the next one computes (pinned host buffers for the overlap). */
+int vg_apply_host(vg_sim *s, const char *transition, const int *call, int ncall,
+                  const int *read, int nread, const int *write, int nwrite,
+                  const int *add_existing, int nadd, int with_edge,
+                  const double *params, int nparams, int type_nr,
+                  const void *const *in_fields, void *const *out_fields, uint64_t n);
 /* Comma-separated list of the registered transition names. */
 const char *vg_transition_names(void);
 
@@ -272,7 +295,10 @@ const char *vg_transition_names(void);
  *      src/EdgeMethods.jl:972-1001 (edges); identities from val4empty,
  *      src/Helpers.jl:44-81.  The result is written as out_dtype
  *      (VG_I64, VG_F64 or VG_BOOL).  has_init/init give the `init`
- *      keyword. */
+ *      keyword.  Agents fold in index order, edges in (target type, target
+ *      row, insertion) order: the reference's order for agents and for
+ *      :SingleType edge types (Vector containers); for the other edge types
+ *      the reference iterates a Dict, whose order is not reproduced. */
 int vg_mapreduce_agents(vg_sim *s, int type_nr, int field, int map_kind,
                         double map_arg, int op, int out_dtype, int has_init,
                         double init, void *out);
@@ -344,7 +370,8 @@ int vg_selftest_fp64(uint64_t n, uint64_t seed, uint64_t *counts_out);
  * `blocks` blocks of 256 threads; in each warp the first active_lanes lanes
  * run iters rounds of 8 independent chains of one operation (mode 0
  * binary64 add, 1 binary64 multiply, 2 binary64 fused multiply-add, 3 the
- * gather kernels' integer-pipe product, 4 32-bit integer multiply-add), the
+ * gather kernels' integer-pipe product, 4 a 32-bit integer chain of a
+ * multiply-add and an or per round), the
  * other lanes branch around.  *ms_out = the launch's CUDA-event duration,
  * *lane_ops_out = operations performed (lanes x rounds x 8). */
 int vg_selftest_rate(int mode, uint32_t blocks, uint32_t iters, uint32_t active_lanes,
@@ -448,6 +475,9 @@ typedef struct vg_job_spec {
   double eps;          /* opinion confidence bound                        */
   double wmax;         /* opinion: cap of the expected degree (<=0: 1e4)  */
   int keep_state;      /* keep the final state for vg_serve_job_state     */
+  int fail_build;      /* failure injection for tests: 1 = the job's build
+                        * raises on the host after its simulation and agents
+                        * exist; the job is retired with an error status    */
 } vg_job_spec;
 typedef struct vg_job_result {
   int64_t id;
@@ -458,7 +488,10 @@ typedef struct vg_job_result {
   uint64_t checksum;                   /* FNV-1a 64 of the final state    */
   double summary;   /* SIR: recovered fraction; opinion: mean opinion      */
   uint64_t device_bytes;
+  int status;       /* 0, or the error code of a job whose build failed      */
+  char error[124];  /* its message (the server and the other jobs go on)     */
 } vg_job_result;
+/* The server runs on the device current when it is created. */
 int vg_serve_create(uint64_t budget_bytes, int max_active, vg_server **out);
 int vg_serve_submit(vg_server *s, const vg_job_spec *spec, int64_t *id_out);
 /* Results of jobs finished since the last poll, at most cap. */

@@ -79,3 +79,46 @@ def test_serving_rejects_bad_jobs(vh):
         spec.model = 7
         with pytest.raises(vh.VahanaError):
             S.submit(spec)
+
+
+def test_failed_build_retires_only_that_job(vh):
+    """A job whose build raises on the host after admission (failure
+    injected after its simulation and agents exist) is retired with an error
+    status; the jobs resident beside it finish bit-identical to their alone
+    runs, and the server keeps accepting jobs."""
+    import time
+    from vahana_gb300 import serve
+    specs = _specs()[:4]
+    bad = serve.sir_job(3000, degree=6, steps=9, seed=4)
+    bad.fail_build = 1
+    with serve.Server(budget_bytes=1 << 34) as S:
+        ids = [S.submit(specs[0]), S.submit(specs[1]), S.submit(bad), S.submit(specs[2]),
+               S.submit(specs[3])]
+        res = {}
+        deadline = time.time() + 300
+        while len(res) < len(ids) and time.time() < deadline:
+            for r in S.poll():
+                res[r["id"]] = r
+            time.sleep(0.01)
+        assert sorted(res) == sorted(ids)
+        failed = res[ids[2]]
+        assert failed["status"] != 0 and "injected" in failed["error"]
+        good = [i for k, i in enumerate(ids) if k != 2]
+        assert all(res[i]["status"] == 0 for i in good)
+        for i, spec in zip(good, specs):
+            got = S.job_state(i, spec)
+            ref = _alone(spec)
+            if spec.model == serve.SIR:
+                np.testing.assert_array_equal(got[0], ref["state"])
+                np.testing.assert_array_equal(got[1], ref["days"])
+            else:
+                np.testing.assert_array_equal(got.view(np.uint64), ref["x"].view(np.uint64))
+        late = serve.sir_job(1500, degree=7, steps=5, seed=12, keep_state=True)
+        j = S.submit(late)
+        S.drain()
+        r = {x["id"]: x for x in S.poll()}
+        assert r[j]["status"] == 0
+        got = S.job_state(j, late)
+        np.testing.assert_array_equal(got[0], _alone(late)["state"])
+        st = S.stats()
+        assert st["done"] == len(ids) + 1 and st["bytes_in_use"] == 0

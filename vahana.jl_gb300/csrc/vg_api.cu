@@ -394,6 +394,11 @@ int vg_sim_create(vg_model *m, const char *name, void *stream, vg_sim **out) {
   API_END
 }
 
+Sim::~Sim() {
+  for (cudaEvent_t e : xchg_events) cudaEventDestroy(e);
+  if (copy_stream) cudaStreamDestroy(copy_stream);
+}
+
 int vg_sim_destroy(vg_sim *s) {
   API_BEGIN
   if (!s) return VG_OK;

@@ -133,12 +133,25 @@ __device__ __forceinline__ int64_t red_i(int op, int64_t a, int64_t b) {
   }
   return 0;
 }
+// Julia's max/min of two floats: a NaN operand gives NaN, +0.0 is larger
+// than -0.0 (the difference's sign decides); order-independent, so the
+// tree and the sequential fold agree
+__device__ __forceinline__ double jl_max(double x, double y) {
+  const double d = __dsub_rn(x, y);
+  const double m = signbit(d) ? y : x;
+  return (isnan(x) || isnan(y)) ? d : m;
+}
+__device__ __forceinline__ double jl_min(double x, double y) {
+  const double d = __dsub_rn(x, y);
+  const double m = signbit(d) ? x : y;
+  return (isnan(x) || isnan(y)) ? d : m;
+}
 __device__ __forceinline__ double red_f(int op, double a, double b) {
   switch (op) {
     case VG_OP_ADD: return __dadd_rn(a, b);
     case VG_OP_MUL: return __dmul_rn(a, b);
-    case VG_OP_MAX: return fmax(a, b);
-    case VG_OP_MIN: return fmin(a, b);
+    case VG_OP_MAX: return jl_max(a, b);
+    case VG_OP_MIN: return jl_min(a, b);
   }
   return 0;
 }
@@ -256,21 +269,57 @@ __global__ void k_reduce_final(const int64_t *pi, const double *pf, int nb, int 
   *of = af;
 }
 
-// sequential left fold in index order: reduced = op(f(x), reduced)
-__global__ void k_reduce_ordered(RedArgs a, int64_t *oi, double *of) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+// Sequential left fold in index order, reduced = op(f(x), reduced), the
+// reference's loop: one chain of dependent operations on thread 0.  The
+// block's other warps map the next tile of elements into shared memory
+// (value bits and whether the element counts) while thread 0 folds the
+// current tile, so the chain never waits for global memory.
+constexpr int ORD_TILE = 2048;
+constexpr int ORD_TPB = 256;
+
+__global__ void __launch_bounds__(ORD_TPB) k_reduce_ordered(RedArgs a, int64_t *oi, double *of) {
+  __shared__ int64_t vbuf[2][ORD_TILE];
+  __shared__ uint8_t live[2][ORD_TILE];
+  const uint64_t ntiles = (a.n + ORD_TILE - 1) / ORD_TILE;
+  auto stage = [&](uint64_t t, int b) {  // warps 1.. map tile t into buffer b
+    const uint64_t base = t * ORD_TILE;
+    for (uint32_t k = threadIdx.x - 32; k < (uint32_t)ORD_TILE; k += blockDim.x - 32) {
+      const uint64_t i = base + k;
+      const bool use = i < a.n && !(a.died && a.died[i]);
+      int64_t vi = 0;
+      double vf = 0.0;
+      if (use) map_val(a.kind, a.arg, a.p, a.dt, i, a.float_acc, &vi, &vf);
+      vbuf[b][k] = a.float_acc ? __double_as_longlong(vf) : vi;
+      live[b][k] = use;
+    }
+  };
+  if (ntiles && threadIdx.x >= 32) stage(0, 0);
+  __syncthreads();
   int64_t ai = a.init_i;
   double af = a.init_f;
-  for (uint64_t i = 0; i < a.n; i++) {
-    if (a.died && a.died[i]) continue;
-    int64_t vi;
-    double vf;
-    map_val(a.kind, a.arg, a.p, a.dt, i, a.float_acc, &vi, &vf);
-    ai = red_i(a.op, vi, ai);
-    af = red_f(a.op, vf, af);
+  for (uint64_t t = 0; t < ntiles; t++) {
+    const int b = (int)(t & 1);
+    if (threadIdx.x >= 32) {
+      if (t + 1 < ntiles) stage(t + 1, b ^ 1);
+    } else if (threadIdx.x == 0) {
+      const uint32_t m = (uint32_t)min((uint64_t)ORD_TILE, a.n - t * ORD_TILE);
+      if (a.float_acc && a.op == VG_OP_ADD) {
+        for (uint32_t k = 0; k < m; k++)
+          if (live[b][k]) af = __dadd_rn(__longlong_as_double(vbuf[b][k]), af);
+      } else if (a.float_acc) {
+        for (uint32_t k = 0; k < m; k++)
+          if (live[b][k]) af = red_f(a.op, __longlong_as_double(vbuf[b][k]), af);
+      } else {
+        for (uint32_t k = 0; k < m; k++)
+          if (live[b][k]) ai = red_i(a.op, vbuf[b][k], ai);
+      }
+    }
+    __syncthreads();
   }
-  *oi = ai;
-  *of = af;
+  if (threadIdx.x == 0) {
+    *oi = ai;
+    *of = af;
+  }
 }
 
 void identity_for(int op, int out_dtype, int has_init, double init, int64_t *ii,
@@ -313,6 +362,26 @@ void neutral_for(int op, int64_t *ni, double *nf) {
   }
 }
 
+// The reference folds sequentially (reduced = op(f(x), reduced)).  Integer
+// and Bool results, and Float max/min, do not depend on the order, so they
+// take the two-pass tree; Float + and * fold in order unless the caller
+// asks for the tree (VG_REDUCE_TREE), whose result may differ in the last
+// bits.
+double host_jl_max(double x, double y) {
+  const double d = x - y;
+  return (std::isnan(x) || std::isnan(y)) ? d : (std::signbit(d) ? y : x);
+}
+double host_jl_min(double x, double y) {
+  const double d = x - y;
+  return (std::isnan(x) || std::isnan(y)) ? d : (std::signbit(d) ? x : y);
+}
+
+bool fold_in_order(int flags, bool float_acc, int op) {
+  if (flags & VG_REDUCE_ORDERED) return true;
+  if (flags & VG_REDUCE_TREE) return false;
+  return float_acc && (op == VG_OP_ADD || op == VG_OP_MUL);
+}
+
 void run_reduce(Sim &s, RedArgs a, int out_dtype, bool ordered, void *out) {
   neutral_for(a.op, &a.neut_i, &a.neut_f);
   int64_t ri = a.init_i;
@@ -323,7 +392,7 @@ void run_reduce(Sim &s, RedArgs a, int out_dtype, bool ordered, void *out) {
     int64_t *oi = d;
     double *of = (double *)(d + 1);
     if (ordered) {
-      k_reduce_ordered<<<1, 32, 0, s.stream>>>(a, oi, of);
+      k_reduce_ordered<<<1, ORD_TPB, 0, s.stream>>>(a, oi, of);
     } else {
       int nb = (int)std::min<uint64_t>(1024, (a.n + TPB - 1) / TPB);
       int64_t *pi = d + 2;
@@ -549,6 +618,60 @@ int vg_apply(vg_sim *h, const char *tname, const int *call, int ncall, const int
   API_END
 }
 
+// apply! with the called type's state exchanged with host memory: upload,
+// the transition, download.  The upload runs on the simulation's stream
+// ahead of the kernels; a transition that completes its rows range by range
+// (bounded_confidence) downloads each finished range on a second stream
+// while it computes the next one; otherwise the new state is downloaded
+// after the transition.  Returns when the new state is in out_fields.
+int vg_apply_host(vg_sim *h, const char *tname, const int *call, int ncall, const int *read,
+                  int nread, const int *write, int nwrite, const int *ae, int nae, int with_edge,
+                  const double *params, int nparams, int type_nr, const void *const *in_fields,
+                  void *const *out_fields, uint64_t n) {
+  API_BEGIN
+  Sim &s = S(h);
+  if (!s.initialized) fail(VG_ERR_ASSERT, "You must call finish_init! before apply!");
+  const AgentTypeDesc &ad = s.model->at(type_nr);
+  AgentStore &a = s.agents[type_nr - 1];
+  if (n > a.n) fail(VG_ERR_ARG, "more values than agent slots");
+  if (s.async) check_device_status(s, "asynchronous transition");
+  for (size_t f = 0; f < ad.fields.size(); f++) {
+    if (!in_fields || !in_fields[f]) continue;
+    VG_CUDA(cudaMemcpyAsync(a.rd[f].p, in_fields[f], n * ad.fields[f].size,
+                            cudaMemcpyHostToDevice, s.stream));
+  }
+  Sim::HostExchange hx;
+  hx.type_nr = type_nr;
+  hx.out = out_fields;
+  hx.n = n;
+  struct Reset {
+    Sim &s;
+    ~Reset() { s.host_xchg = nullptr; }
+  } reset{s};
+  s.host_xchg = &hx;
+  const bool was_async = s.async;
+  s.async = true;  // the transition's errors are read below, after the downloads
+  int rc = vg_apply(h, tname, call, ncall, read, nread, write, nwrite, ae, nae, with_edge, params,
+                    nparams);
+  s.async = was_async;
+  s.host_xchg = nullptr;
+  if (rc != VG_OK) {
+    if (s.copy_stream) cudaStreamSynchronize(s.copy_stream);
+    return rc;
+  }
+  AgentStore &b = s.agents[type_nr - 1];  // after the buffer swap: the new state
+  if (!hx.done && out_fields)
+    for (size_t f = 0; f < ad.fields.size(); f++) {
+      if (!out_fields[f]) continue;
+      VG_CUDA(cudaMemcpyAsync(out_fields[f], b.rd[f].p, n * ad.fields[f].size,
+                              cudaMemcpyDeviceToHost, s.stream));
+    }
+  if (hx.done) VG_CUDA(cudaStreamSynchronize(s.copy_stream));
+  VG_CUDA(cudaStreamSynchronize(s.stream));
+  check_device_status(s, tname);
+  API_END
+}
+
 int vg_mapreduce_agents(vg_sim *h, int nr, int field, int map_kind, double map_arg, int op,
                         int out_dtype, int has_init, double init, void *out) {
   API_BEGIN
@@ -557,7 +680,7 @@ int vg_mapreduce_agents(vg_sim *h, int nr, int field, int map_kind, double map_a
   if (s.intransition && s.check_readable)
     fail(VG_ERR_ASSERT, "You can not call mapreduce inside of a transition function.");
   if (field < 0 || field >= (int)ad.fields.size()) fail(VG_ERR_ARG, "bad field");
-  bool ordered = (op & 0x100) != 0;
+  const int order_flags = op & (VG_REDUCE_ORDERED | VG_REDUCE_TREE);
   op &= 0xff;
   if ((op == VG_OP_AND || op == VG_OP_OR) && (ad.fields[field].dtype == VG_F32 ||
                                               ad.fields[field].dtype == VG_F64) &&
@@ -603,8 +726,8 @@ int vg_mapreduce_agents(vg_sim *h, int nr, int field, int map_kind, double map_a
       switch (op) {
         case VG_OP_ADD: ai = (int64_t)((uint64_t)iv + (uint64_t)ai); af = v + af; break;
         case VG_OP_MUL: ai = (int64_t)((uint64_t)iv * (uint64_t)ai); af = v * af; break;
-        case VG_OP_MAX: ai = std::max(iv, ai); af = std::fmax(v, af); break;
-        case VG_OP_MIN: ai = std::min(iv, ai); af = std::fmin(v, af); break;
+        case VG_OP_MAX: ai = std::max(iv, ai); af = host_jl_max(v, af); break;
+        case VG_OP_MIN: ai = std::min(iv, ai); af = host_jl_min(v, af); break;
         case VG_OP_AND: ai = iv & ai; break;
         case VG_OP_OR: ai = iv | ai; break;
       }
@@ -621,7 +744,7 @@ int vg_mapreduce_agents(vg_sim *h, int nr, int field, int map_kind, double map_a
   r.kind = map_kind;
   r.arg = map_arg;
   r.op = op;
-  run_reduce(s, r, out_dtype, ordered, out);
+  run_reduce(s, r, out_dtype, fold_in_order(order_flags, r.float_acc, op), out);
   API_END
 }
 
@@ -633,12 +756,13 @@ int vg_mapreduce_edges(vg_sim *h, int e, int field, int map_kind, double map_arg
   if (ed.stateless())
     fail(VG_ERR_ASSERT, "mapreduce is not defined for the hint combination of " + ed.name);
   if (field < 0 || field >= (int)ed.fields.size()) fail(VG_ERR_ARG, "bad field");
-  bool ordered = (op & 0x100) != 0;
+  const int order_flags = op & (VG_REDUCE_ORDERED | VG_REDUCE_TREE);
   op &= 0xff;
   RedArgs r{};
   identity_for(op, out_dtype, has_init, init, &r.init_i, &r.init_f);
   int dt = ed.fields[field].dtype;
   r.float_acc = (map_kind == VG_MAP_FIELD && (dt == VG_F32 || dt == VG_F64)) || out_dtype == VG_F64;
+  const bool ordered = fold_in_order(order_flags, r.float_acc, op);
   if (!s.initialized) {
     // Before finish_init! the reference reduces over the (empty) read
     // container: the identity.

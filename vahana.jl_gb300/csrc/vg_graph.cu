@@ -967,6 +967,8 @@ void ensure_schedule(Sim &s, CSR &c, uint32_t thr, uint32_t big_thr, uint64_t n)
   c.sell_src.release();
   c.sell_w.release();
   c.nhub = c.norder = c.nslices = c.nbig = 0;
+  c.chunk_block.clear();
+  c.chunk_rows.clear();
   if (n > 0 && c.row_ptr.p) {
     const uint32_t *rp = c.row_ptr.as<uint32_t>();
     // hub rows by descending degree
@@ -991,6 +993,7 @@ void ensure_schedule(Sim &s, CSR &c, uint32_t thr, uint32_t big_thr, uint64_t n)
     // more, so that the window number stays below the sentinel)
     uint32_t wshift = 13;
     while ((n >> wshift) >= 0xFFFFull) wshift++;
+    c.wshift = wshift;
     Tmp<uint32_t> keys(n, st);
     c.order.alloc(n * 4, &s.footprint);
     k_order_keys<<<nblk(n), TPB, 0, st>>>(rp, c.nrows, n, thr, wshift, keys.p,

@@ -192,7 +192,12 @@ struct CSR {
   DevBuf sell_w;    // f64 [slots]
   uint64_t sched_n = 0;  // agent count the layout covers
   uint32_t hub_threshold = 0;
+  uint32_t wshift = 13;   // window = row >> wshift
   bool schedule_valid = false;
+  // chunked launch of the gather (apply! with host exchange): chunk k runs
+  // slice blocks [chunk_block[k], chunk_block[k + 1]) and completes every
+  // row below chunk_rows[k] (derived from the layout, cached with it)
+  std::vector<uint64_t> chunk_block, chunk_rows;
   // payload field 0 (Float64) holds only multiples of 2^-53 in (0, 1]:
   // -1 not checked yet, 0 no, 1 yes (decides the gather kernels' sum path)
   int unit_grid_weights = -1;
@@ -282,6 +287,19 @@ struct Sim {
   // edge-append buffers of earlier transitions, by edge type, reused by the
   // next apply! that appends to the same type (no allocation per step)
   std::map<int, std::unique_ptr<EdgeAppend>> append_spare;
+  // apply! with host exchange (vg_apply_host): while set, a transition that
+  // finishes its rows range by range may download each finished range of the
+  // called type's new state to `out` on copy_stream (and sets `done`)
+  struct HostExchange {
+    int type_nr = 0;
+    void *const *out = nullptr;
+    uint64_t n = 0;
+    bool done = false;
+  };
+  HostExchange *host_xchg = nullptr;
+  cudaStream_t copy_stream = nullptr;   // created on first use, destroyed with the sim
+  std::vector<cudaEvent_t> xchg_events;  // one per chunk, created on first use
+  ~Sim();
 };
 
 // ---------------------------------------------------------------- kernels

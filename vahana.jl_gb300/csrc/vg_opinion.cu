@@ -70,10 +70,12 @@ struct OpinionArgs {
   uint64_t nslices;
   uint32_t hub_thr;
   unsigned hub_blocks;   // blocks of the other hub rows, 4 per block
+  unsigned blk_base;     // block number of this launch's first block (chunked launches)
   double eps, a, b;
   int a_pow2, b_pow2, a_k, b_k;  // a = 2^a_k, b = 2^b_k (positive normal powers of two)
   float eps_lo, eps_hi;  // float filter: certainly inside / certainly outside
   int grid;              // all weights are multiples of 2^-53 in (0, 1] (exponent 970..1023)
+  CSR *csr;              // host side only: the layout the arguments come from
 };
 
 __device__ __forceinline__ uint64_t bits(double v) { return (uint64_t)__double_as_longlong(v); }
@@ -570,7 +572,7 @@ __device__ __forceinline__ void opinion_block(const OpinionArgs &p, unsigned blk
 
 template <bool GRID>
 __global__ void __launch_bounds__(TPB, 9) k_opinion(OpinionArgs p) {
-  opinion_block<GRID, false>(p, blockIdx.x);
+  opinion_block<GRID, false>(p, p.blk_base + blockIdx.x);
 }
 
 // the block-wide hub rows of one simulation, one block each
@@ -617,6 +619,10 @@ __global__ void k_check_grid(const double *w, uint64_t n, int *bad) {
 static unsigned opinion_args(Sim &s, int e, int T, double eps, double a, double b,
                              uint32_t thr, uint32_t big_thr, OpinionArgs &p,
                              cudaStream_t launch_stream);
+// chunks of a gather launch whose finished rows are downloaded while the
+// next chunk runs (apply! with host exchange)
+constexpr unsigned XCHG_CHUNKS = 8;
+static void launch_chunked(Sim &s, OpinionArgs &p, unsigned grid, Sim::HostExchange &hx);
 
 // apply!(sim, bounded_confidence, [T], [T, E], [T]; params = [E, eps, a, b,
 // hub_thr, block_thr]); defaults eps 0.3, a 0.5, b 1 - a, hub_thr 1536,
@@ -657,11 +663,76 @@ void tr_bounded_confidence(ApplyCtx &c) {
     if (p.grid) k_opinion_big<true><<<nbig, TPB, 0, s.stream>>>(p);
     else k_opinion_big<false><<<nbig, TPB, 0, s.stream>>>(p);
   }
+  Sim::HostExchange *hx = s.host_xchg;
+  if (hx && hx->type_nr == c.call_type && ad.fields.size() == 1 && hx->out && hx->out[0] &&
+      grid > nbig) {
+    launch_chunked(s, p, grid - nbig, *hx);
+    return;
+  }
   if (grid > nbig) {
     if (p.grid) k_opinion<true><<<grid - nbig, TPB, 0, s.stream>>>(p);
     else k_opinion<false><<<grid - nbig, TPB, 0, s.stream>>>(p);
   }
   VG_CUDA(cudaGetLastError());
+}
+
+// Chunk boundaries of the gather launch: chunk k runs the slice blocks
+// [chunk_block[k], chunk_block[k + 1]) (chunk 0 also every hub warp, which
+// lead the grid); the rows are sorted by window (row >> wshift) before
+// degree, so after chunk k every row of the windows below the window of the
+// next chunk's first row is final: chunk_rows[k] = that window << wshift.
+static void chunk_bounds(Sim &s, CSR &cs, uint64_t n, unsigned hub_blocks, unsigned slice_blocks) {
+  const unsigned K = std::max(1u, std::min(XCHG_CHUNKS, slice_blocks));
+  if (cs.chunk_block.size() == K + 1) return;
+  cs.chunk_block.assign(K + 1, 0);
+  cs.chunk_rows.assign(K, n);
+  for (unsigned k = 0; k <= K; k++)
+    cs.chunk_block[k] = hub_blocks + (uint64_t)slice_blocks * k / K;
+  cs.chunk_block[0] = 0;
+  for (unsigned k = 0; k + 1 < K; k++) {
+    // first position in `order` of the block: TPB / 32 slices of 32 rows per block
+    const uint64_t pos = (cs.chunk_block[k + 1] - hub_blocks) * (uint64_t)TPB;
+    if (pos >= cs.norder) continue;
+    uint32_t row = 0;
+    VG_CUDA(cudaMemcpyAsync(&row, cs.order.as<uint32_t>() + pos, 4, cudaMemcpyDeviceToHost,
+                            s.stream));
+    VG_CUDA(cudaStreamSynchronize(s.stream));
+    cs.chunk_rows[k] = std::min<uint64_t>(n, ((uint64_t)row >> cs.wshift) << cs.wshift);
+  }
+}
+
+// The gather in chunks on the simulation's stream; after each chunk the rows
+// it completed are downloaded on the copy stream while the next chunk runs.
+static void launch_chunked(Sim &s, OpinionArgs &p, unsigned grid, Sim::HostExchange &hx) {
+  CSR &cs = *p.csr;
+  chunk_bounds(s, cs, p.n, p.hub_blocks, grid - p.hub_blocks);
+  const unsigned K = (unsigned)cs.chunk_rows.size();
+  if (!s.copy_stream) VG_CUDA(cudaStreamCreateWithFlags(&s.copy_stream, cudaStreamNonBlocking));
+  while (s.xchg_events.size() < K) {
+    cudaEvent_t e;
+    VG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    s.xchg_events.push_back(e);
+  }
+  const uint64_t n = std::min<uint64_t>(hx.n, p.n);
+  uint64_t done_rows = 0;
+  for (unsigned k = 0; k < K; k++) {
+    const unsigned b0 = (unsigned)cs.chunk_block[k], b1 = (unsigned)cs.chunk_block[k + 1];
+    OpinionArgs q = p;
+    q.blk_base = b0;
+    if (b1 > b0) {
+      if (q.grid) k_opinion<true><<<b1 - b0, TPB, 0, s.stream>>>(q);
+      else k_opinion<false><<<b1 - b0, TPB, 0, s.stream>>>(q);
+      VG_CUDA(cudaGetLastError());
+    }
+    const uint64_t upto = k + 1 == K ? n : std::min(n, cs.chunk_rows[k]);
+    if (upto <= done_rows) continue;
+    VG_CUDA(cudaEventRecord(s.xchg_events[k], s.stream));
+    VG_CUDA(cudaStreamWaitEvent(s.copy_stream, s.xchg_events[k], 0));
+    VG_CUDA(cudaMemcpyAsync((double *)hx.out[0] + done_rows, p.xo + done_rows,
+                            (upto - done_rows) * 8, cudaMemcpyDeviceToHost, s.copy_stream));
+    done_rows = upto;
+  }
+  hx.done = true;
 }
 
 // arguments and grid size of one simulation's gather launch; 0 when there
@@ -730,6 +801,7 @@ static unsigned opinion_args(Sim &s, int e, int T, double eps, double a, double 
   p.sell_w = cs.sell_w.as<double>();
   p.nslices = cs.nslices;
   p.hub_blocks = (unsigned)((cs.nhub - cs.nbig + (TPB / 32) - 1) / (TPB / 32));
+  p.csr = &cs;
   return (unsigned)cs.nbig + p.hub_blocks + (unsigned)((cs.nslices + (TPB / 32) - 1) / (TPB / 32));
 }
 

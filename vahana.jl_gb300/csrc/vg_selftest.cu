@@ -112,7 +112,8 @@ __global__ void k_selftest(uint64_t n, uint64_t seed, unsigned long long *counts
 // (the other lanes branch around the loop, so the warp issues with a
 // partial mask).  mode 0: binary64 add, 1: binary64 multiply, 2: fused
 // multiply-add, 3: the gather kernels' integer-pipe product of a 2^-53-grid
-// weight (emu_mul_grid), 4: 32-bit integer multiply-add (the integer pipe).
+// weight (emu_mul_grid), 4: a 32-bit integer chain u = u (u | 1) + c (two
+// integer operations per round).
 // The chains' results are stored so that nothing is optimised away.
 __global__ void k_rate(int mode, uint32_t iters, uint32_t active, double *sink) {
   const uint32_t lane = threadIdx.x & 31;
@@ -160,7 +161,7 @@ __global__ void k_rate(int mode, uint32_t iters, uint32_t active, double *sink) 
     for (int k = 0; k < 8; k++) u[k] = (uint32_t)gid + k;
     for (uint32_t i = 0; i < iters; i++) {
 #pragma unroll
-      for (int k = 0; k < 8; k++) u[k] = u[k] * 1664525u + 1013904223u;
+      for (int k = 0; k < 8; k++) u[k] = u[k] * (u[k] | 1u) + 0x9e3779b9u;  // no closed form
     }
 #pragma unroll
     for (int k = 0; k < 8; k++) v[k] = (double)u[k];

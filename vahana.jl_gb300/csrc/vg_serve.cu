@@ -13,6 +13,7 @@
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
+#include <cstdio>
 #include <cstring>
 #include <deque>
 #include <mutex>
@@ -120,6 +121,7 @@ constexpr int BUILDERS = 4;
 
 struct vg_server {
   std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+  int device = 0;  // the device current at vg_serve_create: every thread runs there
   uint64_t budget = 0, used = 0;
   int max_active = 0;
   cudaStream_t stream = nullptr;
@@ -168,6 +170,7 @@ void build_job(vg_server *S, Job *J, cudaStream_t bst) {
     std::vector<int32_t> days(sp.n, 0);
     const void *cols[2] = {st.data(), days.data()};
     if ((rc = vg_add_agents(J->sim, S->sir_person, sp.n, cols, nullptr))) fail(rc, vg_last_error());
+    if (sp.fail_build) fail(VG_ERR_STATE, "job build failed (injected after its agents were added)");
     if ((rc = vg_gen_uniform_out_edges(J->sim, S->sir_contact, S->sir_person,
                                        (uint32_t)std::lround(sp.mean_degree), sp.seed)))
       fail(rc, vg_last_error());
@@ -192,6 +195,7 @@ void build_job(vg_server *S, Job *J, cudaStream_t bst) {
       x[i] = u64_to_unit(philox_u64(philox_draw(sp.seed, i + 1, 0, TAG_INIT)));
     const void *cols[1] = {x.data()};
     if ((rc = vg_add_agents(J->sim, S->op_agent, sp.n, cols, nullptr))) fail(rc, vg_last_error());
+    if (sp.fail_build) fail(VG_ERR_STATE, "job build failed (injected after its agents were added)");
     uint64_t ne = (uint64_t)std::nearbyint(sp.mean_degree * (double)sp.n);
     if ((rc = vg_gen_chung_lu_edges(J->sim, S->op_edge, S->op_agent, ne, sp.mean_degree, 2.5,
                                     sp.wmax, sp.seed, 0)))
@@ -320,9 +324,29 @@ void fail_server(vg_server *S, const std::string &msg) {
   S->build_cv.notify_all();
 }
 
+// A job whose build fails is retired at once with the error (its partial
+// simulation released); the server and the other jobs go on.
+void retire_failed_build(vg_server *S, Job *J, int code, const std::string &msg) {
+  J->ptab.release();
+  if (J->sim) vg_sim_destroy(J->sim);
+  J->sim = nullptr;
+  vg_job_result &r = J->result;
+  r = vg_job_result{};
+  r.id = J->id;
+  r.model = J->spec.model;
+  r.n = J->spec.n;
+  r.steps = J->spec.steps;
+  r.arrival_s = J->arrival;
+  r.admit_s = J->admit;
+  r.status = code ? code : VG_ERR_STATE;
+  std::snprintf(r.error, sizeof(r.error), "%s", msg.c_str());
+  r.finish_s = now_s(S->t0);
+  J->finish = r.finish_s;
+}
+
 void builder_loop(vg_server *S, int b) {
   try {
-    VG_CUDA(cudaSetDevice(0));
+    VG_CUDA(cudaSetDevice(S->device));
     while (true) {
       Job *J = nullptr;
       {
@@ -335,11 +359,22 @@ void builder_loop(vg_server *S, int b) {
         S->to_build.pop_front();
         S->building++;
       }
-      build_job(S, J, S->build_stream[b]);
+      bool built = true;
+      try {
+        build_job(S, J, S->build_stream[b]);
+      } catch (const Error &e) {
+        retire_failed_build(S, J, e.code, e.msg);
+        built = false;
+      }
       {
         std::lock_guard<std::mutex> lk(S->mu);
         S->building--;
-        S->ready.push_back(J);
+        if (built) {
+          S->ready.push_back(J);
+        } else {
+          S->used -= J->est_bytes;
+          S->done.push_back(J);
+        }
       }
       S->cv.notify_one();
     }
@@ -350,7 +385,7 @@ void builder_loop(vg_server *S, int b) {
 
 void worker_loop(vg_server *S) {
   try {
-    VG_CUDA(cudaSetDevice(0));
+    VG_CUDA(cudaSetDevice(S->device));
     while (true) {
       std::vector<Job *> arrived;
       {
@@ -421,6 +456,7 @@ int vg_serve_create(uint64_t budget_bytes, int max_active, vg_server **out) {
   auto S = std::make_unique<vg_server>();
   S->budget = budget_bytes;
   S->max_active = max_active > 0 ? max_active : 1 << 20;
+  VG_CUDA(cudaGetDevice(&S->device));
   VG_CUDA(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
   int rc;
   if ((rc = vg_model_create(&S->sir_model))) fail(rc, vg_last_error());

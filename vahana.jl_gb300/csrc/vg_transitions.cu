@@ -235,10 +235,29 @@ __device__ __forceinline__ uint64_t order_key(int call_pos, uint64_t i,
   return ((uint64_t)call_pos << 60) | ((i & ((1ull << 40) - 1)) << 20) | seq;
 }
 
-__device__ __forceinline__ int64_t append_slot(const Append &ap, int *status) {
-  unsigned long long k = atomicAdd(ap.counter, 1ull);
-  if (k >= ap.cap) {
-    set_status(status, 301);  // append buffer overflow
+// Slots of the append and removal buffers are reserved per warp: the lanes
+// that add a record in this round vote, the lowest of them reserves all of
+// the warp's slots with one atomicAdd on the buffer's counter, and each lane
+// takes the next slot by its rank among the voters.  Every lane of the warp
+// must call it (full mask; lanes with nothing to add pass want = false).
+// The slot is only a place in the buffer: the record's order key decides its
+// position in the rebuilt container.  -1: nothing wanted, or the buffer is
+// full (err is recorded in the status word).
+constexpr unsigned FULL_WARP = 0xffffffffu;
+
+__device__ __forceinline__ int64_t warp_slot(unsigned long long *counter, uint64_t cap, bool want,
+                                             int *status, int err) {
+  const unsigned voters = __ballot_sync(FULL_WARP, want);
+  if (!voters) return -1;
+  const unsigned lane = threadIdx.x & 31;
+  const int leader = __ffs(voters) - 1;
+  unsigned long long base = 0;
+  if ((int)lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(voters));
+  base = __shfl_sync(FULL_WARP, base, leader);
+  if (!want) return -1;
+  const unsigned long long k = base + __popc(voters & ((1u << lane) - 1u));
+  if (k >= cap) {
+    set_status(status, err);
     return -1;
   }
   return (int64_t)k;
@@ -247,9 +266,9 @@ __device__ __forceinline__ int64_t append_slot(const Append &ap, int *status) {
 // add_edge!(sim, id, id, state) for every swept agent
 __global__ void k_self_edge(Sweep s, Append ap, int call_pos, const uint8_t *pl) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= s.a.n || !sw_begin(s, i)) return;
-  if (s.writes) sw_copy(s, i);
-  int64_t k = append_slot(ap, s.status);
+  const bool live = i < s.a.n && sw_begin(s, i);
+  if (live && s.writes) sw_copy(s, i);
+  const int64_t k = warp_slot(ap.counter, ap.cap, live, s.status, 301);
   if (k < 0) return;
   uint64_t id = ((uint64_t)s.type_nr << SHIFT_TYPE) | (i + 1);
   ap.to[k] = id;
@@ -264,22 +283,26 @@ __global__ void k_self_edge(Sweep s, Append ap, int call_pos, const uint8_t *pl)
 }
 
 // add_edges!(sim, id, edges(sim, id, ET)): re-add every in-edge of the agent
+// (round q: the q-th in-edge of every lane that has one)
 __global__ void k_readd_edges(Sweep s, DevCSRView c, Append ap, int call_pos) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= s.a.n || !sw_begin(s, i)) return;
-  if (s.writes) sw_copy(s, i);
-  if (i >= c.nrows) return;
-  uint64_t id = ((uint64_t)s.type_nr << SHIFT_TYPE) | (i + 1);
-  for (uint32_t e = c.row_ptr[i], q = 0; e < c.row_ptr[i + 1]; e++, q++) {
-    int64_t k = append_slot(ap, s.status);
-    if (k < 0) return;
+  const bool live = i < s.a.n && sw_begin(s, i);
+  if (live && s.writes) sw_copy(s, i);
+  const bool rows = live && i < c.nrows;
+  const uint32_t b = rows ? c.row_ptr[i] : 0u;
+  const uint32_t deg = rows ? c.row_ptr[i + 1] - b : 0u;
+  const uint64_t id = ((uint64_t)s.type_nr << SHIFT_TYPE) | (i + 1);
+  for (uint32_t q = 0; __any_sync(FULL_WARP, q < deg); q++) {
+    const int64_t k = warp_slot(ap.counter, ap.cap, q < deg, s.status, 301);
+    if (k < 0) continue;
+    const uint32_t e = b + q;
     ap.to[k] = id;
     ap.from[k] = ((uint64_t)edge_src_type(c, e) << SHIFT_TYPE) | ((uint64_t)c.src[e] + 1);
     ap.key[k] = order_key(call_pos, i, q);
     for (int f = 0; f < ap.npayload; f++) {
       int sz = ap.psize[f];
-      for (int b = 0; b < sz; b++)
-        ((uint8_t *)ap.payload[f])[k * sz + b] = ((const uint8_t *)c.payload[f])[(uint64_t)e * sz + b];
+      for (int bb = 0; bb < sz; bb++)
+        ((uint8_t *)ap.payload[f])[k * sz + bb] = ((const uint8_t *)c.payload[f])[(uint64_t)e * sz + bb];
     }
   }
 }
@@ -302,42 +325,49 @@ __device__ __forceinline__ bool field_test(int kind, double arg, const void *p, 
   return (ld_i64(p, dt, i) % (int64_t)arg) != 0;
 }
 
-__device__ __forceinline__ bool push_removal(const Removal &r, uint64_t to, uint64_t from,
-                                             uint64_t key, int *status) {
-  unsigned long long k = atomicAdd(r.counter, 1ull);
-  if (k >= r.cap) {
-    set_status(status, 302);  // removal buffer overflow
-    return false;
-  }
+// one removal record per lane with want (every lane of the warp calls it)
+__device__ __forceinline__ void push_removal(const Removal &r, bool want, uint64_t to,
+                                             uint64_t from, uint64_t key, int *status) {
+  const int64_t k = warp_slot(r.counter, r.cap, want, status, 302);
+  if (k < 0) return;
   r.to[k] = to;
   r.from[k] = from;
   r.key[k] = key;
-  return true;
 }
 
 __global__ void k_remove_edges(Sweep s, DevCSRView c, SrcTable t, int kind, double arg, int mode,
                                Removal rm, int call_pos) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= s.a.n || !sw_begin(s, i)) return;
-  if (s.writes) sw_copy(s, i);
+  const bool live = i < s.a.n && sw_begin(s, i);
+  if (live && s.writes) sw_copy(s, i);
   const uint64_t id = ((uint64_t)s.type_nr << SHIFT_TYPE) | (i + 1);
   if (mode == 0) {
-    if (s.nfields > 0 && !field_test(kind, arg, s.a.rd[0], s.fdt[0], i)) return;
-    push_removal(rm, id, REMOVE_ALL, order_key(call_pos, i, 0) + 1, s.status);
+    const bool want = live && (s.nfields == 0 || field_test(kind, arg, s.a.rd[0], s.fdt[0], i));
+    push_removal(rm, want, id, REMOVE_ALL, order_key(call_pos, i, 0) + 1, s.status);
     return;
   }
-  if (i >= c.nrows) return;
+  // round j: the j-th in-edge of every lane that has one; a lane's records
+  // are numbered q in insertion order of the edges that pass the test
+  const bool rows = live && i < c.nrows;
+  const uint32_t b = rows ? c.row_ptr[i] : 0u;
+  const uint32_t deg = rows ? c.row_ptr[i + 1] - b : 0u;
   uint32_t q = 0;
-  for (uint32_t e = c.row_ptr[i]; e < c.row_ptr[i + 1]; e++) {
-    int ty = edge_src_type(c, e);
-    uint32_t j = c.src[e];
-    if (ty <= 0 || ty >= MAX_AGENT_TYPES || !t.ptr[ty]) {
-      set_status(s.status, 202);  // source type not readable
-      continue;
+  for (uint32_t j = 0; __any_sync(FULL_WARP, j < deg); j++) {
+    bool want = false;
+    uint64_t nid = 0;
+    if (j < deg) {
+      const uint32_t e = b + j;
+      const int ty = edge_src_type(c, e);
+      const uint32_t src = c.src[e];
+      if (ty <= 0 || ty >= MAX_AGENT_TYPES || !t.ptr[ty]) {
+        set_status(s.status, 202);  // source type not readable
+      } else if (field_test(kind, arg, t.ptr[ty], t.dt[ty], src)) {
+        want = true;
+        nid = ((uint64_t)ty << SHIFT_TYPE) | ((uint64_t)src + 1);
+      }
     }
-    if (!field_test(kind, arg, t.ptr[ty], t.dt[ty], j)) continue;
-    const uint64_t nid = ((uint64_t)ty << SHIFT_TYPE) | ((uint64_t)j + 1);
-    if (!push_removal(rm, id, nid, order_key(call_pos, i, q++) + 1, s.status)) return;
+    push_removal(rm, want, id, nid, order_key(call_pos, i, q) + 1, s.status);
+    q += want;
   }
 }
 
@@ -371,31 +401,34 @@ __global__ void k_spawn_new(Sweep s, uint64_t n_callers_scope, const uint32_t *f
                             const uint32_t *pos, SpawnArgs g, Append ap, int link_dt,
                             int call_pos) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_callers_scope || !flag[i]) return;
+  const bool caller = i < n_callers_scope && flag[i];
   const uint64_t id = ((uint64_t)s.type_nr << SHIFT_TYPE) | (i + 1);
   for (int j = 0; j < g.k; j++) {
-    const uint64_t q = (uint64_t)pos[i] * g.k + j;
-    const uint64_t nr = q < g.take ? g.reuse[g.nreuse - 1 - q] : g.n_old + 1 + (q - g.take);
+    const uint64_t q = caller ? (uint64_t)pos[i] * g.k + j : 0;
+    const uint64_t nr = !caller ? 0
+                        : q < g.take ? g.reuse[g.nreuse - 1 - q] : g.n_old + 1 + (q - g.take);
     const uint64_t t = nr - 1;
-    for (int f = 0; f < s.nfields; f++) {
-      switch (s.fsize[f]) {
-        case 1: ((uint8_t *)s.a.wr[f])[t] = ((const uint8_t *)s.a.rd[f])[i]; break;
-        case 2: ((uint16_t *)s.a.wr[f])[t] = ((const uint16_t *)s.a.rd[f])[i]; break;
-        case 4: ((uint32_t *)s.a.wr[f])[t] = ((const uint32_t *)s.a.rd[f])[i]; break;
-        case 8: ((uint64_t *)s.a.wr[f])[t] = ((const uint64_t *)s.a.rd[f])[i]; break;
+    if (caller) {
+      for (int f = 0; f < s.nfields; f++) {
+        switch (s.fsize[f]) {
+          case 1: ((uint8_t *)s.a.wr[f])[t] = ((const uint8_t *)s.a.rd[f])[i]; break;
+          case 2: ((uint16_t *)s.a.wr[f])[t] = ((const uint16_t *)s.a.rd[f])[i]; break;
+          case 4: ((uint32_t *)s.a.wr[f])[t] = ((const uint32_t *)s.a.rd[f])[i]; break;
+          case 8: ((uint64_t *)s.a.wr[f])[t] = ((const uint64_t *)s.a.rd[f])[i]; break;
+        }
       }
+      if (s.nfields > 0) {
+        int dt = s.fdt[0];
+        if (is_float(dt)) st_f64(s.a.wr[0], dt, t, ld_f64(s.a.rd[0], dt, i) + g.off[j]);
+        else st_i64(s.a.wr[0], dt, t, ld_i64(s.a.rd[0], dt, i) + (int64_t)g.off[j]);
+      }
+      if (s.mortal) s.a.died_wr[t] = 0;
     }
-    if (s.nfields > 0) {
-      int dt = s.fdt[0];
-      if (is_float(dt)) st_f64(s.a.wr[0], dt, t, ld_f64(s.a.rd[0], dt, i) + g.off[j]);
-      else st_i64(s.a.wr[0], dt, t, ld_i64(s.a.rd[0], dt, i) + (int64_t)g.off[j]);
-    }
-    if (s.mortal) s.a.died_wr[t] = 0;
     if (link_dt < 0) continue;
     const uint64_t nid = ((uint64_t)s.type_nr << SHIFT_TYPE) | nr;
     for (int d = 0; d < 2; d++) {
-      int64_t k = append_slot(ap, s.status);
-      if (k < 0) return;
+      const int64_t k = warp_slot(ap.counter, ap.cap, caller, s.status, 301);
+      if (k < 0) continue;
       ap.from[k] = d == 0 ? nid : id;
       ap.to[k] = d == 0 ? id : nid;
       ap.key[k] = order_key(call_pos, i, 2 * j + d);
@@ -411,26 +444,31 @@ __global__ void k_spawn_new(Sweep s, uint64_t n_callers_scope, const uint32_t *f
 __global__ void k_link_neighbors(Sweep s, DevCSRView c, Append ap, int pl_dt, int has_die,
                                  double die_value, int call_pos) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= s.a.n || !sw_begin(s, i)) return;
+  bool live = i < s.a.n && sw_begin(s, i);
   const int dt0 = s.fdt[0];
-  const double v = s.nfields > 0 ? ld_f64(s.a.rd[0], dt0, i) : 0.0;
-  if (has_die && s.nfields > 0 && v == die_value) {
+  const double v = live && s.nfields > 0 ? ld_f64(s.a.rd[0], dt0, i) : 0.0;
+  if (live && has_die && s.nfields > 0 && v == die_value) {
     if (s.writes) sw_die(s, i);
-    return;
+    live = false;
+  } else if (live && s.writes) {
+    sw_copy(s, i);
   }
-  if (s.writes) sw_copy(s, i);
-  if (i >= c.nrows) return;
+  const bool rows = live && i < c.nrows;
+  const uint32_t b = rows ? c.row_ptr[i] : 0u;
+  const uint32_t deg = rows ? c.row_ptr[i + 1] - b : 0u;
   const uint64_t id = ((uint64_t)s.type_nr << SHIFT_TYPE) | (i + 1);
-  const int64_t vi = s.nfields > 0 ? ld_i64(s.a.rd[0], dt0, i) : 0;
-  uint32_t q = 0;
-  for (uint32_t e = c.row_ptr[i]; e < c.row_ptr[i + 1]; e++) {
-    const uint64_t nid = ((uint64_t)edge_src_type(c, e) << SHIFT_TYPE) | ((uint64_t)c.src[e] + 1);
-    for (int d = 0; d < 2; d++, q++) {
-      int64_t k = append_slot(ap, s.status);
-      if (k < 0) return;
+  const int64_t vi = live && s.nfields > 0 ? ld_i64(s.a.rd[0], dt0, i) : 0;
+  for (uint32_t j = 0; __any_sync(FULL_WARP, j < deg); j++) {
+    const bool has = j < deg;
+    const uint32_t e = b + j;
+    const uint64_t nid =
+        has ? ((uint64_t)edge_src_type(c, e) << SHIFT_TYPE) | ((uint64_t)c.src[e] + 1) : 0;
+    for (int d = 0; d < 2; d++) {
+      const int64_t k = warp_slot(ap.counter, ap.cap, has, s.status, 301);
+      if (k < 0) continue;
       ap.from[k] = d == 0 ? nid : id;
       ap.to[k] = d == 0 ? id : nid;
-      ap.key[k] = order_key(call_pos, i, q);
+      ap.key[k] = order_key(call_pos, i, 2 * j + d);
       if (ap.npayload > 0) {
         if (is_float(pl_dt)) st_f64(ap.payload[0], pl_dt, k, v);
         else st_i64(ap.payload[0], pl_dt, k, vi);

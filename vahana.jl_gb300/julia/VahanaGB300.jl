@@ -16,7 +16,7 @@ module VahanaGB300
 export ModelTypes, register_agenttype!, register_edgetype!, register_param!,
        register_global!, create_model, create_simulation, finish_simulation!,
        copy_simulation, finish_init!, add_agent!, add_agents!, add_edge!, add_edges!,
-       apply!, apply, mapreduce, agentstate, agentstate_flexible, edges, neighborids,
+       apply!, apply, apply_host!, mapreduce, agentstate, agentstate_flexible, edges, neighborids,
        neighborids_iter, neighborstates, neighborstates_iter, neighborstates_flexible,
        neighborstates_flexible_iter, edgestates, edgestates_iter, num_edges, has_edge, num_agents, all_agents,
        all_agentids, add_raster!, connect_raster_neighbors!, move_to!, cellid,
@@ -206,6 +206,33 @@ function apply!(sim::Simulation, f::Symbol, call, read, write;
 end
 apply(sim::Simulation, f::Symbol, call, read, write; kw...) =
     apply!(copy_simulation(sim), f, call, read, write; kw...)
+
+"""
+    apply_host!(sim, transition::Symbol, call, read, write, T, states::Vector{T};
+                add_existing, with_edge, params)
+
+apply! for agent vectors kept in host memory: `states` (the agents of type
+T in index order) are uploaded, the transition runs, and the new states are
+returned as a Vector{T} (vg_apply_host; the download of finished rows
+overlaps the gather kernel of bounded_confidence).
+"""
+function apply_host!(sim::Simulation, f::Symbol, call, read, write, ::Type{T}, states::Vector{T};
+                     add_existing = [], with_edge = nothing, params = Float64[]) where T
+    c, r, w, a = refs(sim, call), refs(sim, read), refs(sim, write), refs(sim, add_existing)
+    we = with_edge === nothing ? Cint(-1) : Cint(sim.model.edges[with_edge])
+    n = length(states)
+    cin = [ft[getfield(s, i) for s in states] for (i, ft) in enumerate(fieldtypes(T))]
+    cout = [Vector{ft}(undef, n) for ft in fieldtypes(T)]
+    pin = Ptr{Cvoid}[pointer(x) for x in cin]
+    pout = Ptr{Cvoid}[pointer(x) for x in cout]
+    GC.@preserve cin cout check(ccall((:vg_apply_host, LIB), Cint,
+                (Ptr{Cvoid}, Cstring, Ptr{Cint}, Cint, Ptr{Cint}, Cint, Ptr{Cint}, Cint,
+                 Ptr{Cint}, Cint, Cint, Ptr{Cdouble}, Cint, Cint, Ptr{Ptr{Cvoid}},
+                 Ptr{Ptr{Cvoid}}, UInt64),
+                sim.h, String(f), c, length(c), r, length(r), w, length(w), a, length(a), we,
+                Float64.(params), length(params), sim.model.agents[T], pin, pout, n))
+    fromcolumns(T, cout, n)
+end
 
 transition_names() =
     Symbol.(split(unsafe_string(ccall((:vg_transition_names, LIB), Cstring, ())), ","))

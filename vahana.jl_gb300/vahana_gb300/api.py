@@ -695,6 +695,36 @@ def apply_(sim, transition, call, read, write, add_existing=(), with_edge=None, 
     return sim
 
 
+def apply_host(sim, transition, call, read, write, T, state, out=None, add_existing=(),
+               with_edge=None, params=()):
+    """apply! with type T's state kept in host memory (vg_apply_host): the
+    columns in `state` (field name -> array of n values) are uploaded, the
+    transition runs, and the new state of those n agents is written into
+    `out` (field name -> preallocated array; allocated when None) and
+    returned.  Pinned arrays (e.g. torch pin_memory tensors' numpy views) let
+    the download overlap the transition's kernels."""
+    t = sim.T(T)
+    n = max([np.size(v) for v in state.values()] or [0])
+    keep, ptr_in = [], (C.c_void_p * max(len(t.fields), 1))()
+    for i, (fname, dt) in enumerate(t.fields):
+        if fname in state:
+            a = np.ascontiguousarray(np.asarray(state[fname], dtype=NP_DTYPES[dt]))
+            keep.append(a)
+            ptr_in[i] = a.ctypes.data
+    if out is None:
+        out = {f: np.empty(n, dtype=NP_DTYPES[dt]) for f, dt in t.fields}
+    ptr_out = (C.c_void_p * max(len(t.fields), 1))()
+    for i, (fname, dt) in enumerate(t.fields):
+        if fname in out:
+            a = out[fname]
+            if a.dtype != np.dtype(NP_DTYPES[dt]) or not a.flags.c_contiguous or a.size < n:
+                raise ValueError("out[%r]: %d contiguous values of %s" % (fname, n, dt))
+            ptr_out[i] = a.ctypes.data
+    args = _apply_args(sim, transition, call, read, write, add_existing, with_edge, params)
+    check(lib().vg_apply_host(sim._h, *args, t.index, ptr_in, ptr_out, n))
+    return out
+
+
 def apply(sim, transition, call, read, write, **kw):
     """apply(sim, f, call, read, write) -- src/Simulation.jl:847-856 (on a copy)"""
     c = copy_simulation(sim)
@@ -702,10 +732,16 @@ def apply(sim, transition, call, read, write, **kw):
     return c
 
 
-def mapreduce(sim, f, op, T, init=None, datatype=None, ordered=False):
+def mapreduce(sim, f, op, T, init=None, datatype=None, ordered=None):
     """mapreduce(sim, f, op, T; init, datatype) -- src/AgentMethods.jl:533-565,
     src/EdgeMethods.jl:972-1001.  `f` is a field name or (cmp, field, value)
-    with cmp in ==, !=, <, >."""
+    with cmp in ==, !=, <, >.
+
+    ordered=None (default): Float + and * fold sequentially in the
+    reference's order (bit-identical), every order-independent reduction
+    takes a parallel tree.  ordered=True forces the sequential fold,
+    ordered=False the tree (Float + and *: within 2 (n - 1) 2^-53 sum|f(x)|
+    of the sequential result)."""
     t = sim.T(T)
     if isinstance(f, str):
         kind, field, arg = MAPS["field"], t.field_index(f), 0.0
@@ -723,7 +759,7 @@ def mapreduce(sim, f, op, T, init=None, datatype=None, ordered=False):
         out_dt, out = 9, C.c_int64()
     if datatype == "bool" and op in ("&", "|") and dt not in ("bool",) and kind == 0:
         out_dt, out = 9, C.c_int64()
-    opc = OPS[op] | (0x100 if ordered else 0)
+    opc = OPS[op] | {None: 0, True: 0x100, False: 0x200}[ordered]
     fn = lib().vg_mapreduce_agents if t.kind == "agent" else lib().vg_mapreduce_edges
     check(fn(sim._h, t.index, field, kind, arg, opc, out_dt, int(init is not None),
              float(init or 0), C.byref(out)))

@@ -15,28 +15,31 @@ class JobSpec(C.Structure):
     _fields_ = [("model", C.c_int), ("n", C.c_uint64), ("mean_degree", C.c_double),
                 ("steps", C.c_int32), ("seed", C.c_uint64), ("beta", C.c_double),
                 ("recovery", C.c_int32), ("eps", C.c_double), ("wmax", C.c_double),
-                ("keep_state", C.c_int)]
+                ("keep_state", C.c_int), ("fail_build", C.c_int)]
 
 
 class JobResult(C.Structure):
     _fields_ = [("id", C.c_int64), ("model", C.c_int), ("n", C.c_uint64), ("steps", C.c_int32),
                 ("arrival_s", C.c_double), ("admit_s", C.c_double), ("finish_s", C.c_double),
                 ("checksum", C.c_uint64), ("summary", C.c_double),
-                ("device_bytes", C.c_uint64)]
+                ("device_bytes", C.c_uint64), ("status", C.c_int), ("error", C.c_char * 124)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["error"] = self.error.decode(errors="replace")
+        return d
 
 
 def sir_job(n, degree=10, steps=50, seed=1, beta=0.05, recovery=7, keep_state=False):
     """The job of models.build_sir(n, degree, beta, recovery, seed) run for `steps`."""
-    return JobSpec(SIR, n, float(degree), steps, seed, beta, recovery, 0.0, 0.0, int(keep_state))
+    return JobSpec(model=SIR, n=n, mean_degree=float(degree), steps=steps, seed=seed, beta=beta,
+                   recovery=recovery, eps=0.0, wmax=0.0, keep_state=int(keep_state))
 
 
 def opinion_job(n, mean_degree=20, steps=50, seed=1, eps=0.3, wmax=1e4, keep_state=False):
     """The job of models.build_opinion(n, mean_degree, 2.5, wmax, eps, seed) run for `steps`."""
-    return JobSpec(OPINION, n, float(mean_degree), steps, seed, 0.0, 0, eps, wmax,
-                   int(keep_state))
+    return JobSpec(model=OPINION, n=n, mean_degree=float(mean_degree), steps=steps, seed=seed,
+                   beta=0.0, recovery=0, eps=eps, wmax=wmax, keep_state=int(keep_state))
 
 
 class Server:
