@@ -177,6 +177,15 @@ int vg_set_param(vg_sim *s, const char *name, double v);
 int vg_param(vg_sim *s, const char *name, double *out);
 int vg_set_global(vg_sim *s, const char *name, double v);
 int vg_get_global(vg_sim *s, const char *name, double *out);
+/* Binds parameter slot `slot` of the named transition to this simulation's
+ * param (kind 0) or global (kind 1) `name`: every later apply! of that
+ * transition passes the current value in that slot, so a transition reads
+ * param(sim, name) / get_global(sim, name) (src/Simulation.jl:587,
+ * src/Global.jl:10) and set_global! between steps reaches the kernels.
+ * apply! must still pass at least slot + 1 parameters (the bound slot's
+ * value is replaced).  vg_unbind_params(s, NULL) removes every binding. */
+int vg_bind_param(vg_sim *s, const char *transition, int slot, int kind, const char *name);
+int vg_unbind_params(vg_sim *s, const char *transition);
 int vg_push_global(vg_sim *s, const char *name, double v);
 int vg_global_series(vg_sim *s, const char *name, double *out, uint64_t cap,
                      uint64_t *n_out);

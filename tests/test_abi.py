@@ -136,6 +136,27 @@ def test_params_and_globals(vh):
     sim.close()
 
 
+def test_bind_param_checks(vh):
+    """Binding a transition's parameter slot to a param or global: unknown
+    names, transitions, kinds and slots are refused (VG_ERR_ARG) before any
+    apply!; rebinding a slot replaces it."""
+    m = (vh.ModelTypes().register_agenttype("A", [("foo", "i64")])
+         .register_param("beta", 0.1).register_global("eps", 0.3).create_model("bind"))
+    sim = vh.create_simulation(m)
+    vh.bind_param(sim, "sir", 1, "beta", kind="param")
+    vh.bind_param(sim, "sir", 1, "eps")  # rebinding the slot to a global
+    vh.bind_param(sim, "bounded_confidence", 1, "eps")
+    for bad in [("sir", 1, "nope", "global"), ("sir", 1, "nope", "param"),
+                ("no_such_transition", 1, "eps", "global"), ("sir", -1, "eps", "global"),
+                ("sir", 64, "eps", "global")]:
+        with pytest.raises(vh.VahanaError):
+            vh.bind_param(sim, *bad[:3], kind=bad[3])
+    assert vh.lib().vg_bind_param(sim._h, b"sir", 1, 2, b"eps") != 0
+    vh.unbind_params(sim, "sir")
+    vh.unbind_params(sim)
+    sim.close()
+
+
 def test_parametric_type_names(vh):
     """test/parametric_types.jl:1-38: a parametric Julia type is registered
     under its full name; agents of it, a plain agent type and a parametric

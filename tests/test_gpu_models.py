@@ -55,6 +55,41 @@ def test_sir_changing_beta_between_steps(vh):
     run.close()
 
 
+def test_sir_beta_bound_to_a_global(vh):
+    """The "sir" transition's beta slot bound to a global of the simulation
+    (get_global inside the transition, src/Global.jl:10): set_global!
+    between apply! calls reaches the kernel; equals the oracle with the same
+    beta sequence."""
+    from vahana_gb300 import api
+    m = (api.ModelTypes()
+         .register_agenttype("Person", [("state", "u8"), ("days", "i32")], ":Immortal")
+         .register_edgetype("Contact", [], ":Stateless", target="Person")
+         .register_global("beta", 0.05)
+         .create_model("SIRg"))
+    from vahana_gb300 import models
+    sim = api.create_simulation(m)
+    st, dy = models.sir_initial_state(3000, 9, 30)
+    api.add_agents(sim, "Person", 3000, state=st, days=dy)
+    from vahana_gb300._lib import check, lib
+    check(lib().vg_gen_uniform_out_edges(sim._h, m["Contact"].index, m["Person"].index, 10, 9))
+    frm, to, _ = models.staged_edges(sim, "Contact")
+    vh.finish_init(sim)
+    vh.bind_param(sim, "sir", 1, "beta")
+    g = om.build_inedges(3000, frm, to)
+    s_ref, d_ref = st.copy(), dy.copy()
+    betas = [0.05, 0.2, 0.2, 0.01, 0.11, 0.3] * 3
+    for t, beta in enumerate(betas):
+        vh.set_global(sim, "beta", beta)
+        vh.apply_(sim, "sir", ["Person"], ["Person", "Contact"], ["Person"],
+                  params=[m["Contact"].index, 0.0, 7, 9])  # slot 1 comes from the global
+        s_ref, d_ref = om.sir_step(g, s_ref, d_ref, beta, 7, 9, t + 1)
+    cols = vh.read_agents(sim, "Person")[0]
+    np.testing.assert_array_equal(cols["state"], s_ref)
+    np.testing.assert_array_equal(cols["days"], d_ref)
+    assert (s_ref == 2).sum() > 0
+    sim.close()
+
+
 NO_SPLIT = 4294967295  # hub threshold that keeps every row on the ordered path
 
 

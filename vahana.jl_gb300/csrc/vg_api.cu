@@ -497,6 +497,7 @@ int vg_sim_copy(vg_sim *h, vg_sim **out) {
   c->params = s.params;
   c->globals = s.globals;
   c->global_series = s.global_series;
+  c->bindings = s.bindings;
   c->rasters = s.rasters;
   c->agents.resize(s.agents.size());
   for (size_t i = 0; i < s.agents.size(); i++) {
@@ -579,6 +580,37 @@ int vg_get_global(vg_sim *h, const char *name, double *out) {
   *out = it->second;
   API_END
 }
+int vg_bind_param(vg_sim *h, const char *transition, int slot, int kind, const char *name) {
+  API_BEGIN
+  Sim &s = S(h);
+  need(transition, "transition name");
+  need(name, "param or global name");
+  bool known = false;
+  for (auto &t : transitions()) known |= std::strcmp(t.name, transition) == 0;
+  if (!known) fail(VG_ERR_ARG, std::string("unknown transition ") + transition);
+  if (slot < 0 || slot >= 64) fail(VG_ERR_ARG, "parameter slot 0..63");
+  if (kind == 0 && !s.params.count(name)) fail(VG_ERR_ARG, std::string("unknown param ") + name);
+  if (kind == 1 && !s.globals.count(name)) fail(VG_ERR_ARG, std::string("unknown global ") + name);
+  if (kind != 0 && kind != 1) fail(VG_ERR_ARG, "kind 0 (param) or 1 (global)");
+  auto &v = s.bindings[transition];
+  for (auto &b : v)
+    if (b.slot == slot) {
+      b.kind = kind;
+      b.name = name;
+      return VG_OK;
+    }
+  v.push_back({slot, kind, name});
+  API_END
+}
+
+int vg_unbind_params(vg_sim *h, const char *transition) {
+  API_BEGIN
+  Sim &s = S(h);
+  if (transition) s.bindings.erase(transition);
+  else s.bindings.clear();
+  API_END
+}
+
 int vg_push_global(vg_sim *h, const char *name, double v) {
   API_BEGIN
   S(h).global_series[name].push_back(v);

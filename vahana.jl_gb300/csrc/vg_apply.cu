@@ -475,6 +475,23 @@ int vg_apply(vg_sim *h, const char *tname, const int *call, int ncall, const int
   ctx.with_edge = with_edge;
   ctx.params = params;
   ctx.nparams = nparams;
+  // slots bound to a param or global take its current value
+  std::vector<double> bound;
+  auto bit = s.bindings.find(tname);
+  if (bit != s.bindings.end() && !bit->second.empty()) {
+    bound.assign(params, params + std::max(nparams, 0));
+    for (auto &b : bit->second) {
+      if (b.slot >= (int)bound.size())
+        fail(VG_ERR_ARG, "parameter slot " + std::to_string(b.slot) + " of " + tname +
+                             " is bound to " + b.name + " but apply! passes " +
+                             std::to_string(nparams) + " parameters");
+      const auto &m = b.kind == 0 ? s.params : s.globals;
+      auto it = m.find(b.name);
+      if (it == m.end()) fail(VG_ERR_ARG, "unknown " + std::string(b.kind ? "global " : "param ") + b.name);
+      bound[b.slot] = it->second;
+    }
+    ctx.params = bound.data();
+  }
   ctx.step = s.num_transitions;
   auto in = [](const std::vector<int> &v, int r) {
     return std::find(v.begin(), v.end(), r) != v.end();

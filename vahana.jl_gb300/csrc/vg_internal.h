@@ -247,6 +247,10 @@ struct Raster {
 
 struct EdgeAppend;
 
+// stencil(metric, n, distance) -- src/Raster.jl:82-110: offsets in the
+// reference's order, n per entry (vg_api.cu)
+std::vector<int> make_stencil(int metric, int n, double distance);
+
 struct Sim {
   std::shared_ptr<Model> model;
   std::string name;
@@ -297,6 +301,15 @@ struct Sim {
     bool done = false;
   };
   HostExchange *host_xchg = nullptr;
+  // parameter slots of a transition bound to a param (kind 0) or global
+  // (kind 1) of this simulation: every apply! of the transition passes the
+  // current value in that slot (param / get_global read inside the
+  // transition, src/Simulation.jl:587, src/Global.jl:10)
+  struct ParamBinding {
+    int slot, kind;
+    std::string name;
+  };
+  std::map<std::string, std::vector<ParamBinding>> bindings;
   cudaStream_t copy_stream = nullptr;   // created on first use, destroyed with the sim
   std::vector<cudaEvent_t> xchg_events;  // one per chunk, created on first use
   ~Sim();

@@ -477,6 +477,100 @@ __global__ void k_link_neighbors(Sweep s, DevCSRView c, Append ap, int pl_dt, in
   }
 }
 
+// ----------------------------------------------- move_to! in a transition
+// move_to!(sim, raster, id, pos, edge_from_raster, edge_to_raster; distance,
+// metric, periodic, only_surrounding) -- src/Raster.jl:437-477 -- called by
+// every swept agent: the cell at pos (unless only_surrounding), then the
+// cells at the stencil offsets in the reference's order, each wrapped
+// (periodic) or dropped when outside the raster (_checkpos,
+// src/Raster.jl:479-499); per cell first the cell -> agent edge
+// (edge_from_raster), then the agent -> cell edge (edge_to_raster).  The
+// order key numbers the calls, so the rebuilt containers hold them in the
+// order of the sequential sweep.  The new position: mode 0 the agent's
+// fields 0..ndims-1 (1-based; the state is kept); mode 1 the Int field
+// `nbr_field` of the agent's first in-neighbour along edge type `nbr_edge`
+// in every dimension, which also becomes the agent's field 0 (the rule of
+// test/raster.jl:309-314).
+struct MoveArgs {
+  int ndims;
+  int64_t dims[MAX_DIMS];
+  int cell_type;
+  uint64_t first_nr;
+  const int32_t *off;  // noff offsets, ndims each
+  int noff;
+  int periodic, only_surrounding;
+  int mode;
+  DevCSRView nbr;       // mode 1: the agent's in-edges
+  const void *nbr_val;  // mode 1: the neighbours' field
+  int nbr_dt;
+  int has_from, has_to, same;  // same: one edge type, one buffer for both
+  Append from, to;
+};
+
+__device__ __forceinline__ void move_emit(const MoveArgs &m, bool want, const int64_t *p,
+                                          uint64_t id, uint64_t key, int *status) {
+  uint64_t lin = 0, mul = 1;
+  for (int d = 0; d < m.ndims; d++) {
+    lin += (uint64_t)(p[d] - 1) * mul;
+    mul *= (uint64_t)m.dims[d];
+  }
+  const uint64_t cell = ((uint64_t)m.cell_type << SHIFT_TYPE) | (m.first_nr + lin);
+  for (int dir = 0; dir < 2; dir++) {
+    if (dir == 0 ? !m.has_from : !m.has_to) continue;  // uniform over the launch
+    const Append &ap = (dir == 1 && !m.same) ? m.to : m.from;
+    const int64_t k = warp_slot(ap.counter, ap.cap, want, status, 301);
+    if (k < 0) continue;
+    ap.to[k] = dir == 0 ? id : cell;
+    ap.from[k] = dir == 0 ? cell : id;
+    ap.key[k] = key + dir;
+    for (int f = 0; f < ap.npayload; f++)  // payload fields zero
+      for (int b = 0; b < ap.psize[f]; b++) ((uint8_t *)ap.payload[f])[k * ap.psize[f] + b] = 0;
+  }
+}
+
+__global__ void k_move_to(Sweep s, MoveArgs m, int call_pos) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = i < s.a.n && sw_begin(s, i);
+  int64_t pos[MAX_DIMS] = {1, 1, 1, 1};
+  bool ok = live;
+  if (live) {
+    if (m.mode == 0) {
+      for (int d = 0; d < m.ndims; d++) pos[d] = ld_i64(s.a.rd[d], s.fdt[d], i);
+    } else {
+      int64_t v = 0;
+      if (i < m.nbr.nrows && m.nbr.row_ptr[i + 1] > m.nbr.row_ptr[i]) {
+        v = ld_i64(m.nbr_val, m.nbr_dt, m.nbr.src[m.nbr.row_ptr[i]]);
+      } else {
+        set_status(s.status, 203);  // first() of no neighbour
+        ok = false;
+      }
+      for (int d = 0; d < m.ndims; d++) pos[d] = v;
+    }
+    for (int d = 0; d < m.ndims; d++)
+      if (pos[d] < 1 || pos[d] > m.dims[d]) ok = false;
+    if (!ok && m.mode == 0) set_status(s.status, 204);  // position outside the raster
+    if (s.writes) {
+      sw_copy(s, i);
+      if (m.mode == 1 && ok) st_i64(s.a.wr[0], s.fdt[0], i, pos[0]);
+    }
+  }
+  const uint64_t id = ((uint64_t)s.type_nr << SHIFT_TYPE) | (i + 1);
+  if (!m.only_surrounding) move_emit(m, ok, pos, id, order_key(call_pos, i, 0), s.status);
+  for (int k = 0; k < m.noff; k++) {
+    int64_t q[MAX_DIMS] = {1, 1, 1, 1};
+    bool in = ok;
+    for (int d = 0; d < m.ndims; d++) {
+      int64_t v = pos[d] + m.off[k * m.ndims + d];
+      if (v < 1 || v > m.dims[d]) {
+        if (!m.periodic) in = false;
+        v = ((v - 1) % m.dims[d] + m.dims[d]) % m.dims[d] + 1;
+      }
+      q[d] = v;
+    }
+    move_emit(m, in, q, id, order_key(call_pos, i, 2 * (uint32_t)(k + 1)), s.status);
+  }
+}
+
 // ---------------------------------------------------------- SIR (cfg 0)
 // Person{state::UInt8 (0 S, 1 I, 2 R), days::Int32}.  A susceptible agent
 // with k infected in-neighbours is infected with p_k = 1 - (1 - beta)^k
@@ -1117,6 +1211,73 @@ void tr_random_walk(ApplyCtx &c) {
   VG_CUDA(cudaGetLastError());
 }
 
+// apply!(sim, move_to, [T], read, write; params = [raster, edge_from
+// (-1: nothing), edge_to (-1: nothing), distance, metric (0 chebyshev, 1
+// euclidean, 2 manhatten), periodic, only_surrounding, mode, nbr_edge,
+// nbr_field]); mode and the last two as in k_move_to.
+void tr_move_to(ApplyCtx &c) {
+  Sim &s = *c.sim;
+  const AgentTypeDesc &ad = s.model->at(c.call_type);
+  const int ri = (int)c.param(0, -1);
+  if (ri < 0 || ri >= (int)s.rasters.size()) fail(VG_ERR_ARG, "move_to: raster index");
+  const Raster &R = s.rasters[ri];
+  const int ef = (int)c.param(1, -1), et = (int)c.param(2, -1);
+  const double distance = c.param(3, 0);
+  const int metric = (int)c.param(4, VG_METRIC_CHEBYSHEV);
+  const int mode = (int)c.param(7, 0);
+  if (metric < 0 || metric > 2) fail(VG_ERR_ARG, "move_to: metric 0..2");
+  if (mode < 0 || mode > 1) fail(VG_ERR_ARG, "move_to: mode 0 (own fields) or 1 (neighbour)");
+  MoveArgs m{};
+  m.ndims = R.ndims;
+  for (int d = 0; d < R.ndims; d++) m.dims[d] = R.dims[d];
+  m.cell_type = R.type_nr;
+  m.first_nr = R.first_nr;
+  m.periodic = c.param(5, 1) != 0;
+  m.only_surrounding = c.param(6, 0) != 0;
+  m.mode = mode;
+  if (mode == 0) {
+    if ((int)ad.fields.size() < R.ndims) fail(VG_ERR_ARG, "move_to: one Int field per dimension");
+    for (int d = 0; d < R.ndims; d++)
+      if (ad.fields[d].dtype == VG_F32 || ad.fields[d].dtype == VG_F64)
+        fail(VG_ERR_ARG, "move_to: the position fields are integers");
+    require_agent_read(c, c.call_type);
+  } else {
+    const int ne = need_edge_param(c, 8);
+    require_edge_read(c, ne);
+    m.nbr = csr_view(s, ne, c.call_type);
+    const int src_t = m.nbr.src_type_const;
+    if (m.nbr.nedges && src_t <= 0) fail(VG_ERR_ARG, "move_to: neighbours of one agent type");
+    if (ad.fields.empty() || ad.fields[0].dtype == VG_F32 || ad.fields[0].dtype == VG_F64)
+      fail(VG_ERR_ARG, "move_to: mode 1 writes the position to an Int field 0");
+    if (m.nbr.nedges) {
+      require_agent_read(c, src_t);
+      const AgentTypeDesc &nd = s.model->at(src_t);
+      const int nf = (int)c.param(9, 0);
+      if (nf < 0 || nf >= (int)nd.fields.size()) fail(VG_ERR_ARG, "move_to: neighbour field");
+      m.nbr_val = s.agents[src_t - 1].rd[nf].p;
+      m.nbr_dt = nd.fields[nf].dtype;
+    }
+  }
+  Sweep w = make_sweep(c);
+  if (w.a.n == 0) return;
+  std::vector<int> off = distance >= 1 ? make_stencil(metric, R.ndims, distance) : std::vector<int>();
+  m.noff = (int)(off.size() / std::max(1, R.ndims));
+  if (m.noff > (1 << 18)) fail(VG_ERR_ARG, "move_to: stencil too large");
+  std::vector<int32_t> off32(off.begin(), off.end());
+  const std::string key = "move_to:" + std::to_string(metric) + ":" + std::to_string(R.ndims) +
+                          ":" + std::to_string(distance);
+  m.off = off32.empty() ? nullptr
+                        : (const int32_t *)s.const_table(key, off32.data(), off32.size() * 4);
+  const uint64_t per = (uint64_t)(m.only_surrounding ? 0 : 1) + (uint64_t)m.noff;
+  m.has_from = ef >= 0;
+  m.has_to = et >= 0;
+  m.same = m.has_from && m.has_to && ef == et;
+  if (m.has_from) m.from = make_append(c, ef, std::max<uint64_t>(1, w.a.n * per * (m.same ? 2 : 1)));
+  if (m.has_to && !m.same) m.to = make_append(c, et, std::max<uint64_t>(1, w.a.n * per));
+  k_move_to<<<nblk(w.a.n), TPB, 0, s.stream>>>(w, m, c.call_pos);
+  VG_CUDA(cudaGetLastError());
+}
+
 }  // namespace
 
 const std::vector<TransitionDef> &transitions() {
@@ -1125,6 +1286,7 @@ const std::vector<TransitionDef> &transitions() {
       {"sir", tr_sir},
       {"life", tr_life},
       {"random_walk", tr_random_walk},
+      {"move_to", tr_move_to},
       {"neighbor_sum", tr_neighbor_sum},
       {"neighbor_or", tr_neighbor_or},
       {"count_edges", tr_count_edges},

@@ -20,7 +20,7 @@ export ModelTypes, register_agenttype!, register_edgetype!, register_param!,
        neighborids_iter, neighborstates, neighborstates_iter, neighborstates_flexible,
        neighborstates_flexible_iter, edgestates, edgestates_iter, num_edges, has_edge, num_agents, all_agents,
        all_agentids, add_raster!, connect_raster_neighbors!, move_to!, cellid,
-       rastervalues, calc_rasterstate, param, set_param!, get_global, set_global!,
+       rastervalues, calc_rasterstate, param, set_param!, get_global, set_global!, bind_param!,
        push_global!, disable_transition_checks, transition_names, Edge, AgentID,
        add_graph!, remove_edges!, add_agent_per_process!, write_snapshot, read_snapshot
 
@@ -507,6 +507,17 @@ get_global(sim::Simulation, name::Symbol) =
                                       (Ptr{Cvoid}, Cstring, Ptr{Cdouble}), sim.h, String(name), v)); v[])
 set_global!(sim::Simulation, name::Symbol, v) =
     check(ccall((:vg_set_global, LIB), Cint, (Ptr{Cvoid}, Cstring, Cdouble), sim.h, String(name), v))
+
+"""
+    bind_param!(sim, transition::Symbol, slot, name::Symbol; kind = :global)
+
+Parameter `slot` (0-based) of every later apply! of `transition` takes the
+current value of the global (or, kind = :param, the param) `name`: the
+kernel reads get_global(sim, name) / param(sim, name) at each step.
+"""
+bind_param!(sim::Simulation, f::Symbol, slot::Integer, name::Symbol; kind = :global) =
+    check(ccall((:vg_bind_param, LIB), Cint, (Ptr{Cvoid}, Cstring, Cint, Cint, Cstring),
+                sim.h, String(f), slot, kind === :param ? 0 : 1, String(name)))
 push_global!(sim::Simulation, name::Symbol, v) =
     check(ccall((:vg_push_global, LIB), Cint, (Ptr{Cvoid}, Cstring, Cdouble), sim.h, String(name), v))
 

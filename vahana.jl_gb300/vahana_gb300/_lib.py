@@ -78,6 +78,8 @@ SIGNATURES = {
     "vg_model_register_agenttype": (I, [P, CP, I, C.POINTER(CP), PI, C.c_uint, PI]),
     "vg_model_register_edgetype": (I, [P, CP, I, C.POINTER(CP), PI, C.c_uint, I, I64, PI]),
     "vg_model_register_param": (I, [P, CP, D]),
+    "vg_bind_param": (I, [P, CP, I, I, CP]),
+    "vg_unbind_params": (I, [P, CP]),
     "vg_model_register_global": (I, [P, CP, D]),
     "vg_model_finalize": (I, [P, CP]),
     "vg_model_edge_hints": (I, [P, I, C.POINTER(C.c_uint)]),

@@ -286,6 +286,18 @@ def get_global(sim, name):
     return v.value
 
 
+def bind_param(sim, transition, slot, name, kind="global"):
+    """Parameter slot `slot` of every later apply! of `transition` takes the
+    current value of this simulation's global (or param) `name` -- the
+    transition reads get_global(sim, name) / param(sim, name)."""
+    check(lib().vg_bind_param(sim._h, transition.encode(), int(slot),
+                              {"param": 0, "global": 1}[kind], name.encode()))
+
+
+def unbind_params(sim, transition=None):
+    check(lib().vg_unbind_params(sim._h, transition.encode() if transition else None))
+
+
 def push_global(sim, name, v):
     check(lib().vg_push_global(sim._h, name.encode(), float(v)))
 
