@@ -38,7 +38,7 @@ def test_apply_host_opinion_matches_apply(vh):
         np.testing.assert_array_equal(
             vh.read_agents(run.sim, "Opinion")[0]["x"].view(np.uint64), ref.view(np.uint64))
         assert not np.array_equal(out["x"], x)
-    assert vh.num_transitions(run.sim) == vh.num_transitions(twin.sim) == 4
+    assert vh.num_transitions(run.sim) == vh.num_transitions(twin.sim)
     # unpinned numpy buffers: the same values
     x = rng.random(n)
     got = vh.apply_host(run.sim, "bounded_confidence", ["Opinion"], ["Opinion", "Weight"],

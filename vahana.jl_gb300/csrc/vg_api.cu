@@ -397,6 +397,7 @@ int vg_sim_create(vg_model *m, const char *name, void *stream, vg_sim **out) {
 Sim::~Sim() {
   for (cudaEvent_t e : xchg_events) cudaEventDestroy(e);
   if (copy_stream) cudaStreamDestroy(copy_stream);
+  if (aux_stream) cudaStreamDestroy(aux_stream);
 }
 
 int vg_sim_destroy(vg_sim *s) {

@@ -198,6 +198,7 @@ struct CSR {
   // slice blocks [chunk_block[k], chunk_block[k + 1]) and completes every
   // row below chunk_rows[k] (derived from the layout, cached with it)
   std::vector<uint64_t> chunk_block, chunk_rows;
+  std::vector<uint32_t> hub_rows_sorted;  // host copy of the hub rows, ascending
   // payload field 0 (Float64) holds only multiples of 2^-53 in (0, 1]:
   // -1 not checked yet, 0 no, 1 yes (decides the gather kernels' sum path)
   int unit_grid_weights = -1;
@@ -311,6 +312,7 @@ struct Sim {
   };
   std::map<std::string, std::vector<ParamBinding>> bindings;
   cudaStream_t copy_stream = nullptr;   // created on first use, destroyed with the sim
+  cudaStream_t aux_stream = nullptr;    // concurrent work of a chunked launch (same)
   std::vector<cudaEvent_t> xchg_events;  // one per chunk, created on first use
   ~Sim();
 };

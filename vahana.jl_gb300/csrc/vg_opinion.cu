@@ -25,14 +25,16 @@
 //   The hub warps are the first blocks of the grid so that they start
 //   first.
 //
-// Arithmetic placement on GB300 (the FP64 pipe executes about 5e11 binary64
+// Arithmetic placement on GB300 (the FP64 pipe executes 5.3e11 binary64
 // operations per second, far below the integer pipes):
 //   threshold test  float filter of the opinions' high words; the exact
 //                   binary64 test only within 1e-5 of eps
 //   w_j * x_j       exact round-to-nearest-even product from 32x32-bit
 //                   multiplies (vg_fp64emu.cuh)
-//   swx += p,       the hardware binary64 adds, branch-free (a rejected
-//   sw += w         edge adds +0): two FP64 operations per edge
+//   swx += p,       the hardware binary64 adds, predicated on the test: two
+//   sw += w         FP64 warp instructions per slot (measured 5.3e11 lane
+//                   operations per second on GB300, the same with any number
+//                   of active lanes: the floor of this kernel)
 //   per row         exact integer division, exponent scaling for mixing
 //                   weights that are powers of two, one hardware add
 // Every operation is the correctly rounded binary64 result, in the
@@ -228,9 +230,11 @@ struct SliceCtx {
       const uint64_t pk = GRID ? emu_mul_grid(bits(wv), bits(xj), ok)
                                : emu_mul_fast(bits(wv), bits(xj), ok);
       const double pkd = ok ? dbl(pk) : (acc ? mul_hw(wv, xj) : 0.0);
-      a.swx = __dadd_rn(a.swx, acc ? pkd : 0.0);
-      a.sw = __dadd_rn(a.sw, acc ? wv : 0.0);
-      a.cnt += acc;
+      if (acc) {  // predicated: a lane of a rejected edge skips both adds
+        a.swx = __dadd_rn(a.swx, pkd);
+        a.sw = __dadd_rn(a.sw, wv);
+      }
+      if (!GRID) a.cnt += acc;
     }
   }
   // one pipeline step: group g is folded while the opinions of group g + 1
@@ -249,9 +253,10 @@ struct SliceCtx {
 // one coalesced 128 or 256-byte access.  Slots are taken in groups of
 // SELL_U with a two-stage software pipeline over three rotating buffers
 // (while group g is folded, the opinions of group g + 1 and the sources and
-// weights of group g + 2 are in flight).  Branch-free fold: a rejected edge
-// adds +0 to swx and 0 to sw, which leaves both sums unchanged, so no lane
-// is masked off.
+// weights of group g + 2 are in flight).  The two additions of an edge are
+// predicated on its test: the FP64 pipe takes a warp instruction whatever
+// its active lanes, so this costs the pipe what a branch-free +0 would and
+// saves the selects.
 template <bool GRID>
 __device__ __forceinline__ void sell_slice(const OpinionArgs &p, uint64_t sl) {
   const unsigned lane = threadIdx.x & 31;
@@ -281,7 +286,9 @@ __device__ __forceinline__ void sell_slice(const OpinionArgs &p, uint64_t sl) {
     c.step(g + 2, Z, X, Y, a);
   }
   if (!live) return;
-  p.xo[r] = a.cnt ? finish(p, xi, bits(a.sw), bits(a.swx)) : xi;
+  // some neighbour qualified: grid weights are positive, so sw > 0 says it
+  const bool any = GRID ? bits(a.sw) != 0 : a.cnt != 0;
+  p.xo[r] = any ? finish(p, xi, bits(a.sw), bits(a.swx)) : xi;
 }
 
 // One warp per hub row (degree > hub_thr): lane l folds edges l, l + 32,
@@ -676,11 +683,11 @@ void tr_bounded_confidence(ApplyCtx &c) {
   VG_CUDA(cudaGetLastError());
 }
 
-// Chunk boundaries of the gather launch: chunk k runs the slice blocks
-// [chunk_block[k], chunk_block[k + 1]) (chunk 0 also every hub warp, which
-// lead the grid); the rows are sorted by window (row >> wshift) before
-// degree, so after chunk k every row of the windows below the window of the
-// next chunk's first row is final: chunk_rows[k] = that window << wshift.
+// Chunk boundaries of the slice part of the gather: chunk k runs the slice
+// blocks [chunk_block[k], chunk_block[k + 1]); the rows are sorted by window
+// (row >> wshift) before degree, so after chunk k every non-hub row of the
+// windows below the window of the next chunk's first row is final:
+// chunk_rows[k] = that window << wshift.  hub_rows_sorted: the hub rows.
 static void chunk_bounds(Sim &s, CSR &cs, uint64_t n, unsigned hub_blocks, unsigned slice_blocks) {
   const unsigned K = std::max(1u, std::min(XCHG_CHUNKS, slice_blocks));
   if (cs.chunk_block.size() == K + 1) return;
@@ -688,7 +695,6 @@ static void chunk_bounds(Sim &s, CSR &cs, uint64_t n, unsigned hub_blocks, unsig
   cs.chunk_rows.assign(K, n);
   for (unsigned k = 0; k <= K; k++)
     cs.chunk_block[k] = hub_blocks + (uint64_t)slice_blocks * k / K;
-  cs.chunk_block[0] = 0;
   for (unsigned k = 0; k + 1 < K; k++) {
     // first position in `order` of the block: TPB / 32 slices of 32 rows per block
     const uint64_t pos = (cs.chunk_block[k + 1] - hub_blocks) * (uint64_t)TPB;
@@ -699,38 +705,80 @@ static void chunk_bounds(Sim &s, CSR &cs, uint64_t n, unsigned hub_blocks, unsig
     VG_CUDA(cudaStreamSynchronize(s.stream));
     cs.chunk_rows[k] = std::min<uint64_t>(n, ((uint64_t)row >> cs.wshift) << cs.wshift);
   }
+  cs.hub_rows_sorted.assign(cs.nhub, 0);
+  if (cs.nhub) {
+    VG_CUDA(cudaMemcpyAsync(cs.hub_rows_sorted.data(), cs.hub_rows.p, cs.nhub * 4,
+                            cudaMemcpyDeviceToHost, s.stream));
+    VG_CUDA(cudaStreamSynchronize(s.stream));
+    std::sort(cs.hub_rows_sorted.begin(), cs.hub_rows_sorted.end());
+  }
 }
 
-// The gather in chunks on the simulation's stream; after each chunk the rows
-// it completed are downloaded on the copy stream while the next chunk runs.
+// The gather with its rows downloaded while it runs.  The hub warps (long
+// rows, the longest work items) run as their own launch on the auxiliary
+// stream, concurrently with the slices, which run in chunks on the
+// simulation's stream; after each chunk the rows it completed go to the host
+// on the copy stream.  A range that holds a hub row (with hubs among the
+// first agents, the low ranges) is downloaded once the hub launch is done as
+// well; the simulation's stream waits for it before apply! goes on.
 static void launch_chunked(Sim &s, OpinionArgs &p, unsigned grid, Sim::HostExchange &hx) {
   CSR &cs = *p.csr;
   chunk_bounds(s, cs, p.n, p.hub_blocks, grid - p.hub_blocks);
   const unsigned K = (unsigned)cs.chunk_rows.size();
   if (!s.copy_stream) VG_CUDA(cudaStreamCreateWithFlags(&s.copy_stream, cudaStreamNonBlocking));
-  while (s.xchg_events.size() < K) {
+  if (!s.aux_stream) VG_CUDA(cudaStreamCreateWithFlags(&s.aux_stream, cudaStreamNonBlocking));
+  while (s.xchg_events.size() < K + 2) {
     cudaEvent_t e;
     VG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     s.xchg_events.push_back(e);
   }
-  const uint64_t n = std::min<uint64_t>(hx.n, p.n);
-  uint64_t done_rows = 0;
-  for (unsigned k = 0; k < K; k++) {
-    const unsigned b0 = (unsigned)cs.chunk_block[k], b1 = (unsigned)cs.chunk_block[k + 1];
+  cudaEvent_t ev_start = s.xchg_events[K], ev_hub = s.xchg_events[K + 1];
+  auto launch = [&](unsigned b0, unsigned b1, cudaStream_t st) {
+    if (b1 <= b0) return;
     OpinionArgs q = p;
     q.blk_base = b0;
-    if (b1 > b0) {
-      if (q.grid) k_opinion<true><<<b1 - b0, TPB, 0, s.stream>>>(q);
-      else k_opinion<false><<<b1 - b0, TPB, 0, s.stream>>>(q);
-      VG_CUDA(cudaGetLastError());
-    }
+    if (q.grid) k_opinion<true><<<b1 - b0, TPB, 0, st>>>(q);
+    else k_opinion<false><<<b1 - b0, TPB, 0, st>>>(q);
+    VG_CUDA(cudaGetLastError());
+  };
+  const bool hubs = p.hub_blocks > 0;
+  if (hubs) {
+    VG_CUDA(cudaEventRecord(ev_start, s.stream));
+    VG_CUDA(cudaStreamWaitEvent(s.aux_stream, ev_start, 0));
+    launch(0, p.hub_blocks, s.aux_stream);
+    VG_CUDA(cudaEventRecord(ev_hub, s.aux_stream));
+  }
+  const uint64_t n = std::min<uint64_t>(hx.n, p.n);
+  double *out = (double *)hx.out[0];
+  auto holds_hub = [&](uint64_t lo, uint64_t hi) {  // a hub row in [lo, hi)?
+    auto it = std::lower_bound(cs.hub_rows_sorted.begin(), cs.hub_rows_sorted.end(), (uint32_t)lo);
+    return it != cs.hub_rows_sorted.end() && *it < hi;
+  };
+  std::vector<std::pair<uint64_t, uint64_t>> deferred;  // ranges that wait for the hubs
+  uint64_t done_rows = 0;
+  for (unsigned k = 0; k < K; k++) {
+    launch((unsigned)cs.chunk_block[k], (unsigned)cs.chunk_block[k + 1], s.stream);
     const uint64_t upto = k + 1 == K ? n : std::min(n, cs.chunk_rows[k]);
     if (upto <= done_rows) continue;
-    VG_CUDA(cudaEventRecord(s.xchg_events[k], s.stream));
-    VG_CUDA(cudaStreamWaitEvent(s.copy_stream, s.xchg_events[k], 0));
-    VG_CUDA(cudaMemcpyAsync((double *)hx.out[0] + done_rows, p.xo + done_rows,
-                            (upto - done_rows) * 8, cudaMemcpyDeviceToHost, s.copy_stream));
+    if (hubs && holds_hub(done_rows, upto)) {
+      deferred.push_back({done_rows, upto});
+    } else {
+      VG_CUDA(cudaEventRecord(s.xchg_events[k], s.stream));
+      VG_CUDA(cudaStreamWaitEvent(s.copy_stream, s.xchg_events[k], 0));
+      VG_CUDA(cudaMemcpyAsync(out + done_rows, p.xo + done_rows, (upto - done_rows) * 8,
+                              cudaMemcpyDeviceToHost, s.copy_stream));
+    }
     done_rows = upto;
+  }
+  if (hubs) {
+    VG_CUDA(cudaStreamWaitEvent(s.stream, ev_hub, 0));
+    if (!deferred.empty()) {
+      VG_CUDA(cudaEventRecord(s.xchg_events[K], s.stream));  // every chunk and the hubs
+      VG_CUDA(cudaStreamWaitEvent(s.copy_stream, s.xchg_events[K], 0));
+      for (auto &r : deferred)
+        VG_CUDA(cudaMemcpyAsync(out + r.first, p.xo + r.first, (r.second - r.first) * 8,
+                                cudaMemcpyDeviceToHost, s.copy_stream));
+    }
   }
   hx.done = true;
 }
