@@ -442,10 +442,25 @@ int vg_batch_create_sir(int n, const int64_t *N, const int32_t *deg,
                         const double *beta, const int32_t *rec,
                         const uint64_t *seeds, int64_t n_init_infected_per_1000,
                         void *stream, vg_batch **out);
-/* Advance every instance by `steps` transitions.  mode 0: one persistent
- * kernel per step over all instances; mode 1: the same, with the step
- * loop captured once in a CUDA graph and replayed. */
+/* Advance every instance by `steps` transitions.  mode 0: one launch per
+ * step over all instances; mode 1: the same, with the step loop captured
+ * once in a CUDA graph and replayed; mode 2: one persistent cooperative
+ * launch for all the steps (grid-wide barrier between steps, bounded: a
+ * wait that runs out is reported as VG_ERR_DEVICE, status 0x5e04); mode 3:
+ * mode 1 or 2, whichever the autotuner measured faster.  The first call
+ * runs the autotuner (on copies of the state). */
 int vg_batch_step(vg_batch *b, int steps, int mode);
+/* The autotuner's choice: persistent (1) or graph replay (0), the
+ * persistent block size, its degree-bucket threshold (agents with more
+ * in-edges take a warp each; 0xFFFFFFFF none) and how many agents are
+ * above it.  Runs the autotuner if it has not run. */
+int vg_batch_tuning(vg_batch *b, int *persistent, int *persistent_tpb,
+                    uint32_t *bucket_threshold, uint64_t *heavy_agents);
+/* Overrides the autotuner: mode 3 then takes the persistent launch
+ * (persistent != 0) or the graph, and the persistent launch uses this block
+ * size (128, 256, 512) and bucket threshold. */
+int vg_batch_set_launch(vg_batch *b, int persistent, int persistent_tpb,
+                        uint32_t bucket_threshold);
 /* Plain path for comparison: step instance i alone with the plain kernels. */
 int vg_batch_step_one(vg_batch *b, int i, int steps);
 int vg_batch_read_states(vg_batch *b, int i, uint8_t *state_out,

@@ -44,3 +44,31 @@ def test_batch_equals_plain_and_oracle(vh):
     info = b.info()
     assert info["agents"] == int(N.sum()) and info["tpb"] in (128, 256, 512)
     b.close()
+
+
+def test_batch_persistent_equals_plain(vh):
+    """The persistent launch (all steps in one cooperative launch, a
+    grid-wide barrier between steps), with and without the warp-per-agent
+    bucket for agents above 8 in-edges, interleaved with the other forms:
+    every instance bit-identical to its plain apply! run."""
+    from vahana_gb300 import models
+    N, deg, beta, rec, seeds = small_params(20)
+    b = models.Batch(N, deg, beta, rec, seeds)
+    t = b.tuning()
+    assert t["persistent_tpb"] in (256, 512)
+    total = 0
+    for mode, steps, forced in ((2, 6, None), (2, 5, None), (1, 4, None), (3, 7, (1, 256, 8)),
+                                (2, 3, (1, 512, 8)), (0, 2, None), (3, 5, (0, 256, 8))):
+        if forced:
+            b.set_launch(*forced)
+        b.step(steps, mode=mode)
+        total += steps
+    assert b.tuning()["heavy_agents"] > 0  # threshold 8: the bucket path ran
+    for i in range(b.n):
+        b.step_one(i, total)
+    for i in range(b.n):
+        sb, db = b.states(i, which=0)
+        sp, dp = b.states(i, which=1)
+        np.testing.assert_array_equal(sb, sp)
+        np.testing.assert_array_equal(db, dp)
+    b.close()

@@ -128,7 +128,7 @@ def test_ensemble_full_size(vh):
     from vahana_gb300 import models
     N, deg, beta, rec, seeds = models.batch_params(512)
     b = models.Batch(N, deg, beta, rec, seeds)
-    b.step(200, mode=1)
+    b.step(200, mode=3)  # the autotuner's form
     for i in range(b.n):
         b.step_one(i, 200)
     bad = []

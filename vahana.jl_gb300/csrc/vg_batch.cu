@@ -10,7 +10,9 @@
 // agent's instance), so a step costs one launch instead of one per
 // instance; the step loop can be captured once in a CUDA graph and
 // replayed.  Launch shape (block size, agents per thread) comes from a
-// small autotuner keyed on the arena's degree histogram.
+// small autotuner keyed on the arena's degree histogram; the persistent
+// form runs every step in one cooperative launch with a grid-wide barrier
+// between steps, and the autotuner picks it when it measures faster.
 //
 // The plain path of the same instances (vg_batch_step_one) runs apply! on
 // the instance's own simulation; both paths produce bit-identical states.
@@ -84,6 +86,125 @@ __global__ void k_batch_sir(BatchArgs a) {
   }
 }
 
+// ---- persistent form: one cooperative launch runs every step.  Blocks
+// meet at a grid-wide barrier between steps (all blocks are resident: the
+// launch is cooperative).  The states a step reads were written by other
+// blocks in the previous step of the same launch, so they are loaded at L2
+// (ld.global.cg), never through a non-coherent cache.  Agents whose
+// in-degree exceeds the bucket threshold (listed in `heavy`) are folded by a
+// warp each (the infected-neighbour count is an integer: any order gives the
+// same k); the others by a thread each.
+struct PersistArgs {
+  BatchArgs a;                 // graph, tables; state pointers unused
+  uint8_t *st[2];
+  int32_t *dy[2];
+  int cur0;                    // buffer of the state before the first step
+  uint32_t steps, step0;       // steps to run, transition number of the first
+  const uint32_t *heavy;       // agents above the bucket threshold (nheavy)
+  uint64_t nheavy;
+  const uint8_t *is_heavy;     // per agent (null: no heavy agents)
+  unsigned *bar;               // [0] arrivals, [1] generation
+};
+
+constexpr uint32_t BAR_SPIN_LIMIT = 1u << 22;
+constexpr int BAR_ERR_WAIT = 0x5e04;
+
+// Sense-free grid barrier on a generation counter; a wait that runs out
+// records BAR_ERR_WAIT and returns false (the launch then ends).
+__device__ bool grid_barrier(unsigned *bar, unsigned nblocks, int *status) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ok = 1;
+    volatile unsigned *gen = bar + 1;
+    const unsigned g = *gen;
+    __threadfence();
+    if (atomicAdd(bar, 1u) == nblocks - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      uint32_t i = 0;
+      while (*gen == g) {
+        if (++i >= BAR_SPIN_LIMIT) {
+          atomicCAS(status, 0, BAR_ERR_WAIT);
+          ok = 0;
+          break;
+        }
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// the rule of transition "sir" for agent i with k infected in-neighbours
+__device__ __forceinline__ void sir_rule(const BatchArgs &a, uint64_t i, uint32_t k, uint8_t s,
+                                         int32_t d, uint32_t step, uint8_t *st_wr,
+                                         int32_t *d_wr) {
+  const uint32_t in = a.inst[i];
+  if (s == 0) {
+    if (k > 0) {
+      if (k >= a.kmax1) {
+        atomicCAS(a.status, 0, 402);
+      } else {
+        const uint64_t nr = i - a.base[in] + 1;
+        const double u = u64_to_unit(philox_u64(philox_draw(a.seed[in], nr, step, TAG_INFECT)));
+        if (u < a.ptab[(uint64_t)in * a.kmax1 + k]) {
+          s = 1;
+          d = 0;
+        }
+      }
+    }
+  } else if (s == 1) {
+    d = d + 1;
+    if (d >= a.rec[in]) s = 2;
+  }
+  st_wr[i] = s;
+  d_wr[i] = d;
+}
+
+__global__ void k_batch_persist(PersistArgs p) {
+  const BatchArgs &a = p.a;
+  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint64_t nwarps = nthreads / 32, wid = tid / 32;
+  const unsigned lane = threadIdx.x & 31;
+  for (uint32_t t = 0; t < p.steps; t++) {
+    const int cur = p.cur0 ^ (int)(t & 1);
+    const uint8_t *st_rd = p.st[cur];
+    const int32_t *d_rd = p.dy[cur];
+    uint8_t *st_wr = p.st[1 - cur];
+    int32_t *d_wr = p.dy[1 - cur];
+    const uint32_t step = p.step0 + t;
+    for (uint64_t i = tid; i < a.n; i += nthreads) {  // thread per agent
+      if (p.is_heavy && p.is_heavy[i]) continue;
+      const uint8_t s = __ldcg(st_rd + i);
+      const int32_t d = __ldcg(d_rd + i);
+      uint32_t k = 0;
+      if (s == 0) {
+        const uint32_t e = a.rp[i + 1];
+        for (uint32_t q = a.rp[i]; q < e; q++) k += (__ldcg(st_rd + a.src[q]) == 1);
+      }
+      sir_rule(a, i, k, s, d, step, st_wr, d_wr);
+    }
+    for (uint64_t h = wid; h < p.nheavy; h += nwarps) {  // warp per heavy agent
+      const uint64_t i = p.heavy[h];
+      const uint8_t s = __ldcg(st_rd + i);
+      const int32_t d = __ldcg(d_rd + i);
+      uint32_t k = 0;
+      if (s == 0) {
+        const uint32_t e = a.rp[i + 1];
+        for (uint32_t q = a.rp[i] + lane; q < e; q += 32) k += (__ldcg(st_rd + a.src[q]) == 1);
+      }
+      k = __reduce_add_sync(0xffffffffu, k);
+      if (lane == 0) sir_rule(a, i, k, s, d, step, st_wr, d_wr);
+    }
+    if (t + 1 < p.steps && !grid_barrier(p.bar, gridDim.x, a.status)) return;
+  }
+}
+
 __global__ void k_offset_rp(const uint32_t *rp, uint64_t nrows, uint32_t ebase, uint32_t *out) {
   uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r <= nrows) out[r] = rp[r] + ebase;
@@ -137,7 +258,23 @@ struct vg_batch {
   int64_t step = 1;  // transition number of the next step (as after finish_init!)
   int tpb = 256, apt = 1;
   bool tuned = false;
-  std::map<uint64_t, std::pair<int, int>> tune_cache;
+  struct Tuned {
+    int tpb, apt, p_tpb;
+    uint32_t p_thr;
+    bool persistent;
+  };
+  std::map<uint64_t, Tuned> tune_cache;
+  // persistent form: block size, bucket threshold (agents with more
+  // in-edges take a warp each; 0xFFFFFFFF: none) and whether the autotuner
+  // found it faster than the graph of per-step launches
+  int p_tpb = 256;
+  uint32_t p_thr = 0xFFFFFFFFu;
+  bool prefer_persistent = false;
+  std::vector<uint32_t> host_rp;       // arena row pointers (autotuner, buckets)
+  uint32_t heavy_thr = 0xFFFFFFFFu;    // threshold the heavy list was built for
+  DevBuf heavy, is_heavy, bar;
+  uint64_t nheavy = 0;
+  DevBuf scratch_st[2], scratch_dy[2];  // autotuner trials run on copies of the state
   // CUDA graphs of `graph_steps` steps, one per starting buffer parity; the
   // step number comes from step_base (device) + the node's offset
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
@@ -169,6 +306,69 @@ BatchArgs batch_args(vg_batch *b, int cur, uint32_t step, const int64_t *step_ba
   return a;
 }
 
+void check_batch_status(vg_batch *b) {
+  int h = 0;
+  VG_CUDA(cudaMemcpyAsync(&h, b->status.p, 4, cudaMemcpyDeviceToHost, b->stream));
+  VG_CUDA(cudaStreamSynchronize(b->stream));
+  if (h) fail(VG_ERR_DEVICE, "batched SIR step: device status " + std::to_string(h));
+}
+
+// the heavy agents (in-degree > thr) of the arena, as a list and as flags
+void build_buckets(vg_batch *b, uint32_t thr) {
+  if (b->heavy_thr == thr && (thr == 0xFFFFFFFFu || b->is_heavy.p)) return;
+  b->heavy_thr = thr;
+  b->nheavy = 0;
+  b->heavy.release();
+  b->is_heavy.release();
+  if (thr == 0xFFFFFFFFu) return;
+  std::vector<uint32_t> h;
+  std::vector<uint8_t> flag(b->total, 0);
+  for (uint64_t i = 0; i < b->total; i++)
+    if (b->host_rp[i + 1] - b->host_rp[i] > thr) {
+      h.push_back((uint32_t)i);
+      flag[i] = 1;
+    }
+  b->nheavy = h.size();
+  b->is_heavy.alloc(std::max<uint64_t>(b->total, 1), &b->footprint);
+  VG_CUDA(cudaMemcpyAsync(b->is_heavy.p, flag.data(), b->total, cudaMemcpyHostToDevice, b->stream));
+  if (!h.empty()) {
+    b->heavy.alloc(h.size() * 4, &b->footprint);
+    VG_CUDA(cudaMemcpyAsync(b->heavy.p, h.data(), h.size() * 4, cudaMemcpyHostToDevice, b->stream));
+  }
+  VG_CUDA(cudaStreamSynchronize(b->stream));
+}
+
+// one cooperative launch of `steps` steps from buffer `cur` (states in
+// st/dy), the first with transition number step0
+void launch_persistent(vg_batch *b, uint8_t *const st[2], int32_t *const dy[2], int cur,
+                       uint32_t step0, uint32_t steps, int tpb, uint32_t thr) {
+  build_buckets(b, thr);
+  if (!b->bar.p) b->bar.alloc(8, &b->footprint);
+  PersistArgs p{};
+  p.a = batch_args(b, cur, step0, nullptr);
+  p.st[0] = st[0];
+  p.st[1] = st[1];
+  p.dy[0] = dy[0];
+  p.dy[1] = dy[1];
+  p.cur0 = cur;
+  p.steps = steps;
+  p.step0 = step0;
+  p.heavy = b->heavy.as<uint32_t>();
+  p.nheavy = b->nheavy;
+  p.is_heavy = b->nheavy ? b->is_heavy.as<uint8_t>() : nullptr;
+  p.bar = b->bar.as<unsigned>();
+  int dev = 0, sms = 0, per_sm = 0;
+  VG_CUDA(cudaGetDevice(&dev));
+  VG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  VG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_persist, tpb, 0));
+  if (per_sm < 1) fail(VG_ERR_CUDA, "persistent batch kernel: no block fits an SM");
+  unsigned grid = (unsigned)(sms * per_sm);  // every block resident: the barrier may wait
+  VG_CUDA(cudaMemsetAsync(b->bar.p, 0, 8, b->stream));
+  void *args[] = {&p};
+  VG_CUDA(cudaLaunchCooperativeKernel((const void *)k_batch_persist, dim3(grid), dim3(tpb), args, 0,
+                                      b->stream));
+}
+
 void launch_step(vg_batch *, const BatchArgs &a, int tpb, int apt, cudaStream_t st) {
   uint64_t threads = (a.n + apt - 1) / apt;
   unsigned g = blocks(threads, tpb);
@@ -179,14 +379,21 @@ void launch_step(vg_batch *, const BatchArgs &a, int tpb, int apt, cudaStream_t 
   }
 }
 
-// Choose (block size, agents per thread) by timing each candidate on the
-// current step; the trial launches write only the write buffers, which the
-// real step overwrites, so the simulation state is unaffected.
+// Choose the launch form by timing candidates on copies of the current
+// state (the simulation state is not touched): per-step launches of the
+// thread-per-agent kernel (block size 128/256/512 x agents per thread
+// 1/2/4, replayed from a CUDA graph when stepping) and the persistent
+// launch (block size 256/512 x bucket threshold: none, or warps for agents
+// above 32 / 64 in-edges).  Keyed on the arena's agents, edges and in-degree
+// histogram (log2 buckets).
 void autotune(vg_batch *b) {
-  // key: agents, edges and a coarse degree histogram (log2 buckets)
-  std::vector<uint32_t> rp(b->total + 1);
-  VG_CUDA(cudaMemcpyAsync(rp.data(), b->rp.p, rp.size() * 4, cudaMemcpyDeviceToHost, b->stream));
-  VG_CUDA(cudaStreamSynchronize(b->stream));
+  if (b->host_rp.empty()) {
+    b->host_rp.resize(b->total + 1);
+    VG_CUDA(cudaMemcpyAsync(b->host_rp.data(), b->rp.p, b->host_rp.size() * 4,
+                            cudaMemcpyDeviceToHost, b->stream));
+    VG_CUDA(cudaStreamSynchronize(b->stream));
+  }
+  const std::vector<uint32_t> &rp = b->host_rp;
   uint64_t hist[16] = {0};
   for (uint64_t i = 0; i < b->total; i++) {
     uint32_t d = rp[i + 1] - rp[i];
@@ -198,46 +405,88 @@ void autotune(vg_batch *b) {
   for (int i = 0; i < 16; i++) key = key * 31 + (hist[i] * 16 / std::max<uint64_t>(b->total, 1));
   auto it = b->tune_cache.find(key);
   if (it != b->tune_cache.end()) {
-    b->tpb = it->second.first;
-    b->apt = it->second.second;
+    b->tpb = it->second.tpb;
+    b->apt = it->second.apt;
+    b->p_tpb = it->second.p_tpb;
+    b->p_thr = it->second.p_thr;
+    b->prefer_persistent = it->second.persistent;
     b->tuned = true;
     return;
   }
-  BatchArgs a = batch_args(b, b->cur, (uint32_t)b->step, nullptr);
+  // trial buffers: copies of the current state
+  for (int k = 0; k < 2; k++) {
+    if (!b->scratch_st[k].p) b->scratch_st[k].alloc(b->total, &b->footprint);
+    if (!b->scratch_dy[k].p) b->scratch_dy[k].alloc(b->total * 4, &b->footprint);
+  }
+  uint8_t *sst[2] = {b->scratch_st[0].as<uint8_t>(), b->scratch_st[1].as<uint8_t>()};
+  int32_t *sdy[2] = {b->scratch_dy[0].as<int32_t>(), b->scratch_dy[1].as<int32_t>()};
+  auto reset = [&]() {
+    VG_CUDA(cudaMemcpyAsync(sst[0], b->st[b->cur].p, b->total, cudaMemcpyDeviceToDevice, b->stream));
+    VG_CUDA(cudaMemcpyAsync(sdy[0], b->dy[b->cur].p, b->total * 4, cudaMemcpyDeviceToDevice,
+                            b->stream));
+  };
+  constexpr uint32_t TRIAL = 8;
   cudaEvent_t e0, e1;
   VG_CUDA(cudaEventCreate(&e0));
   VG_CUDA(cudaEventCreate(&e1));
+  auto timed = [&](auto &&run) {
+    reset();
+    run();  // warm
+    reset();
+    VG_CUDA(cudaEventRecord(e0, b->stream));
+    run();
+    VG_CUDA(cudaEventRecord(e1, b->stream));
+    VG_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    VG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    return ms;
+  };
   float best = 1e30f;
   int bt = 256, ba = 1;
   for (int tpb : {128, 256, 512})
     for (int apt : {1, 2, 4}) {
-      launch_step(b, a, tpb, apt, b->stream);  // warm
-      VG_CUDA(cudaEventRecord(e0, b->stream));
-      for (int r = 0; r < 3; r++) launch_step(b, a, tpb, apt, b->stream);
-      VG_CUDA(cudaEventRecord(e1, b->stream));
-      VG_CUDA(cudaEventSynchronize(e1));
-      float ms = 0;
-      VG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      const float ms = timed([&] {
+        for (uint32_t t = 0; t < TRIAL; t++) {
+          BatchArgs a = batch_args(b, 0, (uint32_t)b->step + t, nullptr);
+          a.st_rd = sst[t & 1];
+          a.d_rd = sdy[t & 1];
+          a.st_wr = sst[1 - (t & 1)];
+          a.d_wr = sdy[1 - (t & 1)];
+          launch_step(b, a, tpb, apt, b->stream);
+        }
+      });
       if (ms < best) {
         best = ms;
         bt = tpb;
         ba = apt;
       }
     }
+  float pbest = 1e30f;
+  int pt = 256;
+  uint32_t pthr = 0xFFFFFFFFu;
+  for (int tpb : {256, 512})
+    for (uint32_t thr : {0xFFFFFFFFu, 64u, 32u}) {
+      const float ms = timed([&] {
+        launch_persistent(b, sst, sdy, 0, (uint32_t)b->step, TRIAL, tpb, thr);
+      });
+      if (ms < pbest) {
+        pbest = ms;
+        pt = tpb;
+        pthr = thr;
+      }
+    }
   VG_CUDA(cudaEventDestroy(e0));
   VG_CUDA(cudaEventDestroy(e1));
+  check_batch_status(b);
   b->tpb = bt;
   b->apt = ba;
+  b->p_tpb = pt;
+  b->p_thr = pthr;
+  b->prefer_persistent = pbest < best;
   b->tuned = true;
-  b->tune_cache[key] = {bt, ba};
+  b->tune_cache[key] = {bt, ba, pt, pthr, b->prefer_persistent};
 }
 
-void check_batch_status(vg_batch *b) {
-  int h = 0;
-  VG_CUDA(cudaMemcpyAsync(&h, b->status.p, 4, cudaMemcpyDeviceToHost, b->stream));
-  VG_CUDA(cudaStreamSynchronize(b->stream));
-  if (h) fail(VG_ERR_DEVICE, "batched SIR step: device status " + std::to_string(h));
-}
 
 }  // namespace
 
@@ -376,13 +625,22 @@ int vg_batch_create_sir(int n, const int64_t *N, const int32_t *deg, const doubl
 
 // mode 0: one launch per step; mode 1: the `steps` launches captured once in
 // a CUDA graph (re-captured when the step count or phase changes) and
-// replayed.
+// replayed; mode 2: one persistent launch for all steps; mode 3: the faster
+// of 1 and 2 as the autotuner measured them.
 int vg_batch_step(vg_batch *b, int steps, int mode) {
   API_BEGIN
   if (!b) fail(VG_ERR_ARG, "null batch");
+  if (mode < 0 || mode > 3) fail(VG_ERR_ARG, "batch: mode 0..3");
   if (steps <= 0) return VG_OK;
   if (!b->tuned) autotune(b);
-  if (mode == 0) {
+  if (mode == 3) mode = b->prefer_persistent ? 2 : 1;
+  if (mode == 2) {
+    uint8_t *st[2] = {b->st[0].as<uint8_t>(), b->st[1].as<uint8_t>()};
+    int32_t *dy[2] = {b->dy[0].as<int32_t>(), b->dy[1].as<int32_t>()};
+    launch_persistent(b, st, dy, b->cur, (uint32_t)b->step, (uint32_t)steps, b->p_tpb, b->p_thr);
+    if (steps % 2) b->cur = 1 - b->cur;
+    b->step += steps;
+  } else if (mode == 0) {
     for (int k = 0; k < steps; k++) {
       BatchArgs a = batch_args(b, b->cur, (uint32_t)b->step, nullptr);
       launch_step(b, a, b->tpb, b->apt, b->stream);
@@ -479,6 +737,34 @@ int vg_batch_read_graph(vg_batch *b, int i, uint32_t *row_ptr_out, uint32_t *src
   *nedges_out = c.nedges;
   if (row_ptr_out) VG_CUDA(cudaMemcpy(row_ptr_out, c.row_ptr.p, (c.nrows + 1) * 4, cudaMemcpyDeviceToHost));
   if (src_out && c.nedges) VG_CUDA(cudaMemcpy(src_out, c.src.p, c.nedges * 4, cudaMemcpyDeviceToHost));
+  API_END
+}
+
+int vg_batch_set_launch(vg_batch *b, int persistent, int persistent_tpb,
+                        uint32_t bucket_threshold) {
+  API_BEGIN
+  if (!b) fail(VG_ERR_ARG, "null batch");
+  if (persistent_tpb != 128 && persistent_tpb != 256 && persistent_tpb != 512)
+    fail(VG_ERR_ARG, "batch: persistent block size 128, 256 or 512");
+  if (!b->tuned) autotune(b);
+  b->prefer_persistent = persistent != 0;
+  b->p_tpb = persistent_tpb;
+  b->p_thr = bucket_threshold;
+  API_END
+}
+
+int vg_batch_tuning(vg_batch *b, int *persistent, int *persistent_tpb,
+                    uint32_t *bucket_threshold, uint64_t *heavy_agents) {
+  API_BEGIN
+  if (!b) fail(VG_ERR_ARG, "null batch");
+  if (!b->tuned) autotune(b);
+  if (persistent) *persistent = b->prefer_persistent;
+  if (persistent_tpb) *persistent_tpb = b->p_tpb;
+  if (bucket_threshold) *bucket_threshold = b->p_thr;
+  if (heavy_agents) {
+    build_buckets(b, b->p_thr);
+    *heavy_agents = b->nheavy;
+  }
   API_END
 }
 

@@ -201,6 +201,16 @@ class Batch:
         return {"agents": a.value, "edges": e.value, "tpb": t.value, "apt": p.value,
                 "device_bytes": db.value}
 
+    def set_launch(self, persistent, tpb=256, bucket_threshold=0xFFFFFFFF):
+        check(lib().vg_batch_set_launch(self._h, int(persistent), int(tpb), int(bucket_threshold)))
+
+    def tuning(self):
+        p, t, n = C.c_int(), C.c_int(), C.c_uint64()
+        thr = C.c_uint32()
+        check(lib().vg_batch_tuning(self._h, C.byref(p), C.byref(t), C.byref(thr), C.byref(n)))
+        return {"persistent": bool(p.value), "persistent_tpb": t.value,
+                "bucket_threshold": thr.value, "heavy_agents": n.value}
+
     def close(self):
         if self._h:
             check(lib().vg_batch_destroy(self._h))
