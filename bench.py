@@ -68,7 +68,7 @@ def parse():
                     choices=["opinion", "batch", "serve", "sir", "life", "fp64"])
     ap.add_argument("--secondary", default="sir,life,batch,serve",
                     help="opinion workload: the other workloads run afterwards, each in "
-                         "its own process (empty: none)")
+                         "its own process ('none': no other workload)")
     ap.add_argument("--no-parity", action="store_true",
                     help="opinion workload: skip the 50-step oracle comparison")
     ap.add_argument("--jobs", type=int, default=512)
@@ -472,7 +472,7 @@ def run_ours(args):
                           "edges (the parity comparison's oracle run)" % (steps, el)}
         del g_oracle
     run.close()
-    if rank == 0 and ws == 1 and args.secondary:
+    if rank == 0 and ws == 1 and args.secondary not in ("", "none"):
         out["secondary"] = run_secondaries(args)
     if rank == 0:
         print(json.dumps(out), flush=True)

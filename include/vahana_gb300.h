@@ -407,6 +407,12 @@ int vg_selftest_scan(uint64_t n, int wide, int in_place, uint64_t seed, uint64_t
  * the kernel's duration.  The context stays usable afterwards. */
 int vg_selftest_scan_timeout(int *status_out, double *ms_out);
 
+/* Failure detection of the persistent ensemble launch's step barrier: two
+ * blocks meet at a barrier that expects three, so both bounded waits run
+ * out (2^16 polls here); *status_out = the status word (0x5e04), *ms_out =
+ * the launch's duration.  The context stays usable. */
+int vg_selftest_barrier_timeout(int *status_out, double *ms_out);
+
 /* ---- allocation-free SIR step ---------------------------------------------
  * No counterpart in the reference.  One step of the "sir" transition on
  * device buffers the caller owns, for callers that cannot let a library

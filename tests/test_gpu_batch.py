@@ -72,3 +72,23 @@ def test_batch_persistent_equals_plain(vh):
         np.testing.assert_array_equal(sb, sp)
         np.testing.assert_array_equal(db, dp)
     b.close()
+
+
+def test_step_barrier_wait_gives_up_with_a_status(vh):
+    """The persistent launch's grid-wide step barrier is bounded: two blocks
+    waiting for a third record 0x5e04 and end; the GPU stays usable (a
+    batch steps correctly afterwards)."""
+    import ctypes as C
+    from vahana_gb300 import models
+    from vahana_gb300._lib import check, lib
+    st, ms = C.c_int(), C.c_double()
+    check(lib().vg_selftest_barrier_timeout(C.byref(st), C.byref(ms)))
+    assert st.value == 0x5e04 and ms.value < 5000
+    N, deg, beta, rec, seeds = small_params(4)
+    b = models.Batch(N, deg, beta, rec, seeds)
+    b.set_launch(1, 256, 0xFFFFFFFF)
+    b.step(3, mode=2)
+    for i in range(b.n):
+        b.step_one(i, 3)
+        np.testing.assert_array_equal(b.states(i, 0)[0], b.states(i, 1)[0])
+    b.close()

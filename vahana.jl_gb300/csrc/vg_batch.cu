@@ -111,7 +111,8 @@ constexpr int BAR_ERR_WAIT = 0x5e04;
 
 // Sense-free grid barrier on a generation counter; a wait that runs out
 // records BAR_ERR_WAIT and returns false (the launch then ends).
-__device__ bool grid_barrier(unsigned *bar, unsigned nblocks, int *status) {
+__device__ bool grid_barrier(unsigned *bar, unsigned nblocks, int *status,
+                             uint32_t limit = BAR_SPIN_LIMIT) {
   __shared__ int ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -126,7 +127,7 @@ __device__ bool grid_barrier(unsigned *bar, unsigned nblocks, int *status) {
     } else {
       uint32_t i = 0;
       while (*gen == g) {
-        if (++i >= BAR_SPIN_LIMIT) {
+        if (++i >= limit) {
           atomicCAS(status, 0, BAR_ERR_WAIT);
           ok = 0;
           break;
@@ -137,6 +138,12 @@ __device__ bool grid_barrier(unsigned *bar, unsigned nblocks, int *status) {
   }
   __syncthreads();
   return ok != 0;
+}
+
+// failure detection without a fault: blocks meet at a barrier that expects
+// one block more than the launch has, so every wait runs out
+__global__ void k_barrier_probe(unsigned *bar, unsigned expect, int *status, uint32_t limit) {
+  grid_barrier(bar, expect, status, limit);
 }
 
 // the rule of transition "sir" for agent i with k infected in-neighbours
@@ -737,6 +744,35 @@ int vg_batch_read_graph(vg_batch *b, int i, uint32_t *row_ptr_out, uint32_t *src
   *nedges_out = c.nedges;
   if (row_ptr_out) VG_CUDA(cudaMemcpy(row_ptr_out, c.row_ptr.p, (c.nrows + 1) * 4, cudaMemcpyDeviceToHost));
   if (src_out && c.nedges) VG_CUDA(cudaMemcpy(src_out, c.src.p, c.nedges * 4, cudaMemcpyDeviceToHost));
+  API_END
+}
+
+int vg_selftest_barrier_timeout(int *status_out, double *ms_out) {
+  API_BEGIN
+  need(status_out, "status pointer");
+  need(ms_out, "duration pointer");
+  unsigned *bar = nullptr;
+  int *status = nullptr;
+  VG_CUDA(cudaMalloc(&bar, 8));
+  VG_CUDA(cudaMalloc(&status, 4));
+  VG_CUDA(cudaMemset(bar, 0, 8));
+  VG_CUDA(cudaMemset(status, 0, 4));
+  cudaEvent_t e0, e1;
+  VG_CUDA(cudaEventCreate(&e0));
+  VG_CUDA(cudaEventCreate(&e1));
+  VG_CUDA(cudaEventRecord(e0));
+  k_barrier_probe<<<2, 64>>>(bar, 3, status, 1u << 16);  // two blocks, three expected
+  VG_CUDA(cudaEventRecord(e1));
+  VG_CUDA(cudaEventSynchronize(e1));
+  VG_CUDA(cudaGetLastError());
+  float ms = 0;
+  VG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  VG_CUDA(cudaMemcpy(status_out, status, 4, cudaMemcpyDeviceToHost));
+  *ms_out = ms;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(bar);
+  cudaFree(status);
   API_END
 }
 

@@ -136,6 +136,7 @@ SIGNATURES = {
     "vg_selftest_sort": (I, [U64, I, I, I, I, U64, PU64]),
     "vg_selftest_scan": (I, [U64, I, I, U64, PU64]),
     "vg_selftest_scan_timeout": (I, [PI, C.POINTER(D)]),
+    "vg_selftest_barrier_timeout": (I, [PI, C.POINTER(D)]),
     "vg_selftest_rate": (I, [I, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(D),
                              C.POINTER(D)]),
     "vg_sir_step_noalloc": (I, [P, P, P, P, P, P, U64, C.c_uint32, D, C.c_int32, U64,
