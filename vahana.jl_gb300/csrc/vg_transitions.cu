@@ -501,8 +501,7 @@ struct MoveArgs {
   int periodic, only_surrounding;
   int mode;
   DevCSRView nbr;       // mode 1: the agent's in-edges
-  const void *nbr_val;  // mode 1: the neighbours' field
-  int nbr_dt;
+  SrcTable nbr_val;     // mode 1: the neighbours' field, per source type
   int has_from, has_to, same;  // same: one edge type, one buffer for both
   Append from, to;
 };
@@ -538,8 +537,13 @@ __global__ void k_move_to(Sweep s, MoveArgs m, int call_pos) {
       for (int d = 0; d < m.ndims; d++) pos[d] = ld_i64(s.a.rd[d], s.fdt[d], i);
     } else {
       int64_t v = 0;
-      if (i < m.nbr.nrows && m.nbr.row_ptr[i + 1] > m.nbr.row_ptr[i]) {
-        v = ld_i64(m.nbr_val, m.nbr_dt, m.nbr.src[m.nbr.row_ptr[i]]);
+      const int ty = i < m.nbr.nrows && m.nbr.row_ptr[i + 1] > m.nbr.row_ptr[i]
+                         ? edge_src_type(m.nbr, m.nbr.row_ptr[i]) : 0;
+      if (ty > 0 && ty < MAX_AGENT_TYPES && m.nbr_val.ptr[ty]) {
+        v = ld_i64(m.nbr_val.ptr[ty], m.nbr_val.dt[ty], m.nbr.src[m.nbr.row_ptr[i]]);
+      } else if (ty != 0) {
+        set_status(s.status, 202);  // source type not readable, or without the field
+        ok = false;
       } else {
         set_status(s.status, 203);  // first() of no neighbour
         ok = false;
@@ -1244,19 +1248,13 @@ void tr_move_to(ApplyCtx &c) {
   } else {
     const int ne = need_edge_param(c, 8);
     require_edge_read(c, ne);
+    require_sources_read(c, ne, c.call_type);
     m.nbr = csr_view(s, ne, c.call_type);
-    const int src_t = m.nbr.src_type_const;
-    if (m.nbr.nedges && src_t <= 0) fail(VG_ERR_ARG, "move_to: neighbours of one agent type");
     if (ad.fields.empty() || ad.fields[0].dtype == VG_F32 || ad.fields[0].dtype == VG_F64)
       fail(VG_ERR_ARG, "move_to: mode 1 writes the position to an Int field 0");
-    if (m.nbr.nedges) {
-      require_agent_read(c, src_t);
-      const AgentTypeDesc &nd = s.model->at(src_t);
-      const int nf = (int)c.param(9, 0);
-      if (nf < 0 || nf >= (int)nd.fields.size()) fail(VG_ERR_ARG, "move_to: neighbour field");
-      m.nbr_val = s.agents[src_t - 1].rd[nf].p;
-      m.nbr_dt = nd.fields[nf].dtype;
-    }
+    const int nf = (int)c.param(9, 0);
+    if (nf < 0) fail(VG_ERR_ARG, "move_to: neighbour field");
+    m.nbr_val = make_src_table(c, nf);
   }
   Sweep w = make_sweep(c);
   if (w.a.n == 0) return;
