@@ -212,10 +212,22 @@ struct RedArgs {
   double neut_f;
 };
 
-// pass 1: per-block partial (deterministic block order)
+// pass 1: per-block partial (deterministic block order): each thread folds
+// its strided elements, each warp combines its 32 lanes by shuffles in a
+// fixed tree, warp 0 combines the warps' results the same way
+__device__ __forceinline__ void warp_combine(int op, int64_t &vi, double &vf) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const int64_t oi = __shfl_down_sync(0xffffffffu, vi, off);
+    const double of = __shfl_down_sync(0xffffffffu, vf, off);
+    vi = red_i(op, oi, vi);
+    vf = red_f(op, of, vf);
+  }
+}
+
 __global__ void k_reduce_partial(RedArgs a, int64_t *pi, double *pf) {
-  __shared__ int64_t si[TPB];
-  __shared__ double sf[TPB];
+  __shared__ int64_t si[TPB / 32];
+  __shared__ double sf[TPB / 32];
   int64_t acc_i = a.neut_i;
   double acc_f = a.neut_f;
   bool have = false;
@@ -240,19 +252,21 @@ __global__ void k_reduce_partial(RedArgs a, int64_t *pi, double *pf) {
     acc_i = a.neut_i;
     acc_f = a.neut_f;
   }
-  si[threadIdx.x] = acc_i;
-  sf[threadIdx.x] = acc_f;
-  __syncthreads();
-  for (int s = TPB / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) {
-      si[threadIdx.x] = red_i(a.op, si[threadIdx.x + s], si[threadIdx.x]);
-      sf[threadIdx.x] = red_f(a.op, sf[threadIdx.x + s], sf[threadIdx.x]);
-    }
-    __syncthreads();
+  const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  warp_combine(a.op, acc_i, acc_f);
+  if (lane == 0) {
+    si[wid] = acc_i;
+    sf[wid] = acc_f;
   }
-  if (threadIdx.x == 0) {
-    pi[blockIdx.x] = si[0];
-    pf[blockIdx.x] = sf[0];
+  __syncthreads();
+  if (wid == 0) {
+    acc_i = lane < TPB / 32 ? si[lane] : a.neut_i;
+    acc_f = lane < TPB / 32 ? sf[lane] : a.neut_f;
+    warp_combine(a.op, acc_i, acc_f);
+    if (lane == 0) {
+      pi[blockIdx.x] = acc_i;
+      pf[blockIdx.x] = acc_f;
+    }
   }
 }
 
