@@ -628,7 +628,7 @@ static unsigned opinion_args(Sim &s, int e, int T, double eps, double a, double 
                              cudaStream_t launch_stream);
 // chunks of a gather launch whose finished rows are downloaded while the
 // next chunk runs (apply! with host exchange)
-constexpr unsigned XCHG_CHUNKS = 8;
+constexpr unsigned XCHG_CHUNKS = 12;
 static void launch_chunked(Sim &s, OpinionArgs &p, unsigned grid, Sim::HostExchange &hx);
 
 // apply!(sim, bounded_confidence, [T], [T, E], [T]; params = [E, eps, a, b,
@@ -693,8 +693,29 @@ static void chunk_bounds(Sim &s, CSR &cs, uint64_t n, unsigned hub_blocks, unsig
   if (cs.chunk_block.size() == K + 1) return;
   cs.chunk_block.assign(K + 1, 0);
   cs.chunk_rows.assign(K, n);
-  for (unsigned k = 0; k <= K; k++)
-    cs.chunk_block[k] = hub_blocks + (uint64_t)slice_blocks * k / K;
+  // equal work per chunk: a block's work is its slices' column slots plus
+  // a fixed cost per row (the low rows of a Chung-Lu graph hold most edges,
+  // so equal block counts would leave the first chunk several times longer)
+  std::vector<uint64_t> base(cs.nslices + 1);
+  VG_CUDA(cudaMemcpyAsync(base.data(), cs.slice_base.p, base.size() * 8, cudaMemcpyDeviceToHost,
+                          s.stream));
+  VG_CUDA(cudaStreamSynchronize(s.stream));
+  constexpr uint64_t ROW_COST = 2;  // slots' worth of work per row (row, degree, result)
+  auto work_to = [&](uint64_t blk) {  // work of slice blocks [0, blk)
+    const uint64_t sl = std::min<uint64_t>(blk * (TPB / 32), cs.nslices);
+    return base[sl] + ROW_COST * 32 * sl;
+  };
+  const uint64_t total = work_to(slice_blocks);
+  cs.chunk_block[0] = hub_blocks;
+  cs.chunk_block[K] = hub_blocks + slice_blocks;
+  uint64_t b = 0;
+  for (unsigned k = 1; k < K; k++) {
+    const uint64_t goal = total * k / K;
+    while (b < slice_blocks && work_to(b) < goal) b++;
+    cs.chunk_block[k] = hub_blocks + std::max<uint64_t>(b, cs.chunk_block[k - 1] - hub_blocks + 1);
+  }
+  for (unsigned k = 1; k < K; k++)
+    cs.chunk_block[k] = std::min<uint64_t>(cs.chunk_block[k], cs.chunk_block[K] - (K - k));
   for (unsigned k = 0; k + 1 < K; k++) {
     // first position in `order` of the block: TPB / 32 slices of 32 rows per block
     const uint64_t pos = (cs.chunk_block[k + 1] - hub_blocks) * (uint64_t)TPB;
