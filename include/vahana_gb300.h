@@ -458,10 +458,13 @@ int vg_batch_create_sir(int n, const int64_t *N, const int32_t *deg,
 int vg_batch_step(vg_batch *b, int steps, int mode);
 /* The autotuner's choice: persistent (1) or graph replay (0), the
  * persistent block size, its degree-bucket threshold (agents with more
- * in-edges take a warp each; 0xFFFFFFFF none) and how many agents are
- * above it.  Runs the autotuner if it has not run. */
+ * in-edges take a warp each; 0xFFFFFFFF none), how many agents are above
+ * it, and the measured milliseconds per step of the best per-step launch
+ * and of the best persistent launch (24-step trials on copies of the state).
+ * Runs the autotuner if it has not run. */
 int vg_batch_tuning(vg_batch *b, int *persistent, int *persistent_tpb,
-                    uint32_t *bucket_threshold, uint64_t *heavy_agents);
+                    uint32_t *bucket_threshold, uint64_t *heavy_agents,
+                    double *step_ms_graph, double *step_ms_persistent);
 /* Overrides the autotuner: mode 3 then takes the persistent launch
  * (persistent != 0) or the graph, and the persistent launch uses this block
  * size (128, 256, 512) and bucket threshold. */

@@ -395,9 +395,8 @@ int vg_sim_create(vg_model *m, const char *name, void *stream, vg_sim **out) {
 }
 
 Sim::~Sim() {
-  for (cudaEvent_t e : xchg_events) cudaEventDestroy(e);
   if (copy_stream) cudaStreamDestroy(copy_stream);
-  if (aux_stream) cudaStreamDestroy(aux_stream);
+  if (xchg_flags_host) cudaFreeHost(xchg_flags_host);
 }
 
 int vg_sim_destroy(vg_sim *s) {

@@ -89,8 +89,9 @@ __global__ void k_batch_sir(BatchArgs a) {
 // ---- persistent form: one cooperative launch runs every step.  Blocks
 // meet at a grid-wide barrier between steps (all blocks are resident: the
 // launch is cooperative).  The states a step reads were written by other
-// blocks in the previous step of the same launch, so they are loaded at L2
-// (ld.global.cg), never through a non-coherent cache.  Agents whose
+// blocks in the previous step of the same launch: they are read with
+// ordinary loads after the barrier's GPU-scope acquire fence (never through
+// the read-only path, which assumes data constant for the whole launch).  Agents whose
 // in-degree exceeds the bucket threshold (listed in `heavy`) are folded by a
 // warp each (the infected-neighbour count is an integer: any order gives the
 // same k); the others by a thread each.
@@ -135,6 +136,9 @@ __device__ bool grid_barrier(unsigned *bar, unsigned nblocks, int *status,
       }
     }
     __threadfence();
+    // acquire at GPU scope: the other blocks' writes of the step are visible
+    // to this block's ordinary (L1-cached) loads after the barrier
+    asm volatile("fence.acq_rel.gpu;" ::: "memory");
   }
   __syncthreads();
   return ok != 0;
@@ -187,23 +191,23 @@ __global__ void k_batch_persist(PersistArgs p) {
     const uint32_t step = p.step0 + t;
     for (uint64_t i = tid; i < a.n; i += nthreads) {  // thread per agent
       if (p.is_heavy && p.is_heavy[i]) continue;
-      const uint8_t s = __ldcg(st_rd + i);
-      const int32_t d = __ldcg(d_rd + i);
+      const uint8_t s = st_rd[i];
+      const int32_t d = d_rd[i];
       uint32_t k = 0;
       if (s == 0) {
         const uint32_t e = a.rp[i + 1];
-        for (uint32_t q = a.rp[i]; q < e; q++) k += (__ldcg(st_rd + a.src[q]) == 1);
+        for (uint32_t q = a.rp[i]; q < e; q++) k += (st_rd[a.src[q]] == 1);
       }
       sir_rule(a, i, k, s, d, step, st_wr, d_wr);
     }
     for (uint64_t h = wid; h < p.nheavy; h += nwarps) {  // warp per heavy agent
       const uint64_t i = p.heavy[h];
-      const uint8_t s = __ldcg(st_rd + i);
-      const int32_t d = __ldcg(d_rd + i);
+      const uint8_t s = st_rd[i];
+      const int32_t d = d_rd[i];
       uint32_t k = 0;
       if (s == 0) {
         const uint32_t e = a.rp[i + 1];
-        for (uint32_t q = a.rp[i] + lane; q < e; q += 32) k += (__ldcg(st_rd + a.src[q]) == 1);
+        for (uint32_t q = a.rp[i] + lane; q < e; q += 32) k += (st_rd[a.src[q]] == 1);
       }
       k = __reduce_add_sync(0xffffffffu, k);
       if (lane == 0) sir_rule(a, i, k, s, d, step, st_wr, d_wr);
@@ -269,6 +273,7 @@ struct vg_batch {
     int tpb, apt, p_tpb;
     uint32_t p_thr;
     bool persistent;
+    float graph_ms, persistent_ms;
   };
   std::map<uint64_t, Tuned> tune_cache;
   // persistent form: block size, bucket threshold (agents with more
@@ -277,6 +282,7 @@ struct vg_batch {
   int p_tpb = 256;
   uint32_t p_thr = 0xFFFFFFFFu;
   bool prefer_persistent = false;
+  float tuned_graph_ms = 0, tuned_persistent_ms = 0;  // best trial of each form
   std::vector<uint32_t> host_rp;       // arena row pointers (autotuner, buckets)
   uint32_t heavy_thr = 0xFFFFFFFFu;    // threshold the heavy list was built for
   DevBuf heavy, is_heavy, bar;
@@ -417,6 +423,8 @@ void autotune(vg_batch *b) {
     b->p_tpb = it->second.p_tpb;
     b->p_thr = it->second.p_thr;
     b->prefer_persistent = it->second.persistent;
+    b->tuned_graph_ms = it->second.graph_ms;
+    b->tuned_persistent_ms = it->second.persistent_ms;
     b->tuned = true;
     return;
   }
@@ -432,7 +440,7 @@ void autotune(vg_batch *b) {
     VG_CUDA(cudaMemcpyAsync(sdy[0], b->dy[b->cur].p, b->total * 4, cudaMemcpyDeviceToDevice,
                             b->stream));
   };
-  constexpr uint32_t TRIAL = 8;
+  constexpr uint32_t TRIAL = 24;
   cudaEvent_t e0, e1;
   VG_CUDA(cudaEventCreate(&e0));
   VG_CUDA(cudaEventCreate(&e1));
@@ -490,8 +498,11 @@ void autotune(vg_batch *b) {
   b->p_tpb = pt;
   b->p_thr = pthr;
   b->prefer_persistent = pbest < best;
+  b->tuned_graph_ms = best / TRIAL;
+  b->tuned_persistent_ms = pbest / TRIAL;
   b->tuned = true;
-  b->tune_cache[key] = {bt, ba, pt, pthr, b->prefer_persistent};
+  b->tune_cache[key] = {bt, ba, pt, pthr, b->prefer_persistent, b->tuned_graph_ms,
+                        b->tuned_persistent_ms};
 }
 
 
@@ -790,10 +801,13 @@ int vg_batch_set_launch(vg_batch *b, int persistent, int persistent_tpb,
 }
 
 int vg_batch_tuning(vg_batch *b, int *persistent, int *persistent_tpb,
-                    uint32_t *bucket_threshold, uint64_t *heavy_agents) {
+                    uint32_t *bucket_threshold, uint64_t *heavy_agents,
+                    double *step_ms_graph, double *step_ms_persistent) {
   API_BEGIN
   if (!b) fail(VG_ERR_ARG, "null batch");
   if (!b->tuned) autotune(b);
+  if (step_ms_graph) *step_ms_graph = b->tuned_graph_ms;
+  if (step_ms_persistent) *step_ms_persistent = b->tuned_persistent_ms;
   if (persistent) *persistent = b->prefer_persistent;
   if (persistent_tpb) *persistent_tpb = b->p_tpb;
   if (bucket_threshold) *bucket_threshold = b->p_thr;

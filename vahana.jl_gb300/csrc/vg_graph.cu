@@ -967,8 +967,9 @@ void ensure_schedule(Sim &s, CSR &c, uint32_t thr, uint32_t big_thr, uint64_t n)
   c.sell_src.release();
   c.sell_w.release();
   c.nhub = c.norder = c.nslices = c.nbig = 0;
-  c.chunk_block.clear();
-  c.chunk_rows.clear();
+  c.range_block.clear();
+  c.range_rows.clear();
+  c.range_window.clear();
   c.hub_rows_sorted.clear();
   if (n > 0 && c.row_ptr.p) {
     const uint32_t *rp = c.row_ptr.as<uint32_t>();

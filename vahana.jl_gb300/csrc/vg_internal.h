@@ -194,10 +194,12 @@ struct CSR {
   uint32_t hub_threshold = 0;
   uint32_t wshift = 13;   // window = row >> wshift
   bool schedule_valid = false;
-  // chunked launch of the gather (apply! with host exchange): chunk k runs
-  // slice blocks [chunk_block[k], chunk_block[k + 1]) and completes every
-  // row below chunk_rows[k] (derived from the layout, cached with it)
-  std::vector<uint64_t> chunk_block, chunk_rows;
+  // row ranges of the gather whose completion the launch reports (apply!
+  // with host exchange): range k is the slice blocks before range_block[k]
+  // (from the previous boundary) and holds the non-hub rows below
+  // range_rows[k]; derived from the layout, cached with it
+  std::vector<uint64_t> range_block, range_rows;
+  std::vector<uint32_t> range_window;  // window of each range's first row
   std::vector<uint32_t> hub_rows_sorted;  // host copy of the hub rows, ascending
   // payload field 0 (Float64) holds only multiples of 2^-53 in (0, 1]:
   // -1 not checked yet, 0 no, 1 yes (decides the gather kernels' sum path)
@@ -294,7 +296,8 @@ struct Sim {
   std::map<int, std::unique_ptr<EdgeAppend>> append_spare;
   // apply! with host exchange (vg_apply_host): while set, a transition that
   // finishes its rows range by range may download each finished range of the
-  // called type's new state to `out` on copy_stream (and sets `done`)
+  // called type's new state to `out` on copy_stream while it runs (and sets
+  // `done`)
   struct HostExchange {
     int type_nr = 0;
     void *const *out = nullptr;
@@ -311,9 +314,13 @@ struct Sim {
     std::string name;
   };
   std::map<std::string, std::vector<ParamBinding>> bindings;
-  cudaStream_t copy_stream = nullptr;   // created on first use, destroyed with the sim
-  cudaStream_t aux_stream = nullptr;    // concurrent work of a chunked launch (same)
-  std::vector<cudaEvent_t> xchg_events;  // one per chunk, created on first use
+  cudaStream_t copy_stream = nullptr;  // created on first use, destroyed with the sim
+  // completion reports of a gather launch: per-range block counters on the
+  // device, per-range flags in mapped pinned host memory (the last block of
+  // a range writes the call's generation), created on first use
+  DevBuf xchg_count;
+  unsigned *xchg_flags_host = nullptr, *xchg_flags_dev = nullptr;
+  unsigned xchg_gen = 0;
   ~Sim();
 };
 

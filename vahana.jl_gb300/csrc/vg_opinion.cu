@@ -72,7 +72,6 @@ struct OpinionArgs {
   uint64_t nslices;
   uint32_t hub_thr;
   unsigned hub_blocks;   // blocks of the other hub rows, 4 per block
-  unsigned blk_base;     // block number of this launch's first block (chunked launches)
   double eps, a, b;
   int a_pow2, b_pow2, a_k, b_k;  // a = 2^a_k, b = 2^b_k (positive normal powers of two)
   float eps_lo, eps_hi;  // float filter: certainly inside / certainly outside
@@ -579,7 +578,38 @@ __device__ __forceinline__ void opinion_block(const OpinionArgs &p, unsigned blk
 
 template <bool GRID>
 __global__ void __launch_bounds__(TPB, 9) k_opinion(OpinionArgs p) {
-  opinion_block<GRID, false>(p, p.blk_base + blockIdx.x);
+  opinion_block<GRID, false>(p, blockIdx.x);
+}
+
+// Completion reports of one gather launch (apply! with host exchange): the
+// hub warps' blocks form range `nranges`, slice blocks below end[k] (and not
+// below end[k - 1]) range k; the block that completes a range writes the
+// call's generation to the range's flag in mapped host memory.
+constexpr unsigned XCHG_RANGES = 16;
+struct Notify {
+  unsigned *count;  // device: blocks finished per range
+  unsigned *flag;   // mapped host memory: generation of the finished range
+  unsigned gen, nranges, hub_blocks;
+  unsigned end[XCHG_RANGES];
+  unsigned expect[XCHG_RANGES + 1];
+};
+
+template <bool GRID>
+__global__ void __launch_bounds__(TPB, 9) k_opinion_notify(OpinionArgs p, Notify nt) {
+  opinion_block<GRID, false>(p, blockIdx.x);
+  __threadfence();  // this thread's results reach L2 before the block reports
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned r = nt.nranges;  // the hub warps
+    if (blockIdx.x >= nt.hub_blocks) {
+      r = 0;
+      while (r + 1 < nt.nranges && blockIdx.x >= nt.end[r]) r++;
+    }
+    if (atomicAdd(nt.count + r, 1u) + 1 == nt.expect[r]) {
+      __threadfence_system();
+      *(volatile unsigned *)(nt.flag + r) = nt.gen;
+    }
+  }
 }
 
 // the block-wide hub rows of one simulation, one block each
@@ -626,10 +656,9 @@ __global__ void k_check_grid(const double *w, uint64_t n, int *bad) {
 static unsigned opinion_args(Sim &s, int e, int T, double eps, double a, double b,
                              uint32_t thr, uint32_t big_thr, OpinionArgs &p,
                              cudaStream_t launch_stream);
-// chunks of a gather launch whose finished rows are downloaded while the
-// next chunk runs (apply! with host exchange)
-constexpr unsigned XCHG_CHUNKS = 12;
-static void launch_chunked(Sim &s, OpinionArgs &p, unsigned grid, Sim::HostExchange &hx);
+// a gather launch whose finished row ranges are downloaded while it runs
+// (apply! with host exchange)
+static void launch_notified(Sim &s, OpinionArgs &p, unsigned grid, Sim::HostExchange &hx);
 
 // apply!(sim, bounded_confidence, [T], [T, E], [T]; params = [E, eps, a, b,
 // hub_thr, block_thr]); defaults eps 0.3, a 0.5, b 1 - a, hub_thr 1536,
@@ -672,8 +701,8 @@ void tr_bounded_confidence(ApplyCtx &c) {
   }
   Sim::HostExchange *hx = s.host_xchg;
   if (hx && hx->type_nr == c.call_type && ad.fields.size() == 1 && hx->out && hx->out[0] &&
-      grid > nbig) {
-    launch_chunked(s, p, grid - nbig, *hx);
+      nbig == 0 && grid > 0) {
+    launch_notified(s, p, grid, *hx);
     return;
   }
   if (grid > nbig) {
@@ -683,48 +712,30 @@ void tr_bounded_confidence(ApplyCtx &c) {
   VG_CUDA(cudaGetLastError());
 }
 
-// Chunk boundaries of the slice part of the gather: chunk k runs the slice
-// blocks [chunk_block[k], chunk_block[k + 1]); the rows are sorted by window
-// (row >> wshift) before degree, so after chunk k every non-hub row of the
-// windows below the window of the next chunk's first row is final:
-// chunk_rows[k] = that window << wshift.  hub_rows_sorted: the hub rows.
-static void chunk_bounds(Sim &s, CSR &cs, uint64_t n, unsigned hub_blocks, unsigned slice_blocks) {
-  const unsigned K = std::max(1u, std::min(XCHG_CHUNKS, slice_blocks));
-  if (cs.chunk_block.size() == K + 1) return;
-  cs.chunk_block.assign(K + 1, 0);
-  cs.chunk_rows.assign(K, n);
-  // equal work per chunk: a block's work is its slices' column slots plus
-  // a fixed cost per row (the low rows of a Chung-Lu graph hold most edges,
-  // so equal block counts would leave the first chunk several times longer)
-  std::vector<uint64_t> base(cs.nslices + 1);
-  VG_CUDA(cudaMemcpyAsync(base.data(), cs.slice_base.p, base.size() * 8, cudaMemcpyDeviceToHost,
-                          s.stream));
-  VG_CUDA(cudaStreamSynchronize(s.stream));
-  constexpr uint64_t ROW_COST = 2;  // slots' worth of work per row (row, degree, result)
-  auto work_to = [&](uint64_t blk) {  // work of slice blocks [0, blk)
-    const uint64_t sl = std::min<uint64_t>(blk * (TPB / 32), cs.nslices);
-    return base[sl] + ROW_COST * 32 * sl;
-  };
-  const uint64_t total = work_to(slice_blocks);
-  cs.chunk_block[0] = hub_blocks;
-  cs.chunk_block[K] = hub_blocks + slice_blocks;
-  uint64_t b = 0;
-  for (unsigned k = 1; k < K; k++) {
-    const uint64_t goal = total * k / K;
-    while (b < slice_blocks && work_to(b) < goal) b++;
-    cs.chunk_block[k] = hub_blocks + std::max<uint64_t>(b, cs.chunk_block[k - 1] - hub_blocks + 1);
-  }
-  for (unsigned k = 1; k < K; k++)
-    cs.chunk_block[k] = std::min<uint64_t>(cs.chunk_block[k], cs.chunk_block[K] - (K - k));
+// Row ranges of the gather: range k is the slice blocks [range_block[k],
+// range_block[k + 1]) (equal block counts); the rows are sorted by window
+// (row >> wshift) before degree, so once range k is done every non-hub row
+// of the windows below the window of range k + 1's first row is final:
+// range_rows[k] = that window << wshift.  hub_rows_sorted: the hub rows.
+static void range_bounds(Sim &s, CSR &cs, uint64_t n, unsigned hub_blocks, unsigned slice_blocks) {
+  const unsigned K = std::max(1u, std::min(XCHG_RANGES, slice_blocks));
+  if (cs.range_block.size() == K + 1) return;
+  cs.range_block.assign(K + 1, 0);
+  cs.range_rows.assign(K, n);
+  cs.range_window.assign(K, 0xFFFFFFFFu);
+  cs.range_window[0] = 0;
+  for (unsigned k = 0; k <= K; k++)
+    cs.range_block[k] = hub_blocks + (uint64_t)slice_blocks * k / K;
   for (unsigned k = 0; k + 1 < K; k++) {
     // first position in `order` of the block: TPB / 32 slices of 32 rows per block
-    const uint64_t pos = (cs.chunk_block[k + 1] - hub_blocks) * (uint64_t)TPB;
+    const uint64_t pos = (cs.range_block[k + 1] - hub_blocks) * (uint64_t)TPB;
     if (pos >= cs.norder) continue;
     uint32_t row = 0;
     VG_CUDA(cudaMemcpyAsync(&row, cs.order.as<uint32_t>() + pos, 4, cudaMemcpyDeviceToHost,
                             s.stream));
     VG_CUDA(cudaStreamSynchronize(s.stream));
-    cs.chunk_rows[k] = std::min<uint64_t>(n, ((uint64_t)row >> cs.wshift) << cs.wshift);
+    cs.range_window[k + 1] = row >> cs.wshift;
+    cs.range_rows[k] = std::min<uint64_t>(n, ((uint64_t)row >> cs.wshift) << cs.wshift);
   }
   cs.hub_rows_sorted.assign(cs.nhub, 0);
   if (cs.nhub) {
@@ -735,71 +746,90 @@ static void chunk_bounds(Sim &s, CSR &cs, uint64_t n, unsigned hub_blocks, unsig
   }
 }
 
-// The gather with its rows downloaded while it runs.  The hub warps (long
-// rows, the longest work items) run as their own launch on the auxiliary
-// stream, concurrently with the slices, which run in chunks on the
-// simulation's stream; after each chunk the rows it completed go to the host
-// on the copy stream.  A range that holds a hub row (with hubs among the
-// first agents, the low ranges) is downloaded once the hub launch is done as
-// well; the simulation's stream waits for it before apply! goes on.
-static void launch_chunked(Sim &s, OpinionArgs &p, unsigned grid, Sim::HostExchange &hx) {
+// The gather as one launch (its load balance intact: the long rows start
+// first and overlap the rest) that reports each finished row range to the
+// host; the host issues the range's download on the copy stream as soon as
+// its flag (and, for a range holding hub rows, the hub warps' flag) shows
+// this call's generation.  No GPU work waits on another: the host polls,
+// and if the launch ends without a report (or fails) the remaining ranges
+// are downloaded after it, so the wait is bounded by the launch itself.
+static void launch_notified(Sim &s, OpinionArgs &p, unsigned grid, Sim::HostExchange &hx) {
   CSR &cs = *p.csr;
-  chunk_bounds(s, cs, p.n, p.hub_blocks, grid - p.hub_blocks);
-  const unsigned K = (unsigned)cs.chunk_rows.size();
+  range_bounds(s, cs, p.n, p.hub_blocks, grid - p.hub_blocks);
+  const unsigned K = (unsigned)cs.range_rows.size();
   if (!s.copy_stream) VG_CUDA(cudaStreamCreateWithFlags(&s.copy_stream, cudaStreamNonBlocking));
-  if (!s.aux_stream) VG_CUDA(cudaStreamCreateWithFlags(&s.aux_stream, cudaStreamNonBlocking));
-  while (s.xchg_events.size() < K + 2) {
-    cudaEvent_t e;
-    VG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    s.xchg_events.push_back(e);
+  if (!s.xchg_flags_host) {
+    void *h = nullptr, *d = nullptr;
+    VG_CUDA(cudaHostAlloc(&h, (XCHG_RANGES + 1) * 4, cudaHostAllocMapped));
+    std::memset(h, 0, (XCHG_RANGES + 1) * 4);
+    VG_CUDA(cudaHostGetDevicePointer(&d, h, 0));
+    s.xchg_flags_host = (unsigned *)h;
+    s.xchg_flags_dev = (unsigned *)d;
+    s.xchg_count.alloc((XCHG_RANGES + 1) * 4, &s.footprint);
   }
-  cudaEvent_t ev_start = s.xchg_events[K], ev_hub = s.xchg_events[K + 1];
-  auto launch = [&](unsigned b0, unsigned b1, cudaStream_t st) {
-    if (b1 <= b0) return;
-    OpinionArgs q = p;
-    q.blk_base = b0;
-    if (q.grid) k_opinion<true><<<b1 - b0, TPB, 0, st>>>(q);
-    else k_opinion<false><<<b1 - b0, TPB, 0, st>>>(q);
-    VG_CUDA(cudaGetLastError());
-  };
-  const bool hubs = p.hub_blocks > 0;
-  if (hubs) {
-    VG_CUDA(cudaEventRecord(ev_start, s.stream));
-    VG_CUDA(cudaStreamWaitEvent(s.aux_stream, ev_start, 0));
-    launch(0, p.hub_blocks, s.aux_stream);
-    VG_CUDA(cudaEventRecord(ev_hub, s.aux_stream));
+  if (++s.xchg_gen == 0) s.xchg_gen = 1;
+  Notify nt{};
+  nt.count = s.xchg_count.as<unsigned>();
+  nt.flag = s.xchg_flags_dev;
+  nt.gen = s.xchg_gen;
+  nt.nranges = K;
+  nt.hub_blocks = p.hub_blocks;
+  for (unsigned k = 0; k < K; k++) {
+    nt.end[k] = (unsigned)cs.range_block[k + 1];
+    nt.expect[k] = (unsigned)(cs.range_block[k + 1] - cs.range_block[k]);
   }
+  nt.expect[K] = p.hub_blocks;
+  VG_CUDA(cudaMemsetAsync(nt.count, 0, (K + 1) * 4, s.stream));
+  if (p.grid) k_opinion_notify<true><<<grid, TPB, 0, s.stream>>>(p, nt);
+  else k_opinion_notify<false><<<grid, TPB, 0, s.stream>>>(p, nt);
+  VG_CUDA(cudaGetLastError());
+
   const uint64_t n = std::min<uint64_t>(hx.n, p.n);
   double *out = (double *)hx.out[0];
-  auto holds_hub = [&](uint64_t lo, uint64_t hi) {  // a hub row in [lo, hi)?
-    auto it = std::lower_bound(cs.hub_rows_sorted.begin(), cs.hub_rows_sorted.end(), (uint32_t)lo);
-    return it != cs.hub_rows_sorted.end() && *it < hi;
-  };
-  std::vector<std::pair<uint64_t, uint64_t>> deferred;  // ranges that wait for the hubs
-  uint64_t done_rows = 0;
+  // rows [lo[k], hi[k]) are the windows from range k's first window up to
+  // range k + 1's; a window's rows may also sit in earlier ranges (a window
+  // can straddle a boundary), so the download waits for ranges first[k]..k,
+  // first[k] being the first range that reaches range k's first window
+  std::vector<uint64_t> lo(K), hi(K);
+  std::vector<unsigned> first(K);
+  std::vector<char> needs_hubs(K), issued(K, 0);
+  uint64_t prev = 0;
   for (unsigned k = 0; k < K; k++) {
-    launch((unsigned)cs.chunk_block[k], (unsigned)cs.chunk_block[k + 1], s.stream);
-    const uint64_t upto = k + 1 == K ? n : std::min(n, cs.chunk_rows[k]);
-    if (upto <= done_rows) continue;
-    if (hubs && holds_hub(done_rows, upto)) {
-      deferred.push_back({done_rows, upto});
-    } else {
-      VG_CUDA(cudaEventRecord(s.xchg_events[k], s.stream));
-      VG_CUDA(cudaStreamWaitEvent(s.copy_stream, s.xchg_events[k], 0));
-      VG_CUDA(cudaMemcpyAsync(out + done_rows, p.xo + done_rows, (upto - done_rows) * 8,
-                              cudaMemcpyDeviceToHost, s.copy_stream));
-    }
-    done_rows = upto;
+    lo[k] = prev;
+    hi[k] = std::max(prev, k + 1 == K ? n : std::min(n, cs.range_rows[k]));
+    auto it = std::lower_bound(cs.hub_rows_sorted.begin(), cs.hub_rows_sorted.end(),
+                               (uint32_t)lo[k]);
+    needs_hubs[k] = p.hub_blocks && it != cs.hub_rows_sorted.end() && *it < hi[k];
+    unsigned j = 0;
+    while (j < k && (j + 1 < K ? cs.range_window[j + 1] : 0xFFFFFFFFu) < cs.range_window[k]) j++;
+    first[k] = j;
+    prev = hi[k];
   }
-  if (hubs) {
-    VG_CUDA(cudaStreamWaitEvent(s.stream, ev_hub, 0));
-    if (!deferred.empty()) {
-      VG_CUDA(cudaEventRecord(s.xchg_events[K], s.stream));  // every chunk and the hubs
-      VG_CUDA(cudaStreamWaitEvent(s.copy_stream, s.xchg_events[K], 0));
-      for (auto &r : deferred)
-        VG_CUDA(cudaMemcpyAsync(out + r.first, p.xo + r.first, (r.second - r.first) * 8,
-                                cudaMemcpyDeviceToHost, s.copy_stream));
+  volatile unsigned *flag = s.xchg_flags_host;
+  auto issue = [&](unsigned k) {
+    if (hi[k] > lo[k])
+      VG_CUDA(cudaMemcpyAsync(out + lo[k], p.xo + lo[k], (hi[k] - lo[k]) * 8,
+                              cudaMemcpyDeviceToHost, s.copy_stream));
+    issued[k] = 1;
+  };
+  unsigned left = K;
+  for (uint64_t poll = 0; left; poll++) {
+    const bool hubs_done = p.hub_blocks == 0 || flag[K] == nt.gen;
+    for (unsigned k = 0; k < K; k++) {
+      if (issued[k] || (needs_hubs[k] && !hubs_done)) continue;
+      bool ready = true;
+      for (unsigned j = first[k]; j <= k && ready; j++) ready = flag[j] == nt.gen;
+      if (ready) {
+        issue(k);
+        left--;
+      }
     }
+    if (left && (poll & 255) == 255 && cudaStreamQuery(s.stream) != cudaErrorNotReady) break;
+  }
+  if (left) {  // the launch ended (or failed) without reporting every range
+    VG_CUDA(cudaStreamSynchronize(s.stream));
+    for (unsigned k = 0; k < K; k++)
+      if (!issued[k]) issue(k);
   }
   hx.done = true;
 }

@@ -207,9 +207,12 @@ class Batch:
     def tuning(self):
         p, t, n = C.c_int(), C.c_int(), C.c_uint64()
         thr = C.c_uint32()
-        check(lib().vg_batch_tuning(self._h, C.byref(p), C.byref(t), C.byref(thr), C.byref(n)))
+        gm, pm = C.c_double(), C.c_double()
+        check(lib().vg_batch_tuning(self._h, C.byref(p), C.byref(t), C.byref(thr), C.byref(n),
+                                    C.byref(gm), C.byref(pm)))
         return {"persistent": bool(p.value), "persistent_tpb": t.value,
-                "bucket_threshold": thr.value, "heavy_agents": n.value}
+                "bucket_threshold": thr.value, "heavy_agents": n.value,
+                "trial_ms_per_step_graph": gm.value, "trial_ms_per_step_persistent": pm.value}
 
     def close(self):
         if self._h:
