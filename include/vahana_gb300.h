@@ -290,8 +290,9 @@ int vg_apply(vg_sim *s, const char *transition, const int *call, int ncall,
  * vg_write_agents, vg_apply and vg_read_agents (src/Simulation.jl:720-821
  * with the state round-tripped through the host, as a Julia caller whose
  * agent vectors live in host memory does).  For "bounded_confidence" the
- * gather runs in row-range chunks and each finished range is downloaded
- * while the next one computes (pinned host buffers for the overlap). */
+ * gather launch reports each finished range of rows and the range is
+ * downloaded while the launch goes on (pinned host buffers for the
+ * overlap). */
 int vg_apply_host(vg_sim *s, const char *transition, const int *call, int ncall,
                   const int *read, int nread, const int *write, int nwrite,
                   const int *add_existing, int nadd, int with_edge,

@@ -651,10 +651,10 @@ int vg_apply(vg_sim *h, const char *tname, const int *call, int ncall, const int
 
 // apply! with the called type's state exchanged with host memory: upload,
 // the transition, download.  The upload runs on the simulation's stream
-// ahead of the kernels; a transition that completes its rows range by range
-// (bounded_confidence) downloads each finished range on a second stream
-// while it computes the next one; otherwise the new state is downloaded
-// after the transition.  Returns when the new state is in out_fields.
+// ahead of the kernels; a transition whose launch reports finished row
+// ranges (bounded_confidence) has each range downloaded on a second stream
+// while the launch goes on; otherwise the new state is downloaded after the
+// transition.  Returns when the new state is in out_fields.
 int vg_apply_host(vg_sim *h, const char *tname, const int *call, int ncall, const int *read,
                   int nread, const int *write, int nwrite, const int *ae, int nae, int with_edge,
                   const double *params, int nparams, int type_nr, const void *const *in_fields,
