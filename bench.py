@@ -77,6 +77,8 @@ def parse():
     ap.add_argument("--plain-sample", type=int, default=24)
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=200)
+    ap.add_argument("--batch-warmup-instances", type=int, default=8,
+                    help="batch workload: instances of the warm-up batch built first (0: none)")
     ap.add_argument("--model-steps", type=int, default=0,
                     help="sir/life workloads: timed steps (default: the model's 100 / 1000)")
     return ap.parse_args()
@@ -527,9 +529,11 @@ def run_batch(args):
     n_inst, steps = args.instances, args.batch_steps
     N, deg, beta, rec, seeds = models.batch_params(n_inst)
     # warm-up on a small batch (graph capture machinery, autotuner)
-    w = models.Batch(N[:8], deg[:8], beta[:8], rec[:8], seeds[:8])
-    w.step(steps, mode=3)
-    w.close()
+    k = args.batch_warmup_instances
+    if k > 0:
+        w = models.Batch(N[:k], deg[:k], beta[:k], rec[:k], seeds[:k])
+        w.step(steps, mode=3)
+        w.close()
     b = models.Batch(N, deg, beta, rec, seeds)
     torch.cuda.synchronize()
     timed = {}

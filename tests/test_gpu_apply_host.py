@@ -73,3 +73,31 @@ def test_apply_host_sir_matches_apply(vh):
     assert (state == 2).sum() > 0
     run.close()
     twin.close()
+
+
+def test_apply_host_ordered_path_and_partial_n(vh):
+    """No hub split (no hub warps: every range reports on its own) and a
+    host exchange of the first n agents only: equal to write + apply! + read
+    of the same agents."""
+    from vahana_gb300 import models
+    n = 200_000
+    run = models.build_opinion(n=n, mean_degree=15, gamma=2.5, wmax=3000, eps=0.3, seed=23)
+    twin = models.build_opinion(n=n, mean_degree=15, gamma=2.5, wmax=3000, eps=0.3, seed=23)
+    vh.finish_init(run.sim)
+    vh.finish_init(twin.sim)
+    params = [run.model["Weight"].index, 0.3, 0.5, 0.5, 4294967295]
+    rng = np.random.default_rng(8)
+    for m in (n, n // 3):
+        x = rng.random(m)
+        got = vh.apply_host(run.sim, "bounded_confidence", ["Opinion"], ["Opinion", "Weight"],
+                            ["Opinion"], "Opinion", {"x": x}, params=params)["x"]
+        vh.write_agents(twin.sim, "Opinion", x=x)
+        vh.apply_(twin.sim, "bounded_confidence", ["Opinion"], ["Opinion", "Weight"],
+                  ["Opinion"], params=params)
+        ref = vh.read_agents(twin.sim, "Opinion")[0]["x"]
+        assert got.size == m
+        np.testing.assert_array_equal(got.view(np.uint64), ref[:m].view(np.uint64))
+        np.testing.assert_array_equal(vh.read_agents(run.sim, "Opinion")[0]["x"].view(np.uint64),
+                                      ref.view(np.uint64))
+    run.close()
+    twin.close()
