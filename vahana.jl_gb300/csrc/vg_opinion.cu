@@ -585,25 +585,37 @@ __global__ void __launch_bounds__(TPB, 9) k_opinion(OpinionArgs p) {
 // hub warps' blocks form range `nranges`, slice blocks below end[k] (and not
 // below end[k - 1]) range k; the block that completes a range writes the
 // call's generation to the range's flag in mapped host memory.
+// A block of this launch runs one block of hub warps or XCHG_GROUP
+// consecutive blocks of slices (the same work, in the same order, as
+// k_opinion's blocks), so that the report at its end -- a barrier, one
+// fence and one atomic -- is paid once per four slice blocks.
 constexpr unsigned XCHG_RANGES = 16;
+constexpr unsigned XCHG_GROUP = 4;
 struct Notify {
   unsigned *count;  // device: blocks finished per range
   unsigned *flag;   // mapped host memory: generation of the finished range
-  unsigned gen, nranges, hub_blocks;
-  unsigned end[XCHG_RANGES];
+  unsigned gen, nranges, hub_blocks, slice_blocks;
+  unsigned end[XCHG_RANGES];  // launch blocks: range k ends before end[k]
   unsigned expect[XCHG_RANGES + 1];
 };
 
 template <bool GRID>
 __global__ void __launch_bounds__(TPB, 9) k_opinion_notify(OpinionArgs p, Notify nt) {
-  opinion_block<GRID, false>(p, blockIdx.x);
-  __threadfence();  // this thread's results reach L2 before the block reports
-  __syncthreads();
+  const unsigned b = blockIdx.x;
+  if (b < nt.hub_blocks) {
+    opinion_block<GRID, false>(p, b);
+  } else {
+    const unsigned v0 = nt.hub_blocks + (b - nt.hub_blocks) * XCHG_GROUP;
+    for (unsigned g = 0; g < XCHG_GROUP; g++)
+      if (v0 + g < nt.hub_blocks + nt.slice_blocks) opinion_block<GRID, false>(p, v0 + g);
+  }
+  __syncthreads();  // the block's results, then one GPU-scope fence (cumulative)
   if (threadIdx.x == 0) {
+    __threadfence();
     unsigned r = nt.nranges;  // the hub warps
-    if (blockIdx.x >= nt.hub_blocks) {
+    if (b >= nt.hub_blocks) {
       r = 0;
-      while (r + 1 < nt.nranges && blockIdx.x >= nt.end[r]) r++;
+      while (r + 1 < nt.nranges && b >= nt.end[r]) r++;
     }
     if (atomicAdd(nt.count + r, 1u) + 1 == nt.expect[r]) {
       __threadfence_system();
@@ -712,23 +724,26 @@ void tr_bounded_confidence(ApplyCtx &c) {
   VG_CUDA(cudaGetLastError());
 }
 
-// Row ranges of the gather: range k is the slice blocks [range_block[k],
-// range_block[k + 1]) (equal block counts); the rows are sorted by window
-// (row >> wshift) before degree, so once range k is done every non-hub row
-// of the windows below the window of range k + 1's first row is final:
-// range_rows[k] = that window << wshift.  hub_rows_sorted: the hub rows.
-static void range_bounds(Sim &s, CSR &cs, uint64_t n, unsigned hub_blocks, unsigned slice_blocks) {
-  const unsigned K = std::max(1u, std::min(XCHG_RANGES, slice_blocks));
+// Row ranges of the gather: range k is the launch blocks [range_block[k],
+// range_block[k + 1]) of the reporting launch (equal counts of its slice
+// blocks, XCHG_GROUP slice blocks of k_opinion each); the rows are sorted by
+// window (row >> wshift) before degree, so once range k is done every
+// non-hub row of the windows below the window of range k + 1's first row is
+// final: range_rows[k] = that window << wshift.  hub_rows_sorted: the hub
+// rows.
+static void range_bounds(Sim &s, CSR &cs, uint64_t n, unsigned hub_blocks, unsigned groups) {
+  const unsigned K = std::max(1u, std::min(XCHG_RANGES, groups));
   if (cs.range_block.size() == K + 1) return;
   cs.range_block.assign(K + 1, 0);
   cs.range_rows.assign(K, n);
   cs.range_window.assign(K, 0xFFFFFFFFu);
   cs.range_window[0] = 0;
   for (unsigned k = 0; k <= K; k++)
-    cs.range_block[k] = hub_blocks + (uint64_t)slice_blocks * k / K;
+    cs.range_block[k] = hub_blocks + (uint64_t)groups * k / K;
   for (unsigned k = 0; k + 1 < K; k++) {
-    // first position in `order` of the block: TPB / 32 slices of 32 rows per block
-    const uint64_t pos = (cs.range_block[k + 1] - hub_blocks) * (uint64_t)TPB;
+    // first position in `order` of the launch block: XCHG_GROUP slice blocks
+    // of TPB / 32 slices of 32 rows each
+    const uint64_t pos = (cs.range_block[k + 1] - hub_blocks) * XCHG_GROUP * (uint64_t)TPB;
     if (pos >= cs.norder) continue;
     uint32_t row = 0;
     VG_CUDA(cudaMemcpyAsync(&row, cs.order.as<uint32_t>() + pos, 4, cudaMemcpyDeviceToHost,
@@ -755,7 +770,9 @@ static void range_bounds(Sim &s, CSR &cs, uint64_t n, unsigned hub_blocks, unsig
 // are downloaded after it, so the wait is bounded by the launch itself.
 static void launch_notified(Sim &s, OpinionArgs &p, unsigned grid, Sim::HostExchange &hx) {
   CSR &cs = *p.csr;
-  range_bounds(s, cs, p.n, p.hub_blocks, grid - p.hub_blocks);
+  const unsigned slice_blocks = grid - p.hub_blocks;
+  const unsigned groups = (slice_blocks + XCHG_GROUP - 1) / XCHG_GROUP;
+  range_bounds(s, cs, p.n, p.hub_blocks, groups);
   const unsigned K = (unsigned)cs.range_rows.size();
   if (!s.copy_stream) VG_CUDA(cudaStreamCreateWithFlags(&s.copy_stream, cudaStreamNonBlocking));
   if (!s.xchg_flags_host) {
@@ -774,14 +791,16 @@ static void launch_notified(Sim &s, OpinionArgs &p, unsigned grid, Sim::HostExch
   nt.gen = s.xchg_gen;
   nt.nranges = K;
   nt.hub_blocks = p.hub_blocks;
+  nt.slice_blocks = slice_blocks;
   for (unsigned k = 0; k < K; k++) {
     nt.end[k] = (unsigned)cs.range_block[k + 1];
     nt.expect[k] = (unsigned)(cs.range_block[k + 1] - cs.range_block[k]);
   }
   nt.expect[K] = p.hub_blocks;
   VG_CUDA(cudaMemsetAsync(nt.count, 0, (K + 1) * 4, s.stream));
-  if (p.grid) k_opinion_notify<true><<<grid, TPB, 0, s.stream>>>(p, nt);
-  else k_opinion_notify<false><<<grid, TPB, 0, s.stream>>>(p, nt);
+  const unsigned launch_blocks = p.hub_blocks + groups;
+  if (p.grid) k_opinion_notify<true><<<launch_blocks, TPB, 0, s.stream>>>(p, nt);
+  else k_opinion_notify<false><<<launch_blocks, TPB, 0, s.stream>>>(p, nt);
   VG_CUDA(cudaGetLastError());
 
   const uint64_t n = std::min<uint64_t>(hx.n, p.n);
