@@ -970,8 +970,6 @@ void ensure_schedule(Sim &s, CSR &c, uint32_t thr, uint32_t big_thr, uint64_t n)
   c.range_block.clear();
   c.range_rows.clear();
   c.range_window.clear();
-  c.group_start.release();
-  c.ngroups = 0;
   c.hub_rows_sorted.clear();
   if (n > 0 && c.row_ptr.p) {
     const uint32_t *rp = c.row_ptr.as<uint32_t>();

@@ -200,11 +200,6 @@ struct CSR {
   // range_rows[k]; derived from the layout, cached with it
   std::vector<uint64_t> range_block, range_rows;
   std::vector<uint32_t> range_window;  // window of each range's first row
-  // the reporting launch's slice blocks: launch block g runs the slice
-  // blocks [group_start[g], group_start[g + 1]) (a few light ones together,
-  // a heavy one alone); on the device and its count
-  DevBuf group_start;
-  uint32_t ngroups = 0;
   std::vector<uint32_t> hub_rows_sorted;  // host copy of the hub rows, ascending
   // payload field 0 (Float64) holds only multiples of 2^-53 in (0, 1]:
   // -1 not checked yet, 0 no, 1 yes (decides the gather kernels' sum path)

@@ -582,39 +582,29 @@ __global__ void __launch_bounds__(TPB, 9) k_opinion(OpinionArgs p) {
 }
 
 // Completion reports of one gather launch (apply! with host exchange): the
-// hub warps' blocks form range `nranges`, slice blocks below end[k] (and not
-// below end[k - 1]) range k; the block that completes a range writes the
+// launch is k_opinion's (the same blocks, the same work); the hub warps'
+// blocks form range `nranges`, slice blocks below end[k] (and not below
+// end[k - 1]) range k.  A block reports once its rows are stored: after the
+// block barrier its first thread fences (GPU scope, cumulative over the
+// block's stores) and adds 1 to its range's counter; the block that
+// completes a range makes the range visible system-wide and writes the
 // call's generation to the range's flag in mapped host memory.
-// A block of this launch runs one block of hub warps or a group of
-// consecutive slice blocks of k_opinion (the same work, in the same order):
-// up to XCHG_GROUP light ones together, a heavy one alone (the long slices
-// of the first windows must keep running side by side), so that the report
-// at a block's end -- a barrier, one fence and one atomic -- is paid about
-// once per XCHG_GROUP slice blocks.
 constexpr unsigned XCHG_RANGES = 16;
-constexpr unsigned XCHG_GROUP = 4;
 struct Notify {
   unsigned *count;  // device: blocks finished per range
   unsigned *flag;   // mapped host memory: generation of the finished range
-  const uint32_t *group_start;  // slice block of each launch block (+ end)
   unsigned gen, nranges, hub_blocks;
-  unsigned end[XCHG_RANGES];  // launch blocks: range k ends before end[k]
-  unsigned expect[XCHG_RANGES + 1];
+  unsigned end[XCHG_RANGES];         // launch blocks: range k ends before end[k]
+  unsigned expect[XCHG_RANGES + 1];  // blocks per range
 };
 
 template <bool GRID>
 __global__ void __launch_bounds__(TPB, 9) k_opinion_notify(OpinionArgs p, Notify nt) {
-  const unsigned b = blockIdx.x;
-  if (b < nt.hub_blocks) {
-    opinion_block<GRID, false>(p, b);
-  } else {
-    const unsigned v0 = nt.group_start[b - nt.hub_blocks];
-    const unsigned v1 = nt.group_start[b - nt.hub_blocks + 1];
-    for (unsigned v = v0; v < v1; v++) opinion_block<GRID, false>(p, nt.hub_blocks + v);
-  }
-  __syncthreads();  // the block's results, then one GPU-scope fence (cumulative)
+  opinion_block<GRID, false>(p, blockIdx.x);
+  __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
+    const unsigned b = blockIdx.x;
     unsigned r = nt.nranges;  // the hub warps
     if (b >= nt.hub_blocks) {
       r = 0;
@@ -727,55 +717,26 @@ void tr_bounded_confidence(ApplyCtx &c) {
   VG_CUDA(cudaGetLastError());
 }
 
-// Groups of slice blocks for the reporting launch (greedy over the slice
-// blocks in order: a group takes the next block while it has fewer than
-// XCHG_GROUP and stays within XCHG_GROUP average blocks of work, a block's
-// work being its slices' column slots plus a per-row cost), then row
-// ranges: range k is the launch blocks [range_block[k], range_block[k + 1])
-// (equal counts of groups); the rows are sorted by window (row >> wshift)
-// before degree, so once range k is done every non-hub row of the windows
-// below the window of range k + 1's first row is final: range_rows[k] =
-// that window << wshift.  hub_rows_sorted: the hub rows.
+// Row ranges of the gather: range k is the launch blocks [range_block[k],
+// range_block[k + 1]) (equal shares of the slice blocks); the rows are
+// sorted by window (row >> wshift) before degree, so once range k is done
+// every non-hub row of the windows below the window of range k + 1's first
+// row is final: range_rows[k] = that window << wshift.  hub_rows_sorted:
+// the hub rows.
 static void range_bounds(Sim &s, CSR &cs, uint64_t n, unsigned hub_blocks, unsigned slice_blocks) {
-  if (cs.ngroups && cs.group_start.p) return;
-  std::vector<uint64_t> base(cs.nslices + 1);
-  VG_CUDA(cudaMemcpyAsync(base.data(), cs.slice_base.p, base.size() * 8, cudaMemcpyDeviceToHost,
-                          s.stream));
-  VG_CUDA(cudaStreamSynchronize(s.stream));
-  constexpr uint64_t ROW_COST = 2;  // slots' worth of work per row (row, degree, result)
-  auto work = [&](uint64_t blk) {   // slice block blk
-    const uint64_t s0 = std::min<uint64_t>(blk * (TPB / 32), cs.nslices);
-    const uint64_t s1 = std::min<uint64_t>(s0 + TPB / 32, cs.nslices);
-    return base[s1] - base[s0] + ROW_COST * 32 * (s1 - s0);
-  };
-  const uint64_t total = base[cs.nslices] + ROW_COST * 32 * cs.nslices;
-  const uint64_t limit = XCHG_GROUP * (total / std::max<uint64_t>(slice_blocks, 1) + 1);
-  std::vector<uint32_t> gs;
-  for (uint64_t b = 0; b < slice_blocks;) {
-    gs.push_back((uint32_t)b);
-    uint64_t w = work(b++);
-    for (unsigned k = 1; k < XCHG_GROUP && b < slice_blocks && w + work(b) <= limit; k++)
-      w += work(b++);
-  }
-  const unsigned groups = (unsigned)gs.size();
-  gs.push_back((uint32_t)slice_blocks);
-  cs.group_start.alloc(gs.size() * 4, &s.footprint);
-  VG_CUDA(cudaMemcpyAsync(cs.group_start.p, gs.data(), gs.size() * 4, cudaMemcpyHostToDevice,
-                          s.stream));
-  VG_CUDA(cudaStreamSynchronize(s.stream));
-  cs.ngroups = groups;
-
-  const unsigned K = std::max(1u, std::min(XCHG_RANGES, groups));
+  if (!cs.range_block.empty() && cs.range_block.back() == hub_blocks + (uint64_t)slice_blocks)
+    return;
+  const unsigned K = std::max(1u, std::min(XCHG_RANGES, slice_blocks));
   cs.range_block.assign(K + 1, 0);
   cs.range_rows.assign(K, n);
   cs.range_window.assign(K, 0xFFFFFFFFu);
   cs.range_window[0] = 0;
   for (unsigned k = 0; k <= K; k++)
-    cs.range_block[k] = hub_blocks + (uint64_t)groups * k / K;
+    cs.range_block[k] = hub_blocks + (uint64_t)slice_blocks * k / K;
   for (unsigned k = 0; k + 1 < K; k++) {
-    // first position in `order` of the launch block's first slice block
-    // (TPB / 32 slices of 32 rows per slice block)
-    const uint64_t pos = (uint64_t)gs[cs.range_block[k + 1] - hub_blocks] * TPB;
+    // first position in `order` of the range's first block (TPB / 32
+    // slices of 32 rows per block)
+    const uint64_t pos = (cs.range_block[k + 1] - hub_blocks) * TPB;
     if (pos >= cs.norder) continue;
     uint32_t row = 0;
     VG_CUDA(cudaMemcpyAsync(&row, cs.order.as<uint32_t>() + pos, 4, cudaMemcpyDeviceToHost,
@@ -804,7 +765,6 @@ static void launch_notified(Sim &s, OpinionArgs &p, unsigned grid, Sim::HostExch
   CSR &cs = *p.csr;
   const unsigned slice_blocks = grid - p.hub_blocks;
   range_bounds(s, cs, p.n, p.hub_blocks, slice_blocks);
-  const unsigned groups = cs.ngroups;
   const unsigned K = (unsigned)cs.range_rows.size();
   if (!s.copy_stream) VG_CUDA(cudaStreamCreateWithFlags(&s.copy_stream, cudaStreamNonBlocking));
   if (!s.xchg_flags_host) {
@@ -823,16 +783,14 @@ static void launch_notified(Sim &s, OpinionArgs &p, unsigned grid, Sim::HostExch
   nt.gen = s.xchg_gen;
   nt.nranges = K;
   nt.hub_blocks = p.hub_blocks;
-  nt.group_start = cs.group_start.as<uint32_t>();
   for (unsigned k = 0; k < K; k++) {
     nt.end[k] = (unsigned)cs.range_block[k + 1];
     nt.expect[k] = (unsigned)(cs.range_block[k + 1] - cs.range_block[k]);
   }
   nt.expect[K] = p.hub_blocks;
   VG_CUDA(cudaMemsetAsync(nt.count, 0, (K + 1) * 4, s.stream));
-  const unsigned launch_blocks = p.hub_blocks + groups;
-  if (p.grid) k_opinion_notify<true><<<launch_blocks, TPB, 0, s.stream>>>(p, nt);
-  else k_opinion_notify<false><<<launch_blocks, TPB, 0, s.stream>>>(p, nt);
+  if (p.grid) k_opinion_notify<true><<<grid, TPB, 0, s.stream>>>(p, nt);
+  else k_opinion_notify<false><<<grid, TPB, 0, s.stream>>>(p, nt);
   VG_CUDA(cudaGetLastError());
 
   const uint64_t n = std::min<uint64_t>(hx.n, p.n);
