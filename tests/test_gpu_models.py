@@ -32,6 +32,41 @@ def test_sir_bit_exact(vh):
     run.close()
 
 
+def test_sir_steps_around_contact_rebuilds(vh):
+    """SIR steps run with programmatic dependent launch (the next step reads
+    its contact rows before waiting for the previous one) only while no edge
+    container was rewritten since the previous step: steps around an
+    identical rebuild of the contacts (add_existing) and around the removal
+    of every contact equal the oracle's steps on the graph of that moment."""
+    from vahana_gb300 import models
+    run = models.build_sir(n=3000, degree=10, beta=0.05, recovery=7, seed=11, n_infected=60)
+    sim, m = run.sim, run.model
+    frm, to, _ = models.staged_edges(sim, "Contact")
+    st0, d0 = vh.read_agents(sim, "Person")[0].values()
+    vh.finish_init(sim)
+    full = om.build_inedges(run.n, frm, to)
+    empty = om.build_inedges(run.n, np.zeros(0, np.int64), np.zeros(0, np.int64))
+    s_ref, d_ref = np.ascontiguousarray(st0, np.uint8), np.ascontiguousarray(d0, np.int32)
+    g, t = full, 1
+    plan = ["sir"] * 4 + ["rebuild"] + ["sir"] * 4 + ["remove"] + ["sir"] * 4
+    for what in plan:
+        if what == "sir":
+            run.step()
+            s_ref, d_ref = om.sir_step(g, s_ref, d_ref, 0.05, 7, 11, t)
+        elif what == "rebuild":  # the same contacts, a new container
+            vh.apply_(sim, "keep", ["Person"], ["Person"], ["Contact"], add_existing=["Contact"])
+        else:  # every Person removes its contacts
+            vh.apply_(sim, "remove_edges", ["Person"], ["Person"], ["Contact"],
+                      params=[m["Contact"].index, 0, 0, 0])
+            g = empty
+        t += 1
+        cols = vh.read_agents(sim, "Person")[0]
+        np.testing.assert_array_equal(cols["state"], s_ref)
+        np.testing.assert_array_equal(cols["days"], d_ref)
+    assert vh.num_edges(sim, "Contact") == 0
+    run.close()
+
+
 def test_sir_changing_beta_between_steps(vh):
     """The infection table (1 - (1 - beta)^k per infected-neighbour count)
     is uploaded once per content: a beta that changes between apply! calls

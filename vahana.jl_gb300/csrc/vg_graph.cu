@@ -388,6 +388,7 @@ bool build_csr_typed(Sim &s, int e, const EdgeAppend &ap, uint64_t n) {
     return false;
   const int T = ap.target_type;
   if (T > (int)s.model->atypes.size() || (ed.singletype() && T != ed.target)) return false;
+  s.csr_epoch++;
   cudaStream_t st = s.stream;
   if (es.csr.size() < (size_t)MAX_AGENT_TYPES) es.csr.resize(MAX_AGENT_TYPES);
   for (int U = 1; U < (int)es.csr.size(); U++)
@@ -481,6 +482,7 @@ void build_csr_from_records(Sim &s, int e, const uint64_t *d_from,
                             const std::vector<const void *> &d_payload,
                             uint64_t n, bool records_sorted_by_key,
                             const uint64_t *d_key, bool merge_existing) {
+  s.csr_epoch++;
   const EdgeTypeDesc &ed = s.model->et(e);
   EdgeStore &es = s.edges[e];
   cudaStream_t st = s.stream;
@@ -684,6 +686,7 @@ static void compact_csr(Sim &s, const EdgeTypeDesc &ed, CSR &c, const uint32_t *
 
 void remove_died_edges(Sim &s, int died_type, const uint8_t *died,
                        uint64_t died_n) {
+  s.csr_epoch++;
   cudaStream_t st = s.stream;
   for (size_t e = 0; e < s.edges.size(); e++) {
     EdgeStore &es = s.edges[e];
@@ -771,6 +774,7 @@ __global__ void k_gather_u64(const uint64_t *in, const uint32_t *perm, uint64_t 
 
 void apply_edge_removals(Sim &s, int e, EdgeRemoval &rm, EdgeAppend *ap, uint64_t &n_records,
                          bool merge_existing) {
+  s.csr_epoch++;
   cudaStream_t st = s.stream;
   const EdgeTypeDesc &ed = s.model->et(e);
   EdgeStore &es = s.edges[e];

@@ -263,6 +263,13 @@ struct Sim {
   bool intransition = false;
   bool check_readable = true;
   int64_t num_transitions = 0;
+  // Incremented whenever work that writes an edge container (CSR) is
+  // enqueued.  A SIR step launched with programmatic dependent launch reads
+  // its contact rows before waiting for the preceding kernel; it does so
+  // only while no CSR write was enqueued since the previous SIR step
+  // (sir_epoch: csr_epoch at that step), so the preceding kernel cannot be
+  // writing them.
+  uint64_t csr_epoch = 1, sir_epoch = 0;
   uint64_t footprint = 0;
   std::vector<AgentStore> agents;  // index = nr - 1
   std::vector<EdgeStore> edges;    // index = edge type index

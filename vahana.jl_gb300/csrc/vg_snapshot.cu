@@ -314,6 +314,7 @@ int vg_sim_load(vg_model *m, const char *path, void *stream, vg_sim **out) {
     }
     const uint64_t ncsr = F.get<uint64_t>();
     if (ncsr > MAX_AGENT_TYPES) fail(VG_ERR_ARG, "corrupt snapshot");
+    s.csr_epoch++;
     es.csr.clear();
     es.csr.resize(ncsr);
     for (uint64_t T = 0; T < ncsr; T++) {

@@ -580,20 +580,41 @@ __global__ void k_move_to(Sweep s, MoveArgs m, int call_pos) {
 // with k infected in-neighbours is infected with p_k = 1 - (1 - beta)^k
 // (p_k from the host table, built by the same repeated multiplication);
 // an infected agent recovers when days reaches `recovery`.
+constexpr int SIR_U = 16;
+
+// One SIR step.  Launched with programmatic dependent launch when the
+// contact rows cannot be written by the preceding kernel (Sim::csr_epoch):
+// this grid lets the next step's grid be scheduled once all its blocks run,
+// and each thread requests its row bounds and first SIR_U sources before
+// griddepcontrol.wait; the states (written by the previous step) and every
+// output are touched only after it.  Without the launch attribute the wait
+// returns at once.  SIR_U sources are requested together, then their
+// states: two memory round trips for a row of up to SIR_U in-edges.
 __global__ void k_sir(const uint32_t *__restrict__ rp, const uint32_t *__restrict__ src,
-                      const uint8_t *__restrict__ st_rd, const int32_t *__restrict__ d_rd,
-                      uint8_t *__restrict__ st_wr, int32_t *__restrict__ d_wr, uint64_t n,
-                      uint64_t nrows, const double *__restrict__ ptab, uint32_t ptab_n,
-                      uint64_t seed, uint32_t step, int32_t recovery, int *status) {
-  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+                      const uint8_t *st_rd, const int32_t *d_rd, uint8_t *st_wr, int32_t *d_wr,
+                      uint64_t n, uint64_t nrows, const double *__restrict__ ptab,
+                      uint32_t ptab_n, uint64_t seed, uint32_t step, int32_t recovery,
+                      int *status) {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool row = i < n && i < nrows;
+  uint32_t q = row ? __ldg(rp + i) : 0u;
+  const uint32_t e = row ? __ldg(rp + i + 1) : 0u;
+  uint32_t sv[SIR_U];
+#pragma unroll
+  for (int u = 0; u < SIR_U; u++) sv[u] = q + u < e ? __ldg(src + q + u) : 0u;
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   if (i >= n) return;
   uint8_t s = st_rd[i];
   int32_t d = d_rd[i];
   if (s == 0) {
     uint32_t k = 0;
-    if (i < nrows) {
-      uint32_t e = rp[i + 1];
-      for (uint32_t q = rp[i]; q < e; q++) k += (__ldg(st_rd + src[q]) == 1);
+    while (q < e) {
+#pragma unroll
+      for (int u = 0; u < SIR_U; u++) k += (q + u < e ? st_rd[sv[u]] : 0) == 1;
+      q += SIR_U;
+#pragma unroll
+      for (int u = 0; u < SIR_U; u++) sv[u] = q + u < e ? __ldg(src + q + u) : 0u;
     }
     if (k > 0) {
       if (k >= ptab_n) {
@@ -1125,12 +1146,22 @@ void tr_sir(ApplyCtx &c) {
   const double *d_ptab = (const double *)s.const_table("sir.p_infect", ptab.data(), ptab.size() * 8);
   DevAgentView a = agent_view(s, c.call_type);
   if (a.n == 0) return;
-  k_sir<<<nblk(a.n), TPB, 0, s.stream>>>(v.row_ptr, v.src, (const uint8_t *)a.rd[0],
-                                         (const int32_t *)a.rd[1], (uint8_t *)a.wr[0],
-                                         (int32_t *)a.wr[1], a.n, v.nrows, d_ptab,
-                                         (uint32_t)ptab.size(), seed, (uint32_t)c.step, rec,
-                                         s.d_status.as<int>());
-  VG_CUDA(cudaGetLastError());
+  // programmatic dependent launch only while no edge container was written
+  // since the previous SIR step (the kernel reads its rows before waiting)
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(nblk(a.n));
+  cfg.blockDim = dim3(TPB);
+  cfg.stream = s.stream;
+  cfg.attrs = attr;
+  cfg.numAttrs = s.sir_epoch == s.csr_epoch ? 1 : 0;
+  VG_CUDA(cudaLaunchKernelEx(&cfg, k_sir, v.row_ptr, v.src, (const uint8_t *)a.rd[0],
+                             (const int32_t *)a.rd[1], (uint8_t *)a.wr[0], (int32_t *)a.wr[1],
+                             a.n, v.nrows, d_ptab, (uint32_t)ptab.size(), seed,
+                             (uint32_t)c.step, rec, s.d_status.as<int>()));
+  s.sir_epoch = s.csr_epoch;
 }
 
 void tr_life(ApplyCtx &c) {

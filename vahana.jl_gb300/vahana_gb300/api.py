@@ -707,6 +707,23 @@ def apply_(sim, transition, call, read, write, add_existing=(), with_edge=None, 
     return sim
 
 
+def prepare_apply(sim, transition, call, read, write, add_existing=(), with_edge=None,
+                  params=()):
+    """A callable that runs apply_(sim, transition, call, read, write, ...)
+    with these arguments, marshalled to C once: the cheapest form of a step
+    loop that repeats one apply! (params or globals bound to parameter
+    slots still take their values at each call)."""
+    args = _apply_args(sim, transition, call, read, write, add_existing, with_edge, params)
+    fn = lib().vg_apply
+
+    def run():
+        rc = fn(sim._h, *args)
+        if rc:
+            check(rc)
+        return sim
+    return run
+
+
 def apply_host(sim, transition, call, read, write, T, state, out=None, add_existing=(),
                with_edge=None, params=()):
     """apply! with type T's state kept in host memory (vg_apply_host): the

@@ -64,10 +64,8 @@ def build_sir(n=100_000, degree=10, beta=0.05, recovery=7, seed=1, stream=None,
     run = Run(sim, model=model, ids=ids, beta=beta, recovery=recovery, seed=seed, n=n,
               degree=degree)
 
-    def step():
-        api.apply_(sim, "sir", ["Person"], ["Person", "Contact"], ["Person"],
-                   params=[model["Contact"].index, beta, recovery, seed])
-    run.step = step
+    run.step = api.prepare_apply(sim, "sir", ["Person"], ["Person", "Contact"], ["Person"],
+                                 params=[model["Contact"].index, beta, recovery, seed])
     run.edges_per_step = lambda: n * degree
     return run
 
@@ -102,10 +100,9 @@ def build_opinion(n=10_000_000, mean_degree=20, gamma=2.5, wmax=1e4, eps=0.3, se
                                       int(seed), 0))
     run = Run(sim, model=model, ids=ids, eps=eps, seed=seed, n=n, nedges=nedges)
 
-    def step():
-        api.apply_(sim, "bounded_confidence", ["Opinion"], ["Opinion", "Weight"], ["Opinion"],
-                   params=[model["Weight"].index, eps, 0.5, 0.5, hub_threshold])
-    run.step = step
+    run.step = api.prepare_apply(sim, "bounded_confidence", ["Opinion"], ["Opinion", "Weight"],
+                                 ["Opinion"],
+                                 params=[model["Weight"].index, eps, 0.5, 0.5, hub_threshold])
     run.edges_per_step = lambda: nedges
     return run
 
@@ -254,11 +251,14 @@ def build_life(width=4096, height=4096, n_walkers=1_000_000, density=0.3, seed=1
         api.add_edges(sim, "OnCell", wids, cells)
     run = Run(sim, model=model, width=width, height=height, n_walkers=n_walkers, seed=seed)
 
+    life = api.prepare_apply(sim, "life", ["Cell"], ["Cell", "Neighbor"], ["Cell"],
+                             params=[model["Neighbor"].index])
+    walk = api.prepare_apply(sim, "random_walk", ["Walker"], ["Walker"], ["Walker", "OnCell"],
+                             params=[model["OnCell"].index, 0, seed])
+
     def step():
-        api.apply_(sim, "life", ["Cell"], ["Cell", "Neighbor"], ["Cell"],
-                   params=[model["Neighbor"].index])
-        api.apply_(sim, "random_walk", ["Walker"], ["Walker"], ["Walker", "OnCell"],
-                   params=[model["OnCell"].index, 0, seed])
+        life()
+        walk()
     run.step = step
     run.edges_per_step = lambda: 8 * width * height + n_walkers
     return run
