@@ -513,68 +513,96 @@ def run_secondaries(args):
 
 def run_batch(args):
     """Batched ensemble: 512 SIR instances (N log-uniform 1e3..1e5, out-degree
-    5..30, beta 0.01..0.1, recovery 5..10, seed = instance index), 200 steps,
-    against the same instances stepped one at a time with the plain kernels
-    (apply! per instance and step).  Batched calls of `steps` steps: the
-    first in the autotuner's form (mode 3; it includes the autotuner and, for
-    the graph form, the capture), then the steady state of the graph replay
-    (mode 1), of the persistent launch (mode 2) and of the autotuner's form
-    (the value).  The plain path steps every instance over the same 4 *
-    steps steps, and every instance's final state must be bit-identical on
-    both paths."""
+    5..30, beta 0.01..0.1, recovery 5..10, seed = instance index), 200 steps
+    from the initial state, against the same instances stepped one at a time
+    with the plain kernels (apply! per instance and step).
+
+    The value is one call of `steps` steps from the initial state in the
+    autotuner's form (mode 3), the autotuner having run before it (its time
+    is reported apart; a graph form's capture stays inside the call).  Each
+    form (graph replay, persistent grid launch, persistent cluster launch)
+    is also timed from the initial state on a fresh copy of the ensemble,
+    then once more over the next `steps` steps (the late epidemic), and
+    every instance's final state of every form must be bit-identical to the
+    plain path's."""
     import torch
     import vahana_gb300 as vh
     from vahana_gb300 import models
     vh.build()
     n_inst, steps = args.instances, args.batch_steps
-    N, deg, beta, rec, seeds = models.batch_params(n_inst)
+    params = models.batch_params(n_inst)
     # warm-up on a small batch (graph capture machinery, autotuner)
     k = args.batch_warmup_instances
     if k > 0:
-        w = models.Batch(N[:k], deg[:k], beta[:k], rec[:k], seeds[:k])
+        w = models.Batch(*[p[:k] for p in params])
         w.step(steps, mode=3)
         w.close()
-    b = models.Batch(N, deg, beta, rec, seeds)
-    torch.cuda.synchronize()
-    timed = {}
-    for name, mode in (("first_call", 3), ("graph", 1), ("persistent", 2), ("auto", 3)):
+
+    def timed_step(b, mode):
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
         b.step(steps, mode=mode)
         torch.cuda.synchronize()
-        timed[name] = time.perf_counter() - t0
+        return time.perf_counter() - t0
+
+    t0 = time.perf_counter()
+    b = models.Batch(*params)
+    torch.cuda.synchronize()
+    t_build = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    tune = b.tuning()  # the autotuner, on copies of the initial state
+    t_tune = time.perf_counter() - t0
+    t_auto = timed_step(b, 3)
     t0 = time.perf_counter()
     for i in range(n_inst):
-        b.step_one(i, 4 * steps)
+        b.step_one(i, steps)
     torch.cuda.synchronize()
     t_plain = time.perf_counter() - t0
-    bad = 0
-    for i in range(n_inst):  # every instance bit-identical batched vs alone
-        sb, db = b.states(i, 0)
-        sp, dp = b.states(i, 1)
-        bad += int(not (np.array_equal(sb, sp) and np.array_equal(db, dp)))
+    plain = [b.states(i, 1) for i in range(n_inst)]
+
+    def differing(bb):
+        bad = 0
+        for i in range(n_inst):
+            sb, db = bb.states(i, 0)
+            bad += int(not (np.array_equal(sb, plain[i][0]) and np.array_equal(db, plain[i][1])))
+        return bad
+
+    bad = {"auto": differing(b)}
     info = b.info()
-    tune = b.tuning()
+    lanes = b.lanes()
+    cluster = b.cluster()
     b.close()
-    plain_rate = n_inst * 4 * steps / t_plain
-    rate = {k: n_inst * steps / v for k, v in timed.items()}
-    v = rate["auto"]
+    forms = {}
+    for name, mode in (("graph_replay", 1), ("persistent_grid", 2), ("persistent_cluster", 4)):
+        bf = models.Batch(*params)
+        bf.tuning()
+        t_first = timed_step(bf, mode)
+        bad[name] = differing(bf)
+        t_late = timed_step(bf, mode)
+        bf.close()
+        forms[name] = {"from_initial": n_inst * steps / t_first,
+                       "late_epidemic": n_inst * steps / t_late}
+    plain_rate = n_inst * steps / t_plain
+    v = n_inst * steps / t_auto
+    nbad = sum(bad.values())
     out = {"metric": "sim-steps/s", "value": v, "unit": "instance-steps/s", "n_gpus": 1,
-           "steps": steps, "warmup": 1, "ms_per_step": 1e3 * timed["auto"] / steps,
+           "steps": steps, "warmup": 1, "ms_per_step": 1e3 * t_auto / steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/i32",
            "data": "synthetic",
            "config": {"workload": "batched_sir_ensemble", "instances": n_inst,
                       "agents": info["agents"], "edges": info["edges"],
-                      "launch": {"tpb": info["tpb"], "agents_per_thread": info["apt"]},
+                      "from": "initial state",
+                      "launch": {"tpb": info["tpb"], "agents_per_lane": lanes,
+                                 "cluster": cluster},
                       "autotuner": tune},
-           "first_call": {"value": rate["first_call"], "seconds": timed["first_call"],
-                          "includes": "autotuner, graph capture when the graph form wins"},
-           "steady": {"graph_replay": rate["graph"], "persistent": rate["persistent"],
-                      "auto": rate["auto"]},
+           "build_seconds": t_build,
+           "autotuner_seconds": t_tune,
+           "first_call_with_autotuner": n_inst * steps / (t_tune + t_auto),
+           "forms": forms,
            "plain_one_at_a_time": plain_rate,
            "speedup_vs_plain": v / plain_rate,
-           "speedup_vs_plain_first_call": rate["first_call"] / plain_rate,
-           "parity": {"instances": n_inst, "steps": 4 * steps,
-                      "instances_differing_batched_vs_alone": bad, "pass": bad == 0}}
+           "parity": {"instances": n_inst, "steps": steps,
+                      "instances_differing_from_plain": bad, "pass": nbad == 0}}
     print(json.dumps(out), flush=True)
 
 

@@ -453,24 +453,46 @@ int vg_batch_create_sir(int n, const int64_t *N, const int32_t *deg,
  * step over all instances; mode 1: the same, with the step loop captured
  * once in a CUDA graph and replayed; mode 2: one persistent cooperative
  * launch for all the steps (grid-wide barrier between steps, bounded: a
- * wait that runs out is reported as VG_ERR_DEVICE, status 0x5e04); mode 3:
- * mode 1 or 2, whichever the autotuner measured faster.  The first call
- * runs the autotuner (on copies of the state). */
+ * wait that runs out is reported as VG_ERR_DEVICE, status 0x5e04); mode 4:
+ * one persistent launch of thread-block clusters, each taking packs of
+ * whole instances from a counter and stepping a pack through all the steps
+ * (the pack's infected-agent masks in the cluster's distributed shared
+ * memory, a hardware cluster barrier between steps, no grid-wide barrier);
+ * mode 3: mode 1, 2 or 4,
+ * whichever the autotuner measured fastest.  The first call runs the
+ * autotuner (on copies of the state). */
 int vg_batch_step(vg_batch *b, int steps, int mode);
-/* The autotuner's choice: persistent (1) or graph replay (0), the
- * persistent block size, its degree-bucket threshold (agents with more
- * in-edges take a warp each; 0xFFFFFFFF none), how many agents are above
- * it, and the measured milliseconds per step of the best per-step launch
- * and of the best persistent launch (24-step trials on copies of the state).
- * Runs the autotuner if it has not run. */
+/* The autotuner's choice of form for mode 3 (0 graph replay, 1 persistent
+ * grid launch, 2 persistent cluster launch), the persistent grid launch's
+ * block size, its degree-bucket threshold (agents with more in-edges take a
+ * warp each; 0xFFFFFFFF none), how many agents are above it, and the
+ * measured milliseconds per step of the best per-step launch, of the best
+ * persistent grid launch and of the best cluster launch (24-step trials on
+ * copies of the state; 0 when no cluster shape fits the arena).  Runs the
+ * autotuner if it has not run. */
 int vg_batch_tuning(vg_batch *b, int *persistent, int *persistent_tpb,
                     uint32_t *bucket_threshold, uint64_t *heavy_agents,
-                    double *step_ms_graph, double *step_ms_persistent);
-/* Overrides the autotuner: mode 3 then takes the persistent launch
- * (persistent != 0) or the graph, and the persistent launch uses this block
- * size (128, 256, 512) and bucket threshold. */
+                    double *step_ms_graph, double *step_ms_persistent,
+                    double *step_ms_cluster);
+/* Overrides the autotuner: mode 3 then takes the graph (persistent = 0),
+ * the persistent grid launch (1) or the cluster launch (2), and the
+ * persistent grid launch uses this block size (128, 256, 512) and bucket
+ * threshold. */
 int vg_batch_set_launch(vg_batch *b, int persistent, int persistent_tpb,
                         uint32_t bucket_threshold);
+/* Shape of the cluster launch: CTAs per cluster (1, 2, 4, 8), threads per
+ * CTA (128, 256, 512) and agents per lane (1, 2); VG_ERR_ARG if a pack's
+ * masks would not fit a CTA's shared memory.  The getter also returns the
+ * number of clusters launched. */
+int vg_batch_set_cluster(vg_batch *b, int ctas, int tpb, int ilp);
+int vg_batch_cluster(vg_batch *b, int *ctas, int *tpb, int *ilp,
+                     unsigned *clusters);
+/* Agents per lane of the per-step launch and of the persistent launch (1, 2
+ * or 4: a lane walks the in-edge rows of its agents together).  The setter
+ * overrides the autotuner's choice (0 keeps the current value); the getter
+ * reads the values in use.  Both run the autotuner if it has not run. */
+int vg_batch_set_lanes(vg_batch *b, int per_step, int persistent);
+int vg_batch_lanes(vg_batch *b, int *per_step, int *persistent);
 /* Plain path for comparison: step instance i alone with the plain kernels. */
 int vg_batch_step_one(vg_batch *b, int i, int steps);
 int vg_batch_read_states(vg_batch *b, int i, uint8_t *state_out,

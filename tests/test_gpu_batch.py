@@ -49,21 +49,57 @@ def test_batch_equals_plain_and_oracle(vh):
 def test_batch_persistent_equals_plain(vh):
     """The persistent launch (all steps in one cooperative launch, a
     grid-wide barrier between steps), with and without the warp-per-agent
-    bucket for agents above 8 in-edges, interleaved with the other forms:
-    every instance bit-identical to its plain apply! run."""
+    bucket for agents above 8 in-edges, interleaved with the other forms,
+    with 1, 2 and 4 agents per lane in both forms: every instance
+    bit-identical to its plain apply! run."""
     from vahana_gb300 import models
     N, deg, beta, rec, seeds = small_params(20)
     b = models.Batch(N, deg, beta, rec, seeds)
     t = b.tuning()
     assert t["persistent_tpb"] in (256, 512)
     total = 0
-    for mode, steps, forced in ((2, 6, None), (2, 5, None), (1, 4, None), (3, 7, (1, 256, 8)),
-                                (2, 3, (1, 512, 8)), (0, 2, None), (3, 5, (0, 256, 8))):
+    for mode, steps, forced, lanes in ((2, 6, None, (1, 1)), (2, 5, None, (2, 4)),
+                                       (1, 4, None, (4, 2)), (3, 7, (1, 256, 8), (1, 1)),
+                                       (2, 3, (1, 512, 8), (2, 4)), (0, 2, None, (4, 2)),
+                                       (3, 5, (0, 256, 8), (2, 2)), (2, 4, (1, 256, 8), (4, 4))):
         if forced:
             b.set_launch(*forced)
+        b.set_lanes(*lanes)
+        assert b.lanes() == {"per_step": lanes[0], "persistent": lanes[1]}
         b.step(steps, mode=mode)
         total += steps
     assert b.tuning()["heavy_agents"] > 0  # threshold 8: the bucket path ran
+    for i in range(b.n):
+        b.step_one(i, total)
+    for i in range(b.n):
+        sb, db = b.states(i, which=0)
+        sp, dp = b.states(i, which=1)
+        np.testing.assert_array_equal(sb, sp)
+        np.testing.assert_array_equal(db, dp)
+    b.close()
+
+
+def test_batch_cluster_equals_plain(vh):
+    """The persistent cluster launch (clusters take packs of instances from
+    a counter, masks in distributed shared memory, a cluster barrier between
+    steps) in several shapes, interleaved with the other forms: every
+    instance bit-identical to its plain apply! run."""
+    from vahana_gb300 import models
+    N, deg, beta, rec, seeds = small_params(24)
+    b = models.Batch(N, deg, beta, rec, seeds)
+    assert b.tuning()["form"] in models.Batch.FORMS
+    total = 0
+    for shape, mode, steps in (((8, 512, 1), 4, 7), ((4, 256, 2), 4, 6), ((1, 128, 1), 4, 3),
+                               ((2, 256, 2), 1, 2), ((2, 256, 2), 4, 5), ((8, 128, 2), 2, 3),
+                               ((8, 128, 2), 4, 4)):
+        b.set_cluster(*shape)
+        c = b.cluster()
+        assert (c["ctas"], c["tpb"], c["ilp"]) == shape and c["clusters"] >= 1
+        b.step(steps, mode=mode)
+        total += steps
+    b.set_launch(2)
+    b.step(5, mode=3)
+    total += 5
     for i in range(b.n):
         b.step_one(i, total)
     for i in range(b.n):

@@ -144,5 +144,14 @@ def test_ensemble_full_size(vh):
                                   int(seeds[i]), 200, first_step=1)
         if not (np.array_equal(sb, s_ref) and np.array_equal(db, d_ref)):
             bad.append(("oracle", i))
+    # the persistent cluster form from the same initial state
+    bc = models.Batch(N, deg, beta, rec, seeds)
+    bc.step(200, mode=4)
+    for i in range(b.n):
+        sc, dc = bc.states(i, which=0)
+        sp, dp = b.states(i, which=1)
+        if not (np.array_equal(sc, sp) and np.array_equal(dc, dp)):
+            bad.append(("cluster", i))
+    bc.close()
     assert bad == []
     b.close()

@@ -151,8 +151,12 @@ SIGNATURES = {
     "vg_batch_read_states2": (I, [P, I, I, C.POINTER(C.c_uint8), C.POINTER(C.c_int32), U64, PU64]),
     "vg_batch_info": (I, [P, PU64, PU64, PI, PI, PU64]),
     "vg_batch_tuning": (I, [P, PI, PI, C.POINTER(C.c_uint32), PU64, C.POINTER(D),
-                            C.POINTER(D)]),
+                            C.POINTER(D), C.POINTER(D)]),
     "vg_batch_set_launch": (I, [P, I, I, C.c_uint32]),
+    "vg_batch_set_lanes": (I, [P, I, I]),
+    "vg_batch_lanes": (I, [P, PI, PI]),
+    "vg_batch_set_cluster": (I, [P, I, I, I]),
+    "vg_batch_cluster": (I, [P, PI, PI, PI, C.POINTER(C.c_uint)]),
     "vg_add_graph": (I, [P, I, U64, PP, I, U64, PU64, PU64, I, PP, PU64]),
     "vg_sim_save": (I, [P, CP]),
     "vg_sim_load": (I, [P, CP, P, C.POINTER(P)]),

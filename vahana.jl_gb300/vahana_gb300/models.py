@@ -199,17 +199,43 @@ class Batch:
                 "device_bytes": db.value}
 
     def set_launch(self, persistent, tpb=256, bucket_threshold=0xFFFFFFFF):
+        """Form of mode 3: 0 graph replay, 1 persistent grid launch (block
+        size tpb, warps for agents above bucket_threshold in-edges), 2
+        persistent cluster launch."""
         check(lib().vg_batch_set_launch(self._h, int(persistent), int(tpb), int(bucket_threshold)))
+
+    def set_lanes(self, per_step=0, persistent=0):
+        """Agents per lane (1, 2, 4) of the per-step and persistent grid
+        launches; 0 keeps the autotuner's value."""
+        check(lib().vg_batch_set_lanes(self._h, int(per_step), int(persistent)))
+
+    def lanes(self):
+        a, p = C.c_int(), C.c_int()
+        check(lib().vg_batch_lanes(self._h, C.byref(a), C.byref(p)))
+        return {"per_step": a.value, "persistent": p.value}
+
+    def set_cluster(self, ctas, tpb, ilp):
+        """Shape of the cluster launch: CTAs per cluster, threads per CTA,
+        agents per lane."""
+        check(lib().vg_batch_set_cluster(self._h, int(ctas), int(tpb), int(ilp)))
+
+    def cluster(self):
+        c, t, i, g = C.c_int(), C.c_int(), C.c_int(), C.c_uint()
+        check(lib().vg_batch_cluster(self._h, C.byref(c), C.byref(t), C.byref(i), C.byref(g)))
+        return {"ctas": c.value, "tpb": t.value, "ilp": i.value, "clusters": g.value}
+
+    FORMS = ("graph", "persistent_grid", "persistent_cluster")
 
     def tuning(self):
         p, t, n = C.c_int(), C.c_int(), C.c_uint64()
         thr = C.c_uint32()
-        gm, pm = C.c_double(), C.c_double()
+        gm, pm, cm = C.c_double(), C.c_double(), C.c_double()
         check(lib().vg_batch_tuning(self._h, C.byref(p), C.byref(t), C.byref(thr), C.byref(n),
-                                    C.byref(gm), C.byref(pm)))
-        return {"persistent": bool(p.value), "persistent_tpb": t.value,
+                                    C.byref(gm), C.byref(pm), C.byref(cm)))
+        return {"form": self.FORMS[p.value], "persistent_tpb": t.value,
                 "bucket_threshold": thr.value, "heavy_agents": n.value,
-                "trial_ms_per_step_graph": gm.value, "trial_ms_per_step_persistent": pm.value}
+                "trial_ms_per_step_graph": gm.value, "trial_ms_per_step_persistent": pm.value,
+                "trial_ms_per_step_cluster": cm.value}
 
     def close(self):
         if self._h:
