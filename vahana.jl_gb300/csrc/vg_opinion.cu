@@ -950,7 +950,9 @@ void launch_opinion_jobs(const std::vector<OpinionJob> &jobs, cudaStream_t st, D
   k_opinion_jobs<<<(unsigned)tiles.size(), TPB, 0, st>>>(args_buf.as<OpinionArgs>(),
                                                         tiles_buf.as<JobTile>());
   VG_CUDA(cudaGetLastError());
-  VG_CUDA(cudaStreamSynchronize(st));  // host vectors are released on return
+  // no wait: a copy from pageable host memory is staged before the call
+  // returns, so the host vectors may go; the device buffers are rewritten by
+  // the next call's copies in stream order, after this launch
 }
 
 }  // namespace vg

@@ -56,6 +56,7 @@ struct Job {
   uint64_t est_bytes = 0;
   std::vector<uint8_t> final_state;
   vg_job_result result{};
+  cudaEvent_t done_ev = nullptr;  // recorded after the job's last tick
 };
 
 struct SirJobDesc {
@@ -117,7 +118,19 @@ __global__ void k_sir_jobs(const SirJobDesc *jobs, const SirTile *tiles, int *st
 // server's stream; BUILDERS builder threads (each with its own stream) build
 // admitted jobs -- graph generation, CSR and gather layout -- while the
 // worker keeps ticking, and hand them over through `ready`.
+//
+// The worker does not wait for a tick before issuing the next: up to
+// MAX_INFLIGHT ticks are queued on the stream (a tick's launches only read
+// descriptors that the stream's own copies wrote before them).  A job that
+// reaches its step count leaves the resident set at once; an event recorded
+// after its last tick tells when its final state may be read, which a copy on
+// a separate stream then does.  Freeing device memory waits for the whole
+// device, so finished jobs' simulations are destroyed in batches
+// (GRAVE_BATCH at a time, when admission needs their budget, or when nothing
+// is resident); their budget is returned then.
 constexpr int BUILDERS = 4;
+constexpr size_t MAX_INFLIGHT = 2;
+constexpr size_t GRAVE_BATCH = 16;
 
 struct vg_server {
   std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
@@ -146,6 +159,13 @@ struct vg_server {
   uint64_t ticks = 0, sim_steps = 0;
   uint64_t footprint = 0;
   DevBuf sir_jobs_buf, sir_tiles_buf, op_args_buf, op_tiles_buf, status;
+  // pipelining (worker thread only)
+  cudaStream_t retire_stream = nullptr;  // final-state copies of finished jobs
+  int *status_host = nullptr;            // pinned: the status word after a tick
+  std::deque<cudaEvent_t> inflight;      // one per queued tick, oldest first
+  std::vector<cudaEvent_t> ev_pool;
+  std::deque<Job *> retiring;            // finished, final state not read yet
+  std::vector<Job *> graveyard;          // read back (in `done`), simulation not freed
 };
 
 namespace {
@@ -206,7 +226,10 @@ void build_job(vg_server *S, Job *J, cudaStream_t bst) {
   }
 }
 
-void retire_job(vg_server *S, Job *J) {
+// the final state of a finished job whose last tick has completed: read
+// back (on the retire stream: the job is no longer touched by the ticks
+// queued after it), hashed and summarised; the simulation stays allocated
+void read_back(vg_server *S, Job *J) {
   Sim &s = *J->sim->s;
   vg_job_result &r = J->result;
   r.id = J->id;
@@ -219,19 +242,19 @@ void retire_job(vg_server *S, Job *J) {
   int T = J->spec.model == 0 ? S->sir_person : S->op_agent;
   AgentStore &A = s.agents[T - 1];
   std::vector<uint8_t> bytes;
+  cudaStream_t rs = S->retire_stream;
   if (J->spec.model == 0) {
     bytes.resize(A.n * 5);
-    VG_CUDA(cudaMemcpyAsync(bytes.data(), A.rd[0].p, A.n, cudaMemcpyDeviceToHost, S->stream));
-    VG_CUDA(cudaMemcpyAsync(bytes.data() + A.n, A.rd[1].p, A.n * 4, cudaMemcpyDeviceToHost,
-                            S->stream));
-    VG_CUDA(cudaStreamSynchronize(S->stream));
+    VG_CUDA(cudaMemcpyAsync(bytes.data(), A.rd[0].p, A.n, cudaMemcpyDeviceToHost, rs));
+    VG_CUDA(cudaMemcpyAsync(bytes.data() + A.n, A.rd[1].p, A.n * 4, cudaMemcpyDeviceToHost, rs));
+    VG_CUDA(cudaStreamSynchronize(rs));
     uint64_t rcount = 0;
     for (uint64_t i = 0; i < A.n; i++) rcount += bytes[i] == 2;
     r.summary = A.n ? (double)rcount / (double)A.n : 0.0;
   } else {
     bytes.resize(A.n * 8);
-    VG_CUDA(cudaMemcpyAsync(bytes.data(), A.rd[0].p, A.n * 8, cudaMemcpyDeviceToHost, S->stream));
-    VG_CUDA(cudaStreamSynchronize(S->stream));
+    VG_CUDA(cudaMemcpyAsync(bytes.data(), A.rd[0].p, A.n * 8, cudaMemcpyDeviceToHost, rs));
+    VG_CUDA(cudaStreamSynchronize(rs));
     double m = 0;
     const double *x = (const double *)bytes.data();
     for (uint64_t i = 0; i < A.n; i++) m += x[i];
@@ -239,11 +262,74 @@ void retire_job(vg_server *S, Job *J) {
   }
   r.checksum = fnv1a(bytes.data(), bytes.size());
   if (J->spec.keep_state) J->final_state = std::move(bytes);
-  J->ptab.release();  // before the simulation whose byte counter it updates
-  vg_sim_destroy(J->sim);
-  J->sim = nullptr;
   r.finish_s = now_s(S->t0);
   J->finish = r.finish_s;
+}
+
+void free_job_sim(Job *J) {
+  J->ptab.release();  // before the simulation whose byte counter it updates
+  if (J->sim) vg_sim_destroy(J->sim);
+  J->sim = nullptr;
+}
+
+void check_status(vg_server *S) {
+  if (*(volatile int *)S->status_host)
+    fail(VG_ERR_DEVICE, "serving tick: device status " + std::to_string(*S->status_host));
+}
+
+// drop the events of completed ticks; with `keep`, wait until at most that
+// many ticks are queued
+void settle_ticks(vg_server *S, size_t keep) {
+  while (!S->inflight.empty()) {
+    cudaEvent_t ev = S->inflight.front();
+    if (S->inflight.size() > keep) {
+      VG_CUDA(cudaEventSynchronize(ev));
+    } else {
+      const cudaError_t q = cudaEventQuery(ev);
+      if (q == cudaErrorNotReady) break;
+      VG_CUDA(q);
+    }
+    S->inflight.pop_front();
+    S->ev_pool.push_back(ev);
+    check_status(S);
+  }
+}
+
+// finished jobs whose last tick has completed (all of them with `wait`):
+// results to `done`, simulations to the graveyard
+void reap_finished(vg_server *S, bool wait) {
+  while (!S->retiring.empty()) {
+    Job *J = S->retiring.front();
+    if (wait) {
+      VG_CUDA(cudaEventSynchronize(J->done_ev));
+    } else {
+      const cudaError_t q = cudaEventQuery(J->done_ev);
+      if (q == cudaErrorNotReady) break;
+      VG_CUDA(q);
+    }
+    check_status(S);
+    read_back(S, J);
+    VG_CUDA(cudaEventDestroy(J->done_ev));
+    J->done_ev = nullptr;
+    S->retiring.pop_front();
+    S->graveyard.push_back(J);
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->done.push_back(J);
+  }
+}
+
+// free the graveyard's simulations (each free waits for the device) and
+// return their budget
+void flush_graveyard(vg_server *S) {
+  if (S->graveyard.empty()) return;
+  uint64_t bytes = 0;
+  for (Job *J : S->graveyard) {
+    free_job_sim(J);
+    bytes += J->est_bytes;
+  }
+  S->graveyard.clear();
+  std::lock_guard<std::mutex> lk(S->mu);
+  S->used -= bytes;
 }
 
 // one transition of every resident job
@@ -299,10 +385,17 @@ void tick(vg_server *S) {
     VG_CUDA(cudaGetLastError());
   }
   if (!oj.empty()) launch_opinion_jobs(oj, st, S->op_args_buf, S->op_tiles_buf, &S->footprint);
-  VG_CUDA(cudaStreamSynchronize(st));
-  int h = 0;
-  VG_CUDA(cudaMemcpy(&h, S->status.p, 4, cudaMemcpyDeviceToHost));
-  if (h) fail(VG_ERR_DEVICE, "serving tick: device status " + std::to_string(h));
+  // the status word as of this tick, read once the tick's event has completed
+  VG_CUDA(cudaMemcpyAsync(S->status_host, S->status.p, 4, cudaMemcpyDeviceToHost, st));
+  cudaEvent_t ev;
+  if (S->ev_pool.empty()) {
+    VG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  } else {
+    ev = S->ev_pool.back();
+    S->ev_pool.pop_back();
+  }
+  VG_CUDA(cudaEventRecord(ev, st));
+  S->inflight.push_back(ev);
   // finish of the transition of every job (as apply! for its immortal type)
   for (Job *J : stepping) {
     Sim &s = *J->sim->s;
@@ -387,6 +480,16 @@ void worker_loop(vg_server *S) {
   try {
     VG_CUDA(cudaSetDevice(S->device));
     while (true) {
+      settle_ticks(S, MAX_INFLIGHT);
+      reap_finished(S, false);
+      bool need_budget = false, idle = false;
+      {
+        std::lock_guard<std::mutex> lk(S->mu);
+        need_budget = !S->queue.empty() && S->used + S->queue.front()->est_bytes > S->budget;
+        idle = S->active.empty() && S->ready.empty();
+      }
+      if (S->graveyard.size() >= GRAVE_BATCH || (need_budget && !S->graveyard.empty()) || idle)
+        flush_graveyard(S);
       std::vector<Job *> arrived;
       {
         std::unique_lock<std::mutex> lk(S->mu);
@@ -398,7 +501,7 @@ void worker_loop(vg_server *S) {
           const size_t inflight = S->active.size() + S->ready.size() + S->to_build.size() +
                                   (size_t)S->building;
           bool fits = S->used + J->est_bytes <= S->budget && (int)inflight < S->max_active;
-          bool alone = inflight == 0;  // a lone job always runs
+          bool alone = inflight == 0 && S->graveyard.empty() && S->retiring.empty();
           if (!fits && !alone) break;
           S->queue.pop_front();
           S->used += J->est_bytes;
@@ -409,6 +512,13 @@ void worker_loop(vg_server *S) {
         if (admitted) S->build_cv.notify_all();
         arrived.swap(S->ready);
         if (arrived.empty() && S->active.empty()) {
+          if (!S->retiring.empty() || !S->graveyard.empty() || !S->inflight.empty()) {
+            lk.unlock();  // nothing to tick: finish the queued work first
+            settle_ticks(S, 0);
+            reap_finished(S, true);
+            flush_graveyard(S);
+            continue;
+          }
           if (S->stop && S->queue.empty() && S->to_build.empty() && S->building == 0) break;
           S->cv.wait_for(lk, std::chrono::milliseconds(2));
           continue;
@@ -416,17 +526,18 @@ void worker_loop(vg_server *S) {
       }
       for (Job *J : arrived) S->active.push_back(J);
       tick(S);
-      std::vector<Job *> still, finished;
-      for (Job *J : S->active) (J->done_steps >= J->spec.steps ? finished : still).push_back(J);
-      for (Job *J : finished) retire_job(S, J);
-      {
-        std::lock_guard<std::mutex> lk(S->mu);
-        S->active.swap(still);
-        for (Job *J : finished) {
-          S->used -= J->est_bytes;
-          S->done.push_back(J);
+      std::vector<Job *> still;
+      for (Job *J : S->active) {
+        if (J->done_steps >= J->spec.steps) {
+          VG_CUDA(cudaEventCreateWithFlags(&J->done_ev, cudaEventDisableTiming));
+          VG_CUDA(cudaEventRecord(J->done_ev, S->stream));
+          S->retiring.push_back(J);
+        } else {
+          still.push_back(J);
         }
       }
+      std::lock_guard<std::mutex> lk(S->mu);
+      S->active.swap(still);
     }
   } catch (const Error &e) {
     fail_server(S, e.msg);
@@ -480,6 +591,9 @@ int vg_serve_create(uint64_t budget_bytes, int max_active, vg_server **out) {
     fail(rc, vg_last_error());
   S->status.alloc(16, &S->footprint);
   VG_CUDA(cudaMemset(S->status.p, 0, 16));
+  VG_CUDA(cudaHostAlloc((void **)&S->status_host, 4, cudaHostAllocDefault));
+  *S->status_host = 0;
+  VG_CUDA(cudaStreamCreateWithFlags(&S->retire_stream, cudaStreamNonBlocking));
   for (int b = 0; b < BUILDERS; b++)
     VG_CUDA(cudaStreamCreateWithFlags(&S->build_stream[b], cudaStreamNonBlocking));
   vg_server *raw = S.release();
@@ -596,11 +710,21 @@ int vg_serve_destroy(vg_server *S) {
     for (Job *J : *q) delete J;
   for (auto *v : {&S->ready, &S->active})
     for (Job *J : *v) {
-      J->ptab.release();
-      if (J->sim) vg_sim_destroy(J->sim);
+      free_job_sim(J);
       delete J;
     }
+  cudaStreamSynchronize(S->stream);  // (after an error: queued ticks end before their jobs go)
+  for (Job *J : S->retiring) {
+    if (J->done_ev) cudaEventDestroy(J->done_ev);
+    free_job_sim(J);
+    delete J;
+  }
+  for (Job *J : S->graveyard) free_job_sim(J);  // (also in done)
   for (Job *J : S->done) delete J;
+  for (cudaEvent_t e : S->inflight) cudaEventDestroy(e);
+  for (cudaEvent_t e : S->ev_pool) cudaEventDestroy(e);
+  if (S->status_host) cudaFreeHost(S->status_host);
+  if (S->retire_stream) cudaStreamDestroy(S->retire_stream);
   vg_model_destroy(S->sir_model);
   vg_model_destroy(S->op_model);
   cudaStream_t st = S->stream;
