@@ -278,6 +278,43 @@ def test_generators_match_host_restatement(vh):
     run.close()
 
 
+@pytest.mark.parametrize("W,H,nw,crowd", [(64, 48, 1500, 1000), (8, 8, 300, 0), (40, 40, 900, 800)])
+def test_walker_rebuild_step_by_step(vh, W, H, nw, crowd):
+    """The walker -> cell containers after every step equal the oracle's, in
+    walker order per cell.  `crowd` walkers start on cell (1, 1), so the
+    first rebuilds hold rows of more than 64 records that then spread out;
+    with more walkers than cells (8 x 8) most rows hold several records."""
+    from vahana_gb300 import models
+    seed = 11
+    a0, x0, y0 = models.life_initial_state(W, H, nw, 0.3, seed)
+    x0[:crowd] = 1
+    y0[:crowd] = 1
+    m = models.life_model()
+    sim = vh.create_simulation(m)
+    vh.add_raster(sim, "raster", (W, H), "Cell", alive=a0)
+    vh.connect_raster_neighbors(sim, "raster", "Neighbor", implicit=True)
+    wids = vh.add_agents(sim, "Walker", nw, x=x0, y=y0)
+    cells = (np.uint64(m["Cell"].index) << np.uint64(56)) | (
+        (x0.astype(np.uint64) - 1) + (y0.astype(np.uint64) - 1) * np.uint64(W) + np.uint64(1))
+    vh.add_edges(sim, "OnCell", wids, cells)
+    vh.finish_init(sim)
+    for step in range(1, 9):
+        vh.apply_(sim, "life", ["Cell"], ["Cell", "Neighbor"], ["Cell"],
+                  params=[m["Neighbor"].index])
+        vh.apply_(sim, "random_walk", ["Walker"], ["Walker"], ["Walker", "OnCell"],
+                  params=[m["OnCell"].index, 0, seed])
+        a_ref, x_ref, y_ref, rp_ref, src_ref = om.run_life_walkers(a0, x0, y0, W, H, seed, step)
+        w = vh.read_agents(sim, "Walker")[0]
+        np.testing.assert_array_equal(w["x"], x_ref)
+        np.testing.assert_array_equal(w["y"], y_ref)
+        rp, frm, _ = vh.read_edges(sim, "OnCell", "Cell")
+        np.testing.assert_array_equal(rp, rp_ref)
+        np.testing.assert_array_equal(frm & np.uint64((1 << 36) - 1), src_ref)
+        if step == 1 and crowd > 64:
+            assert int(np.diff(rp_ref).max()) > 64
+    sim.close()
+
+
 def test_life_walkers_bit_exact(vh):
     from vahana_gb300 import models
     W, H, nw, seed = 96, 80, 700, 5
