@@ -977,6 +977,10 @@ void autotune(vg_batch *b) {
   b->c_ctas = cc;
   b->c_tpb = ct;
   b->c_ilp = ci;
+  // keep only the chosen shape's packing (another is rebuilt on request)
+  const int keep = (cc * 1024 + ct) * 4 + ci;
+  for (auto it2 = b->cplans.begin(); it2 != b->cplans.end();)
+    it2 = it2->first == keep ? std::next(it2) : b->cplans.erase(it2);
   b->form = cbest < std::min(best, pbest) ? 4 : (pbest < best ? 2 : 1);
   b->tuned_graph_ms = best / TRIAL;
   b->tuned_persistent_ms = pbest / TRIAL;
