@@ -282,6 +282,21 @@ int vg_apply(vg_sim *s, const char *transition, const int *call, int ncall,
              const int *read, int nread, const int *write, int nwrite,
              const int *add_existing, int nadd, int with_edge,
              const double *params, int nparams);
+/* apply! prepared once and run many times (src/Simulation.jl:720-821, the
+ * same call as vg_apply): vg_apply_prepare copies the arguments of one
+ * vg_apply call (the transition name is checked here, everything else at
+ * each run, as vg_apply does) and vg_apply_call_run runs that call.  For a
+ * binding whose foreign calls cost more than the step (a Python loop of
+ * small simulations).  The handle refers to the simulation: destroy it
+ * before the simulation. */
+typedef struct vg_apply_call vg_apply_call;
+int vg_apply_prepare(vg_sim *s, const char *transition, const int *call,
+                     int ncall, const int *read, int nread, const int *write,
+                     int nwrite, const int *add_existing, int nadd,
+                     int with_edge, const double *params, int nparams,
+                     vg_apply_call **out);
+int vg_apply_call_run(vg_apply_call *c);
+int vg_apply_call_destroy(vg_apply_call *c);
 /* apply! for a host that keeps the called type's state in its own memory:
  * the n agents' fields of type_nr are uploaded from in_fields (host SoA
  * columns; NULL entries keep the device column), apply!(sim, transition,

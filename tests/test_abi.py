@@ -291,6 +291,12 @@ def test_null_and_bad_arguments_return_errors(vh):
     assert L.vg_serve_destroy(None) == 0
     assert L.vg_batch_create_sir(2, None, None, None, None, None, 10, None, None) == 2
     assert L.vg_batch_step(None, 1, 0) == 2
+    # prepared apply!: a null simulation, a null output, a bad list, a null handle
+    h = C.c_void_p()
+    assert L.vg_apply_prepare(None, b"sir", None, 0, None, 0, None, 0, None, 0, -1, None, 0,
+                              C.byref(h)) == 2
+    assert L.vg_apply_call_run(None) == 2
+    assert L.vg_apply_call_destroy(None) == 0
     assert L.vg_batch_set_launch(None, 0, 256, 0xFFFFFFFF) == 2
     assert L.vg_batch_set_lanes(None, 1, 1) == 2
     assert L.vg_batch_lanes(None, None, None) == 2

@@ -278,6 +278,32 @@ def test_generators_match_host_restatement(vh):
     run.close()
 
 
+def test_prepared_apply_equals_apply(vh):
+    """A prepared apply! (vg_apply_prepare, vg_apply_call_run) runs the same
+    call as apply!: ten SIR steps either way from the same state end in the
+    same state, and before finish_init! the prepared call is refused with the
+    reference's message."""
+    from vahana_gb300 import models
+    r1 = models.build_sir(n=3000, degree=8, seed=4)
+    r2 = models.build_sir(n=3000, degree=8, seed=4)
+    with pytest.raises(AssertionError, match="finish_init"):
+        r1.step()
+    vh.finish_init(r1.sim)
+    vh.finish_init(r2.sim)
+    m = r2.model
+    for _ in range(10):
+        r1.step()
+        vh.apply_(r2.sim, "sir", ["Person"], ["Person", "Contact"], ["Person"],
+                  params=[m["Contact"].index, r2.beta, r2.recovery, r2.seed])
+    a1 = vh.read_agents(r1.sim, "Person")[0]
+    a2 = vh.read_agents(r2.sim, "Person")[0]
+    np.testing.assert_array_equal(a1["state"], a2["state"])
+    np.testing.assert_array_equal(a1["days"], a2["days"])
+    assert int((a1["state"] != 0).sum()) > 3  # the epidemic moved
+    r1.close()
+    r2.close()
+
+
 @pytest.mark.parametrize("W,H,nw,crowd", [(64, 48, 1500, 1000), (8, 8, 300, 0), (40, 40, 900, 800)])
 def test_walker_rebuild_step_by_step(vh, W, H, nw, crowd):
     """The walker -> cell containers after every step equal the oracle's, in

@@ -836,3 +836,71 @@ int vg_mapreduce_edges(vg_sim *h, int e, int field, int map_kind, double map_arg
 }
 
 }  // extern "C"
+
+// A prepared apply!: the arguments of one vg_apply call, copied once.  Each
+// run is that vg_apply call (the same checks, the same transition, params or
+// globals bound to parameter slots read at each run); the handle only spares
+// a caller whose calls are expensive (a foreign-function layer converting
+// thirteen arguments) the per-step conversion.
+struct vg_apply_call {
+  vg_sim *sim = nullptr;
+  std::string name;
+  std::vector<int> call, read, write, ae;  // (each at least one entry long)
+  int ncall = 0, nread = 0, nwrite = 0, nae = 0, with_edge = -1, nparams = 0;
+  std::vector<double> params;
+};
+
+extern "C" {
+
+int vg_apply_prepare(vg_sim *h, const char *tname, const int *call, int ncall, const int *read,
+                     int nread, const int *write, int nwrite, const int *ae, int nae,
+                     int with_edge, const double *params, int nparams, vg_apply_call **out) {
+  API_BEGIN
+  S(h);
+  if (!tname) fail(VG_ERR_ARG, "null transition name");
+  if (!out) fail(VG_ERR_ARG, "null output pointer");
+  bool known = false;
+  for (auto &t : transitions()) known |= std::strcmp(t.name, tname) == 0;
+  if (!known) fail(VG_ERR_ARG, std::string("unknown transition ") + tname);
+  auto list = [](const int *v, int n, const char *what) {
+    if (n < 0 || (n > 0 && !v)) fail(VG_ERR_ARG, std::string("bad ") + what + " list");
+    std::vector<int> r(v, v + n);
+    if (r.empty()) r.push_back(0);
+    return r;
+  };
+  auto c = std::make_unique<vg_apply_call>();
+  c->sim = h;
+  c->name = tname;
+  c->call = list(call, ncall, "call");
+  c->read = list(read, nread, "read");
+  c->write = list(write, nwrite, "write");
+  c->ae = list(ae, nae, "add_existing");
+  c->ncall = ncall;
+  c->nread = nread;
+  c->nwrite = nwrite;
+  c->nae = nae;
+  c->with_edge = with_edge;
+  if (nparams < 0 || (nparams > 0 && !params)) fail(VG_ERR_ARG, "bad parameter list");
+  c->params.assign(params, params + nparams);
+  c->params.push_back(0.0);
+  c->nparams = nparams;
+  *out = c.release();
+  API_END
+}
+
+int vg_apply_call_run(vg_apply_call *c) {
+  if (!c) {
+    set_last_error("null prepared apply! call");
+    return VG_ERR_ARG;
+  }
+  return vg_apply(c->sim, c->name.c_str(), c->call.data(), c->ncall, c->read.data(), c->nread,
+                  c->write.data(), c->nwrite, c->ae.data(), c->nae, c->with_edge,
+                  c->params.data(), c->nparams);
+}
+
+int vg_apply_call_destroy(vg_apply_call *c) {
+  delete c;
+  return VG_OK;
+}
+
+}  // extern "C"

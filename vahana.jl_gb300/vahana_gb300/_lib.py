@@ -119,6 +119,10 @@ SIGNATURES = {
     "vg_num_edges_total": (I, [P, I, I, PU64]),
     "vg_read_edges": (I, [P, I, I, PU64, PU64, PP, PU64, PU64]),
     "vg_apply": (I, [P, CP, PI, I, PI, I, PI, I, PI, I, I, C.POINTER(D), I]),
+    "vg_apply_prepare": (I, [P, CP, PI, I, PI, I, PI, I, PI, I, I, C.POINTER(D), I,
+                             C.POINTER(P)]),
+    "vg_apply_call_run": (I, [P]),
+    "vg_apply_call_destroy": (I, [P]),
     "vg_apply_host": (I, [P, CP, PI, I, PI, I, PI, I, PI, I, I, C.POINTER(D), I, I, PP, PP, U64]),
     "vg_transition_names": (C.c_char_p, []),
     "vg_mapreduce_agents": (I, [P, I, I, I, D, I, I, I, D, P]),

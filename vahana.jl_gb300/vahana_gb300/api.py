@@ -707,21 +707,49 @@ def apply_(sim, transition, call, read, write, add_existing=(), with_edge=None, 
     return sim
 
 
+class PreparedApply:
+    """apply!(sim, transition, call, read, write, ...) prepared once in the
+    library (vg_apply_prepare) and run by a call with one argument
+    (vg_apply_call_run): the same vg_apply call each time (params or
+    globals bound to parameter slots still take their values at each run)."""
+
+    def __init__(self, sim, transition, call, read, write, add_existing=(), with_edge=None,
+                 params=()):
+        self._sim = sim
+        self._h = None
+        args = _apply_args(sim, transition, call, read, write, add_existing, with_edge, params)
+        h = C.c_void_p()
+        check(lib().vg_apply_prepare(sim._h, *args, C.byref(h)))
+        self._h = h.value
+        self._run = lib().vg_apply_call_run
+
+    def __call__(self):
+        if self._sim._h is None:
+            raise RuntimeError("the simulation of this prepared apply! is closed")
+        rc = self._run(self._h)
+        if rc:
+            check(rc)
+        return self._sim
+
+    def close(self):
+        if self._h:
+            lib().vg_apply_call_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def prepare_apply(sim, transition, call, read, write, add_existing=(), with_edge=None,
                   params=()):
     """A callable that runs apply_(sim, transition, call, read, write, ...)
-    with these arguments, marshalled to C once: the cheapest form of a step
-    loop that repeats one apply! (params or globals bound to parameter
-    slots still take their values at each call)."""
-    args = _apply_args(sim, transition, call, read, write, add_existing, with_edge, params)
-    fn = lib().vg_apply
-
-    def run():
-        rc = fn(sim._h, *args)
-        if rc:
-            check(rc)
-        return sim
-    return run
+    with these arguments, prepared in the library once: the cheapest form of
+    a step loop that repeats one apply! (params or globals bound to
+    parameter slots still take their values at each call)."""
+    return PreparedApply(sim, transition, call, read, write, add_existing, with_edge, params)
 
 
 def apply_host(sim, transition, call, read, write, T, state, out=None, add_existing=(),
