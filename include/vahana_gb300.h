@@ -423,9 +423,9 @@ int vg_selftest_scan(uint64_t n, int wide, int in_place, uint64_t seed, uint64_t
  * the kernel's duration.  The context stays usable afterwards. */
 int vg_selftest_scan_timeout(int *status_out, double *ms_out);
 
-/* Failure detection of the persistent ensemble launch's step barrier: two
- * blocks meet at a barrier that expects three, so both bounded waits run
- * out (2^16 polls here); *status_out = the status word (0x5e04), *ms_out =
+/* Failure detection of the persistent ensemble launch's step waits: two
+ * blocks wait for an instance counter that nothing advances, so both
+ * bounded waits run out (2^16 polls here); *status_out = the status word (0x5e04), *ms_out =
  * the launch's duration.  The context stays usable. */
 int vg_selftest_barrier_timeout(int *status_out, double *ms_out);
 
@@ -467,7 +467,8 @@ int vg_batch_create_sir(int n, const int64_t *N, const int32_t *deg,
 /* Advance every instance by `steps` transitions.  mode 0: one launch per
  * step over all instances; mode 1: the same, with the step loop captured
  * once in a CUDA graph and replayed; mode 2: one persistent cooperative
- * launch for all the steps (grid-wide barrier between steps, bounded: a
+ * launch for all the steps (a block ticket of step t waits until the
+ * instances it touches have finished step t - 1; bounded: a
  * wait that runs out is reported as VG_ERR_DEVICE, status 0x5e04); mode 4:
  * one persistent launch of thread-block clusters, each taking packs of
  * whole instances from a counter and stepping a pack through all the steps

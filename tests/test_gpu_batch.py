@@ -47,9 +47,10 @@ def test_batch_equals_plain_and_oracle(vh):
 
 
 def test_batch_persistent_equals_plain(vh):
-    """The persistent launch (all steps in one cooperative launch, a
-    grid-wide barrier between steps), with and without the warp-per-agent
-    bucket for agents above 8 in-edges, interleaved with the other forms,
+    """The persistent launch (all steps in one cooperative launch, a block
+    ticket of step t waiting for its instances' step t - 1), with and without
+    the warp-per-agent bucket for agents above 8 in-edges, interleaved with
+    the other forms,
     with 1, 2 and 4 agents per lane in both forms: every instance
     bit-identical to its plain apply! run."""
     from vahana_gb300 import models
@@ -111,9 +112,9 @@ def test_batch_cluster_equals_plain(vh):
 
 
 def test_step_barrier_wait_gives_up_with_a_status(vh):
-    """The persistent launch's grid-wide step barrier is bounded: two blocks
-    waiting for a third record 0x5e04 and end; the GPU stays usable (a
-    batch steps correctly afterwards)."""
+    """The persistent launch's step waits are bounded: two blocks waiting
+    for an instance counter that nothing advances record 0x5e04 and end;
+    the GPU stays usable (a batch steps correctly afterwards)."""
     import ctypes as C
     from vahana_gb300 import models
     from vahana_gb300._lib import check, lib

@@ -11,8 +11,9 @@
 // instance; the step loop can be captured once in a CUDA graph and
 // replayed.  Neighbour states are read from a bit mask of the infected
 // agents that every step writes beside the states.  Two persistent forms run
-// every step in one launch: a cooperative grid with a grid-wide barrier
-// between steps, and thread-block clusters that each step their own packs of
+// every step in one launch: a cooperative grid whose block tickets wait
+// only for the instances they touch (no grid-wide barrier), and
+// thread-block clusters that each step their own packs of
 // whole instances (masks in distributed shared memory, cluster barriers).
 // A small autotuner keyed on the arena's degree histogram picks the form and
 // its shape (block size, agents per lane, degree buckets, cluster size) by
@@ -190,15 +191,25 @@ __global__ void k_inf_bits(const uint8_t *st, uint64_t n, uint32_t *m) {
   if ((threadIdx.x & 31) == 0) m[i0 >> 5] = b;
 }
 
-// ---- persistent form: one cooperative launch runs every step.  Blocks
-// meet at a grid-wide barrier between steps (all blocks are resident: the
-// launch is cooperative).  The states and masks a step reads were written by
-// other blocks in the previous step of the same launch: they are read with
-// ordinary loads after the barrier's GPU-scope acquire fence (never through
-// the read-only path, which assumes data constant for the whole launch).
-// Agents whose in-degree exceeds the bucket threshold (listed in `heavy`)
-// are folded by a warp each (the infected-neighbour count is an integer: any
-// order gives the same k); the others in warp chunks as in the per-step form.
+// ---- persistent form: one cooperative launch runs every step.  Agents are
+// taken in block tickets, numbered across the steps (ticket T: step T /
+// tickets_per_step, agent range T % tickets_per_step); all blocks are
+// resident (the launch is cooperative) and tickets are handed out in step
+// order.  An agent reads only its own instance's agents, so a ticket of step
+// t waits only until the instances its range touches have finished step t - 1
+// (no grid-wide barrier): every block that finishes a range adds, per
+// instance, the number of its agents in the range to that instance's
+// counter of agent-steps (after a release fence), and a ticket of step t
+// waits until the counter of each of its instances reaches t * N_i (an
+// acquire load; bounded: a wait that runs out records BAR_ERR_WAIT and the
+// launch winds down).  Finishing step t - 1 of an instance also ends every
+// read of step t - 1's read buffer by that instance, so step t may write it.
+// States and masks written by other blocks are read with ordinary loads
+// after the acquire (never through the read-only path, which assumes data
+// constant for the whole launch).  Agents above a degree threshold (listed
+// in `heavy`, sorted) are folded by a warp each, inside the ticket of their
+// range (the infected-neighbour count is an integer: any order gives the
+// same k); the others in warp chunks as in the per-step form.
 struct PersistArgs {
   BatchArgs a;                 // graph, tables; state pointers unused
   uint8_t *st[2];
@@ -206,64 +217,74 @@ struct PersistArgs {
   uint32_t *inf[2];
   int cur0;                    // buffer of the state before the first step
   uint32_t steps, step0;       // steps to run, transition number of the first
-  const uint32_t *heavy;       // agents above the bucket threshold (nheavy)
+  const uint32_t *heavy;       // agents above the bucket threshold (nheavy, ascending)
   uint64_t nheavy;
   const uint8_t *is_heavy;     // per agent (null: no heavy agents)
-  unsigned *bar;               // [0] arrivals, [1] generation
+  unsigned *ticket;            // next ticket (zero at launch)
+  uint32_t *done;              // per instance: agent-steps finished in this launch (zero at launch)
+  const uint32_t *inst_n;      // per instance: agents
+  unsigned rounds;             // chunk rounds per block ticket
 };
 
 constexpr uint32_t BAR_SPIN_LIMIT = 1u << 22;
 constexpr int BAR_ERR_WAIT = 0x5e04;
 
-// Sense-free grid barrier on a generation counter; a wait that runs out
-// records BAR_ERR_WAIT and returns false (the launch then ends).
-__device__ bool grid_barrier(unsigned *bar, unsigned nblocks, int *status,
-                             uint32_t limit = BAR_SPIN_LIMIT) {
-  __shared__ int ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    ok = 1;
-    volatile unsigned *gen = bar + 1;
-    const unsigned g = *gen;
-    __threadfence();
-    if (atomicAdd(bar, 1u) == nblocks - 1) {
-      atomicExch(bar, 0u);
-      __threadfence();
-      atomicAdd(bar + 1, 1u);
-    } else {
-      uint32_t i = 0;
-      while (*gen == g) {
-        if (++i >= limit) {
-          atomicCAS(status, 0, BAR_ERR_WAIT);
-          ok = 0;
-          break;
-        }
-      }
-    }
-    __threadfence();
-    // acquire at GPU scope: the other blocks' writes of the step are visible
-    // to this block's ordinary (L1-cached) loads after the barrier
-    asm volatile("fence.acq_rel.gpu;" ::: "memory");
-  }
-  __syncthreads();
-  return ok != 0;
+__device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t *a) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(a) : "memory");
+  return v;
 }
 
-// failure detection without a fault: blocks meet at a barrier that expects
-// one block more than the launch has, so every wait runs out
-__global__ void k_barrier_probe(unsigned *bar, unsigned expect, int *status, uint32_t limit) {
-  grid_barrier(bar, expect, status, limit);
+// bounded wait until *counter >= target; false (and the status word set)
+// when it runs out or another wait already gave up
+__device__ bool wait_count(const uint32_t *counter, uint32_t target, int *status,
+                           uint32_t limit = BAR_SPIN_LIMIT) {
+  for (uint32_t i = 0; i < limit; i++) {
+    if (ld_acquire_gpu(counter) >= target) return true;
+    if ((i & 1023u) == 1023u && *(volatile int *)status) return false;
+    if (i > 64) __nanosleep(32);
+  }
+  atomicCAS(status, 0, BAR_ERR_WAIT);
+  return false;
+}
+
+// failure detection without a fault: the blocks wait for an instance
+// counter that nothing advances, so every wait runs out
+__global__ void k_barrier_probe(const uint32_t *counter, uint32_t target, int *status,
+                                uint32_t limit) {
+  if (threadIdx.x == 0) wait_count(counter, target, status, limit);
 }
 
 template <int ILP>
 __global__ void k_batch_persist(PersistArgs p) {
+  __shared__ unsigned s_ticket;
+  __shared__ int s_ok;
   const BatchArgs &a = p.a;
-  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
-  const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const uint64_t nwarps = nthreads / 32, wid = tid / 32;
   const unsigned lane = threadIdx.x & 31;
+  const unsigned wpb = blockDim.x / 32, wib = threadIdx.x / 32;
   const bool atomic_bits = p.is_heavy != nullptr;
-  for (uint32_t t = 0; t < p.steps; t++) {
+  const uint64_t span = (uint64_t)wpb * 32 * ILP * p.rounds;
+  const uint64_t tps = (a.n + span - 1) / span;  // tickets per step
+  const uint64_t total = tps * p.steps;
+  for (;;) {
+    if (threadIdx.x == 0) s_ticket = atomicAdd(p.ticket, 1u);
+    __syncthreads();
+    const uint64_t T = s_ticket;
+    __syncthreads();
+    if (T >= total) break;
+    const uint32_t t = (uint32_t)(T / tps);
+    const uint64_t a0 = (T % tps) * span;
+    const uint64_t a1 = a0 + span < a.n ? a0 + span : a.n;
+    const uint32_t i0 = a.inst[a0], i1 = a.inst[a1 - 1];
+    // the range's instances have finished step t - 1
+    if (threadIdx.x == 0) {
+      s_ok = !*(volatile int *)a.status;
+      for (uint32_t i = i0; t > 0 && s_ok && i <= i1; i++)
+        s_ok = wait_count(p.done + i, t * p.inst_n[i], a.status);
+      asm volatile("fence.acq_rel.gpu;" ::: "memory");
+    }
+    __syncthreads();
+    if (!s_ok) break;  // a wait gave up: the launch winds down
     const int cur = p.cur0 ^ (int)(t & 1);
     const uint8_t *st_rd = p.st[cur];
     const int32_t *d_rd = p.dy[cur];
@@ -272,29 +293,46 @@ __global__ void k_batch_persist(PersistArgs p) {
     int32_t *d_wr = p.dy[1 - cur];
     uint32_t *inf_wr = p.inf[1 - cur];
     const uint32_t step = p.step0 + t;
-    for (uint64_t c0 = wid * 32 * ILP; c0 < a.n; c0 += nwarps * 32 * ILP)
+    for (uint64_t c0 = a0 + (uint64_t)wib * 32 * ILP; c0 < a1; c0 += (uint64_t)wpb * 32 * ILP)
       sir_chunk<ILP>(a, st_rd, d_rd, inf_rd, st_wr, d_wr, inf_wr, c0, step, p.is_heavy,
                      atomic_bits);
-    for (uint64_t h = wid; h < p.nheavy; h += nwarps) {  // warp per heavy agent
-      const uint64_t i = p.heavy[h];
-      const uint8_t s = st_rd[i];
-      const int32_t d = d_rd[i];
-      uint32_t k = 0;
-      if (s == 0) {
-        const uint32_t e = a.rp[i + 1];
-        for (uint32_t q = a.rp[i] + lane; q < e; q += 32) k += inf_bit(inf_rd, a.src[q]);
+    if (p.nheavy) {  // the range's heavy agents, a warp each
+      uint64_t lo = 0, hi = p.nheavy;  // first heavy agent >= a0
+      while (lo < hi) {
+        const uint64_t mid = (lo + hi) / 2;
+        if (p.heavy[mid] < a0) lo = mid + 1;
+        else hi = mid;
       }
-      k = __reduce_add_sync(0xffffffffu, k);
-      if (lane == 0) {
-        const uint8_t ns = sir_rule(a, i, k, s, d, step, st_wr, d_wr);
-        const unsigned bit = 1u << (i & 31);
-        if (ns == 1)
-          atomicOr(inf_wr + (i >> 5), bit);
-        else
-          atomicAnd(inf_wr + (i >> 5), ~bit);
+      for (uint64_t h = lo + wib; h < p.nheavy && p.heavy[h] < a1; h += wpb) {
+        const uint64_t i = p.heavy[h];
+        const uint8_t s = st_rd[i];
+        const int32_t d = d_rd[i];
+        uint32_t k = 0;
+        if (s == 0) {
+          const uint32_t e = a.rp[i + 1];
+          for (uint32_t q = a.rp[i] + lane; q < e; q += 32) k += inf_bit(inf_rd, a.src[q]);
+        }
+        k = __reduce_add_sync(0xffffffffu, k);
+        if (lane == 0) {
+          const uint8_t ns = sir_rule(a, i, k, s, d, step, st_wr, d_wr);
+          const unsigned bit = 1u << (i & 31);
+          if (ns == 1)
+            atomicOr(inf_wr + (i >> 5), bit);
+          else
+            atomicAnd(inf_wr + (i >> 5), ~bit);
+        }
       }
     }
-    if (t + 1 < p.steps && !grid_barrier(p.bar, gridDim.x, a.status)) return;
+    __syncthreads();
+    // the range's agents of each instance have finished step t
+    if (threadIdx.x == 0) {
+      __threadfence();
+      for (uint32_t i = i0; i <= i1; i++) {
+        const uint64_t b0 = a.base[i], b1 = b0 + p.inst_n[i];
+        const uint64_t lo = a0 > b0 ? a0 : b0, hi = a1 < b1 ? a1 : b1;
+        atomicAdd(p.done + i, (uint32_t)(hi - lo));
+      }
+    }
   }
 }
 
@@ -521,7 +559,7 @@ struct vg_batch {
   int tpb = 256, apt = 1;
   bool tuned = false;
   struct Tuned {
-    int tpb, apt, p_tpb, p_ilp;
+    int tpb, apt, p_tpb, p_ilp, p_rounds;
     uint32_t p_thr;
     int c_ctas, c_tpb, c_ilp, form;
     float graph_ms, persistent_ms, cluster_ms;
@@ -530,7 +568,7 @@ struct vg_batch {
   // persistent form: block size, bucket threshold (agents with more
   // in-edges take a warp each; 0xFFFFFFFF: none) and whether the autotuner
   // found it faster than the graph of per-step launches
-  int p_tpb = 256, p_ilp = 2;  // (and agents per lane)
+  int p_tpb = 256, p_ilp = 2, p_rounds = 4;  // (and agents per lane, chunk rounds per ticket)
   uint32_t p_thr = 0xFFFFFFFFu;
   // cluster form: CTAs per cluster, threads per CTA, agents per lane; its
   // packings by shape
@@ -542,6 +580,7 @@ struct vg_batch {
   std::vector<uint32_t> host_rp;       // arena row pointers (autotuner, buckets)
   uint32_t heavy_thr = 0xFFFFFFFFu;    // threshold the heavy list was built for
   DevBuf heavy, is_heavy, bar;
+  DevBuf done, inst_n;  // persistent form: agent-steps finished per instance, agents per instance
   uint64_t nheavy = 0;
   DevBuf scratch_st[2], scratch_dy[2], scratch_inf[2];  // autotuner trials run on copies
   // CUDA graphs of `graph_steps` steps, one per starting buffer parity; the
@@ -635,8 +674,10 @@ void launch_persistent_ilp(vg_batch *b, const PersistArgs &p, int tpb) {
   VG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   VG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_persist<ILP>, tpb, 0));
   if (per_sm < 1) fail(VG_ERR_CUDA, "persistent batch kernel: no block fits an SM");
-  unsigned grid = (unsigned)(sms * per_sm);  // every block resident: the barrier may wait
-  VG_CUDA(cudaMemsetAsync(b->bar.p, 0, 8, b->stream));
+  // every block resident: a ticket may wait for blocks holding earlier tickets
+  unsigned grid = (unsigned)(sms * per_sm);
+  VG_CUDA(cudaMemsetAsync(b->bar.p, 0, 16, b->stream));
+  VG_CUDA(cudaMemsetAsync(b->done.p, 0, (uint64_t)b->n * 4, b->stream));
   PersistArgs q = p;
   void *args[] = {&q};
   VG_CUDA(cudaLaunchCooperativeKernel((const void *)k_batch_persist<ILP>, dim3(grid), dim3(tpb),
@@ -644,9 +685,19 @@ void launch_persistent_ilp(vg_batch *b, const PersistArgs &p, int tpb) {
 }
 
 void launch_persistent(vg_batch *b, const StateBufs &bufs, int cur, uint32_t step0,
-                       uint32_t steps, int tpb, uint32_t thr, int ilp) {
+                       uint32_t steps, int tpb, uint32_t thr, int ilp, int rounds) {
   build_buckets(b, thr);
-  if (!b->bar.p) b->bar.alloc(8, &b->footprint);
+  if (!b->bar.p) b->bar.alloc(16, &b->footprint);
+  if (!b->done.p) {
+    b->done.alloc((uint64_t)b->n * 4, &b->footprint);
+    b->inst_n.alloc((uint64_t)b->n * 4, &b->footprint);
+    std::vector<uint32_t> nn(b->N.begin(), b->N.end());
+    VG_CUDA(cudaMemcpyAsync(b->inst_n.p, nn.data(), nn.size() * 4, cudaMemcpyHostToDevice,
+                            b->stream));
+    VG_CUDA(cudaStreamSynchronize(b->stream));
+  }
+  if ((uint64_t)steps * (uint64_t)*std::max_element(b->N.begin(), b->N.end()) >= (1ull << 32))
+    fail(VG_ERR_ARG, "batch: steps x instance size must stay below 2^32 in one persistent launch");
   PersistArgs p{};
   p.a = batch_args(b, cur, step0, nullptr);
   for (int k = 0; k < 2; k++) {
@@ -660,7 +711,10 @@ void launch_persistent(vg_batch *b, const StateBufs &bufs, int cur, uint32_t ste
   p.heavy = b->heavy.as<uint32_t>();
   p.nheavy = b->nheavy;
   p.is_heavy = b->nheavy ? b->is_heavy.as<uint8_t>() : nullptr;
-  p.bar = b->bar.as<unsigned>();
+  p.ticket = b->bar.as<unsigned>();
+  p.done = b->done.as<uint32_t>();
+  p.inst_n = b->inst_n.as<uint32_t>();
+  p.rounds = (unsigned)std::max(rounds, 1);
   switch (ilp) {
     case 1: launch_persistent_ilp<1>(b, p, tpb); break;
     case 2: launch_persistent_ilp<2>(b, p, tpb); break;
@@ -866,6 +920,7 @@ void autotune(vg_batch *b) {
     b->apt = it->second.apt;
     b->p_tpb = it->second.p_tpb;
     b->p_ilp = it->second.p_ilp;
+    b->p_rounds = it->second.p_rounds;
     b->p_thr = it->second.p_thr;
     b->c_ctas = it->second.c_ctas;
     b->c_tpb = it->second.c_tpb;
@@ -935,21 +990,30 @@ void autotune(vg_batch *b) {
       }
     }
   float pbest = 1e30f;
-  int pt = 256, pi = 2;
+  int pt = 256, pi = 2, pr = 4;
   uint32_t pthr = 0xFFFFFFFFu;
   for (int tpb : {256, 512})
     for (int ilp : {1, 2, 4})
-      for (uint32_t thr : {0xFFFFFFFFu, 64u}) {
+      for (int rounds : {2, 4, 8}) {
         const float ms = timed([&] {
-          launch_persistent(b, sb, 0, (uint32_t)b->step, TRIAL, tpb, thr, ilp);
+          launch_persistent(b, sb, 0, (uint32_t)b->step, TRIAL, tpb, 0xFFFFFFFFu, ilp, rounds);
         });
         if (ms < pbest) {
           pbest = ms;
           pt = tpb;
           pi = ilp;
-          pthr = thr;
+          pr = rounds;
         }
       }
+  {  // the degree bucket on the best shape
+    const float ms = timed([&] {
+      launch_persistent(b, sb, 0, (uint32_t)b->step, TRIAL, pt, 64u, pi, pr);
+    });
+    if (ms < pbest) {
+      pbest = ms;
+      pthr = 64u;
+    }
+  }
   float cbest = 1e30f;
   int cc = 8, ct = 512, ci = 1;
   for (int ctas : {4, 8})
@@ -973,6 +1037,7 @@ void autotune(vg_batch *b) {
   b->apt = ba;
   b->p_tpb = pt;
   b->p_ilp = pi;
+  b->p_rounds = pr;
   b->p_thr = pthr;
   b->c_ctas = cc;
   b->c_tpb = ct;
@@ -986,7 +1051,7 @@ void autotune(vg_batch *b) {
   b->tuned_persistent_ms = pbest / TRIAL;
   b->tuned_cluster_ms = cbest < 1e29f ? cbest / TRIAL : 0.0f;
   b->tuned = true;
-  b->tune_cache[key] = {bt,       ba,      pt,      pi,
+  b->tune_cache[key] = {bt,       ba,      pt,      pi,      pr,
                         pthr,     cc,      ct,      ci,
                         b->form,  b->tuned_graph_ms, b->tuned_persistent_ms,
                         b->tuned_cluster_ms};
@@ -1160,7 +1225,7 @@ int vg_batch_step(vg_batch *b, int steps, int mode) {
     VG_CUDA(cudaGetLastError());
   } else if (mode == 2) {
     launch_persistent(b, arena_bufs(b), b->cur, (uint32_t)b->step, (uint32_t)steps, b->p_tpb,
-                      b->p_thr, b->p_ilp);
+                      b->p_thr, b->p_ilp, b->p_rounds);
     if (steps % 2) b->cur = 1 - b->cur;
     b->step += steps;
   } else if (mode == 0) {
@@ -1277,7 +1342,8 @@ int vg_selftest_barrier_timeout(int *status_out, double *ms_out) {
   VG_CUDA(cudaEventCreate(&e0));
   VG_CUDA(cudaEventCreate(&e1));
   VG_CUDA(cudaEventRecord(e0));
-  k_barrier_probe<<<2, 64>>>(bar, 3, status, 1u << 16);  // two blocks, three expected
+  // two blocks wait for an instance counter (zero) to reach 1
+  k_barrier_probe<<<2, 64>>>((const uint32_t *)bar, 1u, status, 1u << 16);
   VG_CUDA(cudaEventRecord(e1));
   VG_CUDA(cudaEventSynchronize(e1));
   VG_CUDA(cudaGetLastError());
