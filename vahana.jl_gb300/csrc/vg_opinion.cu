@@ -625,7 +625,9 @@ __global__ void __launch_bounds__(TPB) k_opinion_big(OpinionArgs p) {
 
 // Many simulations in one launch: block i runs virtual block tiles[i].blk of
 // job tiles[i].job -- the same work, in the same order, as that job's own
-// launch of k_opinion.
+// launch of k_opinion.  Jobs run no block-wide hub rows (the caller checks),
+// so the kernel carries no shared-memory staging and every block keeps the
+// whole unified L1/shared array for the opinion gathers.
 struct JobTile {
   uint32_t job, blk;
 };
@@ -636,8 +638,8 @@ __global__ void __launch_bounds__(TPB, 9) k_opinion_jobs(const OpinionArgs *jobs
   JobTile t = tiles[blockIdx.x];
   if (threadIdx.x == 0) sp = jobs[t.job];
   __syncthreads();
-  if (sp.grid) opinion_block<true, true>(sp, t.blk);
-  else opinion_block<false, true>(sp, t.blk);
+  if (sp.grid) opinion_block<true, false>(sp, t.blk);
+  else opinion_block<false, false>(sp, t.blk);
 }
 
 
@@ -935,6 +937,8 @@ void launch_opinion_jobs(const std::vector<OpinionJob> &jobs, cudaStream_t st, D
     OpinionArgs p{};
     unsigned g = opinion_args(*jobs[j].sim, jobs[j].edge_type, jobs[j].type_nr, jobs[j].eps,
                               jobs[j].a, jobs[j].b, jobs[j].hub_thr, jobs[j].block_thr, p, st);
+    if (p.nbig)
+      fail(VG_ERR_ARG, "the multi-job gather runs no block-wide hub rows (block threshold)");
     args.push_back(p);
     for (unsigned k = 0; k < g; k++) tiles.push_back({(uint32_t)j, k});
   }
