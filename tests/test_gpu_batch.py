@@ -111,6 +111,37 @@ def test_batch_cluster_equals_plain(vh):
     b.close()
 
 
+def test_batch_tiny_instances_every_form(vh):
+    """Three hundred instances of 2..39 agents (one infected each, beta 0.2..0.9):
+    a block ticket of the persistent launch spans many instances, a cluster
+    pack holds dozens, and mask words straddle instance boundaries.  Every
+    form, with every lane count, bit-identical to the plain path."""
+    from vahana_gb300 import models
+    N, deg, beta, rec, seeds = models.batch_params(300, n_lo=2, n_hi=40, deg_lo=1, deg_hi=8,
+                                                   beta_lo=0.2, beta_hi=0.9, rec_lo=2, rec_hi=4)
+    b = models.Batch(N, deg, beta, rec, seeds)
+    total = 0
+    for mode, lanes, forced in ((2, (1, 1), (1, 256, 0xFFFFFFFF)), (1, (2, 2), None),
+                                (4, (4, 4), None), (2, (1, 4), (1, 512, 2)),
+                                (0, (4, 2), None), (2, (2, 2), (1, 128, 0xFFFFFFFF))):
+        if forced:
+            b.set_launch(*forced)
+        b.set_lanes(*lanes)
+        b.step(5, mode=mode)
+        total += 5
+    for i in range(b.n):
+        b.step_one(i, total)
+    moved = 0
+    for i in range(b.n):
+        sb, db = b.states(i, which=0)
+        sp, dp = b.states(i, which=1)
+        np.testing.assert_array_equal(sb, sp)
+        np.testing.assert_array_equal(db, dp)
+        moved += int((sb == 2).sum())
+    assert moved > 300  # the epidemics ran
+    b.close()
+
+
 def test_step_barrier_wait_gives_up_with_a_status(vh):
     """The persistent launch's step waits are bounded: two blocks waiting
     for an instance counter that nothing advances record 0x5e04 and end;
