@@ -909,10 +909,11 @@ __global__ void k_slice_deg(const uint32_t *rp, uint64_t nrows, const uint32_t *
 
 // copy each row's edges into its slice, column-major; padding source 0,
 // weight 0
-__global__ void k_sell_fill(const uint32_t *rp, uint64_t nrows, const uint32_t *src,
-                            const double *w, const uint32_t *order, uint64_t m,
-                            const uint64_t *base, const uint32_t *sdeg, uint32_t *ssrc,
-                            double *sw) {
+__global__ void k_sell_fill(const uint32_t *__restrict__ rp, uint64_t nrows,
+                            const uint32_t *__restrict__ src, const double *__restrict__ w,
+                            const uint32_t *__restrict__ order, uint64_t m,
+                            const uint64_t *__restrict__ base, const uint32_t *__restrict__ sdeg,
+                            uint32_t *__restrict__ ssrc, double *__restrict__ sw) {
   uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   uint64_t nslices_pos = (m + 31) / 32 * 32;
   if (k >= nslices_pos) return;
@@ -926,7 +927,11 @@ __global__ void k_sell_fill(const uint32_t *rp, uint64_t nrows, const uint32_t *
     }
   }
   const uint64_t o = base[sl] + lane;
-  for (uint32_t q = 0; q < sdeg[sl]; q++) {
+  const uint32_t D = sdeg[sl];
+  // (the columns do not overlap the CSR: each lane's loads of a round are
+  // in flight together)
+#pragma unroll 4
+  for (uint32_t q = 0; q < D; q++) {
     ssrc[o + 32ull * q] = q < d ? src[b + q] : 0u;
     sw[o + 32ull * q] = q < d ? w[b + q] : 0.0;
   }
