@@ -32,12 +32,17 @@ __global__ void k_gen_uniform_out(uint64_t N, uint32_t k, uint64_t seed, int typ
 }
 
 // smallest index i with cdf[i] > u (cdf inclusive prefix sums of weights)
-// first i in [lo, hi] with cdf[i] > u, else hi
+// first i in [lo, hi] with cdf[i] > u, else hi.  The cdf and u are
+// non-negative finite doubles, whose order is the order of their bit
+// patterns as unsigned integers: the comparisons run on the integer pipes
+// (the binary64 pipe of this GPU is 64x narrower) with the same outcome.
 __device__ __forceinline__ uint64_t sample_cdf_in(const double *cdf, uint64_t lo, uint64_t hi,
                                                   double u) {
+  const unsigned long long ub = (unsigned long long)__double_as_longlong(u);
+  const long long *cb = reinterpret_cast<const long long *>(cdf);
   while (lo < hi) {
     uint64_t mid = (lo + hi) >> 1;
-    if (cdf[mid] > u) hi = mid; else lo = mid + 1;
+    if ((unsigned long long)cb[mid] > ub) hi = mid; else lo = mid + 1;
   }
   return lo;
 }
