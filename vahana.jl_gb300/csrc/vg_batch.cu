@@ -79,8 +79,8 @@ __device__ __forceinline__ uint8_t sir_rule(const BatchArgs &a, uint64_t i, uint
         atomicCAS(a.status, 0, 402);
       } else {
         const uint64_t nr = i - a.base[in] + 1;
-        const double u = u64_to_unit(philox_u64(philox_draw(a.seed[in], nr, step, TAG_INFECT)));
-        if (u < a.ptab[(uint64_t)in * a.kmax1 + k]) {
+        if (unit_below(philox_u64(philox_draw(a.seed[in], nr, step, TAG_INFECT)),
+                       a.ptab[(uint64_t)in * a.kmax1 + k])) {
           s = 1;
           d = 0;
         }

@@ -82,6 +82,32 @@ VG_HD double u64_to_unit(uint64_t x) {
   return (double)(x >> 11) * (1.0 / 9007199254740992.0);
 }
 
+// the bit pattern of u64_to_unit(x), built with integer operations (exact:
+// the top 53 bits k scaled by 2^-53 have exponent bitlength(k) - 54 and
+// k's bits below its leading one as the fraction)
+VG_HD uint64_t u64_to_unit_bits(uint64_t x) {
+  const uint64_t k = x >> 11;
+  if (k == 0) return 0;
+#ifdef __CUDA_ARCH__
+  const int L = 64 - __clzll((long long)k);
+#else
+  const int L = 64 - __builtin_clzll(k);
+#endif
+  const uint64_t frac = (k << (53 - L)) & ((1ull << 52) - 1);
+  return ((uint64_t)(1023 + L - 54) << 52) | frac;
+}
+
+// u64_to_unit(x) < p for a non-negative finite p, decided on the integer
+// pipes: non-negative doubles are ordered as their bit patterns are
+VG_HD bool unit_below(uint64_t x, double p) {
+  union {
+    double d;
+    uint64_t u;
+  } pb;
+  pb.d = p;
+  return u64_to_unit_bits(x) < pb.u;
+}
+
 // (top53 + 1) * 2^-53: in (0, 1]
 VG_HD double u64_to_unit_open0(uint64_t x) {
   return (double)((x >> 11) + 1) * (1.0 / 9007199254740992.0);

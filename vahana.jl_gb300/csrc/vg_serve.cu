@@ -97,8 +97,7 @@ __global__ void k_sir_jobs(const SirJobDesc *jobs, const SirTile *tiles, int *st
       if (k >= j.ptab_n) {
         atomicCAS(status, 0, 401);
       } else {
-        double u = u64_to_unit(philox_u64(philox_draw(j.seed, i + 1, j.step, TAG_INFECT)));
-        if (u < j.ptab[k]) {
+        if (unit_below(philox_u64(philox_draw(j.seed, i + 1, j.step, TAG_INFECT)), j.ptab[k])) {
           s = 1;
           d = 0;
         }

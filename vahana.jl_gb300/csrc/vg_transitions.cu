@@ -620,8 +620,7 @@ __global__ void k_sir(const uint32_t *__restrict__ rp, const uint32_t *__restric
       if (k >= ptab_n) {
         set_status(status, 401);
       } else {
-        double u = u64_to_unit(philox_u64(philox_draw(seed, i + 1, step, TAG_INFECT)));
-        if (u < ptab[k]) {
+        if (unit_below(philox_u64(philox_draw(seed, i + 1, step, TAG_INFECT)), ptab[k])) {
           s = 1;
           d = 0;
         }
