@@ -250,22 +250,39 @@ namespace {
 // beyond the rows sets the status word (the records come from kernels that
 // declare their types)
 // key: the target row; value: the source's agent_nr - 1, which the stable
-// sort then carries straight into the CSR's source column
+// sort then carries straight into the CSR's source column.  With
+// digit_counts, the kernel also counts the keys' 8-bit digits of `passes`
+// sort passes (the radix sort's upfront count: per block in shared memory,
+// then added to digit_counts[256 p + digit]); the grid then strides.
 __global__ void k_typed_keys(const uint64_t *to, const uint64_t *from, uint64_t n,
                              uint32_t target_type, uint32_t src_type, uint64_t nrows,
-                             uint32_t *keys, uint32_t *src, int *status) {
-  uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  const uint64_t t = to[k], f = from[k];
-  uint64_t r = (t & NR_MASK) - 1;
-  const bool bad = (uint32_t)(t >> SHIFT_TYPE) != target_type || r >= nrows ||
-                   (uint32_t)(f >> SHIFT_TYPE) != src_type;
-  if (bad) {
-    atomicCAS(status, 0, 501);
-    r = 0;
+                             uint32_t *keys, uint32_t *src, int *status,
+                             uint32_t *digit_counts, int passes) {
+  __shared__ uint32_t h[4 * 256];
+  if (digit_counts) {
+    for (int i = threadIdx.x; i < passes * 256; i += blockDim.x) h[i] = 0;
+    __syncthreads();
   }
-  keys[k] = (uint32_t)r;
-  src[k] = (uint32_t)((f & NR_MASK) - 1);
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t t = to[k], f = from[k];
+    uint64_t r = (t & NR_MASK) - 1;
+    const bool bad = (uint32_t)(t >> SHIFT_TYPE) != target_type || r >= nrows ||
+                     (uint32_t)(f >> SHIFT_TYPE) != src_type;
+    if (bad) {
+      atomicCAS(status, 0, 501);
+      r = 0;
+    }
+    keys[k] = (uint32_t)r;
+    src[k] = (uint32_t)((f & NR_MASK) - 1);
+    if (digit_counts)
+      for (int p = 0; p < passes; p++) atomicAdd(&h[p * 256 + ((r >> (8 * p)) & 255u)], 1u);
+  }
+  if (digit_counts) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < passes * 256; i += blockDim.x)
+      if (h[i]) atomicAdd(digit_counts + i, h[i]);
+  }
 }
 
 // row_ptr of the rows 0..nrows from the sorted row keys: rp[r] = the
@@ -426,10 +443,17 @@ bool build_csr_typed(Sim &s, int e, const EdgeAppend &ap, uint64_t n) {
   auto enqueue = [&]() {
     VG_CUDA(cudaMemsetAsync(c.d_max_degree.p, 0, 4, st));
     if (n) {
-      k_typed_keys<<<nblk(n), TPB, 0, st>>>(ap.to.as<uint64_t>(), from, n, (uint32_t)T,
-                                             (uint32_t)ap.src_type, nrows, keys, src,
-                                             s.d_status.as<int>());
-      radix_sort_pairs_u32_in(keys, src, n, bits, st, s.d_status.as<int>(), rc.sort.p);
+      // the sort's digit counts come from the key kernel (one pass over the
+      // records fewer)
+      const bool counted = sort_bytes > 0;
+      const int passes = std::min((bits + 7) / 8, 4);
+      uint32_t *dc = counted ? radix_sort_digit_counts(rc.sort.p) : nullptr;
+      if (counted) VG_CUDA(cudaMemsetAsync(dc, 0, (size_t)passes * 256 * 4, st));
+      const unsigned kb = counted ? std::min<unsigned>(nblk(n), 152 * 4) : nblk(n);
+      k_typed_keys<<<kb, TPB, 0, st>>>(ap.to.as<uint64_t>(), from, n, (uint32_t)T,
+                                       (uint32_t)ap.src_type, nrows, keys, src,
+                                       s.d_status.as<int>(), dc, passes);
+      radix_sort_pairs_u32_in(keys, src, n, bits, st, s.d_status.as<int>(), rc.sort.p, counted);
     }
     k_rp_bounds<<<nblk(n + 1), TPB, 0, st>>>(keys, n, nbr, rc.bstart.as<uint32_t>());
     k_rp_fill<<<(unsigned)nbr, TPB, 0, st>>>(keys, nrows, rc.bstart.as<uint32_t>(),

@@ -450,8 +450,12 @@ void exclusive_scan_u32_in(const uint32_t *in, uint32_t *out, uint64_t n, cudaSt
                            int *err, void *scratch);
 // caller-owned scratch of radix_sort_scratch_bytes() bytes: no allocation
 uint64_t radix_sort_scratch_bytes(uint64_t n, int key_size, int bits);
+// counted: the caller has accumulated the digit counts of every pass (8-bit
+// digit p of each key, at word 256 p + digit) into radix_sort_digit_counts
+// of the same scratch, zeroed before; the sort then skips its own count
 void radix_sort_pairs_u32_in(uint32_t *keys, uint32_t *vals, uint64_t n, int bits,
-                             cudaStream_t st, int *err, void *scratch);
+                             cudaStream_t st, int *err, void *scratch, bool counted = false);
+uint32_t *radix_sort_digit_counts(void *scratch);
 int bits_for(uint64_t maxval);
 
 // graph building (vg_graph.cu)

@@ -465,9 +465,12 @@ RsLayout rs_layout(uint64_t n, int key_size, int bits) {
 // radix_sort_scratch_bytes(n, sizeof(K), bits) bytes owned by the caller;
 // with caller scratch the sort makes no allocation, so it can be recorded
 // into a CUDA graph
+// `counted`: the digit counts of every pass are already in the scratch's
+// first RS_MAXPASS x 256 words (radix_sort_digit_counts), so the upfront
+// count is skipped and those words are left as they are
 template <class K>
 void radix_sort_impl(K *keys, uint32_t *vals, uint64_t n, int bits, cudaStream_t st,
-                     int *err, void *scratch = nullptr) {
+                     int *err, void *scratch = nullptr, bool counted = false) {
   if (n <= 1 || bits <= 0) return;
   if (n >= (1ull << 32)) fail(VG_ERR_NOMEM, "radix sort: more than 2^32 items");
   const RsLayout L = rs_layout(n, (int)sizeof(K), bits);
@@ -475,7 +478,11 @@ void radix_sort_impl(K *keys, uint32_t *vals, uint64_t n, int bits, cudaStream_t
   const uint64_t ntiles = L.ntiles, head = L.head, stat = L.stat, kb = L.kb, vb = L.vb;
   char *buf = (char *)scratch;
   if (!buf) VG_CUDA(cudaMallocAsync((void **)&buf, L.bytes(), st));
-  VG_CUDA(cudaMemsetAsync(buf, 0, head + stat, st));
+  const uint64_t hist_bytes = RS_MAXPASS * 256 * 4;
+  if (counted)
+    VG_CUDA(cudaMemsetAsync(buf + hist_bytes, 0, head + stat - hist_bytes, st));
+  else
+    VG_CUDA(cudaMemsetAsync(buf, 0, head + stat, st));
   uint32_t *ghist = (uint32_t *)buf;
   uint32_t *tickets = (uint32_t *)(buf + RS_MAXPASS * 256 * 4);
   unsigned long long *status = (unsigned long long *)(buf + head);
@@ -485,7 +492,7 @@ void radix_sort_impl(K *keys, uint32_t *vals, uint64_t n, int bits, cudaStream_t
   uint32_t *vb2 = nalt == 2 ? (uint32_t *)(buf + head + stat + 2 * kb + vb) : nullptr;
   const unsigned hblocks =
       (unsigned)std::min<uint64_t>((n + RS_UP_ROUND - 1) / RS_UP_ROUND, 152 * 4);
-  rs_upfront<K><<<hblocks, RS_UP_TPB, 0, st>>>(keys, n, passes, ghist);
+  if (!counted) rs_upfront<K><<<hblocks, RS_UP_TPB, 0, st>>>(keys, n, passes, ghist);
   // the pass's shared memory exceeds the 48 KB of a static allocation
   static const bool smem_ok = [] {
     return cudaFuncSetAttribute(rs_pass<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -545,9 +552,10 @@ uint64_t radix_sort_scratch_bytes(uint64_t n, int key_size, int bits) {
   return rs_layout(n, key_size, bits).bytes();
 }
 void radix_sort_pairs_u32_in(uint32_t *keys, uint32_t *vals, uint64_t n, int bits,
-                             cudaStream_t st, int *err, void *scratch) {
-  radix_sort_impl<uint32_t>(keys, vals, n, bits, st, err, scratch);
+                             cudaStream_t st, int *err, void *scratch, bool counted) {
+  radix_sort_impl<uint32_t>(keys, vals, n, bits, st, err, scratch, counted);
 }
+uint32_t *radix_sort_digit_counts(void *scratch) { return (uint32_t *)scratch; }
 void radix_sort_pairs_u64(uint64_t *keys, uint32_t *vals, uint64_t n, int bits,
                           cudaStream_t st, Sim &s) {
   radix_sort_impl<unsigned long long>((unsigned long long *)keys, vals, n, bits, st,
