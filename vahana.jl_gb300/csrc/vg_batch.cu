@@ -696,29 +696,44 @@ void launch_persistent(vg_batch *b, const StateBufs &bufs, int cur, uint32_t ste
                             b->stream));
     VG_CUDA(cudaStreamSynchronize(b->stream));
   }
-  if ((uint64_t)steps * (uint64_t)*std::max_element(b->N.begin(), b->N.end()) >= (1ull << 32))
-    fail(VG_ERR_ARG, "batch: steps x instance size must stay below 2^32 in one persistent launch");
-  PersistArgs p{};
-  p.a = batch_args(b, cur, step0, nullptr);
-  for (int k = 0; k < 2; k++) {
-    p.st[k] = bufs.st[k];
-    p.dy[k] = bufs.dy[k];
-    p.inf[k] = bufs.inf[k];
-  }
-  p.cur0 = cur;
-  p.steps = steps;
-  p.step0 = step0;
-  p.heavy = b->heavy.as<uint32_t>();
-  p.nheavy = b->nheavy;
-  p.is_heavy = b->nheavy ? b->is_heavy.as<uint8_t>() : nullptr;
-  p.ticket = b->bar.as<unsigned>();
-  p.done = b->done.as<uint32_t>();
-  p.inst_n = b->inst_n.as<uint32_t>();
-  p.rounds = (unsigned)std::max(rounds, 1);
-  switch (ilp) {
-    case 1: launch_persistent_ilp<1>(b, p, tpb); break;
-    case 2: launch_persistent_ilp<2>(b, p, tpb); break;
-    default: launch_persistent_ilp<4>(b, p, tpb); break;
+  // the tickets of a launch (tickets per step x steps) and an instance's
+  // agent-steps (steps x N) are counted in 32 bits: longer runs take
+  // several launches, each starting from the state the last one left
+  rounds = std::max(rounds, 1);
+  const uint64_t span = (uint64_t)tpb * (uint64_t)ilp * (uint64_t)rounds;
+  const uint64_t tps = (b->total + span - 1) / span;
+  const uint64_t maxn = (uint64_t)*std::max_element(b->N.begin(), b->N.end());
+  const uint64_t lim = 0xFFFFFFFFull;
+  const uint64_t tlim = lim - (1ull << 20);  // room for every block's last (unused) ticket
+  const uint32_t chunk =
+      (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(lim / std::max<uint64_t>(maxn, 1),
+                                                         tlim / std::max<uint64_t>(tps, 1)));
+  for (uint32_t done = 0; done < steps;) {
+    const uint32_t c = std::min(steps - done, chunk);
+    PersistArgs p{};
+    p.a = batch_args(b, cur, step0 + done, nullptr);
+    for (int k = 0; k < 2; k++) {
+      p.st[k] = bufs.st[k];
+      p.dy[k] = bufs.dy[k];
+      p.inf[k] = bufs.inf[k];
+    }
+    p.cur0 = cur;
+    p.steps = c;
+    p.step0 = step0 + done;
+    p.heavy = b->heavy.as<uint32_t>();
+    p.nheavy = b->nheavy;
+    p.is_heavy = b->nheavy ? b->is_heavy.as<uint8_t>() : nullptr;
+    p.ticket = b->bar.as<unsigned>();
+    p.done = b->done.as<uint32_t>();
+    p.inst_n = b->inst_n.as<uint32_t>();
+    p.rounds = (unsigned)rounds;
+    switch (ilp) {
+      case 1: launch_persistent_ilp<1>(b, p, tpb); break;
+      case 2: launch_persistent_ilp<2>(b, p, tpb); break;
+      default: launch_persistent_ilp<4>(b, p, tpb); break;
+    }
+    if (c % 2) cur = 1 - cur;
+    done += c;
   }
 }
 
