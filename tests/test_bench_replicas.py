@@ -70,3 +70,30 @@ def test_traffic_summary_matches_the_profile():
     E, N = 200_000_000, 10_000_000
     assert d["algorithmic_bytes_per_launch"] == 12 * E + 20 * N + 4
     assert 12 * E + 20 * N + 4 < t < 20 * E + 20 * N + 12 * E
+
+
+def test_reference_arm_line_on_cpu():
+    """`bench.py --impl reference` (the oracle's C restatement on the host
+    cores, no GPU) prints one JSON line with the contract's fields: the
+    reference tag, a cpu_baseline describing the run, and an e2e block with
+    no host-device copies."""
+    import json
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference",
+                        "--n", "20000", "--steps", "2", "--warmup", "1", "--cpu-seconds", "1"],
+                       capture_output=True, text=True, timeout=600, cwd=root)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["metric"] == "edge-updates/s"
+    assert d["value"] > 0 and d["higher_is_better"] is True and d["n_gpus"] == 1
+    assert d["cpu_baseline"]["kind"] in ("port", "reference")
+    assert d["cpu_baseline"]["cores"] >= 1 and d["cpu_baseline"]["value"] == d["value"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
+    assert d["config"]["workload"] == "bounded_confidence_opinion_chung_lu"
+
