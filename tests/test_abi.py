@@ -57,6 +57,27 @@ def test_registry_rules(vh):
     assert model.has_hint("E5", ":Stateless")
 
 
+def test_prepared_apply_host_rules(vh):
+    """A prepared apply! (vg_apply_prepare / vg_apply_call_run), without a
+    GPU: an unknown transition is refused when the call is prepared; a run
+    before finish_init! is refused with the reference's message (the same
+    vg_apply call); after the simulation is closed the Python handle
+    refuses to run instead of passing a stale simulation."""
+    m = (vh.ModelTypes().register_agenttype("A", [("foo", "i64")])
+         .register_edgetype("E", [("w", "f64")]).create_model("prepared"))
+    sim = vh.create_simulation(m)
+    vh.add_agents(sim, "A", 3, foo=[1, 2, 3])
+    with pytest.raises(Exception, match="unknown transition"):
+        vh.prepare_apply(sim, "no_such_transition", ["A"], ["A"], ["A"])
+    step = vh.prepare_apply(sim, "keep", ["A"], ["A"], ["A"])
+    with pytest.raises(AssertionError, match="finish_init"):
+        step()
+    sim.close()
+    with pytest.raises(RuntimeError, match="closed"):
+        step()
+    step.close()
+
+
 def test_init_phase_staging_and_accessors(vh):
     """Before finish_init!: add_agent!/add_edge! staging, the :SingleEdge
     check of _can_add, num_edges(write=true), accessor hint rules."""
