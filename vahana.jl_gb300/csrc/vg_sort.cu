@@ -343,15 +343,35 @@ __global__ void __launch_bounds__(RS_TPB, 1) rs_pass(const K *kin, const uint32_
   K key[RS_IPT];
   uint32_t val[RS_IPT], rank[RS_IPT];
   int dig[RS_IPT];
+  // every load of the tile is issued before the ranking's warp barriers
+  // (loads placed between them would wait for one another)
+#pragma unroll
+  for (int k = 0; k < RS_IPT; k++) {
+    const uint32_t i = wbase + (uint32_t)k * 32 + lane;
+    key[k] = i < m ? kin[t0 + i] : K(0);
+  }
+#pragma unroll
+  for (int k = 0; k < RS_IPT; k++) {
+    const uint32_t i = wbase + (uint32_t)k * 32 + lane;
+    val[k] = i < m ? vin[t0 + i] : 0u;
+  }
 #pragma unroll
   for (int k = 0; k < RS_IPT; k++) {
     const uint32_t i = wbase + (uint32_t)k * 32 + lane;
     const bool valid = i < m;
-    key[k] = valid ? kin[t0 + i] : K(0);
-    val[k] = valid ? vin[t0 + i] : 0u;
     const int d = valid ? (int)((key[k] >> shift) & 255u) : 256;
     dig[k] = d;
-    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    rank[k] = 0;
+    if (wbase + (uint32_t)k * 32 >= m) continue;  // warp-uniform: no item in this slot
+    // the lanes with the same 9-bit label (digit, or 256 for no item), one
+    // ballot per label bit (measured faster than match.any for full tiles)
+    unsigned peers = 0xffffffffu;
+#pragma unroll
+    for (int bit = 0; bit < 9; bit++) {
+      const bool set = (d >> bit) & 1;
+      const unsigned v = __ballot_sync(0xffffffffu, set);
+      peers &= set ? v : ~v;
+    }
     const uint32_t b = valid ? S.wcnt[w][d] : 0u;
     rank[k] = b + __popc(peers & lt);
     __syncwarp();
@@ -430,13 +450,19 @@ __global__ void __launch_bounds__(RS_TPB, 1) rs_pass(const K *kin, const uint32_
     }
   }
   __syncthreads();
-  for (uint32_t i = threadIdx.x; i < m; i += RS_TPB) {
-    const K kk = S.key[i];
-    const uint32_t dd = (uint32_t)(kk >> shift) & 255u;
-    const uint64_t pos = (uint64_t)S.gbase[dd] + (i - S.dstart[dd]);
-    if (pos < n) {
-      kout[pos] = kk;
-      vout[pos] = S.val[i];
+  // unrolled over the RS_IPT items of a thread, so that their shared loads
+  // overlap
+#pragma unroll
+  for (int k = 0; k < RS_IPT; k++) {
+    const uint32_t i = threadIdx.x + (uint32_t)k * RS_TPB;
+    if (i < m) {
+      const K kk = S.key[i];
+      const uint32_t dd = (uint32_t)(kk >> shift) & 255u;
+      const uint64_t pos = (uint64_t)S.gbase[dd] + (i - S.dstart[dd]);
+      if (pos < n) {
+        kout[pos] = kk;
+        vout[pos] = S.val[i];
+      }
     }
   }
 }
