@@ -263,20 +263,36 @@ __global__ void k_typed_keys(const uint64_t *to, const uint64_t *from, uint64_t 
     for (int i = threadIdx.x; i < passes * 256; i += blockDim.x) h[i] = 0;
     __syncthreads();
   }
-  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
-       k += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t t = to[k], f = from[k];
-    uint64_t r = (t & NR_MASK) - 1;
-    const bool bad = (uint32_t)(t >> SHIFT_TYPE) != target_type || r >= nrows ||
-                     (uint32_t)(f >> SHIFT_TYPE) != src_type;
-    if (bad) {
-      atomicCAS(status, 0, 501);
-      r = 0;
+  // four records per thread and round, their loads issued before the
+  // shared-memory counts (which would otherwise order each load after the
+  // previous record's atomics)
+  constexpr int U = 4;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t k0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k0 < n; k0 += U * stride) {
+    uint64_t tv[U], fv[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const uint64_t k = k0 + u * stride;
+      tv[u] = k < n ? to[k] : 0;
+      fv[u] = k < n ? from[k] : 0;
     }
-    keys[k] = (uint32_t)r;
-    src[k] = (uint32_t)((f & NR_MASK) - 1);
-    if (digit_counts)
-      for (int p = 0; p < passes; p++) atomicAdd(&h[p * 256 + ((r >> (8 * p)) & 255u)], 1u);
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const uint64_t k = k0 + u * stride;
+      if (k >= n) break;
+      const uint64_t t = tv[u], f = fv[u];
+      uint64_t r = (t & NR_MASK) - 1;
+      const bool bad = (uint32_t)(t >> SHIFT_TYPE) != target_type || r >= nrows ||
+                       (uint32_t)(f >> SHIFT_TYPE) != src_type;
+      if (bad) {
+        atomicCAS(status, 0, 501);
+        r = 0;
+      }
+      keys[k] = (uint32_t)r;
+      src[k] = (uint32_t)((f & NR_MASK) - 1);
+      if (digit_counts)
+        for (int p = 0; p < passes; p++) atomicAdd(&h[p * 256 + ((r >> (8 * p)) & 255u)], 1u);
+    }
   }
   if (digit_counts) {
     __syncthreads();
