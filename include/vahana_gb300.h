@@ -514,7 +514,9 @@ int vg_batch_step_one(vg_batch *b, int i, int steps);
 int vg_batch_read_states(vg_batch *b, int i, uint8_t *state_out,
                          int32_t *days_out, uint64_t cap, uint64_t *n_out);
 /* which = 0: instance i's state in the batched arena; which = 1: the state
- * of instance i's own simulation (advanced by vg_batch_step_one). */
+ * of instance i's own simulation (advanced by vg_batch_step_one); any other
+ * value is VG_ERR_ARG.  n_out (and, for vg_batch_read_graph, both counts)
+ * must not be null. */
 int vg_batch_read_states2(vg_batch *b, int i, int which, uint8_t *state_out,
                           int32_t *days_out, uint64_t cap, uint64_t *n_out);
 int vg_batch_read_graph(vg_batch *b, int i, uint32_t *row_ptr_out,

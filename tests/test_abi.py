@@ -284,6 +284,9 @@ def test_null_and_bad_arguments_return_errors(vh):
     assert L.vg_move_to(h, b"r", 1, None, -1, None, -1, None, 0.0, 0, 1, 0) == 2
     assert L.vg_add_graph(h, a, 2, None, e, 2, None, None, 1, None, None) == 2
     assert L.vg_read_staged_edges(h, e, None, None, None, 0, None) == 2
+    assert L.vg_read_edges(h, e, a, None, None, None, None, C.byref(u)) == 2
+    assert b"row count pointer" in L.vg_last_error()
+    assert L.vg_read_edges(h, e, a, None, None, None, C.byref(u), None) == 2
     # :SingleEdge duplicate check against a staged edge, payload omitted
     mse = (vh.ModelTypes().register_agenttype("A", [("foo", "i64")])
            .register_edgetype("SE", [("foo", "i64")], ":SingleEdge").create_model("se"))

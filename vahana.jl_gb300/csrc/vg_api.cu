@@ -1367,6 +1367,8 @@ int vg_read_edges(vg_sim *h, int e, int T, uint64_t *row_ptr_out, uint64_t *from
                   void *const *payload_out, uint64_t *nrows_out, uint64_t *nedges_out) {
   API_BEGIN
   Sim &s = S(h);
+  need(nrows_out, "row count pointer");
+  need(nedges_out, "edge count pointer");
   const EdgeTypeDesc &ed = s.model->et(e);
   EdgeStore &es = s.edges[e];
   if (!s.initialized) fail(VG_ERR_STATE, "call finish_init! first");

@@ -1266,16 +1266,32 @@ int vg_batch_step(vg_batch *b, int steps, int mode) {
     if (!b->graph[p]) {
       cudaStream_t cs;
       VG_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-      VG_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-      int cur = p;
-      for (int k = 0; k < steps; k++) {
-        BatchArgs a = batch_args(b, cur, (uint32_t)k, b->step_base.as<int64_t>());
-        launch_step(b, a, b->tpb, b->apt, cs);
-        cur = 1 - cur;
+      cudaGraph_t g = nullptr;
+      cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+      if (e == cudaSuccess) {
+        try {
+          int cur = p;
+          for (int k = 0; k < steps; k++) {
+            BatchArgs a = batch_args(b, cur, (uint32_t)k, b->step_base.as<int64_t>());
+            launch_step(b, a, b->tpb, b->apt, cs);
+            cur = 1 - cur;
+          }
+        } catch (...) {  // end the capture and free the stream before passing the error on
+          cudaStreamEndCapture(cs, &g);
+          if (g) cudaGraphDestroy(g);
+          cudaStreamDestroy(cs);
+          throw;
+        }
+        e = cudaStreamEndCapture(cs, &g);
       }
-      VG_CUDA(cudaStreamEndCapture(cs, &b->graph_def[p]));
-      VG_CUDA(cudaGraphInstantiate(&b->graph[p], b->graph_def[p], 0));
-      VG_CUDA(cudaStreamDestroy(cs));
+      cudaStreamDestroy(cs);
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph[p], g, 0);
+      if (e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        b->graph[p] = nullptr;
+        VG_CUDA(e);
+      }
+      b->graph_def[p] = g;
     }
     int64_t s0 = b->step;
     VG_CUDA(cudaMemcpyAsync(b->step_base.p, &s0, 8, cudaMemcpyHostToDevice, b->stream));
@@ -1314,6 +1330,8 @@ int vg_batch_read_states2(vg_batch *b, int i, int which, uint8_t *state_out,
     if (rc) fail(rc, vg_last_error());
     return VG_OK;
   }
+  if (which != 0) fail(VG_ERR_ARG, "batch: which 0 (the arena) or 1 (the instance's simulation)");
+  need(n_out, "count pointer");
   uint64_t a0 = 0;
   for (int j = 0; j < i; j++) a0 += (uint64_t)b->N[j];
   uint64_t Ni = (uint64_t)b->N[i];
@@ -1334,6 +1352,8 @@ int vg_batch_read_graph(vg_batch *b, int i, uint32_t *row_ptr_out, uint32_t *src
                         uint64_t *nrows_out, uint64_t *nedges_out) {
   API_BEGIN
   if (!b || i < 0 || i >= b->n) fail(VG_ERR_ARG, "batch: instance index");
+  need(nrows_out, "row count pointer");
+  need(nedges_out, "edge count pointer");
   Sim &S = *b->sims[i]->s;
   CSR &c = S.edges[b->contact].csr[b->person];
   *nrows_out = c.nrows;
