@@ -22,7 +22,8 @@ export ModelTypes, register_agenttype!, register_edgetype!, register_param!,
        all_agentids, add_raster!, connect_raster_neighbors!, move_to!, cellid,
        rastervalues, calc_rasterstate, param, set_param!, get_global, set_global!, bind_param!,
        push_global!, disable_transition_checks, transition_names, Edge, AgentID,
-       add_graph!, remove_edges!, add_agent_per_process!, write_snapshot, read_snapshot
+       add_graph!, remove_edges!, add_agent_per_process!, write_snapshot, read_snapshot,
+       prepare_apply, PreparedApply, release!, set_async!, synchronize
 
 const LIB = get(ENV, "VAHANA_GB300_LIB",
                 joinpath(@__DIR__, "..", "libvahana_gb300.so"))
@@ -59,7 +60,10 @@ mutable struct ModelTypes
     function ModelTypes()
         h = Ref{Ptr{Cvoid}}(C_NULL)
         check(ccall((:vg_model_create, LIB), Cint, (Ptr{Ptr{Cvoid}},), h))
-        new(h[], Dict{DataType, Int}(), Dict{DataType, Int}())
+        m = new(h[], Dict{DataType, Int}(), Dict{DataType, Int}())
+        # simulations keep their own reference to the model's types, so the
+        # handle may go before them
+        finalizer(m -> m.h == C_NULL || ccall((:vg_model_destroy, LIB), Cvoid, (Ptr{Cvoid},), m.h), m)
     end
 end
 
@@ -140,8 +144,20 @@ end
 function copy_simulation(sim::Simulation)
     h = Ref{Ptr{Cvoid}}(C_NULL)
     check(ccall((:vg_sim_copy, LIB), Cint, (Ptr{Cvoid}, Ptr{Ptr{Cvoid}}), sim.h, h))
-    Simulation(h[], sim.model, copy(sim.rasters))
+    c = Simulation(h[], sim.model, copy(sim.rasters))
+    finalizer(s -> s.h == C_NULL || ccall((:vg_sim_destroy, LIB), Cint, (Ptr{Cvoid},), s.h), c)
 end
+
+"""
+    set_async!(sim, on::Bool)
+
+With `on`, apply! returns without waiting for the device; an error that a
+kernel reports surfaces at the next `synchronize(sim)` or read back
+(vg_sim_set_async).  Off by default: every apply! checks.
+"""
+set_async!(sim::Simulation, on::Bool) =
+    check(ccall((:vg_sim_set_async, LIB), Cint, (Ptr{Cvoid}, Cint), sim.h, on ? 1 : 0))
+synchronize(sim::Simulation) = check(ccall((:vg_sim_synchronize, LIB), Cint, (Ptr{Cvoid},), sim.h))
 
 "finish_init!(sim) -- src/Simulation.jl:403-476 (one process)"
 finish_init!(sim::Simulation) =
@@ -206,6 +222,46 @@ function apply!(sim::Simulation, f::Symbol, call, read, write;
 end
 apply(sim::Simulation, f::Symbol, call, read, write; kw...) =
     apply!(copy_simulation(sim), f, call, read, write; kw...)
+
+"""
+    step = prepare_apply(sim, transition::Symbol, call, read, write;
+                         add_existing, with_edge, params)
+    step()   # apply!(sim, transition, call, read, write; ...)
+
+One apply! prepared once and run by calling the result (vg_apply_prepare,
+vg_apply_call_run): the same vg_apply call with its arguments converted and
+copied once, for loops whose per-call argument handling costs more than a
+small simulation's step.  The transition name is checked when the call is
+prepared, everything else at each run.
+"""
+mutable struct PreparedApply
+    h::Ptr{Cvoid}
+    sim::Simulation
+end
+function prepare_apply(sim::Simulation, f::Symbol, call, read, write;
+                       add_existing = [], with_edge = nothing, params = Float64[])
+    c, r, w, a = refs(sim, call), refs(sim, read), refs(sim, write), refs(sim, add_existing)
+    we = with_edge === nothing ? Cint(-1) : Cint(sim.model.edges[with_edge])
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:vg_apply_prepare, LIB), Cint,
+                (Ptr{Cvoid}, Cstring, Ptr{Cint}, Cint, Ptr{Cint}, Cint, Ptr{Cint}, Cint,
+                 Ptr{Cint}, Cint, Cint, Ptr{Cdouble}, Cint, Ptr{Ptr{Cvoid}}),
+                sim.h, String(f), c, length(c), r, length(r), w, length(w), a, length(a), we,
+                Float64.(params), length(params), h))
+    finalizer(release!, PreparedApply(h[], sim))
+end
+"release!(step) frees a prepared apply! (it keeps no device memory)"
+function release!(p::PreparedApply)
+    p.h == C_NULL || ccall((:vg_apply_call_destroy, LIB), Cint, (Ptr{Cvoid},), p.h)
+    p.h = C_NULL
+    nothing
+end
+function (p::PreparedApply)()
+    p.h == C_NULL && error("this prepared apply! was released")
+    p.sim.h == C_NULL && error("the simulation of this prepared apply! is finished")
+    check(ccall((:vg_apply_call_run, LIB), Cint, (Ptr{Cvoid},), p.h))
+    p.sim
+end
 
 """
     apply_host!(sim, transition::Symbol, call, read, write, T, states::Vector{T};
