@@ -5,7 +5,6 @@ host side of this is checked here with two gloo ranks on the CPU."""
 import os
 import socket
 
-import pytest
 import torch.multiprocessing as mp
 
 
